@@ -1,0 +1,356 @@
+"""Throughput of the em2d PIC step (push + deposit + current filter + Yee) on
+GB300, in particle-steps/s.
+
+Workload (one GPU): uniform thermal plasma, 2048 x 2048 cells, dx = dy = 0.1,
+dt = 0.05, periodic, one electron species (m_q = -1), 4 x 4 particles per
+cell (67,108,864 particles), isotropic thermal momentum 0.05, compensated
+level-1 binomial current smoothing along x and y.  Initial particles are
+seeded synthetic data with the reference's loading (ppc lattice, Gaussian
+momenta, per-cell mean removed); all state is float32.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+One JSON line on rank 0.  Under torchrun (N > 1) every rank runs its own
+independent copy of the workload (replicas, weak scaling, no collective on the
+data path); time is the max over ranks.
+
+``--impl reference`` times the reference's CPU algorithm for the same
+workload on the host cores: the reference itself when its build is present
+(oracle/_ref), else the C restatement under oracle/ built with the
+reference's stock -Ofast flags.  Each step of it is a bounded sample of the
+workload (a 1024 x 512 cell sub-box at the same density).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import platform
+import statistics
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s per GB300 (push+deposit+Yee), batched & adjoint vs plain GPU"
+UNIT = "particle-steps/s"
+WORKLOAD = dict(name="em2d uniform thermal plasma 2048x2048, 4x4 ppc (67,108,864 particles)",
+                nx=(2048, 2048), box=(204.8, 204.8), dt=0.05, ppc=(4, 4), uth=0.05, m_q=-1.0,
+                smooth=("compensated", 1, "compensated", 1))
+# algorithmic bytes: particle record read + written (2 x 28 B); per cell:
+# gather E,B (24 B) + deposit J (12 B) in the push kernel, Yee reads E,B,J and
+# writes E,B (60 B), each filter pass reads and writes J (24 B)
+PART_BYTES = 56
+PUSH_CELL_BYTES = 36
+STEP_CELL_BYTES = 96
+SMOOTH_PASS_BYTES = 24
+
+
+def synth_particles(nx, ny, ppc, uth, seed):
+    """Reference-style loading: particles on the ppc lattice of every cell
+    (em2d/particles.c:168-179, 336-349), Gaussian momenta of width uth with the
+    mean of every cell removed (particles.c:96-142).  Seeded numpy generator."""
+    px, py = ppc
+    npc = px * py
+    ncell = nx * ny
+    dt = np.dtype([("ix", "<i4"), ("iy", "<i4"), ("x", "<f4"), ("y", "<f4"),
+                   ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4")])
+    parts = np.empty(ncell * npc, dtype=dt)
+    cell = np.arange(ncell, dtype=np.int64)
+    parts["ix"] = np.repeat((cell % nx).astype(np.int32), npc)
+    parts["iy"] = np.repeat((cell // nx).astype(np.int32), npc)
+    lx = (np.float32(1.0 / px) * (np.arange(px) + 0.5)).astype(np.float32)
+    ly = (np.float32(1.0 / py) * (np.arange(py) + 0.5)).astype(np.float32)
+    parts["x"] = np.tile(np.tile(lx, py), ncell)
+    parts["y"] = np.tile(np.repeat(ly, px), ncell)
+    rng = np.random.default_rng(seed)
+    for f in ("ux", "uy", "uz"):
+        u = rng.standard_normal(ncell * npc, dtype=np.float32) * np.float32(uth)
+        u = u.reshape(ncell, npc)
+        u -= u.mean(axis=1, keepdims=True, dtype=np.float32)
+        parts[f] = u.reshape(-1)
+    return parts
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region: NVML through ctypes (read-only queries)
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    REASONS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap",
+               0x8: "hw_slowdown", 0x10: "sync_boost", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+               0x100: "display_clock_setting"}
+
+    def __init__(self, index):
+        self.ok = False
+        self.samples = []
+        self.reasons = 0
+        try:
+            self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if self.nv.nvmlInit_v2() != 0:
+                return
+            self.h = ctypes.c_void_p()
+            if self.nv.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(self.h)) != 0:
+                return
+            self.ok = True
+        except OSError:
+            return
+
+    def _clock(self, kind, fn="nvmlDeviceGetClockInfo"):
+        v = ctypes.c_uint()
+        r = getattr(self.nv, fn)(self.h, kind, ctypes.byref(v))
+        return v.value if r == 0 else None
+
+    def max_sm(self):
+        return self._clock(1, "nvmlDeviceGetMaxClockInfo") if self.ok else None
+
+    def start(self):
+        if not self.ok:
+            return
+        self.stop_flag = False
+
+        def run():
+            r = ctypes.c_ulonglong()
+            while not self.stop_flag:
+                c = self._clock(1)
+                if c is not None:
+                    self.samples.append(c)
+                if self.nv.nvmlDeviceGetCurrentClocksEventReasons(self.h, ctypes.byref(r)) == 0:
+                    self.reasons |= r.value
+                time.sleep(0.002)
+
+        self.t = threading.Thread(target=run, daemon=True)
+        self.t.start()
+
+    def stop(self):
+        if not self.ok:
+            return None
+        self.stop_flag = True
+        self.t.join()
+        names = [n for b, n in self.REASONS.items() if self.reasons & b and n != "gpu_idle"]
+        return {"sm_mhz": statistics.median(self.samples) if self.samples else None,
+                "sm_max_mhz": self.max_sm(), "samples": len(self.samples), "reasons": names}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the push kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "push_tiles_thermal2048.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU references
+# ---------------------------------------------------------------------------
+def cpu_run(nx, ny, steps, warmup, fast=True):
+    """Times the reference algorithm on the host: oracle/_ref (the reference
+    compiled from its sources) when present, else the oracle port.  Returns
+    (particle-steps/s, kind, particles)."""
+    from oracle import pyoracle
+
+    pyoracle.build()
+    backend = "ref" if pyoracle.ref_available(fast) else "oracle"
+    kind = "reference" if backend == "ref" else "port"
+    W = WORKLOAD
+    dx = W["box"][0] / W["nx"][0]
+    if backend == "oracle":
+        pyoracle.set_rand_seed(12345, 67890, backend=backend, fast=fast, fresh=True)
+    else:
+        pyoracle.set_rand_seed(12345, 67890, backend=backend, fast=fast)
+    s = pyoracle.CpuSim([nx, ny], [nx * dx, ny * dx], W["dt"], backend=backend, fast=fast)
+    s.add_species("electrons", W["m_q"], list(W["ppc"]), ufl=[0, 0, 0], uth=[W["uth"]] * 3)
+    sm = W["smooth"]
+    s.set_smooth(sm[0], sm[1], sm[2], sm[3])
+    n = s.np_(0)
+    s.iter(warmup)
+    t0 = time.perf_counter()
+    s.iter(steps)
+    t = time.perf_counter() - t0
+    return n * steps / t, kind, n
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    nx, ny = 1024, 512
+    v, kind, n = cpu_run(nx, ny, args.steps, args.warmup)
+    W = WORKLOAD
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / v * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": W["name"], "nx": list(W["nx"]), "ppc": list(W["ppc"]),
+                                        "dt": W["dt"], "dx": 0.1, "smoothing": "compensated level 1, x and y"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+                         "sample": f"{nx}x{ny}-cell sub-box of the workload ({n} particles), "
+                                   f"{args.steps} timed steps after {args.warmup} warm-up steps, "
+                                   f"single-threaded C (the reference em2d is single-threaded), "
+                                   f"host {platform.machine()}"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--tile", default="16x16")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist_mod
+
+        torch.cuda.set_device(local)
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def allmax(v):
+        if not dist:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    from zpic_gb300._zc import CudaSim
+
+    W = WORKLOAD
+    nx, ny = W["nx"]
+    tile = tuple(int(v) for v in args.tile.split("x"))
+    parts = synth_particles(nx, ny, W["ppc"], W["uth"], seed=1234 + rank)
+    N = parts.size
+    q = np.float32(-1.0) / np.float32(W["ppc"][0] * W["ppc"][1])
+    sim = CudaSim(W["nx"], W["box"], W["dt"], device=local, tile=tile)
+    sim.add_species(W["m_q"], float(q), W["ppc"], parts)
+    sm = W["smooth"]
+    sim.set_smooth(sm[0], sm[1], sm[2], sm[3])
+
+    # ---- device-resident timed region ----
+    sim.step(args.warmup)
+    sim.set_profiling(True)
+    sim.reset_profile()
+    clk = ClockSampler(local)
+    barrier()
+    sim.synchronize()
+    clk.start()
+    sim.step(args.steps)  # returns after the stream has drained
+    ms = sim.last_ms()
+    clocks = clk.stop()
+    barrier()
+    ms = allmax(ms)
+    prof = sim.profile()
+    sim.set_profiling(False)
+    value = N * args.steps * world / (ms / 1e3)
+
+    # ---- end to end through the C-ABI with host buffers ----
+    import torch
+
+    pinned = torch.empty(parts.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(parts.dtype)
+    pinned[:] = parts
+    fshape = (ny + 3, nx + 3, 3)
+    Eh = torch.zeros(int(np.prod(fshape)), dtype=torch.float32, pin_memory=True).numpy().reshape(fshape)
+    Bh = torch.zeros(int(np.prod(fshape)), dtype=torch.float32, pin_memory=True).numpy().reshape(fshape)
+    barrier()
+    sim.synchronize()
+    t0 = time.perf_counter()
+    sim.set_fields(E=Eh, B=Bh)
+    sim.set_particles(0, pinned)
+    hist = []
+    for _ in range(args.steps):
+        sim.step(1)
+        hist.append(sim.energy())
+    t_e2e = time.perf_counter() - t0
+    barrier()
+    t_e2e = allmax(t_e2e)
+    e2e = N * args.steps * world / t_e2e
+    h2d = (parts.nbytes + Eh.nbytes + Bh.nbytes) / args.steps
+    d2h = (6 + 1) * 8
+
+    # ---- roofline of the dominant kernel (push + deposit) ----
+    push_ms, push_n = prof["push"]
+    push_avg = push_ms / max(push_n, 1)
+    cells = nx * ny
+    push_bytes = N * PART_BYTES + cells * PUSH_CELL_BYTES
+    peak, peak_kind = peaks()
+    achieved = push_bytes / (push_avg / 1e3) / 1e9
+    traffic = ncu_traffic()
+    step_bytes = N * PART_BYTES + cells * (STEP_CELL_BYTES + 4 * SMOOTH_PASS_BYTES)
+    launches = sum(n for _, n in prof.values())
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded reference-style loading)",
+        "config": {"workload": W["name"], "nx": [nx, ny], "dx": 0.1, "dt": W["dt"], "ppc": list(W["ppc"]),
+                   "particles_per_gpu": int(N), "uth": W["uth"],
+                   "smoothing": "compensated level 1, x and y", "tile": list(tile),
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (1.88 GB of particles read and written per step)"},
+        "clocks": clocks,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "how": "fields and particles uploaded from pinned host buffers through the C-ABI, "
+                       "then per step zc_step(1) + zc_energy read-back"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_push_tiles", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": push_bytes,
+                     "avg_launch_ms": push_avg,
+                     "step_achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9},
+        "phases_ms_per_step": {k: round(v[0] / args.steps, 5) for k, v in prof.items() if v[1] or v[0]},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, kind, n = cpu_run(512, 512, 3, 1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+                                "sample": f"512x512-cell sub-box of the workload ({n} particles), 3 timed "
+                                          f"steps, single-threaded C, host {platform.machine()}"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,207 @@
+/*
+ * zpic_cuda.h -- C-ABI of libzpic_cuda, the GB300 (sm_103a) implementation of
+ * the ZPIC em2d electromagnetic PIC time step.
+ *
+ * Plain C types only: pointers, sizes, status codes.  Device state lives
+ * behind an opaque zc_sim handle; every handle owns one CUDA stream, so
+ * handles are independent of each other (the reference itself is
+ * single-threaded and non-reentrant, em2d/random.c:16-17, particles.c:26-27).
+ *
+ * Host buffers use the reference layouts:
+ *   particles  zc_part records, identical to t_part (em2d/particles.h:29-37)
+ *   grids      float3 interleaved, (nx+3)*(ny+3) cells with 1 lower and 2
+ *              upper guard cells per axis, row stride nx+3, cell (0,0) at
+ *              offset 1+(nx+3)  (em2d/emf.c:59-89, em2d/current.c:33-53)
+ *
+ * Nothing here calls exit(): invalid input returns ZC_EINVAL and the message
+ * is kept for zc_last_error(); the reference's exit(-1) behaviour is
+ * restored, where wanted, by the drop-in layer above this ABI.
+ */
+#ifndef ZPIC_CUDA_H
+#define ZPIC_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ZC_API __attribute__((visibility("default")))
+#else
+#define ZC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    ZC_OK = 0,
+    ZC_EINVAL = 1,            /* invalid argument (Courant, smoothing, laser, ...) */
+    ZC_ENOMEM = 2,            /* device or host allocation failed */
+    ZC_ECUDA = 3,             /* a CUDA runtime call failed */
+    ZC_EPARTICLE_ESCAPE = 4,  /* a particle moved more than one cell in a step */
+    ZC_ETIMEOUT = 5,          /* a bounded device wait (TMA barrier) gave up */
+    ZC_EOVERFLOW = 6,         /* particle overflow buffer exhausted: particles lost */
+    ZC_ESTATE = 7             /* call not valid in the current state */
+} zc_status;
+
+/* particle record, same layout as t_part (em2d/particles.h:29-37) */
+typedef struct {
+    int ix, iy;
+    float x, y;
+    float ux, uy, uz;
+} zc_part;
+
+typedef struct zc_sim zc_sim;
+
+typedef struct {
+    int nx[2];              /* cells along x, y */
+    float box[2];           /* box size, simulation units */
+    float dt;               /* time step */
+    int device;             /* CUDA device ordinal */
+    int tile[2];            /* particle tile size in cells (0,0 -> 16 x 16) */
+    int deterministic;      /* 1: fixed-order current deposition, bit-reproducible runs */
+    float tile_slack;       /* spare tile capacity, fraction (<=0 -> 0.5) */
+} zc_sim_desc;
+
+typedef struct {
+    float m_q;              /* mass over charge */
+    float q;                /* charge of one simulation particle (spec->q) */
+    int ppc[2];             /* particles per cell (for reporting only) */
+} zc_species_desc;
+
+/* laser pulse, same fields as t_emf_laser (em2d/emf.h:134-157) */
+typedef struct {
+    int type;               /* 0 plane, 1 gaussian */
+    float start, fwhm, rise, flat, fall;
+    float a0, omega0, polarization;
+    float W0, focus, axis;
+} zc_laser;
+
+typedef struct {
+    int iter;               /* completed steps (emf->iter) */
+    int n_move;             /* moving-window shifts so far */
+    int moving_window;
+    int n_species;
+    int nx[2];
+    int tile[2];
+    int ntiles[2];
+} zc_info;
+
+/* Device view of the grids for zero-copy consumers (e.g. PyTorch): SoA
+ * planes [component][row][column] of `pitch` floats per row, `rows` rows,
+ * buffer coordinates (column i+1, row j+1) for cell (i, j). */
+typedef struct {
+    float *E;               /* 3 planes: Ex, Ey, Ez (B follows E in memory) */
+    float *B;               /* 3 planes: Bx, By, Bz */
+    float *J;               /* 3 planes: Jx, Jy, Jz */
+    size_t plane;           /* floats per plane */
+    int pitch, rows;
+    void *stream;           /* cudaStream_t of the handle */
+} zc_grid_view;
+
+/* Moving-window injection provider: called on the host when the window moves
+ * (spec_move_window, em2d/particles.c:619-640) with the species index and the
+ * updated n_move; it must return the particles of the new right-most column
+ * (cell indices already in the shifted frame).  The buffer stays owned by the
+ * caller until the next call. */
+typedef int (*zc_inject_fn)(void *user, int species, int n_move, const zc_part **parts, int *np);
+
+/* --- lifetime ---------------------------------------------------------- */
+/* replaces emf_new + current_new + the Courant check of sim_new
+ * (em2d/simulation.c:93-112, em2d/emf.c:56-115, em2d/current.c:30-79) */
+ZC_API zc_status zc_sim_create(const zc_sim_desc *desc, zc_sim **out);
+/* replaces sim_delete (em2d/simulation.c:212-222) */
+ZC_API zc_status zc_sim_destroy(zc_sim *sim);
+
+/* --- species ------------------------------------------------------------- */
+/* registers a species whose initial particles were injected on the host by
+ * spec_new (em2d/particles.c:535-612) and uploads them */
+ZC_API zc_status zc_species_create(zc_sim *sim, const zc_species_desc *desc, const zc_part *parts,
+                            int np, int *species_id);
+/* replaces the device particles of a species (host edits between steps,
+ * Species.add / Species.particles writes, python/source/em2d.pyx:238-312) */
+ZC_API zc_status zc_species_set_particles(zc_sim *sim, int species, const zc_part *parts, int np);
+/* appends particles (moving-window injection, em2d/particles.c:476-492) */
+ZC_API zc_status zc_species_inject(zc_sim *sim, int species, const zc_part *parts, int np);
+/* copies the particles back in tile order; *np receives the count; `cap`
+ * is the room in `out` (records).  out == NULL only queries the count. */
+ZC_API zc_status zc_species_get_particles(zc_sim *sim, int species, zc_part *out, int cap, int *np);
+ZC_API zc_status zc_species_count(zc_sim *sim, int species, int *np);
+ZC_API zc_status zc_set_injector(zc_sim *sim, zc_inject_fn fn, void *user);
+
+/* --- configuration ------------------------------------------------------- */
+/* replaces sim_set_smooth (em2d/simulation.c:134-147) */
+ZC_API zc_status zc_set_smooth(zc_sim *sim, int xtype, int xlevel, int ytype, int ylevel);
+/* replaces sim_set_moving_window (em2d/simulation.c:154-163) */
+ZC_API zc_status zc_set_moving_window(zc_sim *sim);
+/* replaces emf_add_laser (em2d/emf.c:242-350) */
+ZC_API zc_status zc_add_laser(zc_sim *sim, const zc_laser *laser);
+/* replaces emf_set_ext_fld (em2d/emf.c:764-831).  type 0 none, 1 uniform
+ * (value in E0/B0), 2 custom (grid in reference layout, evaluated on the
+ * host from the user's callback for every buffer cell). */
+ZC_API zc_status zc_set_ext_fld(zc_sim *sim, int E_type, const float E0[3], const float *E_grid,
+                         int B_type, const float B0[3], const float *B_grid);
+
+/* --- the step ------------------------------------------------------------ */
+/* sim_iter x nsteps (em2d/simulation.c:45-56) */
+ZC_API zc_status zc_step(zc_sim *sim, int nsteps);
+/* the phases of sim_iter, for callers that drive them one by one */
+ZC_API zc_status zc_current_zero(zc_sim *sim);                 /* em2d/current.c:98-107 */
+ZC_API zc_status zc_spec_advance(zc_sim *sim, int species);    /* em2d/particles.c:1104-1269 */
+ZC_API zc_status zc_current_update(zc_sim *sim);               /* em2d/current.c:171-183 */
+ZC_API zc_status zc_emf_advance(zc_sim *sim);                  /* em2d/emf.c:688-716 */
+
+/* --- data ---------------------------------------------------------------- */
+/* E and B in reference layout; either pointer may be NULL */
+ZC_API zc_status zc_set_fields(zc_sim *sim, const float *E_buf, const float *B_buf);
+ZC_API zc_status zc_get_fields(zc_sim *sim, float *E_buf, float *B_buf);
+/* fields seen by the particles (E_part / B_part, em2d/emf.h:96-97) */
+ZC_API zc_status zc_get_particle_fields(zc_sim *sim, float *E_buf, float *B_buf);
+ZC_API zc_status zc_get_current(zc_sim *sim, float *J_buf);
+ZC_API zc_status zc_set_current(zc_sim *sim, const float *J_buf);
+/* field energy per component (emf_get_energy, em2d/emf.c:729-750) and the
+ * time-centred kinetic energy of each species after its last advance
+ * (spec->energy, em2d/particles.c:1231); FP64 reductions on the device */
+ZC_API zc_status zc_energy(zc_sim *sim, double emf_energy[6], double *kin_energy);
+/* charge density of one species on an (nx+1)*(ny+1) grid
+ * (spec_deposit_charge, em2d/particles.c:1289-1324) */
+ZC_API zc_status zc_species_charge(zc_sim *sim, int species, float *charge);
+ZC_API zc_status zc_get_info(zc_sim *sim, zc_info *info);
+ZC_API zc_status zc_grid_view_get(zc_sim *sim, zc_grid_view *view);
+ZC_API zc_status zc_synchronize(zc_sim *sim);
+/* device time (ms) of the last zc_step / phase call, CUDA events */
+ZC_API zc_status zc_last_step_ms(zc_sim *sim, float *ms);
+
+/* --- per-phase device timing ------------------------------------------- */
+/* With profiling on, every phase of the step is bracketed by CUDA events on
+ * the handle's stream; zc_get_profile returns, per phase, the summed device
+ * milliseconds and the number of kernel launches since the last reset.  The
+ * reference's own counters are wall-clock totals of spec_advance and
+ * emf_advance (em2d/particles.c:26-59, em2d/emf.c:27-37). */
+enum {
+    ZC_PHASE_PUSH = 0,      /* fused push + deposit, one CTA per tile */
+    ZC_PHASE_SPILL,         /* push of particles outside the tiles */
+    ZC_PHASE_MIGRATE,       /* tile migration */
+    ZC_PHASE_KIN_ENERGY,    /* kinetic-energy reduction */
+    ZC_PHASE_ZERO,          /* current zeroing */
+    ZC_PHASE_FOLD,          /* current guard-cell fold */
+    ZC_PHASE_SMOOTH,        /* current filter passes */
+    ZC_PHASE_YEE,           /* fused Yee advance */
+    ZC_PHASE_EMF_GC,        /* field guard cells */
+    ZC_PHASE_EXT,           /* external fields */
+    ZC_PHASE_WINDOW,        /* moving-window shift and injection */
+    ZC_NPHASE
+};
+ZC_API zc_status zc_set_profiling(zc_sim *sim, int enable);
+ZC_API zc_status zc_get_profile(zc_sim *sim, double ms[ZC_NPHASE], long long launches[ZC_NPHASE]);
+ZC_API zc_status zc_reset_profile(zc_sim *sim);
+ZC_API const char *zc_phase_name(int phase);
+
+/* message of the last failing call on this thread */
+ZC_API const char *zc_last_error(void);
+ZC_API const char *zc_status_string(zc_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

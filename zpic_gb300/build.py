@@ -1,0 +1,76 @@
+"""Builds libzpic_cuda.so (sm_103a) in-tree with nvcc.
+
+    python -m zpic_gb300.build          # or zpic_gb300.build.build()
+
+Three translation units are compiled in parallel and linked into
+``zpic_gb300/lib/libzpic_cuda.so``.  The physics kernels (particles, fields)
+are compiled with ``--fmad=false`` so that every float32 operation rounds as
+in the reference C code; the host runtime uses the defaults.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "lib")
+BUILD = os.path.join(HERE, "_build")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+UNITS = [
+    ("zc_particles.cu", ["--fmad=false"]),
+    ("zc_fields.cu", ["--fmad=false"]),
+    ("zc_api.cu", []),
+]
+
+
+def nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def build(verbose: bool = False, ptxas_info: bool = False) -> str:
+    """Compiles and links the library; returns its path."""
+    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(BUILD, exist_ok=True)
+    cc = nvcc()
+    common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+                     "-I", os.path.join(os.path.dirname(HERE), "include")]
+    if ptxas_info:
+        common += ["-Xptxas", "-v"]
+
+    def one(unit):
+        src, extra = unit
+        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        out = _run([cc, "-c", os.path.join(CSRC, src), "-o", obj] + common + extra)
+        return obj, out
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        results = list(ex.map(one, UNITS))
+    objs = [o for o, _ in results]
+    if verbose or ptxas_info:
+        for _, out in results:
+            if out.strip():
+                print(out)
+    lib = os.path.join(LIBDIR, "libzpic_cuda.so")
+    tmp = lib + ".tmp"
+    _run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"] * 0)
+    os.replace(tmp, lib)
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, ptxas_info="-v" in sys.argv))

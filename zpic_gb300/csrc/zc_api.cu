@@ -1,0 +1,1205 @@
+// zc_api.cu -- host runtime of libzpic_cuda: the C-ABI declared in
+// include/zpic_cuda.h.  One zc_sim owns one CUDA stream and all its device
+// buffers; nothing here touches global state other than the per-thread
+// error message.
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/zpic_cuda.h"
+#include "zc_kernels.h"
+
+using namespace zc;
+
+namespace {
+
+thread_local std::string g_err;
+
+zc_status fail(zc_status s, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return s;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return fail(ZC_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+#define TRY(call)                     \
+  do {                                \
+    zc_status s_ = (call);            \
+    if (s_ != ZC_OK) return s_;       \
+  } while (0)
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+zc_status load_encoder() {
+  if (g_encode) return ZC_OK;
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+  if (q != cudaDriverEntryPointSuccess || !fn) return fail(ZC_ECUDA, "cuTensorMapEncodeTiled unavailable");
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return ZC_OK;
+}
+
+// 3-D tensor map over `planes` SoA planes of the padded grid
+zc_status make_map(CUtensorMap *m, float *base, const Grid &G, int planes, int bw, int bh) {
+  cuuint64_t dims[3] = {(cuuint64_t)G.pitch, (cuuint64_t)G.rows, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)G.pitch * 4, (cuuint64_t)G.plane * 4};
+  cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, (cuuint32_t)planes};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ZC_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ZC_OK;
+}
+
+template <class T>
+zc_status dalloc(T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(ZC_ENOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T),
+                                    cudaGetErrorString(e));
+  return ZC_OK;
+}
+
+template <class T>
+void dfree(T *&p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+zc_status alloc_particles(Particles &p, long long n) {
+  TRY(dalloc(&p.ix, n));
+  TRY(dalloc(&p.iy, n));
+  TRY(dalloc(&p.x, n));
+  TRY(dalloc(&p.y, n));
+  TRY(dalloc(&p.ux, n));
+  TRY(dalloc(&p.uy, n));
+  TRY(dalloc(&p.uz, n));
+  return ZC_OK;
+}
+
+void free_particles(Particles &p) {
+  dfree(p.ix);
+  dfree(p.iy);
+  dfree(p.x);
+  dfree(p.y);
+  dfree(p.ux);
+  dfree(p.uy);
+  dfree(p.uz);
+}
+
+struct SpeciesState {
+  float m_q = -1, q = 0;
+  int ppc[2] = {1, 1};
+  int iter = 0, n_move = 0;
+  // tile layout
+  int *d_off = nullptr, *d_cap = nullptr, *d_np = nullptr, *d_nstay = nullptr;
+  std::vector<int> h_off, h_cap;
+  long long alloc = 0;   // particles per buffer
+  Particles buf[2] = {};
+  int cur = 0;
+  unsigned *d_key = nullptr;
+  // spill lists (in: processed this step, out: written this step)
+  Particles spill[2] = {};
+  int *d_spill_cnt = nullptr;  // [2]
+  int spill_cap = 0;
+  int spill_cur = 0;
+  // energy
+  double *d_ekin_tile = nullptr, *d_ekin_extra = nullptr, *d_ekin = nullptr;
+};
+
+}  // namespace
+
+struct zc_sim {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int nx = 0, ny = 0;
+  float box[2] = {0, 0}, dx[2] = {0, 0}, dt = 0;
+  Grid G{};
+  float *EB[2] = {nullptr, nullptr};
+  int eb_cur = 0;
+  float *EBp = nullptr, *extE = nullptr, *extB = nullptr;
+  int ext_Et = 0, ext_Bt = 0;
+  float3 ext_E0{0, 0, 0}, ext_B0{0, 0, 0};
+  float *J[2] = {nullptr, nullptr};
+  int j_cur = 0;
+  CUtensorMap tmK_EB[2], tmK_EBp, tmK_J;
+  CUtensorMap tmY_EB[2], tmY_J[2];
+  int TX = 16, TY = 16, ntx = 0, nty = 0, ntiles = 0;
+  Outbox O{};
+  long long ob_alloc = 0;
+  std::vector<SpeciesState> sp;
+  int xtype = 0, ytype = 0, xlevel = 0, ylevel = 0;
+  int mw = 0, n_move = 0, iter = 0;
+  int *d_err = nullptr;
+  int *h_pinned = nullptr;        // [0] error bits, [1..] spill counts
+  double *d_part = nullptr, *d_emf = nullptr;
+  int energy_blocks = 0;
+  float *stage = nullptr;         // AoS staging for grids
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0;
+  zc_inject_fn inj = nullptr;
+  void *inj_user = nullptr;
+  zc_part *h_inj = nullptr;       // pinned injection staging
+  size_t h_inj_cap = 0;
+  cudaEvent_t inj_done = nullptr;
+  Particles inj_list{};
+  long long inj_list_cap = 0;
+  int deterministic = 0;
+  float slack = 0.5f;
+  int accumulated_err = 0;
+  // per-phase profiling: event pairs recorded during a call, summed on sync
+  int profiling = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+  size_t ev_used = 0;
+  double prof_ms[ZC_NPHASE] = {};
+  long long prof_launch[ZC_NPHASE] = {};
+};
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int d) {
+    cudaGetDevice(&prev);
+    if (prev != d) cudaSetDevice(d);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Brackets a phase with events when profiling is on; counts its launches
+// always.
+struct Phase {
+  zc_sim *s;
+  int ph;
+  cudaEvent_t b = nullptr;
+  Phase(zc_sim *s_, int ph_, int nlaunch) : s(s_), ph(ph_) {
+    s->prof_launch[ph] += nlaunch;
+    if (!s->profiling) return;
+    b = next_event();
+    cudaEventRecord(b, s->st);
+  }
+  ~Phase() {
+    if (!b) return;
+    cudaEvent_t e = next_event();
+    cudaEventRecord(e, s->st);
+    s->ev_pending.push_back({ph, {b, e}});
+  }
+  cudaEvent_t next_event() {
+    if (s->ev_used == s->ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      s->ev_pool.push_back(e);
+    }
+    return s->ev_pool[s->ev_used++];
+  }
+};
+
+// sums the recorded phase times (stream must be synchronised)
+void collect_profile(zc_sim *s) {
+  for (auto &p : s->ev_pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) s->prof_ms[p.first] += ms;
+  }
+  s->ev_pending.clear();
+  s->ev_used = 0;
+}
+
+LayoutConst layout(const zc_sim *s) { return LayoutConst{s->TX, s->TY, s->ntx, s->nty, s->nx, s->ny}; }
+
+TileSet tiles(SpeciesState &p, int ntiles) { return TileSet{p.d_off, p.d_cap, p.d_np, p.d_nstay, ntiles}; }
+
+Spill spill_of(SpeciesState &p, int k) { return Spill{p.spill[k], p.d_spill_cnt + k, p.spill_cap}; }
+
+// outbox slots per tile: room for a moving-window column plus crossers
+zc_status ensure_outbox(zc_sim *s, int max_cap) {
+  int per = std::max(256, ((max_cap / 6) + 31) / 32 * 32);
+  long long need = (long long)per * s->ntiles;
+  if (per <= s->O.cap && need <= s->ob_alloc) return ZC_OK;
+  free_particles(s->O.p);
+  dfree(s->O.dst);
+  TRY(alloc_particles(s->O.p, need));
+  TRY(dalloc(&s->O.dst, need));
+  if (!s->O.cnt) TRY(dalloc(&s->O.cnt, s->ntiles));
+  CK(cudaMemsetAsync(s->O.cnt, 0, sizeof(int) * s->ntiles, s->st));
+  s->O.cap = per;
+  s->ob_alloc = need;
+  return ZC_OK;
+}
+
+// Builds the tile layout of a species from per-tile counts and moves its
+// particles (tiles of the current layout, its spill list and an optional
+// new list) into it.  Every tile is then ordered deterministically.
+zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
+  SpeciesState &p = s->sp[k];
+  cudaStream_t st = s->st;
+  const LayoutConst L = layout(s);
+  const int nt = s->ntiles;
+  int *d_cnt = nullptr, *d_fill = nullptr, *d_np_old = nullptr, *d_off_old = nullptr;
+  TRY(dalloc(&d_cnt, nt));
+  TRY(dalloc(&d_fill, nt));
+  CK(cudaMemcpyAsync(d_cnt, p.d_np, sizeof(int) * nt, cudaMemcpyDeviceToDevice, st));
+  TRY(dalloc(&d_np_old, nt));
+  TRY(dalloc(&d_off_old, nt));
+  CK(cudaMemcpyAsync(d_np_old, p.d_np, sizeof(int) * nt, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d_off_old, p.d_off, sizeof(int) * nt, cudaMemcpyDeviceToDevice, st));
+  int *d_list_n = nullptr;
+  TRY(dalloc(&d_list_n, 1));
+  CK(cudaMemcpyAsync(d_list_n, &list_n, sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(launch_count_list(p.spill[p.spill_cur], p.d_spill_cnt + p.spill_cur, p.spill_cap, d_cnt, L, st));
+  if (list && list_n > 0) CK(launch_count_list(*list, d_list_n, list_n, d_cnt, L, st));
+  std::vector<int> cnt(nt);
+  CK(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * nt, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+
+  // capacities: room for the count or for the nominal full-density tile,
+  // whichever is larger, plus slack
+  const long long nominal = (long long)p.ppc[0] * p.ppc[1] * s->TX * s->TY;
+  std::vector<int> off(nt), cap(nt);
+  long long tot = 0;
+  int max_cap = 0;
+  for (int t = 0; t < nt; ++t) {
+    long long base = std::max<long long>(cnt[t], nominal);
+    long long c = (long long)std::ceil(base * (1.0 + s->slack)) + 32;
+    c = (c + 31) / 32 * 32;
+    if (c > (1LL << 30)) return fail(ZC_ENOMEM, "tile capacity too large");
+    off[t] = (int)tot;
+    cap[t] = (int)c;
+    tot += c;
+    max_cap = std::max(max_cap, (int)c);
+  }
+  if (tot >= (1LL << 31)) return fail(ZC_ENOMEM, "species too large for 32-bit tile offsets");
+  TRY(ensure_outbox(s, max_cap));
+
+  Particles nbuf[2] = {};
+  const bool grow = tot > p.alloc;
+  if (grow) {
+    TRY(alloc_particles(nbuf[0], tot));
+    TRY(alloc_particles(nbuf[1], tot));
+  } else {
+    nbuf[0] = p.buf[0];
+    nbuf[1] = p.buf[1];
+  }
+  unsigned *nkey = p.d_key;
+  if (grow || !nkey) {
+    TRY(dalloc(&nkey, tot));
+  }
+  // destination of the scatter: the buffer that does not hold the particles
+  const int src_i = p.cur, tmp_i = 1 - p.cur;
+  Particles tmp = grow ? nbuf[1] : p.buf[tmp_i];
+  CK(cudaMemcpyAsync(p.d_off, off.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(p.d_cap, cap.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
+  CK(launch_copy_tiles(p.buf[src_i], d_off_old, d_np_old, tmp, p.d_off, nkey, d_fill, nt, st));
+  CK(launch_scatter_list(p.spill[p.spill_cur], p.d_spill_cnt + p.spill_cur, p.spill_cap, tmp, p.d_off,
+                         p.d_cap, d_fill, nkey, 1u << 30, L, s->d_err, st));
+  if (list && list_n > 0)
+    CK(launch_scatter_list(*list, d_list_n, list_n, tmp, p.d_off, p.d_cap, d_fill, nkey, 1u << 31, L,
+                           s->d_err, st));
+  CK(cudaMemcpyAsync(p.d_np, cnt.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
+  // order every tile into the other buffer
+  Particles dst = grow ? nbuf[0] : p.buf[src_i];
+  int smax = 0;
+  for (int t = 0; t < nt; ++t) smax = std::max(smax, cnt[t]);
+  const int smem_cap = 16 * 1024;  // keys held in shared memory (8 bytes each); a power of two
+  int sm = 1;
+  while (sm < smax) sm <<= 1;
+  sm = std::min(sm, smem_cap);
+  CK(launch_tile_order(tmp, nkey, p.d_off, p.d_np, dst, nt, std::max(sm, 1), 32, st));
+  CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), st));
+  CK(cudaStreamSynchronize(st));
+  if (grow) {
+    free_particles(p.buf[0]);
+    free_particles(p.buf[1]);
+    if (p.d_key) dfree(p.d_key);
+    p.buf[0] = nbuf[0];
+    p.buf[1] = nbuf[1];
+    p.alloc = tot;
+    p.cur = 0;
+  }
+  p.d_key = nkey;
+  p.h_off = off;
+  p.h_cap = cap;
+  dfree(d_cnt);
+  dfree(d_fill);
+  dfree(d_np_old);
+  dfree(d_off_old);
+  dfree(d_list_n);
+  return ZC_OK;
+}
+
+// host AoS -> device SoA list (temporary), returns the list
+zc_status upload_list(zc_sim *s, const zc_part *parts, int n, Particles &list, int **d_cnt_unused) {
+  (void)d_cnt_unused;
+  TRY(alloc_particles(list, std::max(n, 1)));
+  if (n <= 0) return ZC_OK;
+  void *d_aos = nullptr;
+  CK(cudaMalloc(&d_aos, sizeof(zc_part) * (size_t)n));
+  CK(cudaMemcpyAsync(d_aos, parts, sizeof(zc_part) * (size_t)n, cudaMemcpyHostToDevice, s->st));
+  int *d_cnt = nullptr;
+  TRY(dalloc(&d_cnt, s->ntiles));
+  CK(cudaMemsetAsync(d_cnt, 0, sizeof(int) * s->ntiles, s->st));
+  CK(launch_stage_to_list(d_aos, n, list, d_cnt, layout(s), s->d_err, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  cudaFree(d_aos);
+  dfree(d_cnt);
+  return ZC_OK;
+}
+
+zc_status check_errors(zc_sim *s, bool relayout_spill) {
+  CK(cudaMemcpyAsync(s->h_pinned, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  int e = s->h_pinned[0];
+  if (e) {
+    CK(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->st));
+    s->accumulated_err |= e;
+  }
+  if (relayout_spill && (e & ERR_SPILLED)) {
+    for (size_t k = 0; k < s->sp.size(); ++k) {
+      SpeciesState &p = s->sp[k];
+      int n = 0;
+      CK(cudaMemcpy(&n, p.d_spill_cnt + p.spill_cur, sizeof(int), cudaMemcpyDeviceToHost));
+      if (n > 0) TRY(relayout(s, (int)k, nullptr, 0));
+    }
+  }
+  if (e & ERR_OVERFLOW) return fail(ZC_EOVERFLOW, "particle spill buffer exhausted: particles were lost");
+  if (e & ERR_TIMEOUT) return fail(ZC_ETIMEOUT, "a TMA barrier wait timed out");
+  if (e & ERR_ESCAPE) return fail(ZC_EPARTICLE_ESCAPE, "a particle moved more than one cell or left its tile");
+  return ZC_OK;
+}
+
+zc_status spec_advance_impl(zc_sim *s, int k) {
+  SpeciesState &p = s->sp[k];
+  cudaStream_t st = s->st;
+  // moving window: decided after the push, on the species' own counters
+  // (spec_move_window, particles.c:621)
+  int shift = 0;
+  if (s->mw) {
+    const int it = p.iter + 1;
+    shift = ((it * s->dt) > (s->dx[0] * (p.n_move + 1))) ? 1 : 0;
+  }
+  PushConst C;
+  C.tem = (float)(0.5 * s->dt / p.m_q);
+  C.dt_dx = s->dt / s->dx[0];
+  C.dt_dy = s->dt / s->dx[1];
+  C.qnx = p.q * s->dx[0] / s->dt;
+  C.qny = p.q * s->dx[1] / s->dt;
+  C.q = p.q;
+  C.nx = s->nx;
+  C.ny = s->ny;
+  C.ntx = s->ntx;
+  C.nty = s->nty;
+  C.shift = shift;
+  C.mw = s->mw;
+  const int in = p.spill_cur, out = 1 - p.spill_cur;
+  {
+    Phase ph(s, ZC_PHASE_SPILL, 0);
+    CK(cudaMemsetAsync(p.d_spill_cnt + out, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(p.d_ekin_extra, 0, sizeof(double), st));
+  }
+  PushLaunch a;
+  a.tm_eb = s->EBp ? &s->tmK_EBp : &s->tmK_EB[s->eb_cur];
+  a.tm_j = &s->tmK_J;
+  a.pin = p.buf[p.cur];
+  a.pout = p.buf[1 - p.cur];
+  a.T = tiles(p, s->ntiles);
+  a.O = s->O;
+  a.S = spill_of(p, out);
+  a.ekin_tile = p.d_ekin_tile;
+  a.err = s->d_err;
+  a.C = C;
+  a.ntiles = s->ntiles;
+  a.TX = s->TX;
+  a.TY = s->TY;
+  {
+    Phase ph(s, ZC_PHASE_PUSH, 1);
+    CK(launch_push_tiles(a, st));
+  }
+  const float *EBpart = s->EBp ? s->EBp : s->EB[s->eb_cur];
+  {
+    Phase ph(s, ZC_PHASE_SPILL, 1);
+    CK(launch_push_spill(EBpart, s->J[0], s->G, p.spill[in], p.d_spill_cnt + in, p.spill_cap, spill_of(p, out),
+                         p.d_ekin_extra, s->d_err, C, 152, st));
+  }
+  {
+    Phase ph(s, ZC_PHASE_MIGRATE, 1);
+    CK(launch_migrate(p.buf[1 - p.cur], tiles(p, s->ntiles), s->O, spill_of(p, out), s->d_err, s->ntx, s->nty,
+                      s->mw, st));
+  }
+  p.cur = 1 - p.cur;
+  p.spill_cur = out;
+  {
+    Phase ph(s, ZC_PHASE_KIN_ENERGY, 1);
+    CK(launch_sum_energy(p.d_ekin_tile, s->ntiles, p.d_ekin_extra, p.d_ekin, p.q * p.m_q, s->dx[0], s->dx[1],
+                         st));
+  }
+  p.iter += 1;
+  if (shift) {
+    p.n_move += 1;
+    if (!s->inj) return fail(ZC_ESTATE, "moving window needs an injection provider (zc_set_injector)");
+    const zc_part *parts = nullptr;
+    int n = 0;
+    if (s->inj(s->inj_user, k, p.n_move, &parts, &n) != 0)
+      return fail(ZC_EINVAL, "injection provider failed");
+    if (n > 0) {
+      Phase ph(s, ZC_PHASE_WINDOW, 3);
+      if ((size_t)n > s->h_inj_cap || n > s->inj_list_cap) {
+        CK(cudaStreamSynchronize(st));
+        if (s->h_inj) cudaFreeHost(s->h_inj);
+        size_t c = (size_t)n * 2 + 1024;
+        CK(cudaMallocHost((void **)&s->h_inj, c * sizeof(zc_part)));
+        s->h_inj_cap = c;
+        free_particles(s->inj_list);
+        TRY(alloc_particles(s->inj_list, (long long)c));
+        s->inj_list_cap = (long long)c;
+      } else {
+        CK(cudaEventSynchronize(s->inj_done));  // previous copy out of the pinned buffer is done
+      }
+      std::memcpy(s->h_inj, parts, sizeof(zc_part) * (size_t)n);
+      // pinned AoS -> device list (the list arrays double as the AoS staging)
+      void *d_aos = nullptr;
+      CK(cudaMallocAsync(&d_aos, sizeof(zc_part) * (size_t)n, st));
+      CK(cudaMemcpyAsync(d_aos, s->h_inj, sizeof(zc_part) * (size_t)n, cudaMemcpyHostToDevice, st));
+      CK(cudaEventRecord(s->inj_done, st));
+      int *d_dummy = nullptr;
+      CK(cudaMallocAsync((void **)&d_dummy, sizeof(int) * s->ntiles, st));
+      CK(cudaMemsetAsync(d_dummy, 0, sizeof(int) * s->ntiles, st));
+      CK(launch_stage_to_list(d_aos, n, s->inj_list, d_dummy, layout(s), s->d_err, st));
+      CK(launch_append_list(s->inj_list, n, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur),
+                            layout(s), s->d_err, st));
+      CK(cudaFreeAsync(d_aos, st));
+      CK(cudaFreeAsync(d_dummy, st));
+    }
+  }
+  return ZC_OK;
+}
+
+void smooth_comp(int n, float *sa, float *sb) {  // get_smooth_comp, em2d/current.c:297-304
+  float a = -1;
+  float b = (4.0 + 2.0 * n) / n;
+  float total = 2 * a + b;
+  *sa = a / total;
+  *sb = b / total;
+}
+
+zc_status current_update_impl(zc_sim *s) {
+  cudaStream_t st = s->st;
+  {
+    Phase ph(s, ZC_PHASE_FOLD, s->mw ? 1 : 2);
+    CK(launch_fold(s->J[0], s->G, s->mw, st));
+  }
+  int c = 0;
+  auto px = [&](float a, float b) -> zc_status {
+    Phase ph(s, ZC_PHASE_SMOOTH, 1);
+    CK(launch_smooth_x(s->J[c], s->J[1 - c], s->G, a, b, s->mw, st));
+    c = 1 - c;
+    return ZC_OK;
+  };
+  auto py = [&](float a, float b) -> zc_status {
+    Phase ph(s, ZC_PHASE_SMOOTH, 1);
+    CK(launch_smooth_y(s->J[c], s->J[1 - c], s->G, a, b, st));
+    c = 1 - c;
+    return ZC_OK;
+  };
+  float sa, sb;
+  if (s->xtype != 0) {
+    for (int i = 0; i < s->xlevel; ++i) TRY(px(0.25f, 0.5f));
+    if (s->xtype == 2) {
+      smooth_comp(s->xlevel, &sa, &sb);
+      TRY(px(sa, sb));
+    }
+  }
+  if (s->ytype != 0) {
+    for (int i = 0; i < s->xlevel; ++i) TRY(py(0.25f, 0.5f));  // xlevel, as em2d/current.c:449
+    if (s->ytype == 2) {
+      smooth_comp(s->ylevel, &sa, &sb);
+      TRY(py(sa, sb));
+    }
+  }
+  s->j_cur = c;
+  return ZC_OK;
+}
+
+zc_status emf_advance_impl(zc_sim *s) {
+  cudaStream_t st = s->st;
+  YeeConst Y;
+  const float dth = s->dt / 2.0f;
+  Y.cxb = dth / s->dx[0];
+  Y.cyb = dth / s->dx[1];
+  Y.cxe = s->dt / s->dx[0];
+  Y.cye = s->dt / s->dx[1];
+  Y.dt = s->dt;
+  const int o = 1 - s->eb_cur;
+  {
+    Phase ph(s, ZC_PHASE_YEE, 1);
+    CK(launch_yee(&s->tmY_EB[s->eb_cur], &s->tmY_J[s->j_cur], s->EB[o], s->G, Y, s->d_err, st));
+  }
+  s->eb_cur = o;
+  {
+    Phase ph(s, ZC_PHASE_EMF_GC, 1);
+    CK(launch_emf_gc(s->EB[o], s->G, s->mw, st));
+  }
+  if (s->EBp) {
+    Phase ph(s, ZC_PHASE_EXT, 1);
+    CK(launch_ext_add(s->EB[o], s->EBp, s->extE, s->extB, s->ext_Et, s->ext_Bt, s->ext_E0, s->ext_B0, s->G, st));
+  }
+  s->iter += 1;
+  if (s->mw && (s->iter * s->dt) > s->dx[0] * (s->n_move + 1)) {  // emf_move_window, emf.c:650
+    Phase ph(s, ZC_PHASE_WINDOW, 1);
+    CK(launch_window_shift(s->EB[o], s->EB[1 - o], s->G, st));
+    s->eb_cur = 1 - o;
+    s->n_move += 1;
+  }
+  return ZC_OK;
+}
+
+zc_status current_zero_impl(zc_sim *s) {
+  Phase ph(s, ZC_PHASE_ZERO, 0);
+  CK(cudaMemsetAsync(s->J[0], 0, sizeof(float) * 3 * s->G.plane, s->st));
+  s->j_cur = 0;
+  return ZC_OK;
+}
+
+zc_status iter_impl(zc_sim *s) {
+  TRY(current_zero_impl(s));
+  for (size_t k = 0; k < s->sp.size(); ++k) TRY(spec_advance_impl(s, (int)k));
+  TRY(current_update_impl(s));
+  TRY(emf_advance_impl(s));
+  return ZC_OK;
+}
+
+zc_status grid_up(zc_sim *s, const float *host, float *planes) {
+  const size_t n = (size_t)(s->nx + 3) * (s->ny + 3) * 3;
+  CK(cudaMemcpyAsync(s->stage, host, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
+  CK(launch_aos_to_planes(s->stage, planes, s->G, 3, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status grid_down(zc_sim *s, const float *planes, float *host) {
+  const size_t n = (size_t)(s->nx + 3) * (s->ny + 3) * 3;
+  CK(launch_planes_to_aos(planes, s->stage, s->G, 3, s->st));
+  CK(cudaMemcpyAsync(host, s->stage, n * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status refresh_particle_fields(zc_sim *s) {
+  if (!s->EBp) return ZC_OK;
+  CK(launch_ext_add(s->EB[s->eb_cur], s->EBp, s->extE, s->extB, s->ext_Et, s->ext_Bt, s->ext_E0, s->ext_B0, s->G,
+                    s->st));
+  return ZC_OK;
+}
+
+zc_status check_species(zc_sim *s, int k) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (k < 0 || k >= (int)s->sp.size()) return fail(ZC_EINVAL, "invalid species index %d", k);
+  return ZC_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+const char *zc_last_error(void) { return g_err.c_str(); }
+
+const char *zc_status_string(zc_status s) {
+  switch (s) {
+    case ZC_OK: return "ok";
+    case ZC_EINVAL: return "invalid argument";
+    case ZC_ENOMEM: return "out of memory";
+    case ZC_ECUDA: return "CUDA error";
+    case ZC_EPARTICLE_ESCAPE: return "particle escaped its cell";
+    case ZC_ETIMEOUT: return "device wait timed out";
+    case ZC_EOVERFLOW: return "particle overflow";
+    case ZC_ESTATE: return "invalid state";
+  }
+  return "unknown";
+}
+
+zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
+  if (!d || !out) return fail(ZC_EINVAL, "null argument");
+  *out = nullptr;
+  if (d->nx[0] < 2 || d->nx[1] < 2) return fail(ZC_EINVAL, "grid must be at least 2 x 2 cells");
+  if (!(d->box[0] > 0) || !(d->box[1] > 0) || !(d->dt > 0)) return fail(ZC_EINVAL, "box and dt must be > 0");
+  const float dx0 = d->box[0] / d->nx[0], dx1 = d->box[1] / d->nx[1];
+  // Courant condition (em2d/simulation.c:105-110)
+  const float cour = sqrtf(1.0f / (1.0f / (dx0 * dx0) + 1.0f / (dx1 * dx1)));
+  if (d->dt >= cour)
+    return fail(ZC_EINVAL, "Invalid timestep, courant condition violation, dtmax = %f", cour);
+  int TX = d->tile[0] > 0 ? d->tile[0] : 16, TY = d->tile[1] > 0 ? d->tile[1] : 16;
+  if (!tile_supported(TX, TY)) return fail(ZC_EINVAL, "unsupported tile size %d x %d", TX, TY);
+  if ((long long)(d->nx[0] + 3) * (d->nx[1] + 3) > (1LL << 30)) return fail(ZC_EINVAL, "grid too large");
+  TRY(load_encoder());
+
+  zc_sim *s = new zc_sim();
+  s->device = d->device;
+  DeviceGuard g(s->device);
+  s->nx = d->nx[0];
+  s->ny = d->nx[1];
+  s->box[0] = d->box[0];
+  s->box[1] = d->box[1];
+  s->dx[0] = dx0;
+  s->dx[1] = dx1;
+  s->dt = d->dt;
+  s->TX = TX;
+  s->TY = TY;
+  s->ntx = (s->nx + TX - 1) / TX;
+  s->nty = (s->ny + TY - 1) / TY;
+  s->ntiles = s->ntx * s->nty;
+  s->deterministic = d->deterministic;
+  s->slack = d->tile_slack > 0 ? d->tile_slack : 0.5f;
+  Grid &G = s->G;
+  G.nx = s->nx;
+  G.ny = s->ny;
+  G.pitch = ((s->nx + 3 + 4) + 31) / 32 * 32;
+  G.rows = s->ny + 3;
+  G.plane = (size_t)G.pitch * G.rows;
+  zc_status st = ZC_OK;
+#define TRYC(call)              \
+  do {                          \
+    st = (call);                \
+    if (st != ZC_OK) goto bad;  \
+  } while (0)
+  if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+    st = fail(ZC_ECUDA, "cudaStreamCreate failed");
+    goto bad;
+  }
+  for (int b = 0; b < 2; ++b) {
+    TRYC(dalloc(&s->EB[b], 6 * G.plane));
+    TRYC(dalloc(&s->J[b], 3 * G.plane));
+    cudaMemsetAsync(s->EB[b], 0, sizeof(float) * 6 * G.plane, s->st);
+    cudaMemsetAsync(s->J[b], 0, sizeof(float) * 3 * G.plane, s->st);
+  }
+  TRYC(dalloc(&s->d_err, 1));
+  cudaMemsetAsync(s->d_err, 0, sizeof(int), s->st);
+  if (cudaMallocHost((void **)&s->h_pinned, 64 * sizeof(int)) != cudaSuccess) {
+    st = fail(ZC_ENOMEM, "cudaMallocHost failed");
+    goto bad;
+  }
+  s->energy_blocks = 2 * 152;
+  TRYC(dalloc(&s->d_part, 6 * s->energy_blocks));
+  TRYC(dalloc(&s->d_emf, 6));
+  TRYC(dalloc(&s->stage, (size_t)(s->nx + 3) * (s->ny + 3) * 3));
+  TRYC(dalloc(&s->O.cnt, s->ntiles));
+  cudaMemsetAsync(s->O.cnt, 0, sizeof(int) * s->ntiles, s->st);
+  {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int BW = (TX + 6) & ~3, BH = TY + 3;
+    for (int b = 0; b < 2; ++b) {
+      TRYC(make_map(&s->tmK_EB[b], s->EB[b], G, 6, BW, BH));
+      TRYC(make_map(&s->tmY_EB[b], s->EB[b], G, 6, kYeeBW, kYeeBH));
+      TRYC(make_map(&s->tmY_J[b], s->J[b], G, 3, kYeeBW, kYeeBH));
+    }
+    TRYC(make_map(&s->tmK_J, s->J[0], G, 3, BW, BH));
+  }
+  if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->inj_done, cudaEventDisableTiming) != cudaSuccess) {
+    st = fail(ZC_ECUDA, "cudaEventCreate failed");
+    goto bad;
+  }
+  if (cudaStreamSynchronize(s->st) != cudaSuccess) {
+    st = fail(ZC_ECUDA, "initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
+    goto bad;
+  }
+  *out = s;
+  return ZC_OK;
+bad:
+  zc_sim_destroy(s);
+  return st;
+#undef TRYC
+}
+
+zc_status zc_sim_destroy(zc_sim *s) {
+  if (!s) return ZC_OK;
+  DeviceGuard g(s->device);
+  if (s->st) cudaStreamSynchronize(s->st);
+  for (auto &p : s->sp) {
+    free_particles(p.buf[0]);
+    free_particles(p.buf[1]);
+    free_particles(p.spill[0]);
+    free_particles(p.spill[1]);
+    dfree(p.d_off);
+    dfree(p.d_cap);
+    dfree(p.d_np);
+    dfree(p.d_nstay);
+    dfree(p.d_key);
+    dfree(p.d_spill_cnt);
+    dfree(p.d_ekin_tile);
+    dfree(p.d_ekin_extra);
+    dfree(p.d_ekin);
+  }
+  for (int b = 0; b < 2; ++b) {
+    dfree(s->EB[b]);
+    dfree(s->J[b]);
+  }
+  dfree(s->EBp);
+  dfree(s->extE);
+  dfree(s->extB);
+  free_particles(s->O.p);
+  dfree(s->O.dst);
+  dfree(s->O.cnt);
+  free_particles(s->inj_list);
+  dfree(s->d_err);
+  dfree(s->d_part);
+  dfree(s->d_emf);
+  dfree(s->stage);
+  if (s->h_pinned) cudaFreeHost(s->h_pinned);
+  if (s->h_inj) cudaFreeHost(s->h_inj);
+  for (auto e : s->ev_pool) cudaEventDestroy(e);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->inj_done) cudaEventDestroy(s->inj_done);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+  return ZC_OK;
+}
+
+zc_status zc_species_create(zc_sim *s, const zc_species_desc *d, const zc_part *parts, int np, int *id) {
+  if (!s || !d) return fail(ZC_EINVAL, "null argument");
+  if (np < 0 || (np > 0 && !parts)) return fail(ZC_EINVAL, "invalid particle buffer");
+  if (d->m_q == 0.0f) return fail(ZC_EINVAL, "m_q must be non-zero");
+  DeviceGuard g(s->device);
+  s->sp.emplace_back();
+  const int k = (int)s->sp.size() - 1;
+  SpeciesState &p = s->sp[k];
+  p.m_q = d->m_q;
+  p.q = d->q;
+  p.ppc[0] = std::max(1, d->ppc[0]);
+  p.ppc[1] = std::max(1, d->ppc[1]);
+  p.iter = s->iter;
+  p.n_move = s->n_move;
+  const int nt = s->ntiles;
+  TRY(dalloc(&p.d_off, nt));
+  TRY(dalloc(&p.d_cap, nt));
+  TRY(dalloc(&p.d_np, nt));
+  TRY(dalloc(&p.d_nstay, nt));
+  CK(cudaMemsetAsync(p.d_np, 0, sizeof(int) * nt, s->st));
+  CK(cudaMemsetAsync(p.d_off, 0, sizeof(int) * nt, s->st));
+  CK(cudaMemsetAsync(p.d_cap, 0, sizeof(int) * nt, s->st));
+  TRY(dalloc(&p.d_spill_cnt, 2));
+  CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), s->st));
+  p.spill_cap = std::max(65536, (int)std::min<long long>((long long)np / 32, 1 << 26));
+  TRY(alloc_particles(p.spill[0], p.spill_cap));
+  TRY(alloc_particles(p.spill[1], p.spill_cap));
+  TRY(dalloc(&p.d_ekin_tile, nt));
+  TRY(dalloc(&p.d_ekin_extra, 1));
+  TRY(dalloc(&p.d_ekin, 1));
+  CK(cudaMemsetAsync(p.d_ekin, 0, sizeof(double), s->st));
+  CK(cudaMemsetAsync(p.d_ekin_extra, 0, sizeof(double), s->st));
+  TRY(zc_species_set_particles(s, k, parts, np));
+  if (id) *id = k;
+  return ZC_OK;
+}
+
+zc_status zc_species_set_particles(zc_sim *s, int k, const zc_part *parts, int np) {
+  TRY(check_species(s, k));
+  if (np < 0 || (np > 0 && !parts)) return fail(ZC_EINVAL, "invalid particle buffer");
+  DeviceGuard g(s->device);
+  SpeciesState &p = s->sp[k];
+  CK(cudaMemsetAsync(p.d_np, 0, sizeof(int) * s->ntiles, s->st));
+  CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), s->st));
+  Particles list{};
+  TRY(upload_list(s, parts, np, list, nullptr));
+  zc_status r = relayout(s, k, &list, np);
+  free_particles(list);
+  if (r != ZC_OK) return r;
+  return check_errors(s, false);
+}
+
+zc_status zc_species_inject(zc_sim *s, int k, const zc_part *parts, int np) {
+  TRY(check_species(s, k));
+  if (np <= 0) return ZC_OK;
+  if (!parts) return fail(ZC_EINVAL, "null particle buffer");
+  DeviceGuard g(s->device);
+  SpeciesState &p = s->sp[k];
+  Particles list{};
+  TRY(upload_list(s, parts, np, list, nullptr));
+  CK(launch_append_list(list, np, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur), layout(s), s->d_err,
+                        s->st));
+  CK(cudaStreamSynchronize(s->st));
+  free_particles(list);
+  return check_errors(s, true);
+}
+
+zc_status zc_species_count(zc_sim *s, int k, int *np) {
+  TRY(check_species(s, k));
+  if (!np) return fail(ZC_EINVAL, "null argument");
+  DeviceGuard g(s->device);
+  SpeciesState &p = s->sp[k];
+  std::vector<int> c(s->ntiles);
+  int sc = 0;
+  CK(cudaMemcpyAsync(c.data(), p.d_np, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(&sc, p.d_spill_cnt + p.spill_cur, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  long long tot = std::min(sc, p.spill_cap);
+  for (int v : c) tot += v;
+  *np = (int)tot;
+  return ZC_OK;
+}
+
+zc_status zc_species_get_particles(zc_sim *s, int k, zc_part *out, int cap, int *np) {
+  TRY(check_species(s, k));
+  DeviceGuard g(s->device);
+  SpeciesState &p = s->sp[k];
+  std::vector<int> c(s->ntiles);
+  int sc = 0;
+  CK(cudaMemcpyAsync(c.data(), p.d_np, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(&sc, p.d_spill_cnt + p.spill_cur, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  sc = std::min(sc, p.spill_cap);
+  std::vector<long long> doff(s->ntiles);
+  long long tot = 0;
+  for (int t = 0; t < s->ntiles; ++t) {
+    doff[t] = tot;
+    tot += c[t];
+  }
+  const long long n = tot + sc;
+  if (np) *np = (int)n;
+  if (!out) return ZC_OK;
+  if (cap < n) return fail(ZC_EINVAL, "output buffer holds %d particles, %lld needed", cap, n);
+  if (n == 0) return ZC_OK;
+  long long *d_doff = nullptr;
+  int *d_aos = nullptr;
+  TRY(dalloc(&d_doff, s->ntiles));
+  TRY(dalloc(&d_aos, 7 * n));
+  CK(cudaMemcpyAsync(d_doff, doff.data(), sizeof(long long) * s->ntiles, cudaMemcpyHostToDevice, s->st));
+  CK(launch_gather_aos(p.buf[p.cur], p.d_off, p.d_np, d_doff, d_aos, s->ntiles, s->st));
+  CK(launch_list_to_aos(p.spill[p.spill_cur], p.d_spill_cnt + p.spill_cur, p.spill_cap, d_aos, tot, s->st));
+  CK(cudaMemcpyAsync(out, d_aos, sizeof(zc_part) * (size_t)n, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  dfree(d_doff);
+  dfree(d_aos);
+  return ZC_OK;
+}
+
+zc_status zc_set_injector(zc_sim *s, zc_inject_fn fn, void *user) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  s->inj = fn;
+  s->inj_user = user;
+  return ZC_OK;
+}
+
+zc_status zc_set_smooth(zc_sim *s, int xtype, int xlevel, int ytype, int ylevel) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (xtype < 0 || xtype > 2 || ytype < 0 || ytype > 2) return fail(ZC_EINVAL, "invalid smoothing type");
+  // em2d/simulation.c:136-144
+  if (xtype != 0 && xlevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along x direction");
+  if (ytype != 0 && ylevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along y direction");
+  s->xtype = xtype;
+  s->xlevel = xlevel;
+  s->ytype = ytype;
+  s->ylevel = ylevel;
+  return ZC_OK;
+}
+
+zc_status zc_set_moving_window(zc_sim *s) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  s->mw = 1;
+  return ZC_OK;
+}
+
+zc_status zc_add_laser(zc_sim *s, const zc_laser *in) {
+  if (!s || !in) return fail(ZC_EINVAL, "null argument");
+  zc_laser L = *in;
+  // parameter checks, em2d/emf.c:245-270
+  if (L.fwhm != 0) {
+    if (L.fwhm <= 0) return fail(ZC_EINVAL, "Invalid laser FWHM, must be > 0");
+    L.rise = L.fwhm;
+    L.fall = L.fwhm;
+    L.flat = 0.;
+  }
+  if (L.rise <= 0) return fail(ZC_EINVAL, "Invalid laser RISE, must be > 0");
+  if (L.flat < 0) return fail(ZC_EINVAL, "Invalid laser FLAT, must be >= 0");
+  if (L.fall <= 0) return fail(ZC_EINVAL, "Invalid laser FALL, must be > 0");
+  if (L.type != 0 && L.type != 1) return ZC_OK;  // unknown pulse kinds add nothing (emf.c:341-343)
+  DeviceGuard g(s->device);
+  LaserConst c;
+  c.type = L.type;
+  c.start = L.start;
+  c.rise = L.rise;
+  c.flat = L.flat;
+  c.fall = L.fall;
+  c.a0 = L.a0;
+  c.omega0 = L.omega0;
+  c.polarization = L.polarization;
+  c.W0 = L.W0;
+  c.focus = L.focus;
+  c.axis = L.axis;
+  c.dx = s->dx[0];
+  c.dy = s->dx[1];
+  CK(launch_laser(s->EB[s->eb_cur], s->G, c, s->st));
+  CK(launch_emf_gc(s->EB[s->eb_cur], s->G, s->mw, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status zc_set_ext_fld(zc_sim *s, int Et, const float E0[3], const float *Eg, int Bt, const float B0[3],
+                         const float *Bg) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (Et < 0 || Et > 2 || Bt < 0 || Bt > 2) return fail(ZC_EINVAL, "Invalid external field type");
+  if ((Et == 1 && !E0) || (Bt == 1 && !B0) || (Et == 2 && !Eg) || (Bt == 2 && !Bg))
+    return fail(ZC_EINVAL, "missing external field values");
+  DeviceGuard g(s->device);
+  s->ext_Et = Et;
+  s->ext_Bt = Bt;
+  if (E0) s->ext_E0 = make_float3(E0[0], E0[1], E0[2]);
+  if (B0) s->ext_B0 = make_float3(B0[0], B0[1], B0[2]);
+  if (Et == 2) {
+    if (!s->extE) TRY(dalloc(&s->extE, 3 * s->G.plane));
+    TRY(grid_up(s, Eg, s->extE));
+  }
+  if (Bt == 2) {
+    if (!s->extB) TRY(dalloc(&s->extB, 3 * s->G.plane));
+    TRY(grid_up(s, Bg, s->extB));
+  }
+  if (Et == 0 && Bt == 0) {
+    dfree(s->EBp);
+    return ZC_OK;
+  }
+  if (!s->EBp) {
+    TRY(dalloc(&s->EBp, 6 * s->G.plane));
+    CK(cudaMemsetAsync(s->EBp, 0, sizeof(float) * 6 * s->G.plane, s->st));
+    const int BW = (s->TX + 6) & ~3, BH = s->TY + 3;
+    TRY(make_map(&s->tmK_EBp, s->EBp, s->G, 6, BW, BH));
+  }
+  TRY(refresh_particle_fields(s));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status zc_step(zc_sim *s, int nsteps) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (nsteps < 0) return fail(ZC_EINVAL, "nsteps must be >= 0");
+  DeviceGuard g(s->device);
+  CK(cudaEventRecord(s->ev0, s->st));
+  for (int n = 0; n < nsteps; ++n) {
+    TRY(iter_impl(s));
+    // spill lists are drained into the tiles at least every 16 steps
+    if ((n & 15) == 15 && n + 1 < nsteps) {
+      CK(cudaMemcpyAsync(s->h_pinned, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+      CK(cudaStreamSynchronize(s->st));
+      collect_profile(s);
+      if (s->h_pinned[0] & ERR_SPILLED) TRY(check_errors(s, true));
+    }
+  }
+  CK(cudaEventRecord(s->ev1, s->st));
+  CK(cudaEventSynchronize(s->ev1));
+  cudaEventElapsedTime(&s->last_ms, s->ev0, s->ev1);
+  collect_profile(s);
+  return check_errors(s, true);
+}
+
+zc_status zc_current_zero(zc_sim *s) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  TRY(current_zero_impl(s));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status zc_spec_advance(zc_sim *s, int k) {
+  TRY(check_species(s, k));
+  DeviceGuard g(s->device);
+  CK(cudaEventRecord(s->ev0, s->st));
+  TRY(spec_advance_impl(s, k));
+  CK(cudaEventRecord(s->ev1, s->st));
+  CK(cudaEventSynchronize(s->ev1));
+  cudaEventElapsedTime(&s->last_ms, s->ev0, s->ev1);
+  collect_profile(s);
+  return check_errors(s, true);
+}
+
+zc_status zc_current_update(zc_sim *s) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  TRY(current_update_impl(s));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status zc_emf_advance(zc_sim *s) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  TRY(emf_advance_impl(s));
+  CK(cudaStreamSynchronize(s->st));
+  return check_errors(s, false);
+}
+
+zc_status zc_set_fields(zc_sim *s, const float *E, const float *B) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  if (E) TRY(grid_up(s, E, s->EB[s->eb_cur]));
+  if (B) TRY(grid_up(s, B, s->EB[s->eb_cur] + 3 * s->G.plane));
+  TRY(refresh_particle_fields(s));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status zc_get_fields(zc_sim *s, float *E, float *B) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  if (E) TRY(grid_down(s, s->EB[s->eb_cur], E));
+  if (B) TRY(grid_down(s, s->EB[s->eb_cur] + 3 * s->G.plane, B));
+  return ZC_OK;
+}
+
+zc_status zc_get_particle_fields(zc_sim *s, float *E, float *B) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  const float *src = s->EBp ? s->EBp : s->EB[s->eb_cur];
+  if (E) TRY(grid_down(s, src, E));
+  if (B) TRY(grid_down(s, src + 3 * s->G.plane, B));
+  return ZC_OK;
+}
+
+zc_status zc_get_current(zc_sim *s, float *J) {
+  if (!s || !J) return fail(ZC_EINVAL, "null argument");
+  DeviceGuard g(s->device);
+  return grid_down(s, s->J[s->j_cur], J);
+}
+
+zc_status zc_set_current(zc_sim *s, const float *J) {
+  if (!s || !J) return fail(ZC_EINVAL, "null argument");
+  DeviceGuard g(s->device);
+  TRY(grid_up(s, J, s->J[0]));
+  s->j_cur = 0;
+  return ZC_OK;
+}
+
+zc_status zc_energy(zc_sim *s, double emf[6], double *kin) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  if (emf) {
+    CK(launch_emf_energy(s->EB[s->eb_cur], s->G, s->d_part, s->energy_blocks, s->d_emf, s->dx[0], s->dx[1], s->st));
+    CK(cudaMemcpyAsync(emf, s->d_emf, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  }
+  if (kin)
+    for (size_t k = 0; k < s->sp.size(); ++k)
+      CK(cudaMemcpyAsync(kin + k, s->sp[k].d_ekin, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status zc_species_charge(zc_sim *s, int k, float *charge) {
+  TRY(check_species(s, k));
+  if (!charge) return fail(ZC_EINVAL, "null argument");
+  DeviceGuard g(s->device);
+  SpeciesState &p = s->sp[k];
+  const size_t n = (size_t)(s->nx + 1) * (s->ny + 1);
+  float *d = nullptr;
+  TRY(dalloc(&d, n));
+  CK(cudaMemcpyAsync(d, charge, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
+  CK(launch_charge(p.buf[p.cur], p.d_off, p.d_np, s->ntiles, p.spill[p.spill_cur], p.d_spill_cnt + p.spill_cur,
+                   p.spill_cap, d, s->nx, s->ny, p.q, s->mw, s->st));
+  CK(cudaMemcpyAsync(charge, d, n * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  dfree(d);
+  return ZC_OK;
+}
+
+zc_status zc_get_info(zc_sim *s, zc_info *info) {
+  if (!s || !info) return fail(ZC_EINVAL, "null argument");
+  info->iter = s->iter;
+  info->n_move = s->n_move;
+  info->moving_window = s->mw;
+  info->n_species = (int)s->sp.size();
+  info->nx[0] = s->nx;
+  info->nx[1] = s->ny;
+  info->tile[0] = s->TX;
+  info->tile[1] = s->TY;
+  info->ntiles[0] = s->ntx;
+  info->ntiles[1] = s->nty;
+  return ZC_OK;
+}
+
+zc_status zc_grid_view_get(zc_sim *s, zc_grid_view *v) {
+  if (!s || !v) return fail(ZC_EINVAL, "null argument");
+  v->E = s->EB[s->eb_cur];
+  v->B = s->EB[s->eb_cur] + 3 * s->G.plane;
+  v->J = s->J[s->j_cur];
+  v->plane = s->G.plane;
+  v->pitch = s->G.pitch;
+  v->rows = s->G.rows;
+  v->stream = (void *)s->st;
+  return ZC_OK;
+}
+
+zc_status zc_synchronize(zc_sim *s) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  collect_profile(s);
+  return check_errors(s, true);
+}
+
+zc_status zc_set_profiling(zc_sim *s, int on) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  collect_profile(s);
+  s->profiling = on ? 1 : 0;
+  return ZC_OK;
+}
+
+zc_status zc_get_profile(zc_sim *s, double ms[ZC_NPHASE], long long launches[ZC_NPHASE]) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  collect_profile(s);
+  for (int k = 0; k < ZC_NPHASE; ++k) {
+    if (ms) ms[k] = s->prof_ms[k];
+    if (launches) launches[k] = s->prof_launch[k];
+  }
+  return ZC_OK;
+}
+
+zc_status zc_reset_profile(zc_sim *s) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  collect_profile(s);
+  for (int k = 0; k < ZC_NPHASE; ++k) {
+    s->prof_ms[k] = 0;
+    s->prof_launch[k] = 0;
+  }
+  return ZC_OK;
+}
+
+const char *zc_phase_name(int p) {
+  static const char *names[ZC_NPHASE] = {"push", "spill", "migrate", "kin_energy", "zero", "fold",
+                                         "smooth", "yee", "emf_gc", "ext", "window"};
+  return (p >= 0 && p < ZC_NPHASE) ? names[p] : "unknown";
+}
+
+zc_status zc_last_step_ms(zc_sim *s, float *ms) {
+  if (!s || !ms) return fail(ZC_EINVAL, "null argument");
+  *ms = s->last_ms;
+  return ZC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,425 @@
+// zc_fields.cu -- grid kernels of libzpic_cuda (sm_103a): current guard-cell
+// fold and digital filtering, the fused Yee field advance, field guard
+// cells, external fields, moving window, laser launch and FP64 energies.
+//
+// Compiled with -fmad=false: every cell is computed with the same float32
+// operations, in the same order, as the reference (em2d/current.c,
+// em2d/emf.c), so from the same inputs these kernels return the same bits.
+// All of them are HBM-bound stencils; none is a contraction.
+#include <math.h>
+
+#include "zc_internal.cuh"
+#include "zc_kernels.h"
+
+namespace zc {
+
+__device__ __forceinline__ size_t gidx(const Grid &G, int c, int bx, int by) {
+  return c * G.plane + (size_t)by * G.pitch + bx;
+}
+
+// ---------------------------------------------------------------------------
+// layout conversion: reference float3 AoS buffers <-> SoA planes
+// ---------------------------------------------------------------------------
+__global__ void k_aos_to_planes(const float *aos, float *planes, Grid G, int ncomp) {
+  const int gx = G.nx + 3, gy = G.ny + 3;
+  const int n = gx * gy;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int bx = k % gx, by = k / gx;
+    for (int c = 0; c < ncomp; ++c) planes[gidx(G, c, bx, by)] = aos[(size_t)k * ncomp + c];
+  }
+}
+
+__global__ void k_planes_to_aos(const float *planes, float *aos, Grid G, int ncomp) {
+  const int gx = G.nx + 3, gy = G.ny + 3;
+  const int n = gx * gy;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int bx = k % gx, by = k / gx;
+    for (int c = 0; c < ncomp; ++c) aos[(size_t)k * ncomp + c] = planes[gidx(G, c, bx, by)];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// current guard-cell fold (current_update_gc, em2d/current.c:118-159)
+// ---------------------------------------------------------------------------
+__global__ void k_fold_x(float *J, Grid G) {
+  const int by = blockIdx.x * blockDim.x + threadIdx.x;  // every buffer row
+  if (by >= G.ny + 3) return;
+  for (int c = 0; c < 3; ++c)
+    for (int b = 0; b < 3; ++b) {  // cells -1, 0, 1 receive nx-1, nx, nx+1
+      const size_t lo = gidx(G, c, b, by), hi = gidx(G, c, G.nx + b, by);
+      const float v = J[lo] + J[hi];
+      J[lo] = v;
+      J[hi] = v;
+    }
+}
+
+__global__ void k_fold_y(float *J, Grid G) {
+  const int bx = blockIdx.x * blockDim.x + threadIdx.x;  // every buffer column
+  if (bx >= G.nx + 3) return;
+  for (int c = 0; c < 3; ++c)
+    for (int b = 0; b < 3; ++b) {
+      const size_t lo = gidx(G, c, bx, b), hi = gidx(G, c, bx, G.ny + b);
+      const float v = J[lo] + J[hi];
+      J[lo] = v;
+      J[hi] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// one [sa, sb, sa] filter pass, out of place (kernel_x / kernel_y,
+// em2d/current.c:316-413).  Every buffer cell is written: the filtered
+// interior, the guard cells the reference refreshes, and untouched copies.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float f3pt(float sa, float sb, float l, float m, float u) {
+  return sa * l + sb * m + sa * u;
+}
+
+__global__ void k_smooth_x(const float *Jin, float *Jout, Grid G, float sa, float sb, int mw) {
+  const int gx = G.nx + 3, gy = G.ny + 3;
+  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int by = blockIdx.y;
+  if (bx >= gx || by >= gy) return;
+  const int i = bx - 1, j = by - 1;
+  int src = -1;  // interior column whose filtered value lands here
+  if (j >= 0 && j < G.ny) {
+    if (i >= 0 && i < G.nx) src = bx;
+    else if (!mw) src = (i < 0) ? G.nx : bx - G.nx;  // -1 <- nx-1, nx <- 0, nx+1 <- 1
+  }
+  for (int c = 0; c < 3; ++c) {
+    float v;
+    if (src >= 0) {
+      const size_t s = gidx(G, c, src, by);
+      v = f3pt(sa, sb, Jin[s - 1], Jin[s], Jin[s + 1]);
+    } else {
+      v = Jin[gidx(G, c, bx, by)];
+    }
+    Jout[gidx(G, c, bx, by)] = v;
+  }
+}
+
+__global__ void k_smooth_y(const float *Jin, float *Jout, Grid G, float sa, float sb) {
+  const int gx = G.nx + 3, gy = G.ny + 3;
+  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int by = blockIdx.y;
+  if (bx >= gx || by >= gy) return;
+  const int i = bx - 1, j = by - 1;
+  // the row whose (new) value this cell holds after the y guard refresh
+  const int srow = (j >= 0 && j < G.ny) ? by : ((j < 0) ? G.ny : by - G.ny);
+  const bool filt = (i >= 0 && i < G.nx);  // only interior columns are filtered
+  for (int c = 0; c < 3; ++c) {
+    const size_t s = gidx(G, c, bx, srow);
+    const float v = filt ? f3pt(sa, sb, Jin[s - G.pitch], Jin[s], Jin[s + G.pitch]) : Jin[s];
+    Jout[gidx(G, c, bx, by)] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fused Yee advance: B half step, E full step, B half step
+// (yee_b / yee_e, em2d/emf.c:500-562), one 32 x 16 output tile per CTA.
+// E/B and J tiles with their halo arrive by TMA; B1 and E1 live in shared
+// memory only; the reference's update ranges (B: cells -1..nx, E: 0..nx+1,
+// in buffer coordinates 0..nx+1 and 1..nx+2) are kept exactly so that the
+// guard cells evolve as in the reference (they matter with a moving window).
+// Out of place: EB in (TMA) -> EB out.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_yee(const __grid_constant__ CUtensorMap tm_eb,
+                                             const __grid_constant__ CUtensorMap tm_j, float *EBout, Grid G,
+                                             YeeConst Y, int *err) {
+  constexpr int BW = kYeeBW, BH = kYeeBH, PL = BW * BH;
+  __shared__ __align__(128) float sEB[6 * PL];
+  __shared__ __align__(128) float sJ[3 * PL];
+  __shared__ __align__(8) uint64_t bar;
+  const int bx0 = blockIdx.x * kYeeOX, by0 = blockIdx.y * kYeeOY;
+  const int ox = bx0 - 4, oy = by0 - 1;  // buffer coords of smem (0,0)
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&bar, (6 + 3) * PL * 4);
+    tma_load_3d(sEB, &tm_eb, ox, oy, 0, &bar);
+    tma_load_3d(sJ, &tm_j, ox, oy, 0, &bar);
+  }
+  if (!mbar_wait_bounded(&bar, 0)) {
+    if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
+    if (!mbar_wait_bounded(&bar, 0)) return;  // second bounded wait for the copies in flight
+  }
+
+  float *Ex = sEB, *Ey = sEB + PL, *Ez = sEB + 2 * PL;
+  float *Bx = sEB + 3 * PL, *By = sEB + 4 * PL, *Bz = sEB + 5 * PL;
+  const float *Jx = sJ, *Jy = sJ + PL, *Jz = sJ + 2 * PL;
+  const int nx = G.nx, ny = G.ny;
+
+  // B1 on buffer cells [bx0-1, bx0+OX] x [by0-1, by0+OY]
+  {
+    constexpr int W = kYeeOX + 2, H = kYeeOY + 2;
+    for (int k = threadIdx.x; k < W * H; k += blockDim.x) {
+      const int bx = bx0 - 1 + k % W, by = by0 - 1 + k / W;
+      if (bx < 0 || bx > nx + 1 || by < 0 || by > ny + 1) continue;
+      const int s = (by - oy) * BW + (bx - ox);
+      Bx[s] += (-Y.cyb * (Ez[s + BW] - Ez[s]));
+      By[s] += (Y.cxb * (Ez[s + 1] - Ez[s]));
+      Bz[s] += (-Y.cxb * (Ey[s + 1] - Ey[s]) + Y.cyb * (Ex[s + BW] - Ex[s]));
+    }
+  }
+  __syncthreads();
+  // E1 on buffer cells [bx0, bx0+OX] x [by0, by0+OY]
+  {
+    constexpr int W = kYeeOX + 1, H = kYeeOY + 1;
+    for (int k = threadIdx.x; k < W * H; k += blockDim.x) {
+      const int bx = bx0 + k % W, by = by0 + k / W;
+      if (bx < 1 || bx > nx + 2 || by < 1 || by > ny + 2) continue;
+      const int s = (by - oy) * BW + (bx - ox);
+      Ex[s] += (+Y.cye * (Bz[s] - Bz[s - BW])) - Y.dt * Jx[s];
+      Ey[s] += (-Y.cxe * (Bz[s] - Bz[s - 1])) - Y.dt * Jy[s];
+      Ez[s] += (+Y.cxe * (By[s] - By[s - 1]) - Y.cye * (Bx[s] - Bx[s - BW])) - Y.dt * Jz[s];
+    }
+  }
+  __syncthreads();
+  // B2 on the output tile, then store E1 and B2
+  for (int k = threadIdx.x; k < kYeeOX * kYeeOY; k += blockDim.x) {
+    const int bx = bx0 + k % kYeeOX, by = by0 + k / kYeeOX;
+    if (bx >= nx + 3 || by >= ny + 3) continue;
+    const int s = (by - oy) * BW + (bx - ox);
+    float bxv = Bx[s], byv = By[s], bzv = Bz[s];
+    if (bx <= nx + 1 && by <= ny + 1) {
+      bxv += (-Y.cyb * (Ez[s + BW] - Ez[s]));
+      byv += (Y.cxb * (Ez[s + 1] - Ez[s]));
+      bzv += (-Y.cxb * (Ey[s + 1] - Ey[s]) + Y.cyb * (Ex[s + BW] - Ex[s]));
+    }
+    EBout[gidx(G, 0, bx, by)] = Ex[s];
+    EBout[gidx(G, 1, bx, by)] = Ey[s];
+    EBout[gidx(G, 2, bx, by)] = Ez[s];
+    EBout[gidx(G, 3, bx, by)] = bxv;
+    EBout[gidx(G, 4, bx, by)] = byv;
+    EBout[gidx(G, 5, bx, by)] = bzv;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// periodic guard cells of E and B (emf_update_gc, em2d/emf.c:573-637): x
+// unless the window moves, y always.  Guards only read interior rows.
+// ---------------------------------------------------------------------------
+__global__ void k_emf_gc(float *EB, Grid G, int mw) {
+  const int gx = G.nx + 3, gy = G.ny + 3;
+  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int by = blockIdx.y;
+  if (bx >= gx || by >= gy) return;
+  const bool gxg = (bx == 0 || bx > G.nx), gyg = (by == 0 || by > G.ny);
+  if (!gxg && !gyg) return;
+  int sx = bx, sy = by;
+  if (gxg && !mw) sx = (bx == 0) ? G.nx : bx - G.nx;
+  if (gyg) sy = (by == 0) ? G.ny : by - G.ny;
+  if (sx == bx && sy == by) return;
+  for (int c = 0; c < 6; ++c) EB[gidx(G, c, bx, by)] = EB[gidx(G, c, sx, sy)];
+}
+
+// E_part = E + external, B_part = B + external (emf_update_part_fld,
+// em2d/emf.c:838-914); type 0 copies, 1 uniform, 2 grid
+__global__ void k_ext_add(const float *EB, float *EBp, const float *extE, const float *extB, int Et, int Bt,
+                          float3 E0, float3 B0, Grid G) {
+  const int gx = G.nx + 3, gy = G.ny + 3;
+  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int by = blockIdx.y;
+  if (bx >= gx || by >= gy) return;
+  const float e0[3] = {E0.x, E0.y, E0.z}, b0[3] = {B0.x, B0.y, B0.z};
+  for (int c = 0; c < 6; ++c) {
+    const int t = (c < 3) ? Et : Bt;
+    const size_t k = gidx(G, c, bx, by);
+    float v = EB[k];
+    if (t == 1) v += (c < 3) ? e0[c] : b0[c - 3];
+    else if (t == 2) v += (c < 3) ? extE[gidx(G, c, bx, by)] : extB[gidx(G, c - 3, bx, by)];
+    EBp[k] = v;
+  }
+}
+
+// moving window: fields shift left one cell, right-most columns zeroed
+// (emf_move_window, em2d/emf.c:648-675); out of place
+__global__ void k_window_shift(const float *EBin, float *EBout, Grid G) {
+  const int gx = G.nx + 3, gy = G.ny + 3;
+  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int by = blockIdx.y;
+  if (bx >= gx || by >= gy) return;
+  for (int c = 0; c < 6; ++c)
+    EBout[gidx(G, c, bx, by)] = (bx < G.nx) ? EBin[gidx(G, c, bx + 1, by)] : 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// field energy per component (emf_get_energy, em2d/emf.c:729-750): float
+// squares as in the reference, Kahan-compensated per thread, FP64 across
+// threads and blocks, partials summed in a fixed order
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_emf_energy_partial(const float *EB, Grid G, double *partial) {
+  __shared__ double sred[8];
+  float s[6] = {0, 0, 0, 0, 0, 0}, cc[6] = {0, 0, 0, 0, 0, 0};
+  const int n = G.nx * G.ny;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int bx = k % G.nx + 1, by = k / G.nx + 1;
+    for (int c = 0; c < 6; ++c) {
+      const float f = EB[gidx(G, c, bx, by)];
+      const float y = f * f - cc[c];
+      const float t = s[c] + y;
+      cc[c] = (t - s[c]) - y;
+      s[c] = t;
+    }
+  }
+  for (int c = 0; c < 6; ++c) {
+    const double v = block_sum_double<256>((double)s[c] - (double)cc[c], sred);
+    if (threadIdx.x == 0) partial[blockIdx.x * 6 + c] = v;
+  }
+}
+
+__global__ void k_emf_energy_final(const double *partial, int nblocks, double *out, float dx, float dy) {
+  if (threadIdx.x < 6) {
+    double s = 0;
+    for (int b = 0; b < nblocks; ++b) s += partial[b * 6 + threadIdx.x];
+    out[threadIdx.x] = s * (0.5 * dx * dy);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// laser launch (emf_add_laser, em2d/emf.c:158-350): same double-precision
+// library calls on float arguments as the reference
+// ---------------------------------------------------------------------------
+__device__ float laser_env(const LaserConst &L, float z) {
+  const double half_pi = 1.57079632679489661923132169163975144;
+  if (z > L.start) return 0.0f;
+  if (z > L.start - L.rise) {
+    float u = z - L.start;
+    float e = sin(half_pi * u / L.rise);
+    return e * e;
+  }
+  if (z > L.start - (L.rise + L.flat)) return 1.0f;
+  if (z > L.start - (L.rise + L.flat + L.fall)) {
+    float u = z - (L.start - L.rise - L.flat - L.fall);
+    float e = sin(half_pi * u / L.fall);
+    return e * e;
+  }
+  return 0.0f;
+}
+
+__device__ float laser_gauss(const LaserConst &L, float zpos, float r) {
+  float z = zpos - L.focus;
+  float zr = L.omega0 * (L.W0 * L.W0) / 2;
+  float r2 = r * r;
+  float curv = r2 * z / (zr * zr + z * z);
+  float w2r = (zr * zr) / (zr * zr + z * z);
+  float gouy = atan2((double)z, (double)zr);
+  return sqrt(sqrt((double)w2r)) * exp((double)(-r2 * w2r / (L.W0 * L.W0))) *
+         cos((double)(L.omega0 * (z + curv) - gouy));
+}
+
+__global__ void k_laser_fields(float *EB, Grid G, LaserConst L) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= G.nx || j >= G.ny) return;
+  const float amp = L.omega0 * L.a0;
+  const float cp = cos((double)L.polarization), sp = sin((double)L.polarization);
+  const float z = i * L.dx, z2 = z + L.dx / 2;
+  const float a = amp * laser_env(L, z), a2 = amp * laser_env(L, z2);
+  const int bx = i + 1, by = j + 1;
+  float *Ey = &EB[gidx(G, 1, bx, by)], *Ez = &EB[gidx(G, 2, bx, by)];
+  float *By = &EB[gidx(G, 4, bx, by)], *Bz = &EB[gidx(G, 5, bx, by)];
+  if (L.type == 0) {
+    const float k = L.omega0;
+    *Ey += +a * cos((double)(k * z)) * cp;
+    *Ez += +a * cos((double)(k * z)) * sp;
+    *By += -a2 * cos((double)(k * z2)) * sp;
+    *Bz += +a2 * cos((double)(k * z2)) * cp;
+  } else {
+    const float r = j * L.dy - L.axis, r2 = r + L.dy / 2;
+    *Ey += +a * laser_gauss(L, z, r2) * cp;
+    *Ez += +a * laser_gauss(L, z, r) * sp;
+    *By += -a2 * laser_gauss(L, z2, r) * sp;
+    *Bz += +a2 * laser_gauss(L, z2, r2) * cp;
+  }
+}
+
+// div E = div B = 0 through Ex and Bx, integrated from the right in double,
+// one row per thread in the reference's order (div_corr_x, emf.c:213-231)
+__global__ void k_laser_divcorr(float *EB, Grid G, float dx, float dy) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= G.ny) return;
+  const double rxy = dx / dy;
+  double ex = 0.0, bx = 0.0;
+  const int by = j + 1;
+  for (int i = G.nx - 1; i >= 0; --i) {
+    const int b = i + 1;
+    ex += rxy * (EB[gidx(G, 1, b + 1, by)] - EB[gidx(G, 1, b + 1, by - 1)]);
+    EB[gidx(G, 0, b, by)] = ex;
+    bx += rxy * (EB[gidx(G, 4, b, by + 1)] - EB[gidx(G, 4, b, by)]);
+    EB[gidx(G, 3, b, by)] = bx;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline dim3 grid_rows(const Grid &G, int bs) { return dim3((G.nx + 3 + bs - 1) / bs, G.ny + 3); }
+
+cudaError_t launch_aos_to_planes(const float *aos, float *planes, const Grid &G, int ncomp, cudaStream_t st) {
+  k_aos_to_planes<<<1024, 256, 0, st>>>(aos, planes, G, ncomp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_planes_to_aos(const float *planes, float *aos, const Grid &G, int ncomp, cudaStream_t st) {
+  k_planes_to_aos<<<1024, 256, 0, st>>>(planes, aos, G, ncomp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
+  if (!mw) k_fold_x<<<(G.ny + 3 + 127) / 128, 128, 0, st>>>(J, G);
+  k_fold_y<<<(G.nx + 3 + 127) / 128, 128, 0, st>>>(J, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth_x(const float *Jin, float *Jout, const Grid &G, float sa, float sb, int mw,
+                            cudaStream_t st) {
+  k_smooth_x<<<grid_rows(G, 256), 256, 0, st>>>(Jin, Jout, G, sa, sb, mw);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth_y(const float *Jin, float *Jout, const Grid &G, float sa, float sb, cudaStream_t st) {
+  k_smooth_y<<<grid_rows(G, 256), 256, 0, st>>>(Jin, Jout, G, sa, sb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
+                       const YeeConst &Y, int *err, cudaStream_t st) {
+  dim3 grid((G.nx + 3 + kYeeOX - 1) / kYeeOX, (G.ny + 3 + kYeeOY - 1) / kYeeOY);
+  k_yee<<<grid, 256, 0, st>>>(*tm_eb, *tm_j, EBout, G, Y, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st) {
+  k_emf_gc<<<grid_rows(G, 256), 256, 0, st>>>(EB, G, mw);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ext_add(const float *EB, float *EBp, const float *extE, const float *extB, int Etype, int Btype,
+                           float3 E0, float3 B0, const Grid &G, cudaStream_t st) {
+  k_ext_add<<<grid_rows(G, 256), 256, 0, st>>>(EB, EBp, extE, extB, Etype, Btype, E0, B0, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_window_shift(const float *EBin, float *EBout, const Grid &G, cudaStream_t st) {
+  k_window_shift<<<grid_rows(G, 256), 256, 0, st>>>(EBin, EBout, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, int nblocks, double *out, float dx,
+                              float dy, cudaStream_t st) {
+  k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);
+  k_emf_energy_final<<<1, 32, 0, st>>>(partial, nblocks, out, dx, dy);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_laser(float *EB, const Grid &G, const LaserConst &L, cudaStream_t st) {
+  dim3 grid((G.nx + 127) / 128, G.ny);
+  k_laser_fields<<<grid, 128, 0, st>>>(EB, G, L);
+  if (L.type == 1) k_laser_divcorr<<<(G.ny + 63) / 64, 64, 0, st>>>(EB, G, L.dx, L.dy);
+  return cudaGetLastError();
+}
+
+}  // namespace zc

@@ -1,0 +1,171 @@
+// zc_internal.cuh -- device-side layout and helpers shared by the kernels of
+// libzpic_cuda (GB300, sm_103a).
+//
+// Grid layout in HBM (one allocation per field set):
+//   planes [component][row][column], `pitch` floats per row (a multiple of 32,
+//   so every row starts on a 128-byte boundary and TMA boxes can start on any
+//   multiple of 4 columns), `rows` = ny + 3 rows.
+//   Buffer coordinates: column i+1, row j+1 hold cell (i, j); columns/rows
+//   0, nx+1, nx+2 (resp. ny) are the guard cells of the reference layout
+//   (1 lower, 2 upper; em2d/emf.c:59-89).
+//   E and B share one 6-plane allocation (Ex Ey Ez Bx By Bz) so the particle
+//   kernel stages both with a single 3-D TMA box.
+//
+// Particle layout (one species): structure of arrays ix, iy (int32 cell),
+// x, y (float32 in-cell position in [0,1)), ux, uy, uz (float32 proper
+// velocity) -- the same quantities as t_part (em2d/particles.h:29-37) --
+// partitioned into rectangular tiles of TX x TY cells.  Tile t owns the
+// contiguous segment [off[t], off[t] + cap[t]) of every array and holds np[t]
+// particles at its start.  Two copies (A, B) alternate every step.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace zc {
+
+// error bits accumulated on the device and read back by the host
+enum : int {
+  ERR_TIMEOUT = 1,       // a bounded TMA barrier wait gave up
+  ERR_ESCAPE = 2,        // particle outside its cell/tile (moved > 1 cell)
+  ERR_OVERFLOW = 4,      // spill buffer full: particles lost
+  ERR_SPILLED = 8,       // particles went to the spill buffer (host re-layout due)
+};
+
+struct Particles {       // SoA view of one particle buffer
+  int *ix, *iy;
+  float *x, *y, *ux, *uy, *uz;
+};
+
+struct Grid {            // geometry of the padded SoA grids
+  int nx, ny;            // interior cells
+  int pitch, rows;       // floats per row, rows per plane
+  size_t plane;          // floats per plane (pitch * rows)
+};
+
+// bounded spin limit for mbarrier waits: each try_wait can suspend for a
+// while, so this is many milliseconds at least
+constexpr int kWaitIters = 1 << 20;
+
+// ---------------------------------------------------------------------------
+// PTX wrappers: mbarrier + TMA (cp.async.bulk.tensor) for sm_90+ / sm_103a
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; returns false when the limit ran out
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  for (int it = 0; it < kWaitIters; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// element-wise atomic add of a shared-memory box into global memory
+__device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap *map, const void *src, int x, int y,
+                                                  int z) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group"
+      " [%0, {%2, %3, %4}], [%1];" ::"l"(reinterpret_cast<uint64_t>(map)),
+      "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, const void *src, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group"
+      " [%0, {%2, %3, %4}], [%1];" ::"l"(reinterpret_cast<uint64_t>(map)),
+      "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// block-wide exclusive scan of one int per thread (NT threads, NT % 32 == 0);
+// `swarp` holds NT/32 ints of shared memory; all threads must call it.
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ int block_exclusive_scan(int v, int &total, int *swarp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) swarp[warp] = x;
+  __syncthreads();
+  int before = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < NT / 32; ++w) {
+    int c = swarp[w];
+    before += (w < warp) ? c : 0;
+    tot += c;
+  }
+  __syncthreads();
+  total = tot;
+  return before + x - v;
+}
+
+// block-wide sum of a double, result valid in thread 0; `sred` NT/32 doubles
+template <int NT>
+__device__ __forceinline__ double block_sum_double(double v, double *sred) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) sred[warp] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) s += sred[w];
+  }
+  __syncthreads();
+  return s;
+}
+
+}  // namespace zc

@@ -1,0 +1,114 @@
+// zc_kernels.h -- launch interface between the host runtime (zc_api.cu) and
+// the kernels (zc_particles.cu, zc_fields.cu).
+#pragma once
+
+#include <algorithm>
+
+#include "zc_internal.cuh"
+
+namespace zc {
+
+struct PushConst {
+  float tem, dt_dx, dt_dy, qnx, qny, q;   // particles.c:1111-1117
+  int nx, ny, ntx, nty;
+  int shift;                              // moving-window shift applied this step (0/1)
+  int mw;                                 // absorbing boundaries along x
+};
+
+struct TileSet {
+  const int *off, *cap;
+  int *np, *nstay;
+  int ntiles;
+};
+
+struct Outbox {                           // particles leaving a tile, per tile `cap` slots
+  Particles p;
+  int *dst, *cnt;
+  int cap;
+};
+
+struct Spill {                            // particles without room in a tile
+  Particles p;
+  int *cnt;
+  int cap;
+};
+
+struct LayoutConst {
+  int TX, TY, ntx, nty, nx, ny;
+};
+
+struct PushLaunch {
+  const CUtensorMap *tm_eb, *tm_j;
+  Particles pin, pout;
+  TileSet T;
+  Outbox O;
+  Spill S;
+  double *ekin_tile;
+  int *err;
+  PushConst C;
+  int ntiles, TX, TY;
+};
+
+// particles
+bool tile_supported(int TX, int TY);
+cudaError_t launch_push_tiles(const PushLaunch &a, cudaStream_t st);
+cudaError_t launch_push_spill(const float *EB, float *J, const Grid &G, const Particles &sin, const int *sin_cnt,
+                              int sin_cap, const Spill &S, double *ekin, int *err, const PushConst &C,
+                              int nblocks, cudaStream_t st);
+cudaError_t launch_migrate(const Particles &pout, const TileSet &T, const Outbox &O, const Spill &S, int *err,
+                           int ntx, int nty, int mw, cudaStream_t st);
+cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, int *cnt, const LayoutConst &L,
+                                 int *err, cudaStream_t st);
+cudaError_t launch_count_list(const Particles &list, const int *n_ptr, int n_cap, int *cnt, const LayoutConst &L,
+                              cudaStream_t st);
+cudaError_t launch_copy_tiles(const Particles &src, const int *off_old, const int *np_old, const Particles &dst,
+                              const int *off_new, unsigned *key, int *fill, int ntiles, cudaStream_t st);
+cudaError_t launch_scatter_list(const Particles &list, const int *n_ptr, int n_cap, const Particles &dst,
+                                const int *off, const int *cap, int *fill, unsigned *key, unsigned key0,
+                                const LayoutConst &L, int *err, cudaStream_t st);
+cudaError_t launch_tile_order(const Particles &src, const unsigned *key, const int *off, const int *np,
+                              const Particles &dst, int ntiles, int smax, int stride_p, cudaStream_t st);
+cudaError_t launch_append_list(const Particles &list, int n, const Particles &buf, const TileSet &T,
+                               const Spill &S, const LayoutConst &L, int *err, cudaStream_t st);
+cudaError_t launch_gather_aos(const Particles &buf, const int *off, const int *np, const long long *dst_off,
+                              int *aos, int ntiles, cudaStream_t st);
+cudaError_t launch_list_to_aos(const Particles &list, const int *n_ptr, int n_cap, int *aos, long long d0,
+                               cudaStream_t st);
+cudaError_t launch_charge(const Particles &buf, const int *off, const int *np, int ntiles, const Particles &spill,
+                          const int *spill_cnt, int spill_cap, float *rho, int nx, int ny, float q, int mw,
+                          cudaStream_t st);
+cudaError_t launch_sum_energy(const double *tiles, int ntiles, const double *extra, double *out, float q_mq,
+                              float dx, float dy, cudaStream_t st);
+
+// fields
+struct YeeConst {
+  float cxb, cyb;                         // (dt/2)/dx, (dt/2)/dy  (emf.c:507-508)
+  float cxe, cye, dt;                     // dt/dx, dt/dy, dt      (emf.c:540-541)
+};
+
+cudaError_t launch_aos_to_planes(const float *aos, float *planes, const Grid &G, int ncomp, cudaStream_t st);
+cudaError_t launch_planes_to_aos(const float *planes, float *aos, const Grid &G, int ncomp, cudaStream_t st);
+cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st);
+cudaError_t launch_smooth_x(const float *Jin, float *Jout, const Grid &G, float sa, float sb, int mw,
+                            cudaStream_t st);
+cudaError_t launch_smooth_y(const float *Jin, float *Jout, const Grid &G, float sa, float sb, cudaStream_t st);
+cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
+                       const YeeConst &Y, int *err, cudaStream_t st);
+cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st);
+cudaError_t launch_ext_add(const float *EB, float *EBp, const float *extE, const float *extB, int Etype, int Btype,
+                           float3 E0, float3 B0, const Grid &G, cudaStream_t st);
+cudaError_t launch_window_shift(const float *EBin, float *EBout, const Grid &G, cudaStream_t st);
+cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, int nblocks, double *out, float dx,
+                              float dy, cudaStream_t st);
+struct LaserConst {
+  int type;
+  float start, rise, flat, fall, a0, omega0, polarization, W0, focus, axis;
+  float dx, dy;
+};
+cudaError_t launch_laser(float *EB, const Grid &G, const LaserConst &L, cudaStream_t st);
+
+constexpr int kYeeOX = 32, kYeeOY = 16;   // Yee output tile (buffer cells)
+constexpr int kYeeBW = kYeeOX + 8;        // TMA box: 4 columns of halo each side
+constexpr int kYeeBH = kYeeOY + 3;
+
+}  // namespace zc
