@@ -10,7 +10,8 @@ def ext_grid(fn, nx, ny, dx, dy):
     g = np.zeros((ny + 3, nx + 3, 3), dtype=np.float32)
     for j in range(-1, ny + 2):
         for i in range(-1, nx + 2):
-            g[j + 1, i + 1] = fn(i, np.float32(dx), j, np.float32(dy))
+            # the callback sees the cell sizes as the C float values, in double
+            g[j + 1, i + 1] = fn(i, float(np.float32(dx)), j, float(np.float32(dy)))
     return g
 
 
@@ -63,7 +64,8 @@ def mirror(name, tile=(16, 16), deck=None, cpu=None, injector=None):
     if "ext_fld" in d:
         e = _resolve(d["ext_fld"])
         nx, ny = d["nx"]
-        dx, dy = d["box"][0] / nx, d["box"][1] / ny
+        dx = np.float32(d["box"][0]) / np.float32(nx)
+        dy = np.float32(d["box"][1]) / np.float32(ny)
         kw = {}
         for f in ("E", "B"):
             t = e.get(f + "_type", "none")

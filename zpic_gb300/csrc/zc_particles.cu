@@ -177,11 +177,14 @@ __device__ __forceinline__ void deposit_zigzag(const D &dep, int ix, int iy, int
 }
 
 // gather + Boris + move + deposit for one particle at cell (i, j) of the
-// accessor frame; returns the kinetic-energy term utsq/(gamma+1)
+// accessor frame; returns the kinetic-energy term utsq/(gamma+1).  `bad` is
+// set when the motion breaks the one-cell-per-step assumption of the
+// deposit (|dx| >= 1 cell, or not a number).  A trimmed position of exactly
+// 1.0f (x1 = -tiny, then +1 rounds up) is legal, as in the reference.
 template <class F, class D>
 __device__ __forceinline__ float advance_particle(const F &fld, const D &dep, int i, int j, float &x,
                                                   float &y, float &ux, float &uy, float &uz, int &di,
-                                                  int &dj, const PushConst &C) {
+                                                  int &dj, bool &bad, const PushConst &C) {
   // staggered bilinear gather (particles.c:1029-1071)
   const int ih = i + ((x < 0.5f) ? -1 : 0);
   const int jh = j + ((y < 0.5f) ? -1 : 0);
@@ -225,6 +228,7 @@ __device__ __forceinline__ float advance_particle(const F &fld, const D &dep, in
   const float rg = 1.0f / sqrtf(1.0f + ux * ux + uy * uy + uz * uz);
   const float mx = C.dt_dx * rg * ux;
   const float my = C.dt_dy * rg * uy;
+  bad = !(fabsf(mx) < 1.0f && fabsf(my) < 1.0f);
   float x1 = x + mx, y1 = y + my;
   di = (x1 >= 1.0f) - (x1 < 0.0f);
   dj = (y1 >= 1.0f) - (y1 < 0.0f);
@@ -341,9 +345,10 @@ __global__ void __launch_bounds__(NT) k_push_tiles(const __grid_constant__ CUten
         iy = cy0 + lj;
       }
       int di, dj;
-      const float kin = advance_particle(fld, dep, li, lj, x, y, ux, uy, uz, di, dj, C);
+      bool bad;
+      const float kin = advance_particle(fld, dep, li, lj, x, y, ux, uy, uz, di, dj, bad, C);
       kahan_add(ks, kc, kin);
-      if (!(x >= 0.f && x < 1.f && y >= 0.f && y < 1.f)) errbits |= ERR_ESCAPE;
+      if (bad) errbits |= ERR_ESCAPE;
       if (apply_boundary(ix, iy, di, dj, C)) {
         dest = ix / TX + (iy / TY) * C.ntx;
         code = (dest == t) ? 1 : 2;
@@ -410,7 +415,9 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Gr
       iy = min(max(iy, 0), C.ny - 1);
     }
     int di, dj;
-    const float kin = advance_particle(fld, dep, ix, iy, x, y, ux, uy, uz, di, dj, C);
+    bool bad;
+    const float kin = advance_particle(fld, dep, ix, iy, x, y, ux, uy, uz, di, dj, bad, C);
+    if (bad) errbits |= ERR_ESCAPE;
     kahan_add(ks, kc, kin);
     if (apply_boundary(ix, iy, di, dj, C)) spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
   }
