@@ -197,6 +197,24 @@ ZC_API zc_status zc_get_profile(zc_sim *sim, double ms[ZC_NPHASE], long long lau
 ZC_API zc_status zc_reset_profile(zc_sim *sim);
 ZC_API const char *zc_phase_name(int phase);
 
+/* --- field energy without device allocation ----------------------------- */
+/* No counterpart in the reference.  Computes the six field-energy components
+ * (the first output of zc_energy) of caller-owned device grids -- E and B
+ * each as three SoA planes of `plane` floats, rows of `pitch` floats, cell
+ * (i, j) at [(j+1)*pitch + i+1], i.e. the layout of zc_grid_view -- into
+ * `energy` (6 doubles of device memory), enqueued on `stream` (a
+ * cudaStream_t, NULL for the default stream).  It allocates nothing: for
+ * callers whose time loop cannot call cudaMalloc/cudaFree (device memory
+ * already owned by another allocator, or no room for the synchronisation
+ * those calls bring).  Its scratch is a fixed device array of
+ * ZC_STATIC_MAX_ROWS rows; larger grids are rejected with ZC_EINVAL.  The
+ * first call on a device looks up that array's address, so make it before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race and must be serialised. */
+#define ZC_STATIC_MAX_ROWS 8192
+ZC_API zc_status zc_field_energy_static(const float *E, const float *B, size_t plane, int pitch, int nx,
+                                        int ny, float dx, float dy, double *energy, void *stream);
+
 /* message of the last failing call on this thread */
 ZC_API const char *zc_last_error(void);
 ZC_API const char *zc_status_string(zc_status s);

@@ -35,7 +35,7 @@ EXPORTS = [
     "zc_get_fields", "zc_get_particle_fields", "zc_get_current", "zc_set_current", "zc_energy",
     "zc_species_charge", "zc_get_info", "zc_grid_view_get", "zc_synchronize", "zc_last_step_ms",
     "zc_last_error", "zc_status_string", "zc_set_profiling", "zc_get_profile", "zc_reset_profile",
-    "zc_phase_name",
+    "zc_phase_name", "zc_field_energy_static",
 ]
 NPHASE = 11
 
@@ -122,6 +122,7 @@ def load(path: str = LIB_PATH):
         "zc_set_profiling": [P, I],
         "zc_get_profile": [P, P, P],
         "zc_reset_profile": [P],
+        "zc_field_energy_static": [P, P, C.c_size_t, I, I, I, C.c_float, C.c_float, P, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

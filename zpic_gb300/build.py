@@ -25,6 +25,7 @@ UNITS = [
     ("zc_particles.cu", ["--fmad=false"]),
     ("zc_fields.cu", ["--fmad=false"]),
     ("zc_api.cu", []),
+    ("zc_noalloc.cu", []),
 ]
 
 

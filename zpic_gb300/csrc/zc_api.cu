@@ -128,6 +128,8 @@ struct SpeciesState {
 
 }  // namespace
 
+void zc::set_error_message(const char *msg) { g_err = msg ? msg : ""; }
+
 struct zc_sim {
   int device = 0;
   cudaStream_t st = nullptr;

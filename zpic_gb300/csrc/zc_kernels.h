@@ -107,6 +107,9 @@ struct LaserConst {
 };
 cudaError_t launch_laser(float *EB, const Grid &G, const LaserConst &L, cudaStream_t st);
 
+// sets the message returned by zc_last_error() on this thread
+void set_error_message(const char *msg);
+
 constexpr int kYeeOX = 32, kYeeOY = 16;   // Yee output tile (buffer cells)
 constexpr int kYeeBW = kYeeOX + 8;        // TMA box: 4 columns of halo each side
 constexpr int kYeeBH = kYeeOY + 3;
