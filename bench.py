@@ -223,6 +223,11 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--tile", default="16x16")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--exact", action="store_true",
+                    help="bit-exact push build (every float32 op rounded as the reference C)")
+    ap.add_argument("--sort-every", type=int, default=0)
+    ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -254,13 +259,17 @@ def main():
 
     from zpic_gb300._zc import CudaSim
 
-    W = WORKLOAD
+    W = dict(WORKLOAD)
+    if args.nx:
+        W.update(nx=(args.nx, args.nx), box=(args.nx * 0.1, args.nx * 0.1),
+                 name=f"em2d uniform thermal plasma {args.nx}x{args.nx}, 4x4 ppc")
     nx, ny = W["nx"]
     tile = tuple(int(v) for v in args.tile.split("x"))
     parts = synth_particles(nx, ny, W["ppc"], W["uth"], seed=1234 + rank)
     N = parts.size
     q = np.float32(-1.0) / np.float32(W["ppc"][0] * W["ppc"][1])
-    sim = CudaSim(W["nx"], W["box"], W["dt"], device=local, tile=tile)
+    sim = CudaSim(W["nx"], W["box"], W["dt"], device=local, tile=tile, fast_math=not args.exact,
+                  sort_every=args.sort_every)
     sim.add_species(W["m_q"], float(q), W["ppc"], parts)
     sm = W["smooth"]
     sim.set_smooth(sm[0], sm[1], sm[2], sm[3])
@@ -285,6 +294,11 @@ def main():
     # ---- end to end through the C-ABI with host buffers ----
     import torch
 
+    if args.no_e2e:
+        args_steps_e2e = 0
+    else:
+        args_steps_e2e = args.steps
+
     pinned = torch.empty(parts.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(parts.dtype)
     pinned[:] = parts
     fshape = (ny + 3, nx + 3, 3)
@@ -293,16 +307,17 @@ def main():
     barrier()
     sim.synchronize()
     t0 = time.perf_counter()
-    sim.set_fields(E=Eh, B=Bh)
-    sim.set_particles(0, pinned)
+    if args_steps_e2e:
+        sim.set_fields(E=Eh, B=Bh)
+        sim.set_particles(0, pinned)
     hist = []
-    for _ in range(args.steps):
+    for _ in range(args_steps_e2e):
         sim.step(1)
         hist.append(sim.energy())
     t_e2e = time.perf_counter() - t0
     barrier()
     t_e2e = allmax(t_e2e)
-    e2e = N * args.steps * world / t_e2e
+    e2e = N * args_steps_e2e * world / t_e2e if args_steps_e2e else None
     h2d = (parts.nbytes + Eh.nbytes + Bh.nbytes) / args.steps
     d2h = (6 + 1) * 8
 
@@ -325,6 +340,8 @@ def main():
         "config": {"workload": W["name"], "nx": [nx, ny], "dx": 0.1, "dt": W["dt"], "ppc": list(W["ppc"]),
                    "particles_per_gpu": int(N), "uth": W["uth"],
                    "smoothing": "compensated level 1, x and y", "tile": list(tile),
+                   "push_build": "exact (no FMA contraction)" if args.exact else "fast (FMA contraction)",
+                   "cell_sort_every": args.sort_every or 8,
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (1.88 GB of particles read and written per step)"},
         "clocks": clocks,

@@ -61,6 +61,9 @@ typedef struct {
     int tile[2];            /* particle tile size in cells (0,0 -> 16 x 16) */
     int deterministic;      /* 1: fixed-order current deposition, bit-reproducible runs */
     float tile_slack;       /* spare tile capacity, fraction (<=0 -> 0.5) */
+    int fast_math;          /* 0: push rounds every float32 operation as the reference C
+                               (bit-identical particles); 1: FMA-contracted push */
+    int sort_every;         /* steps between per-tile cell sorts (0 -> 8, <0 never) */
 } zc_sim_desc;
 
 typedef struct {
@@ -190,6 +193,7 @@ enum {
     ZC_PHASE_EMF_GC,        /* field guard cells */
     ZC_PHASE_EXT,           /* external fields */
     ZC_PHASE_WINDOW,        /* moving-window shift and injection */
+    ZC_PHASE_SORT,          /* per-tile cell sort */
     ZC_NPHASE
 };
 ZC_API zc_status zc_set_profiling(zc_sim *sim, int enable);

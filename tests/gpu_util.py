@@ -51,13 +51,14 @@ def column_injector(deck, cpu):
     return inject
 
 
-def mirror(name, tile=(16, 16), deck=None, cpu=None, injector=None):
-    """Builds the deck on the oracle and mirrors its state onto the GPU."""
+def mirror(name, tile=(16, 16), deck=None, cpu=None, injector=None, **kw):
+    """Builds the deck on the oracle and mirrors its state onto the GPU
+    (extra keywords go to CudaSim: fast_math, sort_every, ...)."""
     from zpic_gb300._zc import CudaSim
 
     d = deck or DECKS[name]
     cpu = cpu or build_cpu(name, deck=d)
-    g = CudaSim(d["nx"], d["box"], d["dt"], tile=tile)
+    g = CudaSim(d["nx"], d["box"], d["dt"], tile=tile, **kw)
     for k, sp in enumerate(d["species"]):
         g.add_species(sp["m_q"], cpu.q(k), sp["ppc"], cpu.particles(k))
     g.set_fields(E=cpu.E(), B=cpu.B())
@@ -100,3 +101,13 @@ def field_err(a, b):
         na = np.linalg.norm(a[..., c] - b[..., c])
         errs.append(0.0 if nb == 0 and na == 0 else na / max(nb, 1e-30))
     return max(errs)
+
+
+def field_err_joint(a, b):
+    """Relative L2 error of the whole vector field (all three components
+    together) over the interior."""
+    a = np.asarray(a, dtype=np.float64)[1:-2, 1:-2]
+    b = np.asarray(b, dtype=np.float64)[1:-2, 1:-2]
+    nb = np.linalg.norm(b)
+    na = np.linalg.norm(a - b)
+    return 0.0 if nb == 0 and na == 0 else na / max(nb, 1e-30)

@@ -37,7 +37,7 @@ EXPORTS = [
     "zc_last_error", "zc_status_string", "zc_set_profiling", "zc_get_profile", "zc_reset_profile",
     "zc_phase_name", "zc_field_energy_static",
 ]
-NPHASE = 11
+NPHASE = 12
 
 
 class ZcError(RuntimeError):
@@ -48,7 +48,8 @@ class ZcError(RuntimeError):
 
 class SimDesc(C.Structure):
     _fields_ = [("nx", C.c_int * 2), ("box", C.c_float * 2), ("dt", C.c_float), ("device", C.c_int),
-                ("tile", C.c_int * 2), ("deterministic", C.c_int), ("tile_slack", C.c_float)]
+                ("tile", C.c_int * 2), ("deterministic", C.c_int), ("tile_slack", C.c_float),
+                ("fast_math", C.c_int), ("sort_every", C.c_int)]
 
 
 class SpeciesDesc(C.Structure):
@@ -150,7 +151,8 @@ def _p(a: np.ndarray):
 class CudaSim:
     """One em2d simulation on the GPU (a ``zc_sim`` handle)."""
 
-    def __init__(self, nx, box, dt, device=0, tile=(16, 16), deterministic=False, tile_slack=0.5):
+    def __init__(self, nx, box, dt, device=0, tile=(16, 16), deterministic=False, tile_slack=0.5,
+                 fast_math=False, sort_every=0):
         self.lib = load()
         d = SimDesc()
         d.nx[0], d.nx[1] = int(nx[0]), int(nx[1])
@@ -160,6 +162,8 @@ class CudaSim:
         d.tile[0], d.tile[1] = int(tile[0]), int(tile[1])
         d.deterministic = int(bool(deterministic))
         d.tile_slack = float(tile_slack)
+        d.fast_math = int(bool(fast_math))
+        d.sort_every = int(sort_every)
         h = C.c_void_p()
         _ck(self.lib.zc_sim_create(C.byref(d), C.byref(h)))
         self.h = h

@@ -2,10 +2,12 @@
 
     python -m zpic_gb300.build          # or zpic_gb300.build.build()
 
-Three translation units are compiled in parallel and linked into
-``zpic_gb300/lib/libzpic_cuda.so``.  The physics kernels (particles, fields)
-are compiled with ``--fmad=false`` so that every float32 operation rounds as
-in the reference C code; the host runtime uses the defaults.
+The translation units are compiled in parallel and linked into
+``zpic_gb300/lib/libzpic_cuda.so``.  The physics kernels (exact push,
+particles, fields) are compiled with ``--fmad=false`` so that every float32
+operation rounds as in the reference C code; the fast push build allows FMA
+contraction and approximate float32 division / square root; the host runtime
+uses the defaults.
 """
 from __future__ import annotations
 
@@ -22,6 +24,8 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = [
+    ("zc_push_exact.cu", ["--fmad=false"]),
+    ("zc_push_fast.cu", ["--fmad=true", "--prec-div=false", "--prec-sqrt=false"]),
     ("zc_particles.cu", ["--fmad=false"]),
     ("zc_fields.cu", ["--fmad=false"]),
     ("zc_api.cu", []),

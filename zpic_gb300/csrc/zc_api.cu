@@ -111,7 +111,7 @@ struct SpeciesState {
   int ppc[2] = {1, 1};
   int iter = 0, n_move = 0;
   // tile layout
-  int *d_off = nullptr, *d_cap = nullptr, *d_np = nullptr, *d_nstay = nullptr;
+  int *d_off = nullptr, *d_cap = nullptr, *d_np = nullptr;
   std::vector<int> h_off, h_cap;
   long long alloc = 0;   // particles per buffer
   Particles buf[2] = {};
@@ -122,6 +122,12 @@ struct SpeciesState {
   int *d_spill_cnt = nullptr;  // [2]
   int spill_cap = 0;
   int spill_cur = 0;
+  // outboxes: leavers posted by one push, pulled by the next (ob[ob_in]
+  // holds the pending ones; its counts are all zero when nothing is pending)
+  Outbox ob[2] = {};
+  long long ob_alloc = 0;
+  int ob_in = 0;
+  bool pending = false;
   // energy
   double *d_ekin_tile = nullptr, *d_ekin_extra = nullptr, *d_ekin = nullptr;
 };
@@ -146,8 +152,6 @@ struct zc_sim {
   CUtensorMap tmK_EB[2], tmK_EBp, tmK_J;
   CUtensorMap tmY_EB[2], tmY_J[2];
   int TX = 16, TY = 16, ntx = 0, nty = 0, ntiles = 0;
-  Outbox O{};
-  long long ob_alloc = 0;
   std::vector<SpeciesState> sp;
   int xtype = 0, ytype = 0, xlevel = 0, ylevel = 0;
   int mw = 0, n_move = 0, iter = 0;
@@ -166,6 +170,8 @@ struct zc_sim {
   Particles inj_list{};
   long long inj_list_cap = 0;
   int deterministic = 0;
+  int fast = 0;                   // FMA build of the push kernels
+  int sort_every = 8;             // steps between per-tile cell sorts
   float slack = 0.5f;
   int accumulated_err = 0;
   // per-phase profiling: event pairs recorded during a call, summed on sync
@@ -230,23 +236,38 @@ void collect_profile(zc_sim *s) {
 
 LayoutConst layout(const zc_sim *s) { return LayoutConst{s->TX, s->TY, s->ntx, s->nty, s->nx, s->ny}; }
 
-TileSet tiles(SpeciesState &p, int ntiles) { return TileSet{p.d_off, p.d_cap, p.d_np, p.d_nstay, ntiles}; }
+TileSet tiles(SpeciesState &p, int ntiles) { return TileSet{p.d_off, p.d_cap, p.d_np, ntiles}; }
 
 Spill spill_of(SpeciesState &p, int k) { return Spill{p.spill[k], p.d_spill_cnt + k, p.spill_cap}; }
 
 // outbox slots per tile: room for a moving-window column plus crossers
-zc_status ensure_outbox(zc_sim *s, int max_cap) {
-  int per = std::max(256, ((max_cap / 6) + 31) / 32 * 32);
+// (more leavers than slots go to the spill list)
+zc_status ensure_outbox(zc_sim *s, SpeciesState &p, int max_cap) {
+  int per = std::max(128, ((max_cap / 8) + 31) / 32 * 32);
   long long need = (long long)per * s->ntiles;
-  if (per <= s->O.cap && need <= s->ob_alloc) return ZC_OK;
-  free_particles(s->O.p);
-  dfree(s->O.dst);
-  TRY(alloc_particles(s->O.p, need));
-  TRY(dalloc(&s->O.dst, need));
-  if (!s->O.cnt) TRY(dalloc(&s->O.cnt, s->ntiles));
-  CK(cudaMemsetAsync(s->O.cnt, 0, sizeof(int) * s->ntiles, s->st));
-  s->O.cap = per;
-  s->ob_alloc = need;
+  if (per <= p.ob[0].cap && need <= p.ob_alloc) return ZC_OK;
+  for (int b = 0; b < 2; ++b) {
+    free_particles(p.ob[b].p);
+    dfree(p.ob[b].dst);
+    TRY(alloc_particles(p.ob[b].p, need));
+    TRY(dalloc(&p.ob[b].dst, need));
+    if (!p.ob[b].cnt) TRY(dalloc(&p.ob[b].cnt, s->ntiles));
+    CK(cudaMemsetAsync(p.ob[b].cnt, 0, sizeof(int) * s->ntiles, s->st));
+    p.ob[b].cap = per;
+  }
+  p.ob_alloc = need;
+  p.pending = false;
+  return ZC_OK;
+}
+
+// moves the particles still waiting in the outboxes into their tiles
+zc_status settle(zc_sim *s, SpeciesState &p) {
+  if (!p.pending) return ZC_OK;
+  Phase ph(s, ZC_PHASE_MIGRATE, 1);
+  CK(launch_settle(p.buf[p.cur], tiles(p, s->ntiles), p.ob[p.ob_in], spill_of(p, p.spill_cur), s->d_err, s->ntx,
+                   s->nty, s->mw, s->st));
+  CK(cudaMemsetAsync(p.ob[p.ob_in].cnt, 0, sizeof(int) * s->ntiles, s->st));
+  p.pending = false;
   return ZC_OK;
 }
 
@@ -256,6 +277,7 @@ zc_status ensure_outbox(zc_sim *s, int max_cap) {
 zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   SpeciesState &p = s->sp[k];
   cudaStream_t st = s->st;
+  TRY(settle(s, p));
   const LayoutConst L = layout(s);
   const int nt = s->ntiles;
   int *d_cnt = nullptr, *d_fill = nullptr, *d_np_old = nullptr, *d_off_old = nullptr;
@@ -292,7 +314,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
     max_cap = std::max(max_cap, (int)c);
   }
   if (tot >= (1LL << 31)) return fail(ZC_ENOMEM, "species too large for 32-bit tile offsets");
-  TRY(ensure_outbox(s, max_cap));
+  TRY(ensure_outbox(s, p, max_cap));
 
   Particles nbuf[2] = {};
   const bool grow = tot > p.alloc;
@@ -327,7 +349,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   int sm = 1;
   while (sm < smax) sm <<= 1;
   sm = std::min(sm, smem_cap);
-  CK(launch_tile_order(tmp, nkey, p.d_off, p.d_np, dst, nt, std::max(sm, 1), 32, st));
+  CK(launch_tile_order(tmp, nkey, p.d_off, p.d_np, dst, nt, std::max(sm, 1), L, st));
   CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), st));
   CK(cudaStreamSynchronize(st));
   if (grow) {
@@ -425,7 +447,8 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   a.pin = p.buf[p.cur];
   a.pout = p.buf[1 - p.cur];
   a.T = tiles(p, s->ntiles);
-  a.O = s->O;
+  a.Oin = p.ob[p.ob_in];
+  a.O = p.ob[1 - p.ob_in];
   a.S = spill_of(p, out);
   a.ekin_tile = p.d_ekin_tile;
   a.err = s->d_err;
@@ -433,6 +456,15 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   a.ntiles = s->ntiles;
   a.TX = s->TX;
   a.TY = s->TY;
+  a.fast = s->fast;
+  if (s->sort_every > 0 && p.iter % s->sort_every == 0) {
+    // keep the tiles sorted by cell (the push warps then share cells)
+    Phase ph(s, ZC_PHASE_SORT, 1);
+    CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles, st));
+    p.cur = 1 - p.cur;
+    a.pin = p.buf[p.cur];
+    a.pout = p.buf[1 - p.cur];
+  }
   {
     Phase ph(s, ZC_PHASE_PUSH, 1);
     CK(launch_push_tiles(a, st));
@@ -441,13 +473,10 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   {
     Phase ph(s, ZC_PHASE_SPILL, 1);
     CK(launch_push_spill(EBpart, s->J[0], s->G, p.spill[in], p.d_spill_cnt + in, p.spill_cap, spill_of(p, out),
-                         p.d_ekin_extra, s->d_err, C, 152, st));
+                         p.d_ekin_extra, s->d_err, C, 152, s->fast, st));
   }
-  {
-    Phase ph(s, ZC_PHASE_MIGRATE, 1);
-    CK(launch_migrate(p.buf[1 - p.cur], tiles(p, s->ntiles), s->O, spill_of(p, out), s->d_err, s->ntx, s->nty,
-                      s->mw, st));
-  }
+  p.ob_in = 1 - p.ob_in;
+  p.pending = true;
   p.cur = 1 - p.cur;
   p.spill_cur = out;
   {
@@ -673,6 +702,8 @@ zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
   s->nty = (s->ny + TY - 1) / TY;
   s->ntiles = s->ntx * s->nty;
   s->deterministic = d->deterministic;
+  s->fast = d->fast_math ? 1 : 0;
+  s->sort_every = d->sort_every > 0 ? d->sort_every : (d->sort_every < 0 ? 0 : 8);
   s->slack = d->tile_slack > 0 ? d->tile_slack : 0.5f;
   Grid &G = s->G;
   G.nx = s->nx;
@@ -706,8 +737,6 @@ zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
   TRYC(dalloc(&s->d_part, 6 * s->energy_blocks));
   TRYC(dalloc(&s->d_emf, 6));
   TRYC(dalloc(&s->stage, (size_t)(s->nx + 3) * (s->ny + 3) * 3));
-  TRYC(dalloc(&s->O.cnt, s->ntiles));
-  cudaMemsetAsync(s->O.cnt, 0, sizeof(int) * s->ntiles, s->st);
   {
     constexpr int dummy = 0;
     (void)dummy;
@@ -748,7 +777,11 @@ zc_status zc_sim_destroy(zc_sim *s) {
     dfree(p.d_off);
     dfree(p.d_cap);
     dfree(p.d_np);
-    dfree(p.d_nstay);
+    for (int b = 0; b < 2; ++b) {
+      free_particles(p.ob[b].p);
+      dfree(p.ob[b].dst);
+      dfree(p.ob[b].cnt);
+    }
     dfree(p.d_key);
     dfree(p.d_spill_cnt);
     dfree(p.d_ekin_tile);
@@ -762,9 +795,6 @@ zc_status zc_sim_destroy(zc_sim *s) {
   dfree(s->EBp);
   dfree(s->extE);
   dfree(s->extB);
-  free_particles(s->O.p);
-  dfree(s->O.dst);
-  dfree(s->O.cnt);
   free_particles(s->inj_list);
   dfree(s->d_err);
   dfree(s->d_part);
@@ -799,7 +829,6 @@ zc_status zc_species_create(zc_sim *s, const zc_species_desc *d, const zc_part *
   TRY(dalloc(&p.d_off, nt));
   TRY(dalloc(&p.d_cap, nt));
   TRY(dalloc(&p.d_np, nt));
-  TRY(dalloc(&p.d_nstay, nt));
   CK(cudaMemsetAsync(p.d_np, 0, sizeof(int) * nt, s->st));
   CK(cudaMemsetAsync(p.d_off, 0, sizeof(int) * nt, s->st));
   CK(cudaMemsetAsync(p.d_cap, 0, sizeof(int) * nt, s->st));
@@ -825,6 +854,9 @@ zc_status zc_species_set_particles(zc_sim *s, int k, const zc_part *parts, int n
   SpeciesState &p = s->sp[k];
   CK(cudaMemsetAsync(p.d_np, 0, sizeof(int) * s->ntiles, s->st));
   CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), s->st));
+  for (int b = 0; b < 2; ++b)
+    if (p.ob[b].cnt) CK(cudaMemsetAsync(p.ob[b].cnt, 0, sizeof(int) * s->ntiles, s->st));
+  p.pending = false;
   Particles list{};
   TRY(upload_list(s, parts, np, list, nullptr));
   zc_status r = relayout(s, k, &list, np);
@@ -839,6 +871,7 @@ zc_status zc_species_inject(zc_sim *s, int k, const zc_part *parts, int np) {
   if (!parts) return fail(ZC_EINVAL, "null particle buffer");
   DeviceGuard g(s->device);
   SpeciesState &p = s->sp[k];
+  TRY(settle(s, p));
   Particles list{};
   TRY(upload_list(s, parts, np, list, nullptr));
   CK(launch_append_list(list, np, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur), layout(s), s->d_err,
@@ -853,6 +886,7 @@ zc_status zc_species_count(zc_sim *s, int k, int *np) {
   if (!np) return fail(ZC_EINVAL, "null argument");
   DeviceGuard g(s->device);
   SpeciesState &p = s->sp[k];
+  TRY(settle(s, p));
   std::vector<int> c(s->ntiles);
   int sc = 0;
   CK(cudaMemcpyAsync(c.data(), p.d_np, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
@@ -868,6 +902,7 @@ zc_status zc_species_get_particles(zc_sim *s, int k, zc_part *out, int cap, int 
   TRY(check_species(s, k));
   DeviceGuard g(s->device);
   SpeciesState &p = s->sp[k];
+  TRY(settle(s, p));
   std::vector<int> c(s->ntiles);
   int sc = 0;
   CK(cudaMemcpyAsync(c.data(), p.d_np, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
@@ -1112,6 +1147,7 @@ zc_status zc_species_charge(zc_sim *s, int k, float *charge) {
   if (!charge) return fail(ZC_EINVAL, "null argument");
   DeviceGuard g(s->device);
   SpeciesState &p = s->sp[k];
+  TRY(settle(s, p));
   const size_t n = (size_t)(s->nx + 1) * (s->ny + 1);
   float *d = nullptr;
   TRY(dalloc(&d, n));
@@ -1194,7 +1230,7 @@ zc_status zc_reset_profile(zc_sim *s) {
 
 const char *zc_phase_name(int p) {
   static const char *names[ZC_NPHASE] = {"push", "spill", "migrate", "kin_energy", "zero", "fold",
-                                         "smooth", "yee", "emf_gc", "ext", "window"};
+                                         "smooth", "yee", "emf_gc", "ext", "window", "sort"};
   return (p >= 0 && p < ZC_NPHASE) ? names[p] : "unknown";
 }
 

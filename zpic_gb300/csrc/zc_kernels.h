@@ -17,7 +17,7 @@ struct PushConst {
 
 struct TileSet {
   const int *off, *cap;
-  int *np, *nstay;
+  int *np;
   int ntiles;
 };
 
@@ -41,22 +41,58 @@ struct PushLaunch {
   const CUtensorMap *tm_eb, *tm_j;
   Particles pin, pout;
   TileSet T;
-  Outbox O;
+  Outbox Oin, O;                          // pending incoming (previous step), leavers (this step)
   Spill S;
   double *ekin_tile;
   int *err;
   PushConst C;
   int ntiles, TX, TY;
+  int fast;                               // 1: FMA build of the push kernels
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void store_particle(const Particles &p, long long k, int ix, int iy, float x, float y,
+                                               float ux, float uy, float uz) {
+  p.ix[k] = ix;
+  p.iy[k] = iy;
+  p.x[k] = x;
+  p.y[k] = y;
+  p.ux[k] = ux;
+  p.uy[k] = uy;
+  p.uz[k] = uz;
+}
+
+// appends a particle to a spill list; flags the host (re-layout due) and
+// records an overflow when the list is full
+__device__ __forceinline__ void spill_particle(const Spill &S, int *errbits, int ix, int iy, float x, float y,
+                                               float ux, float uy, float uz) {
+  const int q = atomicAdd(S.cnt, 1);
+  *errbits |= ERR_SPILLED;
+  if (q < S.cap) store_particle(S.p, q, ix, iy, x, y, ux, uy, uz);
+  else *errbits |= ERR_OVERFLOW;
+}
+#endif
 
 // particles
 bool tile_supported(int TX, int TY);
 cudaError_t launch_push_tiles(const PushLaunch &a, cudaStream_t st);
+cudaError_t launch_push_tiles_exact(const PushLaunch &a, cudaStream_t st);
+cudaError_t launch_push_tiles_fast(const PushLaunch &a, cudaStream_t st);
 cudaError_t launch_push_spill(const float *EB, float *J, const Grid &G, const Particles &sin, const int *sin_cnt,
                               int sin_cap, const Spill &S, double *ekin, int *err, const PushConst &C,
-                              int nblocks, cudaStream_t st);
-cudaError_t launch_migrate(const Particles &pout, const TileSet &T, const Outbox &O, const Spill &S, int *err,
-                           int ntx, int nty, int mw, cudaStream_t st);
+                              int nblocks, int fast, cudaStream_t st);
+cudaError_t launch_push_spill_exact(const float *EB, float *J, const Grid &G, const Particles &sin,
+                                    const int *sin_cnt, int sin_cap, const Spill &S, double *ekin, int *err,
+                                    const PushConst &C, int nblocks, cudaStream_t st);
+cudaError_t launch_push_spill_fast(const float *EB, float *J, const Grid &G, const Particles &sin,
+                                   const int *sin_cnt, int sin_cap, const Spill &S, double *ekin, int *err,
+                                   const PushConst &C, int nblocks, cudaStream_t st);
+// stable counting sort of every tile by cell (src -> dst, same layout)
+cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, const int *np,
+                            const LayoutConst &L, int ntiles, cudaStream_t st);
+// moves the particles pending in an outbox into their tiles (appended)
+cudaError_t launch_settle(const Particles &buf, const TileSet &T, const Outbox &O, const Spill &S, int *err,
+                          int ntx, int nty, int mw, cudaStream_t st);
 cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, int *cnt, const LayoutConst &L,
                                  int *err, cudaStream_t st);
 cudaError_t launch_count_list(const Particles &list, const int *n_ptr, int n_cap, int *cnt, const LayoutConst &L,
@@ -67,7 +103,7 @@ cudaError_t launch_scatter_list(const Particles &list, const int *n_ptr, int n_c
                                 const int *off, const int *cap, int *fill, unsigned *key, unsigned key0,
                                 const LayoutConst &L, int *err, cudaStream_t st);
 cudaError_t launch_tile_order(const Particles &src, const unsigned *key, const int *off, const int *np,
-                              const Particles &dst, int ntiles, int smax, int stride_p, cudaStream_t st);
+                              const Particles &dst, int ntiles, int smax, const LayoutConst &L, cudaStream_t st);
 cudaError_t launch_append_list(const Particles &list, int n, const Particles &buf, const TileSet &T,
                                const Spill &S, const LayoutConst &L, int *err, cudaStream_t st);
 cudaError_t launch_gather_aos(const Particles &buf, const int *off, const int *np, const long long *dst_off,

@@ -1,430 +1,20 @@
-// zc_particles.cu -- particle kernels of libzpic_cuda (sm_103a).
+// zc_particles.cu -- particle bookkeeping kernels of libzpic_cuda (sm_103a):
+// tile migration, per-tile cell sort, re-layout (upload, injection, capacity
+// changes), download, charge density and the kinetic-energy sum.  The push
+// and deposit kernels themselves live in zc_push_impl.cuh (compiled twice,
+// exact and fast, by zc_push_exact.cu / zc_push_fast.cu).
 //
-// Compiled with -fmad=false: the per-particle arithmetic rounds operation by
-// operation exactly like the reference C (em2d/particles.c), so a particle
-// advanced here from the same fields lands on the same bits.
-//
-//   k_push_tiles    one CTA per particle tile: TMA-stages the tile's E/B halo
-//                   into shared memory, pushes every particle of the tile
-//                   (staggered bilinear gather + relativistic Boris + zigzag
-//                   charge-conserving deposit into a shared-memory J tile),
-//                   compacts the particles that stay, posts the ones that
-//                   leave to the tile's outbox, then adds the J tile into
-//                   global J with one TMA reduce-add.
-//   k_push_spill    the same physics for particles that did not fit a tile
-//                   (global-memory gather and atomics; normally empty).
-//   k_migrate       one CTA per tile: pulls the particles bound for it out of
-//                   the outboxes of its (up to 8) neighbours.
-//   re-layout       upload, moving-window injection and capacity changes.
+//   k_migrate     one CTA per tile: appends the particles bound for it that
+//                 wait in the outboxes of its (up to 8) neighbours (the push
+//                 does this itself; this kernel settles the outboxes before
+//                 the particles are read back, counted or re-laid out).
+//   k_cellsort    one CTA per tile: counting sort of the tile by cell, so
+//                 that the lanes of a push warp share cells.
+//   re-layout     upload, moving-window injection and capacity changes.
 #include "zc_internal.cuh"
 #include "zc_kernels.h"
 
 namespace zc {
-
-// ---------------------------------------------------------------------------
-// field / current accessors: shared-memory tile (with a 1-cell lower halo)
-// or the global padded planes
-// ---------------------------------------------------------------------------
-template <int BW, int PL>
-struct TileFields {
-  const float *s;
-  __device__ __forceinline__ float operator()(int c, int i, int j) const {
-    return s[c * PL + (j + 1) * BW + (i + 1)];
-  }
-};
-template <int BW, int PL>
-struct TileCurrent {
-  float *s;
-  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
-    atomicAdd(&s[c * PL + (j + 1) * BW + (i + 1)], v);
-  }
-};
-struct GlobalFields {
-  const float *g;
-  int pitch;
-  size_t plane;
-  __device__ __forceinline__ float operator()(int c, int i, int j) const {
-    return __ldg(&g[c * plane + (size_t)(j + 1) * pitch + (i + 1)]);
-  }
-};
-struct GlobalCurrent {
-  float *g;
-  int pitch;
-  size_t plane;
-  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
-    atomicAdd(&g[c * plane + (size_t)(j + 1) * pitch + (i + 1)], v);
-  }
-};
-
-// ---------------------------------------------------------------------------
-// per-particle physics (restates em2d/particles.c:1029-1226)
-// ---------------------------------------------------------------------------
-template <class F>
-__device__ __forceinline__ float lerp2(const F &f, int c, int a, int b, float wa, float wb) {
-  return (f(c, a, b) * (1.0f - wa) + f(c, a + 1, b) * wa) * (1.0f - wb) +
-         (f(c, a, b + 1) * (1.0f - wa) + f(c, a + 1, b + 1) * wa) * wb;
-}
-
-struct Seg {
-  float x0, x1, y0, y1, dx, dy, qvz;
-  int ix, iy;
-};
-
-// current of one straight segment inside one cell (particles.c:886-922)
-template <class D>
-__device__ __forceinline__ void deposit_segment(const D &dep, const Seg &v, float qnx, float qny) {
-  const float s0x0 = 1.0f - v.x0, s0x1 = v.x0;
-  const float s1x0 = 1.0f - v.x1, s1x1 = v.x1;
-  const float s0y0 = 1.0f - v.y0, s0y1 = v.y0;
-  const float s1y0 = 1.0f - v.y1, s1y1 = v.y1;
-  const float jx = qnx * v.dx;
-  const float jy = qny * v.dy;
-  const float ay0 = 0.5f * (s0y0 + s1y0), ay1 = 0.5f * (s0y1 + s1y1);
-  const float ax0 = 0.5f * (s0x0 + s1x0), ax1 = 0.5f * (s0x1 + s1x1);
-  dep.add(0, v.ix, v.iy, jx * ay0);
-  dep.add(0, v.ix, v.iy + 1, jx * ay1);
-  dep.add(1, v.ix, v.iy, jy * ax0);
-  dep.add(1, v.ix + 1, v.iy, jy * ax1);
-  const float q = v.qvz;
-  dep.add(2, v.ix, v.iy, q * (s0x0 * s0y0 + s1x0 * s1y0 + (s0x0 * s1y0 - s1x0 * s0y0) / 2.0f));
-  dep.add(2, v.ix + 1, v.iy, q * (s0x1 * s0y0 + s1x1 * s1y0 + (s0x1 * s1y0 - s1x1 * s0y0) / 2.0f));
-  dep.add(2, v.ix, v.iy + 1, q * (s0x0 * s0y1 + s1x0 * s1y1 + (s0x0 * s1y1 - s1x0 * s0y1) / 2.0f));
-  dep.add(2, v.ix + 1, v.iy + 1, q * (s0x1 * s0y1 + s1x1 * s1y1 + (s0x1 * s1y1 - s1x1 * s0y1) / 2.0f));
-}
-
-// splits segment `a` at the y cell edge: `a` keeps the part before the edge,
-// the returned segment holds the rest (particles.c:842-871)
-__device__ __forceinline__ Seg split_y(Seg &a, int dj) {
-  const int yb = (dj == 1);
-  const float f = (a.y1 - yb) / a.dy;
-  const float xc = a.x0 + a.dx * (1.0f - f);
-  Seg n;
-  n.y0 = 1 - yb;
-  n.y1 = a.y1 - dj;
-  n.dy = a.dy * f;
-  n.iy = a.iy + dj;
-  n.x0 = xc;
-  n.x1 = a.x1;
-  n.dx = a.dx * f;
-  n.ix = a.ix;
-  n.qvz = a.qvz * f;
-  a.y1 = yb;
-  a.dy *= (1.0f - f);
-  a.dx *= (1.0f - f);
-  a.x1 = xc;
-  a.qvz *= (1.0f - f);
-  return n;
-}
-
-// zigzag deposit of one particle motion (particles.c:773-924), the virtual
-// particle cases unrolled so that no per-thread array is indexed
-template <class D>
-__device__ __forceinline__ void deposit_zigzag(const D &dep, int ix, int iy, int di, int dj, float x0,
-                                               float y0, float dx, float dy, float qnx, float qny,
-                                               float qvz) {
-  Seg a;
-  a.x0 = x0;
-  a.y0 = y0;
-  a.dx = dx;
-  a.dy = dy;
-  a.x1 = x0 + dx;
-  a.y1 = y0 + dy;
-  a.qvz = qvz * 0.5f;  // qvz/2.0 in the reference: exact halving either way
-  a.ix = ix;
-  a.iy = iy;
-  if (di == 0 && dj == 0) {
-    deposit_segment(dep, a, qnx, qny);
-    return;
-  }
-  if (di != 0) {
-    const int xb = (di == 1);
-    const float f = (x0 + dx - xb) / dx;
-    const float yc = y0 + dy * (1.0f - f);
-    Seg b;
-    b.x0 = 1 - xb;
-    b.x1 = (x0 + dx) - di;
-    b.dx = dx * f;
-    b.ix = ix + di;
-    b.y0 = yc;
-    b.y1 = a.y1;
-    b.dy = dy * f;
-    b.iy = iy;
-    b.qvz = a.qvz * f;
-    a.x1 = xb;
-    a.dx *= (1.0f - f);
-    a.dy *= (1.0f - f);
-    a.y1 = yc;
-    a.qvz *= (1.0f - f);
-    if (dj != 0) {
-      if (a.y1 < 0.0f || a.y1 >= 1.0f) {
-        // the first piece crosses the y edge; the x tail lies past it
-        Seg c = split_y(a, dj);
-        b.y0 -= dj;
-        b.y1 -= dj;
-        b.iy += dj;
-        deposit_segment(dep, c, qnx, qny);
-      } else {
-        Seg c = split_y(b, dj);
-        deposit_segment(dep, c, qnx, qny);
-      }
-    }
-    deposit_segment(dep, b, qnx, qny);
-  } else {
-    Seg c = split_y(a, dj);
-    deposit_segment(dep, c, qnx, qny);
-  }
-  deposit_segment(dep, a, qnx, qny);
-}
-
-// gather + Boris + move + deposit for one particle at cell (i, j) of the
-// accessor frame; returns the kinetic-energy term utsq/(gamma+1).  `bad` is
-// set when the motion breaks the one-cell-per-step assumption of the
-// deposit (|dx| >= 1 cell, or not a number).  A trimmed position of exactly
-// 1.0f (x1 = -tiny, then +1 rounds up) is legal, as in the reference.
-template <class F, class D>
-__device__ __forceinline__ float advance_particle(const F &fld, const D &dep, int i, int j, float &x,
-                                                  float &y, float &ux, float &uy, float &uz, int &di,
-                                                  int &dj, bool &bad, const PushConst &C) {
-  // staggered bilinear gather (particles.c:1029-1071)
-  const int ih = i + ((x < 0.5f) ? -1 : 0);
-  const int jh = j + ((y < 0.5f) ? -1 : 0);
-  const float w1h = x + ((x < 0.5f) ? 0.5f : -0.5f);
-  const float w2h = y + ((y < 0.5f) ? 0.5f : -0.5f);
-  float ex = lerp2(fld, 0, ih, j, w1h, y);
-  float ey = lerp2(fld, 1, i, jh, x, w2h);
-  float ez = lerp2(fld, 2, i, j, x, y);
-  float bx = lerp2(fld, 3, i, jh, x, w2h);
-  float by = lerp2(fld, 4, ih, j, w1h, y);
-  float bz = lerp2(fld, 5, ih, jh, w1h, w2h);
-
-  // relativistic Boris push (particles.c:1145-1187)
-  const float tem = C.tem;
-  ex *= tem;
-  ey *= tem;
-  ez *= tem;
-  float tx = ux + ex, ty = uy + ey, tz = uz + ez;
-  const float u2 = tx * tx + ty * ty + tz * tz;
-  const float g = sqrtf(1.0f + u2);
-  const float kin = u2 / (g + 1);
-  const float tg = tem / g;
-  bx *= tg;
-  by *= tg;
-  bz *= tg;
-  const float s2 = 2.0f / (1.0f + bx * bx + by * by + bz * bz);
-  float vx = tx + ty * bz - tz * by;
-  float vy = ty + tz * bx - tx * bz;
-  float vz = tz + tx * by - ty * bx;
-  bx *= s2;
-  by *= s2;
-  bz *= s2;
-  tx += vy * bz - vz * by;
-  ty += vz * bx - vx * bz;
-  tz += vx * by - vy * bx;
-  ux = tx + ex;
-  uy = ty + ey;
-  uz = tz + ez;
-
-  // move and cell crossing (particles.c:1194-1207, ltrim :1081-1084)
-  const float rg = 1.0f / sqrtf(1.0f + ux * ux + uy * uy + uz * uz);
-  const float mx = C.dt_dx * rg * ux;
-  const float my = C.dt_dy * rg * uy;
-  bad = !(fabsf(mx) < 1.0f && fabsf(my) < 1.0f);
-  float x1 = x + mx, y1 = y + my;
-  di = (x1 >= 1.0f) - (x1 < 0.0f);
-  dj = (y1 >= 1.0f) - (y1 < 0.0f);
-  x1 -= di;
-  y1 -= dj;
-  const float qvz = C.q * uz * rg;
-  deposit_zigzag(dep, i, j, di, dj, x, y, mx, my, C.qnx, C.qny, qvz);
-  x = x1;
-  y = y1;
-  return kin;
-}
-
-// new cell after the move, window shift and boundary; false when the
-// particle left through an absorbing x boundary (particles.c:1234-1259)
-__device__ __forceinline__ bool apply_boundary(int &ix, int &iy, int di, int dj, const PushConst &C) {
-  ix += di - C.shift;
-  iy += dj;
-  iy += ((iy < 0) ? C.ny : 0) - ((iy >= C.ny) ? C.ny : 0);
-  if (C.mw) return ix >= 0 && ix < C.nx;
-  ix += ((ix < 0) ? C.nx : 0) - ((ix >= C.nx) ? C.nx : 0);
-  return true;
-}
-
-__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
-  const float y = v - c;
-  const float t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-
-__device__ __forceinline__ void store_particle(const Particles &p, long long k, int ix, int iy, float x,
-                                               float y, float ux, float uy, float uz) {
-  p.ix[k] = ix;
-  p.iy[k] = iy;
-  p.x[k] = x;
-  p.y[k] = y;
-  p.ux[k] = ux;
-  p.uy[k] = uy;
-  p.uz[k] = uz;
-}
-
-__device__ __forceinline__ void spill_particle(const Spill &S, int *errbits, int ix, int iy, float x, float y,
-                                               float ux, float uy, float uz) {
-  const int q = atomicAdd(S.cnt, 1);
-  *errbits |= ERR_SPILLED;
-  if (q < S.cap) store_particle(S.p, q, ix, iy, x, y, ux, uy, uz);
-  else *errbits |= ERR_OVERFLOW;
-}
-
-// ---------------------------------------------------------------------------
-// K1: push + deposit, one CTA per tile
-// ---------------------------------------------------------------------------
-template <int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
-                                                   const __grid_constant__ CUtensorMap tm_j, Particles pin,
-                                                   Particles pout, TileSet T, Outbox O, Spill S,
-                                                   double *ekin_tile, int *err, PushConst C) {
-  constexpr int BW = (TX + 3 + 3) & ~3;  // halo box width, multiple of 4 floats
-  constexpr int BH = TY + 3;
-  constexpr int PL = BW * BH;
-  __shared__ __align__(128) float sEB[6 * PL];
-  __shared__ __align__(128) float sJ[3 * PL];
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ int swarp[NT / 32];
-  __shared__ double sred[NT / 32];
-
-  const int t = blockIdx.x;
-  const int tx = t % C.ntx, ty = t / C.ntx;
-  const int cx0 = tx * TX, cy0 = ty * TY;  // first cell of the tile = buffer coords of its halo
-  int errbits = 0;
-
-  if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    mbar_expect_tx(&bar, 6 * PL * 4);
-    tma_load_3d(sEB, &tm_eb, cx0, cy0, 0, &bar);
-  }
-  for (int k = threadIdx.x; k < 3 * PL; k += NT) sJ[k] = 0.f;
-  const bool loaded = mbar_wait_bounded(&bar, 0);
-  if (!loaded) errbits |= ERR_TIMEOUT;
-  __syncthreads();
-
-  const TileFields<BW, PL> fld{sEB};
-  const TileCurrent<BW, PL> dep{sJ};
-  const long long base = T.off[t];
-  const int n = T.np[t];
-  const long long obase = (long long)t * O.cap;
-  int run_stay = 0, run_leave = 0;
-  float ks = 0.f, kc = 0.f;
-
-  for (int k0 = 0; k0 < n; k0 += NT) {
-    const int k = k0 + threadIdx.x;
-    int code = 0;  // 1 stays in the tile, 2 leaves it
-    int ix = 0, iy = 0, dest = 0;
-    float x = 0.f, y = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
-    if (k < n) {
-      const long long g = base + k;
-      ix = pin.ix[g];
-      iy = pin.iy[g];
-      x = pin.x[g];
-      y = pin.y[g];
-      ux = pin.ux[g];
-      uy = pin.uy[g];
-      uz = pin.uz[g];
-      int li = ix - cx0, lj = iy - cy0;
-      if ((unsigned)li >= (unsigned)TX || (unsigned)lj >= (unsigned)TY) {
-        errbits |= ERR_ESCAPE;  // not in this tile: keep the accesses inside the halo
-        li = min(max(li, 0), TX - 1);
-        lj = min(max(lj, 0), TY - 1);
-        ix = cx0 + li;
-        iy = cy0 + lj;
-      }
-      int di, dj;
-      bool bad;
-      const float kin = advance_particle(fld, dep, li, lj, x, y, ux, uy, uz, di, dj, bad, C);
-      kahan_add(ks, kc, kin);
-      if (bad) errbits |= ERR_ESCAPE;
-      if (apply_boundary(ix, iy, di, dj, C)) {
-        dest = ix / TX + (iy / TY) * C.ntx;
-        code = (dest == t) ? 1 : 2;
-      }
-    }
-    int tot;
-    const int pre = block_exclusive_scan<NT>((code == 1) | ((code == 2) << 16), tot, swarp);
-    if (code == 1) {
-      store_particle(pout, base + run_stay + (pre & 0xffff), ix, iy, x, y, ux, uy, uz);
-    } else if (code == 2) {
-      const int s = run_leave + (pre >> 16);
-      if (s < O.cap) {
-        store_particle(O.p, obase + s, ix, iy, x, y, ux, uy, uz);
-        O.dst[obase + s] = dest;
-      } else {
-        spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
-      }
-    }
-    run_stay += tot & 0xffff;
-    run_leave += tot >> 16;
-  }
-
-  if (threadIdx.x == 0) {
-    T.nstay[t] = run_stay;
-    O.cnt[t] = min(run_leave, O.cap);
-  }
-  const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
-  if (threadIdx.x == 0) ekin_tile[t] = e;
-
-  // all shared-memory atomics done: hand the J tile to the TMA unit
-  fence_proxy_async_smem();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (loaded) {
-      tma_reduce_add_3d(&tm_j, sJ, cx0, cy0, 0);
-      bulk_commit();
-      bulk_wait_read0();
-    } else if (!mbar_wait_bounded(&bar, 0)) {
-      errbits |= ERR_TIMEOUT;  // second bounded wait for the load still in flight
-    }
-  }
-  if (errbits) atomicOr(err, errbits);
-}
-
-// ---------------------------------------------------------------------------
-// spill push: same physics from global memory (rarely non-empty)
-// ---------------------------------------------------------------------------
-template <int NT>
-__global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Grid G, Particles sin,
-                                                   const int *sin_cnt, int sin_cap, Spill S, double *ekin,
-                                                   int *err, PushConst C) {
-  __shared__ double sred[NT / 32];
-  const int n = min(*sin_cnt, sin_cap);
-  const GlobalFields fld{EB, G.pitch, G.plane};
-  const GlobalCurrent dep{J, G.pitch, G.plane};
-  int errbits = 0;
-  float ks = 0.f, kc = 0.f;
-  for (int k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
-    int ix = sin.ix[k], iy = sin.iy[k];
-    float x = sin.x[k], y = sin.y[k], ux = sin.ux[k], uy = sin.uy[k], uz = sin.uz[k];
-    if (ix < 0 || ix >= C.nx || iy < 0 || iy >= C.ny) {
-      errbits |= ERR_ESCAPE;
-      ix = min(max(ix, 0), C.nx - 1);
-      iy = min(max(iy, 0), C.ny - 1);
-    }
-    int di, dj;
-    bool bad;
-    const float kin = advance_particle(fld, dep, ix, iy, x, y, ux, uy, uz, di, dj, bad, C);
-    if (bad) errbits |= ERR_ESCAPE;
-    kahan_add(ks, kc, kin);
-    if (apply_boundary(ix, iy, di, dj, C)) spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
-  }
-  const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
-  if (threadIdx.x == 0 && e != 0.0) atomicAdd(ekin, e);
-  if (errbits) atomicOr(err, errbits);
-}
 
 // ---------------------------------------------------------------------------
 // K2: migrate the outboxes into the destination tiles, one CTA per tile
@@ -458,7 +48,7 @@ __global__ void __launch_bounds__(NT) k_migrate(Particles pout, TileSet T, Outbo
   }
   __syncthreads();
   int errbits = 0;
-  const int stay = T.nstay[t];
+  const int stay = T.np[t];
   const long long start = (long long)T.off[t] + stay;
   const int room = T.cap[t] - stay;
   int placed = 0;
@@ -559,22 +149,69 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
   }
 }
 
-// Orders every tile deterministically: sort by key (origin order), then
-// interleave with stride P so that neighbouring threads of the push kernel
-// work on particles of different cells (fewer shared-memory atomic
-// collisions).  One CTA per tile; tiles larger than the shared-memory sort
-// capacity are copied in key-unsorted order.
+// Counting sort of every tile by local cell (one CTA of 1024 threads per
+// tile, src -> dst at the same offsets): a shared-memory histogram, a scan,
+// then every particle takes the next slot of its cell.  The order inside a
+// cell follows the atomics' timing.  The reference sorts its whole buffer by
+// cell every n_sort steps for cache reuse (spec_sort,
+// em2d/particles.c:942-1007); here the per-tile sort keeps the lanes of a
+// push warp on shared cells.
+__global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst, const int *off, const int *np,
+                                                   LayoutConst L) {
+  constexpr int MAXC = 1024;
+  __shared__ int cursor[MAXC];
+  __shared__ int swarp[32];
+  const int t = blockIdx.x;
+  const int ncell = L.TX * L.TY;
+  const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
+  const int n = np[t];
+  const long long b = off[t];
+  for (int c = threadIdx.x; c < ncell; c += 1024) cursor[c] = 0;
+  __syncthreads();
+  auto cell_of = [&](long long g) {
+    const int c = (src.ix[g] - cx0) + (src.iy[g] - cy0) * L.TX;
+    return min(max(c, 0), ncell - 1);
+  };
+  for (int k = threadIdx.x; k < n; k += 1024) atomicAdd(&cursor[cell_of(b + k)], 1);
+  __syncthreads();
+  {
+    const int v = (threadIdx.x < ncell) ? cursor[threadIdx.x] : 0;
+    int tot;
+    const int pre = block_exclusive_scan<1024>(v, tot, swarp);
+    if (threadIdx.x < ncell) cursor[threadIdx.x] = pre;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += 1024) {
+    const long long s = b + k;
+    const int slot = atomicAdd(&cursor[cell_of(s)], 1);
+    store_particle(dst, b + slot, src.ix[s], src.iy[s], src.x[s], src.y[s], src.ux[s], src.uy[s], src.uz[s]);
+  }
+}
+
+// Orders every tile deterministically after a re-layout: by cell, and
+// within a cell by the key (origin order).  One CTA per tile; tiles larger
+// than the shared-memory sort capacity are copied unsorted (the periodic cell
+// sort fixes them).
 __global__ void k_tile_order(Particles src, const unsigned *key, const int *off, const int *np,
-                             Particles dst, int smax, int stride_p) {
-  extern __shared__ unsigned long long sk[];  // (key << 32) | local index
+                             Particles dst, int smax, LayoutConst L) {
+  extern __shared__ unsigned long long sk[];  // (cell << 52) | (key << 20) | local index
   const int t = blockIdx.x;
   const int n = np[t];
   const long long b = off[t];
-  if (n <= smax) {
+  const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
+  const bool sorted = (n <= smax) && (n < (1 << 20));
+  if (sorted) {
     int m = 1;
     while (m < n) m <<= 1;
-    for (int k = threadIdx.x; k < m; k += blockDim.x)
-      sk[k] = (k < n) ? (((unsigned long long)key[b + k] << 32) | (unsigned)k) : ~0ull;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+      unsigned long long v = ~0ull;
+      if (k < n) {
+        const unsigned cell = (unsigned)((src.ix[b + k] - cx0) + (src.iy[b + k] - cy0) * L.TX) & 0xfffu;
+        v = ((unsigned long long)cell << 52) | ((unsigned long long)(key[b + k] & 0xffffffffu) << 20) |
+            (unsigned)k;
+      }
+      sk[k] = v;
+    }
     __syncthreads();
     for (int size = 2; size <= m; size <<= 1)
       for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -592,13 +229,9 @@ __global__ void k_tile_order(Particles src, const unsigned *key, const int *off,
         __syncthreads();
       }
   }
-  const int P = stride_p;
-  const int q = n / P, r = n % P;
   for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int from = (n <= smax) ? (int)(sk[p] & 0xffffffffu) : p;
-    const int res = p % P;
-    const int to = res * q + min(res, r) + p / P;
-    const long long s = b + from, d = b + to;
+    const int from = sorted ? (int)(sk[p] & 0xfffffu) : p;
+    const long long s = b + from, d = b + p;
     store_particle(dst, d, src.ix[s], src.iy[s], src.x[s], src.y[s], src.ux[s], src.uy[s], src.uz[s]);
   }
 }
@@ -722,44 +355,31 @@ __global__ void k_sum_energy(const double *tiles, int ntiles, const double *extr
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
-template <int TX, int TY>
-static cudaError_t launch_push_t(const PushLaunch &a, cudaStream_t st) {
-  constexpr int NT = (TX * TY >= 256) ? 256 : 128;
-  k_push_tiles<TX, TY, NT><<<a.ntiles, NT, 0, st>>>(*a.tm_eb, *a.tm_j, a.pin, a.pout, a.T, a.O, a.S,
-                                                     a.ekin_tile, a.err, a.C);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_push_tiles(const PushLaunch &a, cudaStream_t st) {
-  const int TX = a.TX, TY = a.TY;
-#define ZC_TILE(X, Y) \
-  if (TX == X && TY == Y) return launch_push_t<X, Y>(a, st);
-  ZC_TILE(16, 16)
-  ZC_TILE(8, 8)
-  ZC_TILE(16, 8)
-  ZC_TILE(32, 16)
-  ZC_TILE(32, 32)
-  ZC_TILE(8, 16)
-  ZC_TILE(16, 32)
-#undef ZC_TILE
-  return cudaErrorInvalidValue;
-}
-
 bool tile_supported(int TX, int TY) {
   return (TX == 16 && TY == 16) || (TX == 8 && TY == 8) || (TX == 16 && TY == 8) || (TX == 32 && TY == 16) ||
          (TX == 32 && TY == 32) || (TX == 8 && TY == 16) || (TX == 16 && TY == 32);
 }
 
+cudaError_t launch_push_tiles(const PushLaunch &a, cudaStream_t st) {
+  return a.fast ? launch_push_tiles_fast(a, st) : launch_push_tiles_exact(a, st);
+}
+
 cudaError_t launch_push_spill(const float *EB, float *J, const Grid &G, const Particles &sin, const int *sin_cnt,
                               int sin_cap, const Spill &S, double *ekin, int *err, const PushConst &C,
-                              int nblocks, cudaStream_t st) {
-  k_push_spill<256><<<nblocks, 256, 0, st>>>(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C);
+                              int nblocks, int fast, cudaStream_t st) {
+  return fast ? launch_push_spill_fast(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C, nblocks, st)
+              : launch_push_spill_exact(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C, nblocks, st);
+}
+
+cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, const int *np,
+                            const LayoutConst &L, int ntiles, cudaStream_t st) {
+  k_cellsort<<<ntiles, 1024, 0, st>>>(src, dst, off, np, L);
   return cudaGetLastError();
 }
 
-cudaError_t launch_migrate(const Particles &pout, const TileSet &T, const Outbox &O, const Spill &S, int *err,
-                           int ntx, int nty, int mw, cudaStream_t st) {
-  k_migrate<256><<<ntx * nty, 256, 0, st>>>(pout, T, O, S, err, ntx, nty, mw);
+cudaError_t launch_settle(const Particles &buf, const TileSet &T, const Outbox &O, const Spill &S, int *err,
+                          int ntx, int nty, int mw, cudaStream_t st) {
+  k_migrate<256><<<ntx * nty, 256, 0, st>>>(buf, T, O, S, err, ntx, nty, mw);
   return cudaGetLastError();
 }
 
@@ -791,13 +411,13 @@ cudaError_t launch_scatter_list(const Particles &list, const int *n_ptr, int n_c
 }
 
 cudaError_t launch_tile_order(const Particles &src, const unsigned *key, const int *off, const int *np,
-                              const Particles &dst, int ntiles, int smax, int stride_p, cudaStream_t st) {
+                              const Particles &dst, int ntiles, int smax, const LayoutConst &L, cudaStream_t st) {
   const size_t sh = (size_t)smax * sizeof(unsigned long long);
   if (sh > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_tile_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
     if (e != cudaSuccess) return e;
   }
-  k_tile_order<<<ntiles, 1024, sh, st>>>(src, key, off, np, dst, smax, stride_p);
+  k_tile_order<<<ntiles, 1024, sh, st>>>(src, key, off, np, dst, smax, L);
   return cudaGetLastError();
 }
 

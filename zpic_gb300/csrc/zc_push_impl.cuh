@@ -1,0 +1,625 @@
+// zc_push_impl.cuh -- particle push + current deposit kernels.
+//
+// Included twice, inside namespaces zc::exact and zc::fast, by
+// zc_push_exact.cu (compiled with --fmad=false and IEEE division / square
+// root: every float32 operation rounds as in the reference C, particles
+// advanced from the same fields land on the same bits) and zc_push_fast.cu
+// (FMA contraction and the hardware's approximate float32 division and
+// square root: same algorithm, results within a few float32 ulps per
+// operation of the exact build).
+//
+//   k_push_tiles  one CTA per particle tile (TX x TY cells).  The tile's E/B
+//                 with a 1-lower / 2-upper cell halo arrive in shared memory
+//                 by one 3-D TMA box; every particle of the tile is pushed
+//                 (staggered bilinear gather, relativistic Boris, move) and
+//                 its current deposited with the zigzag scheme into a shared
+//                 J tile; the J tile is added to global J with one TMA
+//                 reduce-add.  Tiles are kept sorted by cell, so the lanes of
+//                 a warp mostly share a cell: their gathers are broadcasts,
+//                 and the current of the segment every particle starts with
+//                 (it lies in the particle's own cell) is summed across the
+//                 lanes of a cell with a segmented warp-shuffle reduction
+//                 before one lane per cell issues the shared-memory atomics.
+//                 Cell-crossing motions (a few per cent) wait in a per-warp
+//                 shared-memory queue and are split and deposited 32 at a
+//                 time, so the split code runs with full warps.  Particles
+//                 that stay are compacted in order; particles that leave go
+//                 to the tile's outbox, from which the destination tile pulls
+//                 them at the start of the next step's push.
+//   k_push_spill  the same physics for particles that did not fit a tile,
+//                 from global memory (normally empty).
+//
+// Requires zc_internal.cuh and zc_kernels.h to be included first.
+
+// ---------------------------------------------------------------------------
+// field / current accessors: shared-memory tile (1-cell lower halo) or the
+// global padded planes
+// ---------------------------------------------------------------------------
+template <int BW, int PL>
+struct TileFields {
+  const float *s;
+  __device__ __forceinline__ float operator()(int c, int i, int j) const {
+    return s[c * PL + (j + 1) * BW + (i + 1)];
+  }
+};
+template <int BW, int PL>
+struct TileCurrent {
+  float *s;
+  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
+    atomicAdd(&s[c * PL + (j + 1) * BW + (i + 1)], v);
+  }
+};
+struct GlobalFields {
+  const float *g;
+  int pitch;
+  size_t plane;
+  __device__ __forceinline__ float operator()(int c, int i, int j) const {
+    return __ldg(&g[c * plane + (size_t)(j + 1) * pitch + (i + 1)]);
+  }
+};
+struct GlobalCurrent {
+  float *g;
+  int pitch;
+  size_t plane;
+  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
+    atomicAdd(&g[c * plane + (size_t)(j + 1) * pitch + (i + 1)], v);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// per-particle physics (restates em2d/particles.c:773-924, 1029-1226)
+// ---------------------------------------------------------------------------
+template <class F>
+__device__ __forceinline__ float lerp2(const F &f, int c, int a, int b, float wa, float wb) {
+  return (f(c, a, b) * (1.0f - wa) + f(c, a + 1, b) * wa) * (1.0f - wb) +
+         (f(c, a, b + 1) * (1.0f - wa) + f(c, a + 1, b + 1) * wa) * wb;
+}
+
+struct Seg {
+  float x0, x1, y0, y1, dx, dy, qvz;
+  int ix, iy;
+};
+
+// the 8 current contributions of one straight segment inside one cell
+// (particles.c:886-922): Jx at (ix,iy),(ix,iy+1); Jy at (ix,iy),(ix+1,iy);
+// Jz at the four corners (ix,iy),(ix+1,iy),(ix,iy+1),(ix+1,iy+1)
+struct SegCurrent {
+  float v[8];
+};
+
+__device__ __forceinline__ SegCurrent segment_current(const Seg &s, float qnx, float qny) {
+  const float s0x0 = 1.0f - s.x0, s0x1 = s.x0;
+  const float s1x0 = 1.0f - s.x1, s1x1 = s.x1;
+  const float s0y0 = 1.0f - s.y0, s0y1 = s.y0;
+  const float s1y0 = 1.0f - s.y1, s1y1 = s.y1;
+  const float jx = qnx * s.dx;
+  const float jy = qny * s.dy;
+  const float ay0 = 0.5f * (s0y0 + s1y0), ay1 = 0.5f * (s0y1 + s1y1);
+  const float ax0 = 0.5f * (s0x0 + s1x0), ax1 = 0.5f * (s0x1 + s1x1);
+  const float q = s.qvz;
+  SegCurrent r;
+  r.v[0] = jx * ay0;
+  r.v[1] = jx * ay1;
+  r.v[2] = jy * ax0;
+  r.v[3] = jy * ax1;
+  r.v[4] = q * (s0x0 * s0y0 + s1x0 * s1y0 + (s0x0 * s1y0 - s1x0 * s0y0) / 2.0f);
+  r.v[5] = q * (s0x1 * s0y0 + s1x1 * s1y0 + (s0x1 * s1y0 - s1x1 * s0y0) / 2.0f);
+  r.v[6] = q * (s0x0 * s0y1 + s1x0 * s1y1 + (s0x0 * s1y1 - s1x0 * s0y1) / 2.0f);
+  r.v[7] = q * (s0x1 * s0y1 + s1x1 * s1y1 + (s0x1 * s1y1 - s1x1 * s0y1) / 2.0f);
+  return r;
+}
+
+template <class D>
+__device__ __forceinline__ void add_current(const D &dep, int ix, int iy, const SegCurrent &c) {
+  dep.add(0, ix, iy, c.v[0]);
+  dep.add(0, ix, iy + 1, c.v[1]);
+  dep.add(1, ix, iy, c.v[2]);
+  dep.add(1, ix + 1, iy, c.v[3]);
+  dep.add(2, ix, iy, c.v[4]);
+  dep.add(2, ix + 1, iy, c.v[5]);
+  dep.add(2, ix, iy + 1, c.v[6]);
+  dep.add(2, ix + 1, iy + 1, c.v[7]);
+}
+
+// splits segment `a` at the y cell edge: `a` keeps the part before the edge,
+// the returned segment holds the rest (particles.c:842-871)
+__device__ __forceinline__ Seg split_y(Seg &a, int dj) {
+  const int yb = (dj == 1);
+  const float f = (a.y1 - yb) / a.dy;
+  const float xc = a.x0 + a.dx * (1.0f - f);
+  Seg n;
+  n.y0 = 1 - yb;
+  n.y1 = a.y1 - dj;
+  n.dy = a.dy * f;
+  n.iy = a.iy + dj;
+  n.x0 = xc;
+  n.x1 = a.x1;
+  n.dx = a.dx * f;
+  n.ix = a.ix;
+  n.qvz = a.qvz * f;
+  a.y1 = yb;
+  a.dy *= (1.0f - f);
+  a.dx *= (1.0f - f);
+  a.x1 = xc;
+  a.qvz *= (1.0f - f);
+  return n;
+}
+
+// Zigzag trajectory split (particles.c:773-879): returns the first segment,
+// which always starts in the particle's own cell; the (at most two) further
+// segments of a cell-crossing motion are deposited right away.
+template <class D>
+__device__ __forceinline__ Seg zigzag_first(const D &dep, int ix, int iy, int di, int dj, float x0, float y0,
+                                            float dx, float dy, float qnx, float qny, float qvz) {
+  Seg a;
+  a.x0 = x0;
+  a.y0 = y0;
+  a.dx = dx;
+  a.dy = dy;
+  a.x1 = x0 + dx;
+  a.y1 = y0 + dy;
+  a.qvz = qvz * 0.5f;  // qvz/2.0 in the reference: exact halving either way
+  a.ix = ix;
+  a.iy = iy;
+  if (di != 0) {
+    const int xb = (di == 1);
+    const float f = (x0 + dx - xb) / dx;
+    const float yc = y0 + dy * (1.0f - f);
+    Seg b;
+    b.x0 = 1 - xb;
+    b.x1 = (x0 + dx) - di;
+    b.dx = dx * f;
+    b.ix = ix + di;
+    b.y0 = yc;
+    b.y1 = a.y1;
+    b.dy = dy * f;
+    b.iy = iy;
+    b.qvz = a.qvz * f;
+    a.x1 = xb;
+    a.dx *= (1.0f - f);
+    a.dy *= (1.0f - f);
+    a.y1 = yc;
+    a.qvz *= (1.0f - f);
+    if (dj != 0) {
+      if (a.y1 < 0.0f || a.y1 >= 1.0f) {
+        // the first piece crosses the y edge; the x tail lies past it
+        const Seg c = split_y(a, dj);
+        b.y0 -= dj;
+        b.y1 -= dj;
+        b.iy += dj;
+        add_current(dep, c.ix, c.iy, segment_current(c, qnx, qny));
+      } else {
+        const Seg c = split_y(b, dj);
+        add_current(dep, c.ix, c.iy, segment_current(c, qnx, qny));
+      }
+    }
+    add_current(dep, b.ix, b.iy, segment_current(b, qnx, qny));
+  } else if (dj != 0) {
+    const Seg c = split_y(a, dj);
+    add_current(dep, c.ix, c.iy, segment_current(c, qnx, qny));
+  }
+  return a;
+}
+
+// gather + Boris + move for one particle at cell (i, j) of the accessor
+// frame (particles.c:1029-1207); leaves the displacement in (mx, my) and the
+// cell shift in (di, dj), returns the kinetic-energy term utsq/(gamma+1).
+// `bad` flags a motion of one cell or more (or NaN), which the deposit does
+// not support.  A trimmed position of exactly 1.0f (x1 = -tiny, +1 rounds up)
+// is legal, as in the reference.
+template <class F>
+__device__ __forceinline__ float push_particle(const F &fld, int i, int j, float &x, float &y, float &ux,
+                                               float &uy, float &uz, float &mx, float &my, float &x1, float &y1,
+                                               int &di, int &dj, float &qvz, bool &bad, const PushConst &C) {
+  const int ih = i + ((x < 0.5f) ? -1 : 0);
+  const int jh = j + ((y < 0.5f) ? -1 : 0);
+  const float w1h = x + ((x < 0.5f) ? 0.5f : -0.5f);
+  const float w2h = y + ((y < 0.5f) ? 0.5f : -0.5f);
+  float ex = lerp2(fld, 0, ih, j, w1h, y);
+  float ey = lerp2(fld, 1, i, jh, x, w2h);
+  float ez = lerp2(fld, 2, i, j, x, y);
+  float bx = lerp2(fld, 3, i, jh, x, w2h);
+  float by = lerp2(fld, 4, ih, j, w1h, y);
+  float bz = lerp2(fld, 5, ih, jh, w1h, w2h);
+
+  const float tem = C.tem;
+  ex *= tem;
+  ey *= tem;
+  ez *= tem;
+  float tx = ux + ex, ty = uy + ey, tz = uz + ez;
+  const float u2 = tx * tx + ty * ty + tz * tz;
+  const float g = sqrtf(1.0f + u2);
+  const float kin = u2 / (g + 1);
+  const float tg = tem / g;
+  bx *= tg;
+  by *= tg;
+  bz *= tg;
+  const float s2 = 2.0f / (1.0f + bx * bx + by * by + bz * bz);
+  float vx = tx + ty * bz - tz * by;
+  float vy = ty + tz * bx - tx * bz;
+  float vz = tz + tx * by - ty * bx;
+  bx *= s2;
+  by *= s2;
+  bz *= s2;
+  tx += vy * bz - vz * by;
+  ty += vz * bx - vx * bz;
+  tz += vx * by - vy * bx;
+  ux = tx + ex;
+  uy = ty + ey;
+  uz = tz + ez;
+
+  const float rg = 1.0f / sqrtf(1.0f + ux * ux + uy * uy + uz * uz);
+  mx = C.dt_dx * rg * ux;
+  my = C.dt_dy * rg * uy;
+  bad = !(fabsf(mx) < 1.0f && fabsf(my) < 1.0f);
+  x1 = x + mx;
+  y1 = y + my;
+  di = (x1 >= 1.0f) - (x1 < 0.0f);
+  dj = (y1 >= 1.0f) - (y1 < 0.0f);
+  x1 -= di;
+  y1 -= dj;
+  qvz = C.q * uz * rg;
+  return kin;
+}
+
+// new cell after the move, window shift and boundary; false when the
+// particle left through an absorbing x boundary (particles.c:1234-1259)
+__device__ __forceinline__ bool apply_boundary(int &ix, int &iy, int di, int dj, const PushConst &C) {
+  ix += di - C.shift;
+  iy += dj;
+  iy += ((iy < 0) ? C.ny : 0) - ((iy >= C.ny) ? C.ny : 0);
+  if (C.mw) return ix >= 0 && ix < C.nx;
+  ix += ((ix < 0) ? C.nx : 0) - ((ix >= C.nx) ? C.nx : 0);
+  return true;
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// ---------------------------------------------------------------------------
+// K1: push + deposit, one CTA per tile.  The input of tile t is its own
+// particles plus the particles that the previous step posted for it in the
+// outboxes of its (up to 8) neighbouring tiles (`Oin`); leavers of this step
+// go to this tile's slot of `O`.  Stayers are compacted into the tile's
+// segment of `pout`: every warp reserves its slots with one shared-memory
+// atomic, so the lanes of a warp keep their (cell-sorted) order while the
+// order of the warps' runs follows their timing.  The main loop has no
+// block-wide barrier.
+// ---------------------------------------------------------------------------
+template <int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
+                                                   const __grid_constant__ CUtensorMap tm_j, Particles pin,
+                                                   Particles pout, TileSet T, Outbox Oin, Outbox O, Spill S,
+                                                   double *ekin_tile, int *err, PushConst C) {
+  constexpr int BW = (TX + 3 + 3) & ~3;  // halo box width, multiple of 4 floats
+  constexpr int BH = TY + 3;
+  constexpr int PL = BW * BH;
+  constexpr int NW = NT / 32;
+  __shared__ __align__(128) float sEB[6 * PL];
+  __shared__ __align__(128) float sJ[3 * PL];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double sred[NW];
+  // per-warp queue of cell-crossing motions, deposited 32 at a time so that
+  // the split code runs with full warps (QCAP = 2 x 32)
+  constexpr int QCAP = 64;
+  __shared__ float qf[NW][5][QCAP];  // x0, y0, dx, dy, qvz
+  __shared__ int qi[NW][QCAP];       // local cell and shifts, packed
+  __shared__ int nb[8], s_nnb;        // distinct neighbour tiles
+  __shared__ int s_stay, s_leave;     // output counters (warp-aggregated atomics)
+
+  const int t = blockIdx.x;
+  const int tx = t % C.ntx, ty = t / C.ntx;
+  const int cx0 = tx * TX, cy0 = ty * TY;  // first cell of the tile = buffer coords of its halo
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int errbits = 0;
+  int qcount = 0;  // warp-uniform
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    int c = 0;
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!dx && !dy) continue;
+        int x = tx + dx, y = ty + dy;
+        y += (y < 0) ? C.nty : 0;
+        y -= (y >= C.nty) ? C.nty : 0;
+        if (x < 0 || x >= C.ntx) {
+          if (C.mw) continue;
+          x = (x + C.ntx) % C.ntx;
+        }
+        const int id = x + y * C.ntx;
+        bool dup = (id == t);
+        for (int m = 0; m < c; ++m) dup |= (nb[m] == id);
+        if (!dup) nb[c++] = id;
+      }
+    s_nnb = c;
+    s_stay = 0;
+    s_leave = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&bar, 6 * PL * 4);
+    tma_load_3d(sEB, &tm_eb, cx0, cy0, 0, &bar);
+  }
+  for (int k = threadIdx.x; k < 3 * PL; k += NT) sJ[k] = 0.f;
+  const bool loaded = mbar_wait_bounded(&bar, 0);
+  if (!loaded) errbits |= ERR_TIMEOUT;
+  __syncthreads();
+
+  const TileFields<BW, PL> fld{sEB};
+  const TileCurrent<BW, PL> dep{sJ};
+  const long long base = T.off[t];
+  const int cap = T.cap[t];
+  const int n_own = T.np[t];
+  const long long obase = (long long)t * O.cap;
+  const int nnb = s_nnb;
+  float ks = 0.f, kc = 0.f;
+
+  // deposits queued motion e of this warp (all segments, direct atomics)
+  auto deposit_queued = [&](int e) {
+    const int w = qi[warp][e];
+    const int qli = w & 0xff, qlj = (w >> 8) & 0xff, qdi = ((w >> 16) & 3) - 1, qdj = ((w >> 18) & 3) - 1;
+    const Seg a = zigzag_first(dep, qli, qlj, qdi, qdj, qf[warp][0][e], qf[warp][1][e], qf[warp][2][e],
+                               qf[warp][3][e], C.qnx, C.qny, qf[warp][4][e]);
+    add_current(dep, a.ix, a.iy, segment_current(a, C.qnx, C.qny));
+  };
+
+  // one particle per lane: push, deposit, boundary, compaction; the 32 lanes
+  // of a warp call it together (warp-level collectives only)
+  auto process = [&](bool valid, int ix, int iy, float x, float y, float ux, float uy, float uz) {
+    int code = 0;  // 1 stays in the tile, 2 leaves it
+    int li = 0, lj = 0, dest = 0;
+    bool split = false;
+    float sx0 = 0.f, sy0 = 0.f, smx = 0.f, smy = 0.f, sqvz = 0.f;
+    int spk = 0;
+    SegCurrent cur;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cur.v[q] = 0.f;
+    if (valid) {
+      li = ix - cx0;
+      lj = iy - cy0;
+      if ((unsigned)li >= (unsigned)TX || (unsigned)lj >= (unsigned)TY) {
+        errbits |= ERR_ESCAPE;  // not in this tile: keep the accesses inside the halo
+        li = min(max(li, 0), TX - 1);
+        lj = min(max(lj, 0), TY - 1);
+        ix = cx0 + li;
+        iy = cy0 + lj;
+      }
+      float mx, my, x1, y1, qvz;
+      int di, dj;
+      bool bad;
+      const float kin = push_particle(fld, li, lj, x, y, ux, uy, uz, mx, my, x1, y1, di, dj, qvz, bad, C);
+      kahan_add(ks, kc, kin);
+      if (bad) errbits |= ERR_ESCAPE;
+      split = (di != 0) || (dj != 0);
+      if (split) {
+        sx0 = x;
+        sy0 = y;
+        smx = mx;
+        smy = my;
+        sqvz = qvz;
+        spk = li | (lj << 8) | ((di + 1) << 16) | ((dj + 1) << 18);
+      } else {
+        // the whole motion stays in the cell: one segment (particles.c:781-797)
+        Seg a;
+        a.x0 = x;
+        a.y0 = y;
+        a.dx = mx;
+        a.dy = my;
+        a.x1 = x + mx;
+        a.y1 = y + my;
+        a.qvz = qvz * 0.5f;
+        a.ix = li;
+        a.iy = lj;
+        cur = segment_current(a, C.qnx, C.qny);
+      }
+      x = x1;
+      y = y1;
+      if (apply_boundary(ix, iy, di, dj, C)) {
+        dest = ix / TX + (iy / TY) * C.ntx;
+        code = (dest == t) ? 1 : 2;
+      }
+    }
+
+    // segmented warp reduction of the single-segment currents over runs of
+    // lanes that start in the same cell (the runs are contiguous because
+    // the tile is sorted by cell; unsorted input only makes runs shorter)
+    {
+      const int key = valid ? (li + lj * TX) : -1 - lane;
+      const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+      const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+      const unsigned lastmask = __ballot_sync(0xffffffffu, lane == 31 || knext != key);
+      const int run_last = __ffs(lastmask & (0xffffffffu << lane)) - 1;
+      const unsigned longrun = __ballot_sync(0xffffffffu, run_last > lane);
+      if (longrun) {
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const bool take = lane + off <= run_last;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float o = __shfl_down_sync(0xffffffffu, cur.v[q], off);
+            if (take) cur.v[q] += o;
+          }
+        }
+      }
+      const bool head = valid && (lane == 0 || kprev != key);
+      if (head) add_current(dep, li, lj, cur);
+    }
+
+    // queue the cell-crossing motions; deposit them once a full warp's worth
+    // is waiting
+    {
+      const unsigned sm = __ballot_sync(0xffffffffu, split);
+      if (sm) {
+        if (split) {
+          const int e = qcount + __popc(sm & ((1u << lane) - 1));
+          qf[warp][0][e] = sx0;
+          qf[warp][1][e] = sy0;
+          qf[warp][2][e] = smx;
+          qf[warp][3][e] = smy;
+          qf[warp][4][e] = sqvz;
+          qi[warp][e] = spk;
+        }
+        qcount += __popc(sm);
+        __syncwarp();
+        if (qcount >= 32) {
+          qcount -= 32;
+          deposit_queued(qcount + lane);
+          __syncwarp();
+        }
+      }
+    }
+
+    // output slots: one shared-memory atomic per warp and kind; lanes keep
+    // their order inside the warp's run
+    const unsigned mstay = __ballot_sync(0xffffffffu, code == 1);
+    const unsigned mleave = __ballot_sync(0xffffffffu, code == 2);
+    int sb = 0, lb = 0;
+    if (lane == 0) {
+      if (mstay) sb = atomicAdd(&s_stay, __popc(mstay));
+      if (mleave) lb = atomicAdd(&s_leave, __popc(mleave));
+    }
+    sb = __shfl_sync(0xffffffffu, sb, 0);
+    lb = __shfl_sync(0xffffffffu, lb, 0);
+    const unsigned below = (1u << lane) - 1;
+    if (code == 1) {
+      const int s = sb + __popc(mstay & below);
+      if (s < cap) store_particle(pout, base + s, ix, iy, x, y, ux, uy, uz);
+      else spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
+    } else if (code == 2) {
+      const int s = lb + __popc(mleave & below);
+      if (s < O.cap) {
+        store_particle(O.p, obase + s, ix, iy, x, y, ux, uy, uz);
+        O.dst[obase + s] = dest;
+      } else {
+        spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
+      }
+    }
+  };
+
+  // own particles: warp w takes chunks w, w + NW, ... of 32
+  for (int k0 = warp * 32; k0 < n_own; k0 += NT) {
+    const int k = k0 + lane;
+    const bool valid = k < n_own;
+    const long long g = base + (valid ? k : 0);
+    process(valid, valid ? pin.ix[g] : 0, valid ? pin.iy[g] : 0, valid ? pin.x[g] : 0.f, valid ? pin.y[g] : 0.f,
+            valid ? pin.ux[g] : 0.f, valid ? pin.uy[g] : 0.f, valid ? pin.uz[g] : 0.f);
+  }
+
+  // incoming particles: the warps walk the neighbours' outboxes in chunks of
+  // 32 slots and push the ones bound for this tile
+  for (int m = 0; m < nnb; ++m) {
+    const int src = nb[m];
+    const int n = Oin.cnt[src];
+    const long long ob = (long long)src * Oin.cap;
+    for (int e0 = warp * 32; e0 < n; e0 += NT) {
+      const int e = e0 + lane;
+      const bool valid = e < n && Oin.dst[ob + e] == t;
+      if (!__any_sync(0xffffffffu, valid)) continue;
+      const long long q = ob + (valid ? e : 0);
+      process(valid, valid ? Oin.p.ix[q] : 0, valid ? Oin.p.iy[q] : 0, valid ? Oin.p.x[q] : 0.f,
+              valid ? Oin.p.y[q] : 0.f, valid ? Oin.p.ux[q] : 0.f, valid ? Oin.p.uy[q] : 0.f,
+              valid ? Oin.p.uz[q] : 0.f);
+    }
+  }
+
+  if (lane < qcount) deposit_queued(lane);  // what is left in the queue
+
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T.np[t] = min(s_stay, cap);
+    O.cnt[t] = min(s_leave, O.cap);
+  }
+  const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
+  if (threadIdx.x == 0) ekin_tile[t] = e;
+
+  // all shared-memory atomics done: hand the J tile to the TMA unit
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (loaded) {
+      tma_reduce_add_3d(&tm_j, sJ, cx0, cy0, 0);
+      bulk_commit();
+      bulk_wait_read0();
+    } else if (!mbar_wait_bounded(&bar, 0)) {
+      errbits |= ERR_TIMEOUT;  // second bounded wait for the load still in flight
+    }
+  }
+  if (errbits) atomicOr(err, errbits);
+}
+
+// ---------------------------------------------------------------------------
+// spill push: same physics from global memory (rarely non-empty)
+// ---------------------------------------------------------------------------
+template <int NT>
+__global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Grid G, Particles sin,
+                                                   const int *sin_cnt, int sin_cap, Spill S, double *ekin,
+                                                   int *err, PushConst C) {
+  __shared__ double sred[NT / 32];
+  const int n = min(*sin_cnt, sin_cap);
+  const GlobalFields fld{EB, G.pitch, G.plane};
+  const GlobalCurrent dep{J, G.pitch, G.plane};
+  int errbits = 0;
+  float ks = 0.f, kc = 0.f;
+  for (int k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
+    int ix = sin.ix[k], iy = sin.iy[k];
+    float x = sin.x[k], y = sin.y[k], ux = sin.ux[k], uy = sin.uy[k], uz = sin.uz[k];
+    if (ix < 0 || ix >= C.nx || iy < 0 || iy >= C.ny) {
+      errbits |= ERR_ESCAPE;
+      ix = min(max(ix, 0), C.nx - 1);
+      iy = min(max(iy, 0), C.ny - 1);
+    }
+    float mx, my, x1, y1, qvz;
+    int di, dj;
+    bool bad;
+    const float kin = push_particle(fld, ix, iy, x, y, ux, uy, uz, mx, my, x1, y1, di, dj, qvz, bad, C);
+    if (bad) errbits |= ERR_ESCAPE;
+    kahan_add(ks, kc, kin);
+    const Seg a = zigzag_first(dep, ix, iy, di, dj, x, y, mx, my, C.qnx, C.qny, qvz);
+    add_current(dep, ix, iy, segment_current(a, C.qnx, C.qny));
+    x = x1;
+    y = y1;
+    if (apply_boundary(ix, iy, di, dj, C)) spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
+  }
+  const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
+  if (threadIdx.x == 0 && e != 0.0) atomicAdd(ekin, e);
+  if (errbits) atomicOr(err, errbits);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <int TX, int TY>
+static cudaError_t launch_push_t(const PushLaunch &a, cudaStream_t st) {
+  constexpr int NT = (TX * TY >= 256) ? 256 : 128;
+  k_push_tiles<TX, TY, NT><<<a.ntiles, NT, 0, st>>>(*a.tm_eb, *a.tm_j, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
+                                                     a.ekin_tile, a.err, a.C);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_push_tiles_variant(const PushLaunch &a, cudaStream_t st) {
+  const int TX = a.TX, TY = a.TY;
+#define ZC_TILE(X, Y) \
+  if (TX == X && TY == Y) return launch_push_t<X, Y>(a, st);
+  ZC_TILE(16, 16)
+  ZC_TILE(8, 8)
+  ZC_TILE(16, 8)
+  ZC_TILE(32, 16)
+  ZC_TILE(32, 32)
+  ZC_TILE(8, 16)
+  ZC_TILE(16, 32)
+#undef ZC_TILE
+  return cudaErrorInvalidValue;
+}
+
+static cudaError_t launch_push_spill_variant(const float *EB, float *J, const Grid &G, const Particles &sin,
+                                             const int *sin_cnt, int sin_cap, const Spill &S, double *ekin,
+                                             int *err, const PushConst &C, int nblocks, cudaStream_t st) {
+  k_push_spill<256><<<nblocks, 256, 0, st>>>(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C);
+  return cudaGetLastError();
+}
