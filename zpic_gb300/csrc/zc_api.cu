@@ -86,24 +86,14 @@ void dfree(T *&p) {
 }
 
 zc_status alloc_particles(Particles &p, long long n) {
-  TRY(dalloc(&p.ix, n));
-  TRY(dalloc(&p.iy, n));
-  TRY(dalloc(&p.x, n));
-  TRY(dalloc(&p.y, n));
-  TRY(dalloc(&p.ux, n));
-  TRY(dalloc(&p.uy, n));
-  TRY(dalloc(&p.uz, n));
+  TRY(dalloc(&p.u, n));
+  TRY(dalloc(&p.xy, n));
   return ZC_OK;
 }
 
 void free_particles(Particles &p) {
-  dfree(p.ix);
-  dfree(p.iy);
-  dfree(p.x);
-  dfree(p.y);
-  dfree(p.ux);
-  dfree(p.uy);
-  dfree(p.uz);
+  dfree(p.u);
+  dfree(p.xy);
 }
 
 struct SpeciesState {
@@ -539,33 +529,33 @@ zc_status current_update_impl(zc_sim *s) {
     Phase ph(s, ZC_PHASE_FOLD, s->mw ? 1 : 2);
     CK(launch_fold(s->J[0], s->G, s->mw, st));
   }
-  int c = 0;
-  auto px = [&](float a, float b) -> zc_status {
-    Phase ph(s, ZC_PHASE_SMOOTH, 1);
-    CK(launch_smooth_x(s->J[c], s->J[1 - c], s->G, a, b, s->mw, st));
-    c = 1 - c;
-    return ZC_OK;
-  };
-  auto py = [&](float a, float b) -> zc_status {
-    Phase ph(s, ZC_PHASE_SMOOTH, 1);
-    CK(launch_smooth_y(s->J[c], s->J[1 - c], s->G, a, b, st));
-    c = 1 - c;
-    return ZC_OK;
-  };
+  // pass coefficients (current_smooth, em2d/current.c:427-459; the y
+  // binomial pass count is xlevel, as at current.c:449)
+  SmoothPasses px{}, py{};
   float sa, sb;
   if (s->xtype != 0) {
-    for (int i = 0; i < s->xlevel; ++i) TRY(px(0.25f, 0.5f));
+    for (int i = 0; i < s->xlevel; ++i) px.sa[px.n] = 0.25f, px.sb[px.n++] = 0.5f;
     if (s->xtype == 2) {
       smooth_comp(s->xlevel, &sa, &sb);
-      TRY(px(sa, sb));
+      px.sa[px.n] = sa, px.sb[px.n++] = sb;
     }
   }
   if (s->ytype != 0) {
-    for (int i = 0; i < s->xlevel; ++i) TRY(py(0.25f, 0.5f));  // xlevel, as em2d/current.c:449
+    for (int i = 0; i < s->xlevel; ++i) py.sa[py.n] = 0.25f, py.sb[py.n++] = 0.5f;
     if (s->ytype == 2) {
       smooth_comp(s->ylevel, &sa, &sb);
-      TRY(py(sa, sb));
+      py.sa[py.n] = sa, py.sb[py.n++] = sb;
     }
+  }
+  int c = 0;
+  if (px.n > 0) {
+    Phase ph(s, ZC_PHASE_SMOOTH, 1);
+    CK(launch_smooth_x_all(s->J[0], s->G, px, s->mw, st));
+  }
+  if (py.n > 0) {
+    Phase ph(s, ZC_PHASE_SMOOTH, 1);
+    CK(launch_smooth_y_all(s->J[0], s->J[1], s->G, py, st));
+    c = 1;
   }
   s->j_cur = c;
   return ZC_OK;
@@ -683,7 +673,8 @@ zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
     return fail(ZC_EINVAL, "Invalid timestep, courant condition violation, dtmax = %f", cour);
   int TX = d->tile[0] > 0 ? d->tile[0] : 16, TY = d->tile[1] > 0 ? d->tile[1] : 16;
   if (!tile_supported(TX, TY)) return fail(ZC_EINVAL, "unsupported tile size %d x %d", TX, TY);
-  if ((long long)(d->nx[0] + 3) * (d->nx[1] + 3) > (1LL << 30)) return fail(ZC_EINVAL, "grid too large");
+  if ((long long)(d->nx[0] + 3) * (d->nx[1] + 3) > (1LL << 30) || d->nx[0] > 65535 || d->nx[1] > 65535)
+    return fail(ZC_EINVAL, "grid too large (at most 65535 cells per axis, 2^30 cells)");
   TRY(load_encoder());
 
   zc_sim *s = new zc_sim();
@@ -947,6 +938,8 @@ zc_status zc_set_smooth(zc_sim *s, int xtype, int xlevel, int ytype, int ylevel)
   // em2d/simulation.c:136-144
   if (xtype != 0 && xlevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along x direction");
   if (ytype != 0 && ylevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along y direction");
+  if ((xtype != 0 && xlevel >= kMaxSmoothPasses) || (ytype != 0 && xlevel >= kMaxSmoothPasses))
+    return fail(ZC_EINVAL, "smoothing level above %d is not supported", kMaxSmoothPasses - 1);
   s->xtype = xtype;
   s->xlevel = xlevel;
   s->ytype = ytype;

@@ -114,6 +114,121 @@ __global__ void k_smooth_y(const float *Jin, float *Jout, Grid G, float sa, floa
 }
 
 // ---------------------------------------------------------------------------
+// all filter passes along one axis in one kernel.  Passes along x act on
+// every interior row independently: a CTA loads its row (guards included)
+// into shared memory, runs the passes there -- refreshing the periodic x
+// guards after each pass unless the window moves, as kernel_x does -- and
+// writes the row back in place.  Passes along y are periodic convolutions
+// over the interior rows (kernel_y refreshes the y guards after each pass),
+// except that the first pass reads the y guard rows as they are (the x
+// passes leave them at their pre-filter values): a CTA takes a strip of 32
+// columns and ROWS rows plus one halo row per pass on each side, runs the
+// passes in shared memory and writes its rows (and the y guard rows they
+// feed) out of place.  Every cell sees the same float
+// operations in the same order as with one kernel per pass.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_smooth_x_all(float *J, Grid G, SmoothPasses P, int mw) {
+  extern __shared__ float srow[];  // [2][3][gx]
+  const int gx = G.nx + 3;
+  const int by = blockIdx.x + 1;   // interior row
+  for (int c = 0; c < 3; ++c)
+    for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) srow[c * gx + bx] = J[gidx(G, c, bx, by)];
+  __syncthreads();
+  int cur = 0;
+  for (int p = 0; p < P.n; ++p) {
+    const float sa = P.sa[p], sb = P.sb[p];
+    for (int c = 0; c < 3; ++c) {
+      const float *r = srow + (cur * 3 + c) * gx;
+      float *o = srow + ((1 - cur) * 3 + c) * gx;
+      for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) {
+        float v;
+        if (bx >= 1 && bx <= G.nx) v = f3pt(sa, sb, r[bx - 1], r[bx], r[bx + 1]);
+        else if (mw) v = r[bx];
+        else {
+          const int s = (bx == 0) ? G.nx : bx - G.nx;  // guard <- filtered interior value
+          v = f3pt(sa, sb, r[s - 1], r[s], r[s + 1]);
+        }
+        o[bx] = v;
+      }
+    }
+    __syncthreads();
+    cur = 1 - cur;
+  }
+  for (int c = 0; c < 3; ++c)
+    for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) J[gidx(G, c, bx, by)] = srow[(cur * 3 + c) * gx + bx];
+}
+
+constexpr int kSmoothYRows = 64;   // interior rows per CTA
+constexpr int kSmoothYCols = 32;   // columns per CTA (one warp across)
+
+__global__ void __launch_bounds__(256) k_smooth_y_all(const float *Jin, float *Jout, Grid G, SmoothPasses P) {
+  extern __shared__ float sbuf[];  // [2][3][ROWS + 2H][COLS], then guard rows [2][3][COLS]
+  const int H = P.n;
+  const int R = kSmoothYRows + 2 * H;
+  constexpr int W = kSmoothYCols;
+  const int gx = G.nx + 3;
+  const int cc = threadIdx.x & 31, r0 = threadIdx.x >> 5;   // column, first row of this thread
+  const int bx = blockIdx.x * W + cc;
+  const bool col_ok = bx < gx;
+  const bool filt = bx >= 1 && bx <= G.nx;                   // only interior columns are filtered
+  const int j0 = blockIdx.y * kSmoothYRows;                  // first interior row of the strip
+  float *glo = sbuf + 6 * R * W, *ghi = glo + 3 * W;         // y guard rows -1 and ny as stored
+  if (r0 == 0)
+    for (int c = 0; c < 3; ++c) {
+      glo[c * W + cc] = col_ok ? Jin[gidx(G, c, bx, 0)] : 0.f;
+      ghi[c * W + cc] = col_ok ? Jin[gidx(G, c, bx, G.ny + 1)] : 0.f;
+    }
+  // rows j0-H .. j0+ROWS+H-1, wrapped periodically over the interior rows
+  for (int rr = r0; rr < R; rr += 8) {
+    int j = (j0 - H + rr) % G.ny;
+    if (j < 0) j += G.ny;
+    for (int c = 0; c < 3; ++c) sbuf[(c * R + rr) * W + cc] = col_ok ? Jin[gidx(G, c, bx, j + 1)] : 0.f;
+  }
+  __syncthreads();
+  int cur = 0;
+  for (int p = 0; p < P.n; ++p) {
+    const float sa = P.sa[p], sb = P.sb[p];
+    const float *in = sbuf + cur * 3 * R * W;
+    float *out = sbuf + (1 - cur) * 3 * R * W;
+    for (int rr = r0; rr < R; rr += 8) {
+      bool lo_guard = false, hi_guard = false;
+      if (p == 0) {
+        int jm = (j0 - H + rr) % G.ny;
+        if (jm < 0) jm += G.ny;
+        lo_guard = (jm == 0);
+        hi_guard = (jm == G.ny - 1);
+      }
+      const bool inside = rr > p && rr < R - 1 - p;
+      for (int c = 0; c < 3; ++c) {
+        const int k = (c * R + rr) * W + cc;
+        float v = in[k];
+        if (inside && filt) {
+          const float lo = lo_guard ? glo[c * W + cc] : in[k - W];
+          const float hi = hi_guard ? ghi[c * W + cc] : in[k + W];
+          v = f3pt(sa, sb, lo, in[k], hi);
+        }
+        out[k] = v;
+      }
+    }
+    __syncthreads();
+    cur = 1 - cur;
+  }
+  if (!col_ok) return;
+  const float *res = sbuf + cur * 3 * R * W;
+  for (int rr = r0; rr < kSmoothYRows; rr += 8) {
+    const int j = j0 + rr;
+    if (j >= G.ny) break;
+    for (int c = 0; c < 3; ++c) {
+      const float v = res[(c * R + rr + H) * W + cc];
+      Jout[gidx(G, c, bx, j + 1)] = v;
+      // y guard rows are periodic copies of the filtered interior rows
+      if (j == G.ny - 1) Jout[gidx(G, c, bx, 0)] = v;
+      if (j < 2) Jout[gidx(G, c, bx, G.ny + 1 + j)] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // fused Yee advance: B half step, E full step, B half step
 // (yee_b / yee_e, em2d/emf.c:500-562), one 32 x 16 output tile per CTA.
 // E/B and J tiles with their halo arrive by TMA; B1 and E1 live in shared
@@ -382,6 +497,28 @@ cudaError_t launch_smooth_x(const float *Jin, float *Jout, const Grid &G, float 
 
 cudaError_t launch_smooth_y(const float *Jin, float *Jout, const Grid &G, float sa, float sb, cudaStream_t st) {
   k_smooth_y<<<grid_rows(G, 256), 256, 0, st>>>(Jin, Jout, G, sa, sb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth_x_all(float *J, const Grid &G, const SmoothPasses &P, int mw, cudaStream_t st) {
+  const size_t sh = sizeof(float) * 6 * (size_t)(G.nx + 3);
+  if (sh > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_smooth_x_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+    if (e != cudaSuccess) return e;
+  }
+  k_smooth_x_all<<<G.ny, 256, sh, st>>>(J, G, P, mw);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth_y_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &P,
+                                cudaStream_t st) {
+  const size_t sh = sizeof(float) * 6 * ((size_t)(kSmoothYRows + 2 * P.n) + 1) * kSmoothYCols;
+  if (sh > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_smooth_y_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+    if (e != cudaSuccess) return e;
+  }
+  dim3 grid((G.nx + 3 + kSmoothYCols - 1) / kSmoothYCols, (G.ny + kSmoothYRows - 1) / kSmoothYRows);
+  k_smooth_y_all<<<grid, 256, sh, st>>>(Jin, Jout, G, P);
   return cudaGetLastError();
 }
 

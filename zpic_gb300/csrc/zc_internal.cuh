@@ -11,12 +11,15 @@
 //   E and B share one 6-plane allocation (Ex Ey Ez Bx By Bz) so the particle
 //   kernel stages both with a single 3-D TMA box.
 //
-// Particle layout (one species): structure of arrays ix, iy (int32 cell),
-// x, y (float32 in-cell position in [0,1)), ux, uy, uz (float32 proper
-// velocity) -- the same quantities as t_part (em2d/particles.h:29-37) --
-// partitioned into rectangular tiles of TX x TY cells.  Tile t owns the
-// contiguous segment [off[t], off[t] + cap[t]) of every array and holds np[t]
-// particles at its start.  Two copies (A, B) alternate every step.
+// Particle layout (one species): two arrays of 16- and 8-byte records,
+//   u[k]  = (ux, uy, uz, cell)   float32 proper velocity; the cell indices
+//           ix | iy << 16 stored in the bits of the fourth word
+//   xy[k] = (x, y)               float32 in-cell position in [0, 1]
+// -- the same quantities as t_part (em2d/particles.h:29-37), 24 bytes per
+// particle moved with two vector accesses -- partitioned into rectangular
+// tiles of TX x TY cells.  Tile t owns the contiguous segment
+// [off[t], off[t] + cap[t]) and holds np[t] particles at its start.  Two
+// copies (A, B) alternate every step.
 #pragma once
 
 #include <cuda.h>
@@ -33,10 +36,49 @@ enum : int {
   ERR_SPILLED = 8,       // particles went to the spill buffer (host re-layout due)
 };
 
-struct Particles {       // SoA view of one particle buffer
-  int *ix, *iy;
-  float *x, *y, *ux, *uy, *uz;
+struct Particles {       // one particle buffer
+  float4 *u;             // ux, uy, uz, packed cell
+  float2 *xy;            // x, y
 };
+
+struct PRec {            // one particle in registers
+  int ix, iy;
+  float x, y, ux, uy, uz;
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ PRec load_particle(const Particles &p, long long k) {
+  const float4 u = p.u[k];
+  const float2 r = p.xy[k];
+  const unsigned c = (unsigned)__float_as_int(u.w);
+  PRec q;
+  q.ix = (int)(c & 0xffffu);
+  q.iy = (int)(c >> 16);
+  q.x = r.x;
+  q.y = r.y;
+  q.ux = u.x;
+  q.uy = u.y;
+  q.uz = u.z;
+  return q;
+}
+
+__device__ __forceinline__ void load_cell(const Particles &p, long long k, int &ix, int &iy) {
+  const unsigned c = (unsigned)__float_as_int(p.u[k].w);
+  ix = (int)(c & 0xffffu);
+  iy = (int)(c >> 16);
+}
+
+// cells are in [0, 65535] (grids are limited to 65535 cells per axis)
+__device__ __forceinline__ void store_particle(const Particles &p, long long k, int ix, int iy, float x, float y,
+                                               float ux, float uy, float uz) {
+  p.u[k] = make_float4(ux, uy, uz, __int_as_float((int)((unsigned)ix | ((unsigned)iy << 16))));
+  p.xy[k] = make_float2(x, y);
+}
+
+__device__ __forceinline__ void store_particle(const Particles &p, long long k, const PRec &q) {
+  store_particle(p, k, q.ix, q.iy, q.x, q.y, q.ux, q.uy, q.uz);
+}
+#endif
 
 struct Grid {            // geometry of the padded SoA grids
   int nx, ny;            // interior cells

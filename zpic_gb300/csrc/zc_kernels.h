@@ -51,17 +51,6 @@ struct PushLaunch {
 };
 
 #ifdef __CUDACC__
-__device__ __forceinline__ void store_particle(const Particles &p, long long k, int ix, int iy, float x, float y,
-                                               float ux, float uy, float uz) {
-  p.ix[k] = ix;
-  p.iy[k] = iy;
-  p.x[k] = x;
-  p.y[k] = y;
-  p.ux[k] = ux;
-  p.uy[k] = uy;
-  p.uz[k] = uz;
-}
-
 // appends a particle to a spill list; flags the host (re-layout due) and
 // records an overflow when the list is full
 __device__ __forceinline__ void spill_particle(const Spill &S, int *errbits, int ix, int iy, float x, float y,
@@ -70,6 +59,10 @@ __device__ __forceinline__ void spill_particle(const Spill &S, int *errbits, int
   *errbits |= ERR_SPILLED;
   if (q < S.cap) store_particle(S.p, q, ix, iy, x, y, ux, uy, uz);
   else *errbits |= ERR_OVERFLOW;
+}
+
+__device__ __forceinline__ void spill_particle(const Spill &S, int *errbits, const PRec &r) {
+  spill_particle(S, errbits, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
 }
 #endif
 
@@ -128,6 +121,15 @@ cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st);
 cudaError_t launch_smooth_x(const float *Jin, float *Jout, const Grid &G, float sa, float sb, int mw,
                             cudaStream_t st);
 cudaError_t launch_smooth_y(const float *Jin, float *Jout, const Grid &G, float sa, float sb, cudaStream_t st);
+// all filter passes along one axis in one launch
+constexpr int kMaxSmoothPasses = 16;
+struct SmoothPasses {
+  int n;
+  float sa[kMaxSmoothPasses], sb[kMaxSmoothPasses];
+};
+cudaError_t launch_smooth_x_all(float *J, const Grid &G, const SmoothPasses &P, int mw, cudaStream_t st);
+cudaError_t launch_smooth_y_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &P,
+                                cudaStream_t st);
 cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
                        const YeeConst &Y, int *err, cudaStream_t st);
 cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st);

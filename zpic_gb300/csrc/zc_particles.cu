@@ -65,11 +65,9 @@ __global__ void __launch_bounds__(NT) k_migrate(Particles pout, TileSet T, Outbo
         const long long q = ob + e;
         const int s = placed + pre;
         if (s < room)
-          store_particle(pout, start + s, O.p.ix[q], O.p.iy[q], O.p.x[q], O.p.y[q], O.p.ux[q], O.p.uy[q],
-                         O.p.uz[q]);
+          store_particle(pout, start + s, load_particle(O.p, q));
         else
-          spill_particle(S, &errbits, O.p.ix[q], O.p.iy[q], O.p.x[q], O.p.y[q], O.p.ux[q], O.p.uy[q],
-                         O.p.uz[q]);
+          spill_particle(S, &errbits, load_particle(O.p, q));
       }
       placed += tot;
     }
@@ -98,13 +96,8 @@ __global__ void k_stage_to_list(const float4 *aos7, int n, Particles list, int *
       ix = min(max(ix, 0), L.nx - 1);
       iy = min(max(iy, 0), L.ny - 1);
     }
-    list.ix[k] = ix;
-    list.iy[k] = iy;
-    list.x[k] = __int_as_float(r[2]);
-    list.y[k] = __int_as_float(r[3]);
-    list.ux[k] = __int_as_float(r[4]);
-    list.uy[k] = __int_as_float(r[5]);
-    list.uz[k] = __int_as_float(r[6]);
+    store_particle(list, k, ix, iy, __int_as_float(r[2]), __int_as_float(r[3]), __int_as_float(r[4]),
+                   __int_as_float(r[5]), __int_as_float(r[6]));
     atomicAdd(&cnt[tile_of(ix, iy, L)], 1);
   }
 }
@@ -113,7 +106,11 @@ __global__ void k_stage_to_list(const float4 *aos7, int n, Particles list, int *
 __global__ void k_count_list(Particles list, const int *n_ptr, int n_cap, int *cnt, LayoutConst L) {
   const int n = min(*n_ptr, n_cap);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-    atomicAdd(&cnt[tile_of(list.ix[k], list.iy[k], L)], 1);
+  {
+    int ix, iy;
+    load_cell(list, k, ix, iy);
+    atomicAdd(&cnt[tile_of(ix, iy, L)], 1);
+  }
 }
 
 // tile particles keep their tile and their order: copy to the new offsets
@@ -123,8 +120,7 @@ __global__ void k_copy_tiles(Particles src, const int *off_old, const int *np_ol
   const int n = np_old[t];
   const long long a = off_old[t], b = off_new[t];
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    store_particle(dst, b + k, src.ix[a + k], src.iy[a + k], src.x[a + k], src.y[a + k], src.ux[a + k],
-                   src.uy[a + k], src.uz[a + k]);
+    store_particle(dst, b + k, load_particle(src, a + k));
     if (key) key[b + k] = (unsigned)k;
   }
   if (threadIdx.x == 0) fill[t] = n;
@@ -136,12 +132,12 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
                                int *err) {
   const int n = min(*n_ptr, n_cap);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int t = tile_of(list.ix[k], list.iy[k], L);
+    const PRec r = load_particle(list, k);
+    const int t = tile_of(r.ix, r.iy, L);
     const int s = atomicAdd(&fill[t], 1);
     if (s < cap[t]) {
       const long long q = (long long)off[t] + s;
-      store_particle(dst, q, list.ix[k], list.iy[k], list.x[k], list.y[k], list.ux[k], list.uy[k],
-                     list.uz[k]);
+      store_particle(dst, q, r);
       if (key) key[q] = key0 + (unsigned)k;
     } else {
       atomicOr(err, ERR_OVERFLOW);  // capacities are sized from exact counts: cannot happen
@@ -169,7 +165,9 @@ __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst,
   for (int c = threadIdx.x; c < ncell; c += 1024) cursor[c] = 0;
   __syncthreads();
   auto cell_of = [&](long long g) {
-    const int c = (src.ix[g] - cx0) + (src.iy[g] - cy0) * L.TX;
+    int ix, iy;
+    load_cell(src, g, ix, iy);
+    const int c = (ix - cx0) + (iy - cy0) * L.TX;
     return min(max(c, 0), ncell - 1);
   };
   for (int k = threadIdx.x; k < n; k += 1024) atomicAdd(&cursor[cell_of(b + k)], 1);
@@ -184,7 +182,7 @@ __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst,
   for (int k = threadIdx.x; k < n; k += 1024) {
     const long long s = b + k;
     const int slot = atomicAdd(&cursor[cell_of(s)], 1);
-    store_particle(dst, b + slot, src.ix[s], src.iy[s], src.x[s], src.y[s], src.ux[s], src.uy[s], src.uz[s]);
+    store_particle(dst, b + slot, load_particle(src, s));
   }
 }
 
@@ -206,7 +204,9 @@ __global__ void k_tile_order(Particles src, const unsigned *key, const int *off,
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
       unsigned long long v = ~0ull;
       if (k < n) {
-        const unsigned cell = (unsigned)((src.ix[b + k] - cx0) + (src.iy[b + k] - cy0) * L.TX) & 0xfffu;
+        int ix, iy;
+        load_cell(src, b + k, ix, iy);
+        const unsigned cell = (unsigned)((ix - cx0) + (iy - cy0) * L.TX) & 0xfffu;
         v = ((unsigned long long)cell << 52) | ((unsigned long long)(key[b + k] & 0xffffffffu) << 20) |
             (unsigned)k;
       }
@@ -232,7 +232,7 @@ __global__ void k_tile_order(Particles src, const unsigned *key, const int *off,
   for (int p = threadIdx.x; p < n; p += blockDim.x) {
     const int from = sorted ? (int)(sk[p] & 0xfffffu) : p;
     const long long s = b + from, d = b + p;
-    store_particle(dst, d, src.ix[s], src.iy[s], src.x[s], src.y[s], src.ux[s], src.uy[s], src.uz[s]);
+    store_particle(dst, d, load_particle(src, s));
   }
 }
 
@@ -242,18 +242,17 @@ __global__ void k_append_list(Particles list, int n, Particles buf, TileSet T, S
                               int *err) {
   int errbits = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    int ix = list.ix[k], iy = list.iy[k];
-    if (ix < 0 || ix >= L.nx || iy < 0 || iy >= L.ny) {
+    const PRec r = load_particle(list, k);
+    if (r.ix < 0 || r.ix >= L.nx || r.iy < 0 || r.iy >= L.ny) {
       errbits |= ERR_ESCAPE;
       continue;
     }
-    const int t = tile_of(ix, iy, L);
+    const int t = tile_of(r.ix, r.iy, L);
     const int s = atomicAdd(&T.np[t], 1);
     if (s < T.cap[t])
-      store_particle(buf, (long long)T.off[t] + s, ix, iy, list.x[k], list.y[k], list.ux[k], list.uy[k],
-                     list.uz[k]);
+      store_particle(buf, (long long)T.off[t] + s, r);
     else
-      spill_particle(S, &errbits, ix, iy, list.x[k], list.y[k], list.ux[k], list.uy[k], list.uz[k]);
+      spill_particle(S, &errbits, r);
   }
   if (errbits) atomicOr(err, errbits);
 }
@@ -272,13 +271,14 @@ __global__ void k_gather_aos(Particles buf, const int *off, const int *np, const
   const long long a = off[t], d = dst_off[t];
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     int *r = aos + 7LL * (d + k);
-    r[0] = buf.ix[a + k];
-    r[1] = buf.iy[a + k];
-    r[2] = __float_as_int(buf.x[a + k]);
-    r[3] = __float_as_int(buf.y[a + k]);
-    r[4] = __float_as_int(buf.ux[a + k]);
-    r[5] = __float_as_int(buf.uy[a + k]);
-    r[6] = __float_as_int(buf.uz[a + k]);
+    const PRec q = load_particle(buf, a + k);
+    r[0] = q.ix;
+    r[1] = q.iy;
+    r[2] = __float_as_int(q.x);
+    r[3] = __float_as_int(q.y);
+    r[4] = __float_as_int(q.ux);
+    r[5] = __float_as_int(q.uy);
+    r[6] = __float_as_int(q.uz);
   }
 }
 
@@ -286,13 +286,14 @@ __global__ void k_list_to_aos(Particles list, const int *n_ptr, int n_cap, int *
   const int n = min(*n_ptr, n_cap);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     int *r = aos + 7LL * (d0 + k);
-    r[0] = list.ix[k];
-    r[1] = list.iy[k];
-    r[2] = __float_as_int(list.x[k]);
-    r[3] = __float_as_int(list.y[k]);
-    r[4] = __float_as_int(list.ux[k]);
-    r[5] = __float_as_int(list.uy[k]);
-    r[6] = __float_as_int(list.uz[k]);
+    const PRec q = load_particle(list, k);
+    r[0] = q.ix;
+    r[1] = q.iy;
+    r[2] = __float_as_int(q.x);
+    r[3] = __float_as_int(q.y);
+    r[4] = __float_as_int(q.ux);
+    r[5] = __float_as_int(q.uy);
+    r[6] = __float_as_int(q.uz);
   }
 }
 
@@ -305,8 +306,9 @@ __global__ void k_charge_tiles(Particles buf, const int *off, const int *np, flo
   const int n = np[t];
   const long long a = off[t];
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int c = buf.ix[a + k] + nrow * buf.iy[a + k];
-    const float w1 = buf.x[a + k], w2 = buf.y[a + k];
+    const PRec r = load_particle(buf, a + k);
+    const int c = r.ix + nrow * r.iy;
+    const float w1 = r.x, w2 = r.y;
     atomicAdd(&rho[c], (1.0f - w1) * (1.0f - w2) * q);
     atomicAdd(&rho[c + 1], (w1) * (1.0f - w2) * q);
     atomicAdd(&rho[c + nrow], (1.0f - w1) * (w2) * q);
@@ -317,8 +319,9 @@ __global__ void k_charge_tiles(Particles buf, const int *off, const int *np, flo
 __global__ void k_charge_list(Particles list, const int *n_ptr, int n_cap, float *rho, int nrow, float q) {
   const int n = min(*n_ptr, n_cap);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int c = list.ix[k] + nrow * list.iy[k];
-    const float w1 = list.x[k], w2 = list.y[k];
+    const PRec r = load_particle(list, k);
+    const int c = r.ix + nrow * r.iy;
+    const float w1 = r.x, w2 = r.y;
     atomicAdd(&rho[c], (1.0f - w1) * (1.0f - w2) * q);
     atomicAdd(&rho[c + 1], (w1) * (1.0f - w2) * q);
     atomicAdd(&rho[c + nrow], (1.0f - w1) * (w2) * q);

@@ -291,7 +291,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 // block-wide barrier.
 // ---------------------------------------------------------------------------
 template <int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
+__global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
                                                    const __grid_constant__ CUtensorMap tm_j, Particles pin,
                                                    Particles pout, TileSet T, Outbox Oin, Outbox O, Spill S,
                                                    double *ekin_tile, int *err, PushConst C) {
@@ -506,9 +506,9 @@ __global__ void __launch_bounds__(NT) k_push_tiles(const __grid_constant__ CUten
   for (int k0 = warp * 32; k0 < n_own; k0 += NT) {
     const int k = k0 + lane;
     const bool valid = k < n_own;
-    const long long g = base + (valid ? k : 0);
-    process(valid, valid ? pin.ix[g] : 0, valid ? pin.iy[g] : 0, valid ? pin.x[g] : 0.f, valid ? pin.y[g] : 0.f,
-            valid ? pin.ux[g] : 0.f, valid ? pin.uy[g] : 0.f, valid ? pin.uz[g] : 0.f);
+    PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (valid) r = load_particle(pin, base + k);
+    process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
   }
 
   // incoming particles: the warps walk the neighbours' outboxes in chunks of
@@ -521,10 +521,9 @@ __global__ void __launch_bounds__(NT) k_push_tiles(const __grid_constant__ CUten
       const int e = e0 + lane;
       const bool valid = e < n && Oin.dst[ob + e] == t;
       if (!__any_sync(0xffffffffu, valid)) continue;
-      const long long q = ob + (valid ? e : 0);
-      process(valid, valid ? Oin.p.ix[q] : 0, valid ? Oin.p.iy[q] : 0, valid ? Oin.p.x[q] : 0.f,
-              valid ? Oin.p.y[q] : 0.f, valid ? Oin.p.ux[q] : 0.f, valid ? Oin.p.uy[q] : 0.f,
-              valid ? Oin.p.uz[q] : 0.f);
+      PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (valid) r = load_particle(Oin.p, ob + e);
+      process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
     }
   }
 
@@ -567,8 +566,9 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Gr
   int errbits = 0;
   float ks = 0.f, kc = 0.f;
   for (int k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
-    int ix = sin.ix[k], iy = sin.iy[k];
-    float x = sin.x[k], y = sin.y[k], ux = sin.ux[k], uy = sin.uy[k], uz = sin.uz[k];
+    const PRec r = load_particle(sin, k);
+    int ix = r.ix, iy = r.iy;
+    float x = r.x, y = r.y, ux = r.ux, uy = r.uy, uz = r.uz;
     if (ix < 0 || ix >= C.nx || iy < 0 || iy >= C.ny) {
       errbits |= ERR_ESCAPE;
       ix = min(max(ix, 0), C.nx - 1);
