@@ -308,6 +308,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   constexpr int QCAP = 64;
   __shared__ float qf[NW][5][QCAP];  // x0, y0, dx, dy, qvz
   __shared__ int qi[NW][QCAP];       // local cell and shifts, packed
+  __shared__ __align__(16) float4 pf_u[NW][2][32];   // prefetched particles, per warp, double buffered
+  __shared__ __align__(16) float2 pf_xy[NW][2][32];
   __shared__ int nb[8], s_nnb;        // distinct neighbour tiles
   __shared__ int s_stay, s_leave;     // output counters (warp-aggregated atomics)
 
@@ -353,6 +355,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
 
   const TileFields<BW, PL> fld{sEB};
   const TileCurrent<BW, PL> dep{sJ};
+  const PushConst Cl = C;
   const long long base = T.off[t];
   const int cap = T.cap[t];
   const int n_own = T.np[t];
@@ -365,86 +368,71 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     const int w = qi[warp][e];
     const int qli = w & 0xff, qlj = (w >> 8) & 0xff, qdi = ((w >> 16) & 3) - 1, qdj = ((w >> 18) & 3) - 1;
     const Seg a = zigzag_first(dep, qli, qlj, qdi, qdj, qf[warp][0][e], qf[warp][1][e], qf[warp][2][e],
-                               qf[warp][3][e], C.qnx, C.qny, qf[warp][4][e]);
-    add_current(dep, a.ix, a.iy, segment_current(a, C.qnx, C.qny));
+                               qf[warp][3][e], Cl.qnx, Cl.qny, qf[warp][4][e]);
+    add_current(dep, a.ix, a.iy, segment_current(a, Cl.qnx, Cl.qny));
   };
 
   // one particle per lane: push, deposit, boundary, compaction; the 32 lanes
   // of a warp call it together (warp-level collectives only)
   auto process = [&](bool valid, int ix, int iy, float x, float y, float ux, float uy, float uz) {
-    int code = 0;  // 1 stays in the tile, 2 leaves it
-    int li = 0, lj = 0, dest = 0;
-    bool split = false;
-    float sx0 = 0.f, sy0 = 0.f, smx = 0.f, smy = 0.f, sqvz = 0.f;
-    int spk = 0;
-    SegCurrent cur;
+    // every lane runs the same instructions; invalid lanes carry a zero
+    // particle and are masked out by `valid` where it matters
+    int li = ix - cx0, lj = iy - cy0;
+    errbits |= (valid && ((unsigned)li >= (unsigned)TX || (unsigned)lj >= (unsigned)TY)) ? ERR_ESCAPE : 0;
+    li = min(max(li, 0), TX - 1);  // keeps the accesses inside the halo
+    lj = min(max(lj, 0), TY - 1);
+    ix = cx0 + li;
+    iy = cy0 + lj;
+    float mx, my, x1, y1, qvz;
+    int di, dj;
+    bool bad;
+    const float kin = push_particle(fld, li, lj, x, y, ux, uy, uz, mx, my, x1, y1, di, dj, qvz, bad, Cl);
+    kahan_add(ks, kc, valid ? kin : 0.f);
+    errbits |= (valid && bad) ? ERR_ESCAPE : 0;
+    const bool split = valid && ((di != 0) || (dj != 0));
+    // the whole motion inside the cell: one segment (particles.c:781-797);
+    // crossing motions are queued below and contribute nothing here
+    Seg a;
+    a.x0 = x;
+    a.y0 = y;
+    a.dx = mx;
+    a.dy = my;
+    a.x1 = x + mx;
+    a.y1 = y + my;
+    a.qvz = qvz * 0.5f;
+    a.ix = li;
+    a.iy = lj;
+    SegCurrent cur = segment_current(a, Cl.qnx, Cl.qny);
+    const bool single = valid && !split;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) cur.v[q] = 0.f;
-    if (valid) {
-      li = ix - cx0;
-      lj = iy - cy0;
-      if ((unsigned)li >= (unsigned)TX || (unsigned)lj >= (unsigned)TY) {
-        errbits |= ERR_ESCAPE;  // not in this tile: keep the accesses inside the halo
-        li = min(max(li, 0), TX - 1);
-        lj = min(max(lj, 0), TY - 1);
-        ix = cx0 + li;
-        iy = cy0 + lj;
-      }
-      float mx, my, x1, y1, qvz;
-      int di, dj;
-      bool bad;
-      const float kin = push_particle(fld, li, lj, x, y, ux, uy, uz, mx, my, x1, y1, di, dj, qvz, bad, C);
-      kahan_add(ks, kc, kin);
-      if (bad) errbits |= ERR_ESCAPE;
-      split = (di != 0) || (dj != 0);
-      if (split) {
-        sx0 = x;
-        sy0 = y;
-        smx = mx;
-        smy = my;
-        sqvz = qvz;
-        spk = li | (lj << 8) | ((di + 1) << 16) | ((dj + 1) << 18);
-      } else {
-        // the whole motion stays in the cell: one segment (particles.c:781-797)
-        Seg a;
-        a.x0 = x;
-        a.y0 = y;
-        a.dx = mx;
-        a.dy = my;
-        a.x1 = x + mx;
-        a.y1 = y + my;
-        a.qvz = qvz * 0.5f;
-        a.ix = li;
-        a.iy = lj;
-        cur = segment_current(a, C.qnx, C.qny);
-      }
-      x = x1;
-      y = y1;
-      if (apply_boundary(ix, iy, di, dj, C)) {
-        dest = ix / TX + (iy / TY) * C.ntx;
-        code = (dest == t) ? 1 : 2;
-      }
-    }
+    for (int q = 0; q < 8; ++q) cur.v[q] = single ? cur.v[q] : 0.f;
+    const float sx0 = x, sy0 = y, smx = mx, smy = my, sqvz = qvz;
+    const int spk = li | (lj << 8) | ((di + 1) << 16) | ((dj + 1) << 18);
+    x = x1;
+    y = y1;
+    const bool keep = apply_boundary(ix, iy, di, dj, Cl);
+    const int dest = ix / TX + (iy / TY) * Cl.ntx;
+    const int code = (valid && keep) ? ((dest == t) ? 1 : 2) : 0;  // 1 stays, 2 leaves
 
     // segmented warp reduction of the single-segment currents over runs of
     // lanes that start in the same cell (the runs are contiguous because
-    // the tile is sorted by cell; unsorted input only makes runs shorter)
+    // the tile is sorted by cell; unsorted input only makes runs shorter);
+    // as many halving steps as the longest run needs
     {
       const int key = valid ? (li + lj * TX) : -1 - lane;
       const int knext = __shfl_down_sync(0xffffffffu, key, 1);
       const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
       const unsigned lastmask = __ballot_sync(0xffffffffu, lane == 31 || knext != key);
       const int run_last = __ffs(lastmask & (0xffffffffu << lane)) - 1;
-      const unsigned longrun = __ballot_sync(0xffffffffu, run_last > lane);
-      if (longrun) {
+      const unsigned maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(run_last - lane + 1));
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          const bool take = lane + off <= run_last;
+      for (int off = 1; off < 32; off <<= 1) {
+        if ((unsigned)off >= maxlen) break;
+        const bool take = lane + off <= run_last;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const float o = __shfl_down_sync(0xffffffffu, cur.v[q], off);
-            if (take) cur.v[q] += o;
-          }
+        for (int q = 0; q < 8; ++q) {
+          const float o = __shfl_down_sync(0xffffffffu, cur.v[q], off);
+          if (take) cur.v[q] += o;
         }
       }
       const bool head = valid && (lane == 0 || kprev != key);
@@ -502,13 +490,43 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     }
   };
 
-  // own particles: warp w takes chunks w, w + NW, ... of 32
-  for (int k0 = warp * 32; k0 < n_own; k0 += NT) {
-    const int k = k0 + lane;
-    const bool valid = k < n_own;
-    PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (valid) r = load_particle(pin, base + k);
-    process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
+  // own particles: warp w takes chunks w, w + NW, ... of 32; the next
+  // chunk is copied into shared memory while this one is pushed
+  {
+    int b = 0;
+    if (warp * 32 + lane < n_own) {
+      cp_async16(&pf_u[warp][0][lane], &pin.u[base + warp * 32 + lane]);
+      cp_async8(&pf_xy[warp][0][lane], &pin.xy[base + warp * 32 + lane]);
+    }
+    cp_async_commit();
+    for (int k0 = warp * 32; k0 < n_own; k0 += NT) {
+      const int kn = k0 + NT + lane;
+      if (kn < n_own) {
+        cp_async16(&pf_u[warp][b ^ 1][lane], &pin.u[base + kn]);
+        cp_async8(&pf_xy[warp][b ^ 1][lane], &pin.xy[base + kn]);
+      }
+      cp_async_commit();
+      cp_async_wait<1>();  // this chunk's copies are in
+      const int k = k0 + lane;
+      const bool valid = k < n_own;
+      PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (valid) {
+        const float4 u = pf_u[warp][b][lane];
+        const float2 xy = pf_xy[warp][b][lane];
+        const unsigned c = (unsigned)__float_as_int(u.w);
+        r.ix = (int)(c & 0xffffu);
+        r.iy = (int)(c >> 16);
+        r.x = xy.x;
+        r.y = xy.y;
+        r.ux = u.x;
+        r.uy = u.y;
+        r.uz = u.z;
+      }
+      __syncwarp();
+      process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
+      b ^= 1;
+    }
+    cp_async_wait<0>();
   }
 
   // incoming particles: the warps walk the neighbours' outboxes in chunks of
