@@ -213,6 +213,86 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# batched parameter scan
+# ---------------------------------------------------------------------------
+def run_scan(args):
+    """256 two-stream runs (grids 64..256 per axis, ppc 2..8 per axis,
+    drift 0.2..0.8, thermal 0.02..0.2, dt = 0.9 Courant, 300 steps, energy
+    history every step): batched against the same runs one after another
+    through the plain path."""
+    from zpic_gb300 import batch  # before anything creates a CUDA context
+
+    import torch
+
+    n_runs = args.scan_runs
+    steps = args.steps if args.steps_given else 300
+    runs = batch.weibel_scan(n_runs=n_runs, steps=steps)
+    tile, rates = batch.autotune_tile(runs, candidates=((16, 16), (32, 16), (16, 8)), sample=64, steps=32)
+    nps = sum(r.particles() * r.steps for r in runs)
+
+    def fresh(graphs):
+        t0 = time.perf_counter()
+        sims = batch.load_sims(runs, tile=tile, sort_every=args.sort_every, graphs=graphs)
+        return sims, time.perf_counter() - t0
+
+    # warm-up: one small batch (graph capture and instantiation paths, clocks)
+    warm = batch.load_sims(runs[:8], tile=tile, sort_every=args.sort_every)
+    batch.run_batched(warm, [batch.ScanRun(r.nx, r.ppc, r.uz, r.uth, r.dx, r.dt, r.seed, 32) for r in runs[:8]])
+    for s_ in warm:
+        s_.close()
+
+    sims, t_load = fresh(True)
+    clk = ClockSampler(0)
+    clk.start()
+    t0 = time.perf_counter()
+    res = batch.run_batched(sims, runs, group=args.scan_group or None)
+    t_wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    hist_bytes = sum(h.nbytes for h in res.histories)
+    part_bytes = sum(r.particles() * 28 for r in runs)
+    finals = [float(h[-1].sum()) for h in res.histories]
+    for s_ in sims:
+        s_.close()
+    torch.cuda.empty_cache()
+
+    sims, _ = fresh(False)
+    seq = batch.run_sequential(sims, runs)
+    for s_ in sims:
+        s_.close()
+    torch.cuda.empty_cache()
+    sims, _ = fresh(True)
+    seq_g = batch.run_sequential(sims, runs)
+    for s_ in sims:
+        s_.close()
+    line = {
+        "metric": METRIC, "value": res.rate, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 1,
+        "ms_per_step": res.device_ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (reference loading, run k seeded 12345+k, 67890+k)",
+        "config": {"workload": f"batched scan: {n_runs} two-stream runs, grids 64..256 per axis (dx=0.1), "
+                               f"ppc 2..8 per axis, uz 0.2..0.8, uth 0.02..0.2, dt=0.9 CFL, {steps} steps, "
+                               f"energy history every step",
+                   "particles_total": int(sum(r.particles() for r in runs)), "tile": list(tile),
+                   "batch_groups": res.groups, "fast_math": True},
+        "batched": {"rate": res.rate, "device_ms": res.device_ms, "wall_s": t_wall, **res.extra},
+        "sequential_plain": {"rate": seq.rate, "device_ms": seq.device_ms, "wall_s": seq.wall_s, **seq.extra,
+                             "how": "each run alone through zc_step (eager launches), one after another"},
+        "sequential_graphs": {"rate": seq_g.rate, "device_ms": seq_g.device_ms, "wall_s": seq_g.wall_s,
+                              "how": "each run alone through zc_step with graph replay, one after another"},
+        "speedup_vs_sequential": res.rate / seq.rate,
+        "speedup_vs_sequential_graphs": res.rate / seq_g.rate,
+        "autotune_rates": {f"{t[0]}x{t[1]}": v for t, v in rates.items()},
+        "e2e": {"value": nps / (t_wall + t_load), "unit": UNIT,
+                "h2d_bytes_per_step": part_bytes / steps, "d2h_bytes_per_step": hist_bytes / steps,
+                "how": "host particle loading and upload of every run, batched stepping, energy histories "
+                       "read back; wall clock"},
+        "clocks": clocks,
+        "energy_final_mean": float(np.mean(finals)),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def main():
@@ -228,9 +308,15 @@ def main():
                     help="bit-exact push build (every float32 op rounded as the reference C)")
     ap.add_argument("--sort-every", type=int, default=0)
     ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
+    ap.add_argument("--workload", default="plain", choices=["plain", "scan"])
+    ap.add_argument("--scan-runs", type=int, default=256)
+    ap.add_argument("--scan-group", type=int, default=0, help="runs per batch graph (0: all)")
     args = ap.parse_args()
+    args.steps_given = any(a.startswith("--steps") for a in sys.argv[1:])
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "scan":
+        return run_scan(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -88,6 +88,8 @@ typedef struct {
     int nx[2];
     int tile[2];
     int ntiles[2];
+    int relayouts;          /* tile re-layouts so far (uploads, spills drained) */
+    int captures;           /* graph captures so far (zc_set_graphs, batches) */
 } zc_info;
 
 /* Device view of the grids for zero-copy consumers (e.g. PyTorch): SoA
@@ -194,12 +196,53 @@ enum {
     ZC_PHASE_EXT,           /* external fields */
     ZC_PHASE_WINDOW,        /* moving-window shift and injection */
     ZC_PHASE_SORT,          /* per-tile cell sort */
+    ZC_PHASE_HISTORY,       /* per-step energy history */
     ZC_NPHASE
 };
 ZC_API zc_status zc_set_profiling(zc_sim *sim, int enable);
 ZC_API zc_status zc_get_profile(zc_sim *sim, double ms[ZC_NPHASE], long long launches[ZC_NPHASE]);
 ZC_API zc_status zc_reset_profile(zc_sim *sim);
 ZC_API const char *zc_phase_name(int phase);
+
+/* --- graph replay ---------------------------------------------------------- */
+/* With graphs on, zc_step runs whole blocks of steps (2 x sort_every steps,
+ * or 2 with sorting off) as one captured CUDA graph, with eager steps up to
+ * the first block boundary and after the last whole block.  Results are
+ * those of eager steps.  Not used with a moving window (its injection calls
+ * back into the host) or while profiling.  Any change of layout or
+ * configuration recaptures the block.  Off by default.  No counterpart in
+ * the reference (its step is a host loop, em2d/simulation.c:45-56). */
+ZC_API zc_status zc_set_graphs(zc_sim *sim, int enable);
+
+/* --- per-step energy history -------------------------------------------- */
+/* Records, after every step, one row of 6 + n_species doubles on the
+ * device: the field energy per component (as zc_energy) and the kinetic
+ * energy of each species, for up to `max_steps` steps (later steps are not
+ * recorded).  The rows the reference's sim_report_energy prints once per
+ * call (em2d/simulation.c:183-205) become a device array read once at the
+ * end.  Species must be created first.  max_steps = 0 turns it off. */
+ZC_API zc_status zc_history_enable(zc_sim *sim, int max_steps);
+/* copies up to `cap_rows` rows into `out` (row-major); *nrows receives the
+ * rows recorded, *ncols the row length.  out == NULL only queries. */
+ZC_API zc_status zc_history_get(zc_sim *sim, double *out, int cap_rows, int *nrows, int *ncols);
+ZC_API zc_status zc_history_reset(zc_sim *sim);
+
+/* --- batched runs (parameter scans) ---------------------------------------- */
+/* A batch advances many independent simulations together: one CUDA graph
+ * holds a block of steps of every member as parallel branches, so small
+ * grids that cannot fill the GPU alone share it, and one launch per block
+ * replaces hundreds.  Members keep their own handles (data access, energy,
+ * history) and must share the block length (same sort_every) and have no
+ * moving window.  Replaces the reference's process-level fan-out of a
+ * parameter scan (mods/em1d_param_scan/main.c:112-133); each member gives
+ * the results it gives alone. */
+typedef struct zc_batch zc_batch;
+ZC_API zc_status zc_batch_create(zc_sim *const *sims, int nsims, zc_batch **out);
+/* advances every member by nsteps */
+ZC_API zc_status zc_batch_step(zc_batch *batch, int nsteps);
+/* device time (ms) of the last zc_batch_step, CUDA events */
+ZC_API zc_status zc_batch_last_ms(zc_batch *batch, float *ms);
+ZC_API zc_status zc_batch_destroy(zc_batch *batch);
 
 /* --- field energy without device allocation ----------------------------- */
 /* No counterpart in the reference.  Computes the six field-energy components

@@ -121,12 +121,18 @@ static void spec_thermal_u(zo_spec *sp, int first, int last)
         sp->p[k].uy = sp->uth[1] * zo_rand_norm();
         sp->p[k].uz = sp->uth[2] * zo_rand_norm();
     }
-    /* the reference indexes the per-cell table with stride nx[1]
-     * (particles.c:104-105,116); kept as is */
-    const int ncell = sp->nx[0] * sp->nx[1];
+    /* the reference indexes its per-cell table of nx[0]*nx[1] entries with
+     * stride nx[1] (particles.c:104-105,116); kept as is.  With nx[1] >
+     * nx[0] its indices run past the table (undefined behaviour there):
+     * here the table is long enough for every index and all its entries
+     * are normalised, i.e. the mean of each cell is removed.  With nx[1] <=
+     * nx[0] this is the reference's arithmetic exactly. */
     const int stride = sp->nx[1];
-    zo_f3 *mean = (zo_f3 *)calloc((size_t)ncell, sizeof(zo_f3));
-    int *cnt = (int *)calloc((size_t)ncell, sizeof(int));
+    const int ncell = sp->nx[0] * sp->nx[1];
+    const int nidx = (sp->nx[0] - 1) + stride * (sp->nx[1] - 1) + 1;
+    const int ntab = nidx > ncell ? nidx : ncell;
+    zo_f3 *mean = (zo_f3 *)calloc((size_t)ntab, sizeof(zo_f3));
+    int *cnt = (int *)calloc((size_t)ntab, sizeof(int));
     for (int k = first; k <= last; k++) {
         int c = sp->p[k].ix + stride * sp->p[k].iy;
         mean[c].x += sp->p[k].ux;
@@ -134,7 +140,7 @@ static void spec_thermal_u(zo_spec *sp, int first, int last)
         mean[c].z += sp->p[k].uz;
         cnt[c] += 1;
     }
-    for (int c = 0; c < ncell; c++) {
+    for (int c = 0; c < ntab; c++) {
         float inv = (cnt[c] > 0) ? 1.0f / cnt[c] : 0;
         mean[c].x *= inv;
         mean[c].y *= inv;

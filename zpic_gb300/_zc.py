@@ -35,9 +35,10 @@ EXPORTS = [
     "zc_get_fields", "zc_get_particle_fields", "zc_get_current", "zc_set_current", "zc_energy",
     "zc_species_charge", "zc_get_info", "zc_grid_view_get", "zc_synchronize", "zc_last_step_ms",
     "zc_last_error", "zc_status_string", "zc_set_profiling", "zc_get_profile", "zc_reset_profile",
-    "zc_phase_name", "zc_field_energy_static",
+    "zc_phase_name", "zc_field_energy_static", "zc_set_graphs", "zc_history_enable", "zc_history_get",
+    "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
 ]
-NPHASE = 12
+NPHASE = 13
 
 
 class ZcError(RuntimeError):
@@ -66,7 +67,7 @@ class Laser(C.Structure):
 class Info(C.Structure):
     _fields_ = [("iter", C.c_int), ("n_move", C.c_int), ("moving_window", C.c_int),
                 ("n_species", C.c_int), ("nx", C.c_int * 2), ("tile", C.c_int * 2),
-                ("ntiles", C.c_int * 2)]
+                ("ntiles", C.c_int * 2), ("relayouts", C.c_int), ("captures", C.c_int)]
 
 
 class GridView(C.Structure):
@@ -124,6 +125,14 @@ def load(path: str = LIB_PATH):
         "zc_get_profile": [P, P, P],
         "zc_reset_profile": [P],
         "zc_field_energy_static": [P, P, C.c_size_t, I, I, I, C.c_float, C.c_float, P, P],
+        "zc_set_graphs": [P, I],
+        "zc_history_enable": [P, I],
+        "zc_history_get": [P, P, I, C.POINTER(I), C.POINTER(I)],
+        "zc_history_reset": [P],
+        "zc_batch_create": [P, I, C.POINTER(P)],
+        "zc_batch_step": [P, I],
+        "zc_batch_last_ms": [P, C.POINTER(C.c_float)],
+        "zc_batch_destroy": [P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -336,7 +345,7 @@ class CudaSim:
         _ck(self.lib.zc_get_info(self.h, C.byref(i)))
         return {"iter": i.iter, "n_move": i.n_move, "moving_window": i.moving_window,
                 "n_species": i.n_species, "tile": (i.tile[0], i.tile[1]),
-                "ntiles": (i.ntiles[0], i.ntiles[1])}
+                "ntiles": (i.ntiles[0], i.ntiles[1]), "relayouts": i.relayouts, "captures": i.captures}
 
     def set_profiling(self, on=True):
         _ck(self.lib.zc_set_profiling(self.h, int(bool(on))))
@@ -355,3 +364,58 @@ class CudaSim:
         v = GridView()
         _ck(self.lib.zc_grid_view_get(self.h, C.byref(v)))
         return v
+
+    def set_graphs(self, on=True):
+        """Replays whole blocks of steps as one captured CUDA graph."""
+        _ck(self.lib.zc_set_graphs(self.h, int(bool(on))))
+
+    def history_enable(self, max_steps):
+        """Records the field and kinetic energies after every step on the
+        device (up to ``max_steps`` rows)."""
+        _ck(self.lib.zc_history_enable(self.h, int(max_steps)))
+
+    def history_reset(self):
+        _ck(self.lib.zc_history_reset(self.h))
+
+    def history(self) -> np.ndarray:
+        """[steps, 6 + n_species]: field energy per component, then the
+        kinetic energy of each species, one row per step."""
+        n, c = C.c_int(), C.c_int()
+        _ck(self.lib.zc_history_get(self.h, None, 0, C.byref(n), C.byref(c)))
+        out = np.zeros((n.value, c.value), dtype=np.float64)
+        if n.value:
+            _ck(self.lib.zc_history_get(self.h, _p(out), n.value, C.byref(n), C.byref(c)))
+        return out
+
+
+class CudaBatch:
+    """Independent simulations advanced together (a ``zc_batch`` handle):
+    one CUDA graph runs a block of steps of every member as parallel
+    branches.  The members stay usable on their own."""
+
+    def __init__(self, sims):
+        self.lib = load()
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
+        h = C.c_void_p()
+        _ck(self.lib.zc_batch_create(arr, len(self.sims), C.byref(h)))
+        self.h = h
+
+    def step(self, n=1):
+        _ck(self.lib.zc_batch_step(self.h, int(n)))
+
+    def last_ms(self) -> float:
+        v = C.c_float()
+        _ck(self.lib.zc_batch_last_ms(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.zc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

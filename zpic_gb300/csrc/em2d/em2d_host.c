@@ -62,15 +62,30 @@ EXPORT double timer_resolution(void) { return 1.0e-6; }
 /* ------------------------------------------------------------------------- */
 /* random numbers: multiply-with-carry pair (Marsaglia) + polar Box-Muller   */
 /* ------------------------------------------------------------------------- */
-static uint32_t g_w = 12345, g_z = 67890;   /* the reference's default seeds */
-static int g_spare_ok = 0;
-static double g_spare = 0.0;
+/* One generator per host thread: a single-threaded program sees the
+ * reference's process-global generator (random.c:16-17); threads that load
+ * different runs of a scan at once do not share (or race on) one state. */
+static __thread uint32_t g_w = 12345, g_z = 67890;   /* the reference's default seeds */
+static __thread int g_spare_ok = 0;
+static __thread double g_spare = 0.0;
 
 EXPORT void set_rand_seed(uint32_t w, uint32_t z)
 {
     /* the cached deviate is kept, as in the reference */
     g_w = w;
     g_z = z;
+}
+
+/* No counterpart in the reference: seeds the generator and drops the cached
+ * deviate, i.e. the state of a newly started process after set_rand_seed.
+ * A scan that loads each run this way gives every run the particles it gets
+ * as a process of its own, whatever order the runs are loaded in. */
+EXPORT void rand_seed_fresh(uint32_t w, uint32_t z)
+{
+    g_w = w;
+    g_z = z;
+    g_spare_ok = 0;
+    g_spare = 0.0;
 }
 
 EXPORT uint32_t rand_uint32(void)
@@ -205,10 +220,18 @@ static void load_momenta(t_species *sp, int first, int last)
         sp->part[k].uy = sp->uth[1] * rand_norm();
         sp->part[k].uz = sp->uth[2] * rand_norm();
     }
+    /* The per-cell table is indexed with stride nx[1], as the reference
+     * indexes its table of nx[0]*nx[1] entries (particles.c:104-105,116).
+     * With nx[1] > nx[0] the reference's indices run past its table
+     * (undefined behaviour); here the table holds every index and all its
+     * entries are normalised, so each cell's mean is removed.  With
+     * nx[1] <= nx[0] the arithmetic is the reference's exactly. */
+    const int stride = sp->nx[1];
     const int ncell = sp->nx[0] * sp->nx[1];
-    const int stride = sp->nx[1];  /* as the reference indexes its table */
-    float3 *mean = (float3 *)calloc((size_t)ncell, sizeof(float3));
-    int *cnt = (int *)calloc((size_t)ncell, sizeof(int));
+    const int nidx = (sp->nx[0] - 1) + stride * (sp->nx[1] - 1) + 1;
+    const int ntab = nidx > ncell ? nidx : ncell;
+    float3 *mean = (float3 *)calloc((size_t)ntab, sizeof(float3));
+    int *cnt = (int *)calloc((size_t)ntab, sizeof(int));
     if (!mean || !cnt) die("(*error*) out of memory");
     for (int k = first; k <= last; k++) {
         const int c = sp->part[k].ix + stride * sp->part[k].iy;
@@ -217,7 +240,7 @@ static void load_momenta(t_species *sp, int first, int last)
         mean[c].z += sp->part[k].uz;
         cnt[c] += 1;
     }
-    for (int c = 0; c < ncell; c++) {
+    for (int c = 0; c < ntab; c++) {
         const float w = (cnt[c] > 0) ? 1.0f / cnt[c] : 0;
         mean[c].x *= w;
         mean[c].y *= w;

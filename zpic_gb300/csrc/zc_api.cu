@@ -4,6 +4,7 @@
 // error message.
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -122,6 +123,27 @@ struct SpeciesState {
   double *d_ekin_tile = nullptr, *d_ekin_extra = nullptr, *d_ekin = nullptr;
 };
 
+// host state that a step changes (buffer parities and counters)
+struct Counters {
+  int iter = 0, n_move = 0;
+  std::vector<int> sp_iter, sp_n_move, cur, spill_cur, ob_in;
+  std::vector<bool> pending;
+  int eb_cur = 0, j_cur = 0;
+  long long launch[ZC_NPHASE] = {};
+};
+
+// a captured run of steps, valid from the state it was captured in
+struct StepGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int nsteps = 0;
+  bool valid = false;
+  unsigned long long id = 0;  // unique per capture (batch graphs hold copies)
+  Counters before, after;
+};
+
+std::atomic<unsigned long long> g_capture_id{0};
+
 }  // namespace
 
 void zc::set_error_message(const char *msg) { g_err = msg ? msg : ""; }
@@ -146,7 +168,7 @@ struct zc_sim {
   int xtype = 0, ytype = 0, xlevel = 0, ylevel = 0;
   int mw = 0, n_move = 0, iter = 0;
   int *d_err = nullptr;
-  int *h_pinned = nullptr;        // [0] error bits, [1..] spill counts
+  int *h_pinned = nullptr;        // [0] error bits, [2..3] error bits after a block
   double *d_part = nullptr, *d_emf = nullptr;
   int energy_blocks = 0;
   float *stage = nullptr;         // AoS staging for grids
@@ -171,6 +193,19 @@ struct zc_sim {
   size_t ev_used = 0;
   double prof_ms[ZC_NPHASE] = {};
   long long prof_launch[ZC_NPHASE] = {};
+  // replay of captured steps (CUDA graphs): a whole block, and a shorter
+  // prefix of a block for the remainder of a call
+  int use_graph = 0;
+  StepGraph blk, tail;
+  int n_relayout = 0, n_capture = 0;
+  cudaEvent_t ev_blk[2] = {nullptr, nullptr};
+  // per-step energy history on the device: row = 6 field components, then
+  // the kinetic energy of every species
+  double *d_hist = nullptr;
+  int *d_hist_n = nullptr;
+  int hist_cap = 0, hist_cols = 0, hist_blocks = 0;
+  double **d_ekin_ptrs = nullptr;
+  double *d_hist_part = nullptr;
 };
 
 namespace {
@@ -261,12 +296,16 @@ zc_status settle(zc_sim *s, SpeciesState &p) {
   return ZC_OK;
 }
 
+void invalidate_graph(zc_sim *s);
+
 // Builds the tile layout of a species from per-tile counts and moves its
 // particles (tiles of the current layout, its spill list and an optional
 // new list) into it.  Every tile is then ordered deterministically.
 zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   SpeciesState &p = s->sp[k];
   cudaStream_t st = s->st;
+  invalidate_graph(s);
+  s->n_relayout += 1;
   TRY(settle(s, p));
   const LayoutConst L = layout(s);
   const int nt = s->ntiles;
@@ -389,11 +428,15 @@ zc_status check_errors(zc_sim *s, bool relayout_spill) {
     s->accumulated_err |= e;
   }
   if (relayout_spill && (e & ERR_SPILLED)) {
+    // Spilled particles are advanced every step by the spill kernel (global
+    // atomics, slower per particle than the tiles); a re-layout (host
+    // synchronous, new tile capacities) drains them once enough have piled
+    // up to matter, well before the spill list can fill.
     for (size_t k = 0; k < s->sp.size(); ++k) {
       SpeciesState &p = s->sp[k];
       int n = 0;
       CK(cudaMemcpy(&n, p.d_spill_cnt + p.spill_cur, sizeof(int), cudaMemcpyDeviceToHost));
-      if (n > 0) TRY(relayout(s, (int)k, nullptr, 0));
+      if (n >= std::max(1024, p.spill_cap / 32)) TRY(relayout(s, (int)k, nullptr, 0));
     }
   }
   if (e & ERR_OVERFLOW) return fail(ZC_EOVERFLOW, "particle spill buffer exhausted: particles were lost");
@@ -606,6 +649,173 @@ zc_status iter_impl(zc_sim *s) {
   for (size_t k = 0; k < s->sp.size(); ++k) TRY(spec_advance_impl(s, (int)k));
   TRY(current_update_impl(s));
   TRY(emf_advance_impl(s));
+  if (s->d_hist) {
+    Phase ph(s, ZC_PHASE_HISTORY, 2);
+    CK(launch_energy_history(s->EB[s->eb_cur], s->G, s->d_hist_part, s->hist_blocks, s->d_hist, s->d_hist_n,
+                             s->hist_cap, s->hist_cols, s->d_ekin_ptrs, (int)s->sp.size(), s->dx[0], s->dx[1],
+                             s->st));
+  }
+  return ZC_OK;
+}
+
+void drop_graph(StepGraph &g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g.exec = nullptr;
+  g.graph = nullptr;
+  g.valid = false;
+}
+
+void invalidate_graph(zc_sim *s) {
+  drop_graph(s->blk);
+  drop_graph(s->tail);
+}
+
+// steps per captured block: the buffer parities (particle buffers, outboxes,
+// spill lists, field buffers) and the periodic cell sort repeat after it
+int block_period(const zc_sim *s) { return s->sort_every > 0 ? 2 * s->sort_every : 2; }
+
+Counters save_counters(const zc_sim *s) {
+  Counters c;
+  c.iter = s->iter;
+  c.n_move = s->n_move;
+  for (const auto &p : s->sp) {
+    c.sp_iter.push_back(p.iter);
+    c.sp_n_move.push_back(p.n_move);
+    c.cur.push_back(p.cur);
+    c.spill_cur.push_back(p.spill_cur);
+    c.ob_in.push_back(p.ob_in);
+    c.pending.push_back(p.pending);
+  }
+  c.eb_cur = s->eb_cur;
+  c.j_cur = s->j_cur;
+  for (int k = 0; k < ZC_NPHASE; ++k) c.launch[k] = s->prof_launch[k];
+  return c;
+}
+
+// the buffer parities a captured graph starts from
+bool same_parities(const Counters &a, const Counters &b) {
+  return a.cur == b.cur && a.spill_cur == b.spill_cur && a.ob_in == b.ob_in && a.eb_cur == b.eb_cur &&
+         (a.iter % 2) == (b.iter % 2);
+}
+
+// the graph g holds n steps from the current state (block-aligned)
+bool graph_ready(const zc_sim *s, const StepGraph &g, int n) {
+  return g.valid && g.nsteps == n && s->iter % block_period(s) == 0 && same_parities(g.before, save_counters(s));
+}
+
+// Captures n steps, starting at a block boundary, as a graph.  Capturing
+// does not run anything: the host state advanced by the capture is put
+// back afterwards.
+zc_status capture_steps(zc_sim *s, int n, StepGraph &G) {
+  drop_graph(G);
+  if (s->iter % block_period(s) != 0) return fail(ZC_ESTATE, "graph capture off a block boundary");
+  const Counters before = save_counters(s);
+  const int prof = s->profiling;
+  s->profiling = 0;
+  CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+  zc_status st = ZC_OK;
+  for (int k = 0; k < n && st == ZC_OK; ++k) st = iter_impl(s);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s->st, &g);
+  s->profiling = prof;
+  const Counters after = save_counters(s);
+  // put the host state back (nothing ran yet)
+  s->iter = before.iter;
+  s->n_move = before.n_move;
+  for (size_t k = 0; k < s->sp.size(); ++k) {
+    SpeciesState &p = s->sp[k];
+    p.iter = before.sp_iter[k];
+    p.n_move = before.sp_n_move[k];
+    p.cur = before.cur[k];
+    p.spill_cur = before.spill_cur[k];
+    p.ob_in = before.ob_in[k];
+    p.pending = before.pending[k];
+  }
+  s->eb_cur = before.eb_cur;
+  s->j_cur = before.j_cur;
+  for (int k = 0; k < ZC_NPHASE; ++k) s->prof_launch[k] = before.launch[k];
+  if (st != ZC_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return fail(ZC_ECUDA, "stream capture failed: %s", cudaGetErrorString(e));
+  cudaGraphExec_t x = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(ZC_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(ei));
+  }
+  G.graph = g;
+  G.exec = x;
+  G.nsteps = n;
+  G.before = before;
+  G.after = after;
+  G.valid = true;
+  G.id = ++g_capture_id;
+  s->n_capture += 1;
+  return ZC_OK;
+}
+
+// the host side of running a captured graph
+void account_steps(zc_sim *s, const StepGraph &g) {
+  const int n = g.nsteps;
+  s->iter += n;
+  for (size_t k = 0; k < s->sp.size(); ++k) {
+    SpeciesState &p = s->sp[k];
+    p.iter += n;
+    p.pending = g.after.pending[k];
+    p.cur = g.after.cur[k];
+    p.spill_cur = g.after.spill_cur[k];
+    p.ob_in = g.after.ob_in[k];
+  }
+  s->eb_cur = g.after.eb_cur;
+  s->j_cur = g.after.j_cur;
+  for (int k = 0; k < ZC_NPHASE; ++k) s->prof_launch[k] += g.after.launch[k] - g.before.launch[k];
+}
+
+// Captured blocks replace eager steps when graphs are on and nothing in the
+// step needs the host: no moving window (its injection calls back into the
+// host) and no per-phase event timing.
+bool graph_possible(const zc_sim *s) { return s->use_graph && !s->mw && !s->profiling && !s->sp.empty(); }
+
+// Runs *nsteps by graph replay where it can: eager steps up to a block
+// boundary, whole blocks, then the rest as a prefix of a block (its graph is
+// kept for the next call that ends the same way).  The error word of each
+// block is copied out behind it and read while the next block runs; a spill
+// is drained (which re-lays the species out and invalidates the graphs)
+// before going on.
+zc_status step_graph(zc_sim *s, int *nsteps) {
+  const int P = block_period(s);
+  while (*nsteps > 0 && s->iter % P != 0) {
+    TRY(iter_impl(s));
+    --*nsteps;
+  }
+  int launched = 0;
+  while (*nsteps >= P) {
+    if (!graph_ready(s, s->blk, P)) TRY(capture_steps(s, P, s->blk));
+    CK(cudaGraphLaunch(s->blk.exec, s->st));
+    account_steps(s, s->blk);
+    *nsteps -= P;
+    const int b = launched & 1;
+    CK(cudaMemcpyAsync(s->h_pinned + 2 + b, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaEventRecord(s->ev_blk[b], s->st));
+    if (launched > 0) {
+      CK(cudaEventSynchronize(s->ev_blk[1 - b]));
+      if (s->h_pinned[3 - b]) {
+        CK(cudaStreamSynchronize(s->st));
+        s->h_pinned[2] = s->h_pinned[3] = 0;
+        TRY(check_errors(s, true));
+      }
+    }
+    ++launched;
+  }
+  if (*nsteps > 0) {
+    if (!graph_ready(s, s->tail, *nsteps)) TRY(capture_steps(s, *nsteps, s->tail));
+    CK(cudaGraphLaunch(s->tail.exec, s->st));
+    account_steps(s, s->tail);
+    *nsteps = 0;
+  }
   return ZC_OK;
 }
 
@@ -740,7 +950,9 @@ zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
     TRYC(make_map(&s->tmK_J, s->J[0], G, 3, BW, BH));
   }
   if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
-      cudaEventCreateWithFlags(&s->inj_done, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&s->inj_done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->ev_blk[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->ev_blk[1], cudaEventDisableTiming) != cudaSuccess) {
     st = fail(ZC_ECUDA, "cudaEventCreate failed");
     goto bad;
   }
@@ -797,6 +1009,13 @@ zc_status zc_sim_destroy(zc_sim *s) {
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->inj_done) cudaEventDestroy(s->inj_done);
+  for (auto e : s->ev_blk)
+    if (e) cudaEventDestroy(e);
+  invalidate_graph(s);
+  dfree(s->d_hist);
+  dfree(s->d_hist_n);
+  dfree(s->d_hist_part);
+  dfree(s->d_ekin_ptrs);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
   return ZC_OK;
@@ -806,7 +1025,9 @@ zc_status zc_species_create(zc_sim *s, const zc_species_desc *d, const zc_part *
   if (!s || !d) return fail(ZC_EINVAL, "null argument");
   if (np < 0 || (np > 0 && !parts)) return fail(ZC_EINVAL, "invalid particle buffer");
   if (d->m_q == 0.0f) return fail(ZC_EINVAL, "m_q must be non-zero");
+  if (s->d_hist) return fail(ZC_ESTATE, "species must be created before the energy history is enabled");
   DeviceGuard g(s->device);
+  invalidate_graph(s);
   s->sp.emplace_back();
   const int k = (int)s->sp.size() - 1;
   SpeciesState &p = s->sp[k];
@@ -940,6 +1161,7 @@ zc_status zc_set_smooth(zc_sim *s, int xtype, int xlevel, int ytype, int ylevel)
   if (ytype != 0 && ylevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along y direction");
   if ((xtype != 0 && xlevel >= kMaxSmoothPasses) || (ytype != 0 && xlevel >= kMaxSmoothPasses))
     return fail(ZC_EINVAL, "smoothing level above %d is not supported", kMaxSmoothPasses - 1);
+  invalidate_graph(s);
   s->xtype = xtype;
   s->xlevel = xlevel;
   s->ytype = ytype;
@@ -949,6 +1171,7 @@ zc_status zc_set_smooth(zc_sim *s, int xtype, int xlevel, int ytype, int ylevel)
 
 zc_status zc_set_moving_window(zc_sim *s) {
   if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  invalidate_graph(s);
   s->mw = 1;
   return ZC_OK;
 }
@@ -995,6 +1218,7 @@ zc_status zc_set_ext_fld(zc_sim *s, int Et, const float E0[3], const float *Eg, 
   if ((Et == 1 && !E0) || (Bt == 1 && !B0) || (Et == 2 && !Eg) || (Bt == 2 && !Bg))
     return fail(ZC_EINVAL, "missing external field values");
   DeviceGuard g(s->device);
+  invalidate_graph(s);
   s->ext_Et = Et;
   s->ext_Bt = Bt;
   if (E0) s->ext_E0 = make_float3(E0[0], E0[1], E0[2]);
@@ -1027,6 +1251,7 @@ zc_status zc_step(zc_sim *s, int nsteps) {
   if (nsteps < 0) return fail(ZC_EINVAL, "nsteps must be >= 0");
   DeviceGuard g(s->device);
   CK(cudaEventRecord(s->ev0, s->st));
+  if (graph_possible(s)) TRY(step_graph(s, &nsteps));
   for (int n = 0; n < nsteps; ++n) {
     TRY(iter_impl(s));
     // spill lists are drained into the tiles at least every 16 steps
@@ -1165,6 +1390,8 @@ zc_status zc_get_info(zc_sim *s, zc_info *info) {
   info->tile[1] = s->TY;
   info->ntiles[0] = s->ntx;
   info->ntiles[1] = s->nty;
+  info->relayouts = s->n_relayout;
+  info->captures = s->n_capture;
   return ZC_OK;
 }
 
@@ -1222,14 +1449,330 @@ zc_status zc_reset_profile(zc_sim *s) {
 }
 
 const char *zc_phase_name(int p) {
-  static const char *names[ZC_NPHASE] = {"push", "spill", "migrate", "kin_energy", "zero", "fold",
-                                         "smooth", "yee", "emf_gc", "ext", "window", "sort"};
+  static const char *names[ZC_NPHASE] = {"push", "spill", "migrate", "kin_energy", "zero",  "fold",   "smooth",
+                                         "yee",  "emf_gc", "ext",   "window",     "sort", "history"};
   return (p >= 0 && p < ZC_NPHASE) ? names[p] : "unknown";
 }
 
 zc_status zc_last_step_ms(zc_sim *s, float *ms) {
   if (!s || !ms) return fail(ZC_EINVAL, "null argument");
   *ms = s->last_ms;
+  return ZC_OK;
+}
+
+zc_status zc_set_graphs(zc_sim *s, int on) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  if (!on) invalidate_graph(s);
+  s->use_graph = on ? 1 : 0;
+  return ZC_OK;
+}
+
+zc_status zc_history_enable(zc_sim *s, int max_steps) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (max_steps < 0) return fail(ZC_EINVAL, "max_steps must be >= 0");
+  if (s->sp.size() + 6 > 64) return fail(ZC_EINVAL, "energy history holds at most 58 species");
+  DeviceGuard g(s->device);
+  CK(cudaStreamSynchronize(s->st));
+  invalidate_graph(s);
+  dfree(s->d_hist);
+  dfree(s->d_hist_n);
+  dfree(s->d_hist_part);
+  dfree(s->d_ekin_ptrs);
+  s->hist_cap = 0;
+  s->hist_cols = 0;
+  if (max_steps == 0) return ZC_OK;
+  const int cols = 6 + (int)s->sp.size();
+  // a small grid gets few blocks (each thread sums >= 4 cells), so that a
+  // per-step history stays cheap
+  const long long cells = (long long)s->nx * s->ny;
+  s->hist_blocks = (int)std::max<long long>(1, std::min<long long>(s->energy_blocks, (cells + 1023) / 1024));
+  TRY(dalloc(&s->d_hist, (size_t)max_steps * cols));
+  TRY(dalloc(&s->d_hist_n, 1));
+  TRY(dalloc(&s->d_hist_part, 6 * (size_t)s->hist_blocks));
+  TRY(dalloc(&s->d_ekin_ptrs, std::max<size_t>(1, s->sp.size())));
+  std::vector<double *> ptrs;
+  for (auto &p : s->sp) ptrs.push_back(p.d_ekin);
+  if (!ptrs.empty())
+    CK(cudaMemcpyAsync(s->d_ekin_ptrs, ptrs.data(), sizeof(double *) * ptrs.size(), cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemsetAsync(s->d_hist_n, 0, sizeof(int), s->st));
+  CK(cudaStreamSynchronize(s->st));
+  s->hist_cap = max_steps;
+  s->hist_cols = cols;
+  return ZC_OK;
+}
+
+zc_status zc_history_get(zc_sim *s, double *out, int cap_rows, int *nrows, int *ncols) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  int n = 0;
+  if (s->d_hist) {
+    CK(cudaMemcpyAsync(&n, s->d_hist_n, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+  }
+  if (nrows) *nrows = n;
+  if (ncols) *ncols = s->hist_cols;
+  if (!out || n == 0) return ZC_OK;
+  if (cap_rows < n) return fail(ZC_EINVAL, "output buffer holds %d rows, %d recorded", cap_rows, n);
+  CK(cudaMemcpyAsync(out, s->d_hist, sizeof(double) * (size_t)n * s->hist_cols, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+zc_status zc_history_reset(zc_sim *s) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (!s->d_hist) return ZC_OK;
+  DeviceGuard g(s->device);
+  CK(cudaMemsetAsync(s->d_hist_n, 0, sizeof(int), s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// batched runs
+// ===========================================================================
+struct zc_batch {
+  std::vector<zc_sim *> sims;
+  int device = 0;
+  int period = 0;
+  cudaStream_t st = nullptr;
+  // one graph per run length (a whole block, a prefix for the remainder):
+  // every member's captured steps as a parallel branch
+  struct Parent {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int nsteps = 0;
+    bool valid = false;
+    std::vector<unsigned long long> ids;  // the member captures it copies
+    std::vector<cudaGraphNode_t> nodes;   // their child nodes
+  } blk, tail;
+  int **d_errp = nullptr;   // every member's error word
+  int *d_errs = nullptr;    // their copy after a block, [2][n]
+  int *h_errs = nullptr;    // pinned, [2][n]
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_blk[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> ev_sim;  // one per member, joins of its stream
+  float last_ms = 0;
+};
+
+namespace {
+
+void drop_parent(zc_batch::Parent &g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g = zc_batch::Parent{};
+}
+
+// makes `pg` run n steps of every member from its current state,
+// recapturing what is stale
+zc_status batch_ready(zc_batch *b, zc_batch::Parent &pg, int n) {
+  const bool have = pg.valid && pg.nsteps == n && pg.ids.size() == b->sims.size();
+  bool ok = have;
+  for (size_t k = 0; k < b->sims.size(); ++k) {
+    zc_sim *s = b->sims[k];
+    StepGraph &g = (n == b->period) ? s->blk : s->tail;
+    if (!graph_ready(s, g, n)) TRY(capture_steps(s, n, g));
+    if (have && pg.ids[k] != g.id) {
+      // a member was captured again (after a re-layout): its copy in the
+      // instantiated graph takes the new parameters in place when the
+      // topology is unchanged, else everything is rebuilt
+      if (cudaGraphExecChildGraphNodeSetParams(pg.exec, pg.nodes[k], g.graph) == cudaSuccess) {
+        pg.ids[k] = g.id;
+      } else {
+        cudaGetLastError();
+        ok = false;
+      }
+    }
+  }
+  if (ok) return ZC_OK;
+  drop_parent(pg);
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  for (zc_sim *s : b->sims) {
+    StepGraph &sg = (n == b->period) ? s->blk : s->tail;
+    cudaGraphNode_t node;
+    const cudaError_t e = cudaGraphAddChildGraphNode(&node, g, nullptr, 0, sg.graph);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return fail(ZC_ECUDA, "cudaGraphAddChildGraphNode failed: %s", cudaGetErrorString(e));
+    }
+    pg.nodes.push_back(node);
+  }
+  cudaGraphExec_t x = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(ZC_ECUDA, "batch graph instantiation failed: %s", cudaGetErrorString(e));
+  }
+  pg.graph = g;
+  pg.exec = x;
+  pg.nsteps = n;
+  pg.valid = true;
+  pg.ids.clear();
+  for (zc_sim *s : b->sims) pg.ids.push_back(((n == b->period) ? s->blk : s->tail).id);
+  return ZC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+zc_status zc_batch_create(zc_sim *const *sims, int nsims, zc_batch **out) {
+  if (!sims || nsims <= 0 || !out) return fail(ZC_EINVAL, "invalid batch members");
+  *out = nullptr;
+  const int dev = sims[0] ? sims[0]->device : 0;
+  int period = 0;
+  for (int k = 0; k < nsims; ++k) {
+    zc_sim *s = sims[k];
+    if (!s) return fail(ZC_EINVAL, "null member %d", k);
+    if (s->device != dev) return fail(ZC_EINVAL, "members must share one device");
+    if (s->mw) return fail(ZC_EINVAL, "member %d has a moving window", k);
+    if (s->sp.empty()) return fail(ZC_EINVAL, "member %d has no species", k);
+    if (k == 0) period = block_period(s);
+    if (block_period(s) != period) return fail(ZC_EINVAL, "members must share sort_every");
+    for (int j = 0; j < k; ++j)
+      if (sims[j] == s) return fail(ZC_EINVAL, "member %d appears twice", k);
+  }
+  DeviceGuard g(dev);
+  zc_batch *b = new zc_batch();
+  b->sims.assign(sims, sims + nsims);
+  b->device = dev;
+  b->period = period;
+  zc_status st = ZC_OK;
+  auto bad = [&](zc_status r) {
+    zc_batch_destroy(b);
+    return r;
+  };
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bad(fail(ZC_ECUDA, "cudaStreamCreate failed"));
+  if ((st = dalloc(&b->d_errp, nsims)) != ZC_OK) return bad(st);
+  if ((st = dalloc(&b->d_errs, 2 * (size_t)nsims)) != ZC_OK) return bad(st);
+  if (cudaMallocHost((void **)&b->h_errs, 2 * sizeof(int) * nsims) != cudaSuccess)
+    return bad(fail(ZC_ENOMEM, "cudaMallocHost failed"));
+  std::vector<int *> ptrs;
+  for (zc_sim *s : b->sims) ptrs.push_back(s->d_err);
+  if (cudaMemcpy(b->d_errp, ptrs.data(), sizeof(int *) * nsims, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bad(fail(ZC_ECUDA, "upload of member error words failed"));
+  if (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_blk[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_blk[1], cudaEventDisableTiming) != cudaSuccess)
+    return bad(fail(ZC_ECUDA, "cudaEventCreate failed"));
+  b->ev_sim.assign(nsims, nullptr);
+  for (auto &e : b->ev_sim)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      return bad(fail(ZC_ECUDA, "cudaEventCreate failed"));
+  *out = b;
+  return ZC_OK;
+}
+
+zc_status zc_batch_destroy(zc_batch *b) {
+  if (!b) return ZC_OK;
+  DeviceGuard g(b->device);
+  if (b->st) cudaStreamSynchronize(b->st);
+  drop_parent(b->blk);
+  drop_parent(b->tail);
+  dfree(b->d_errp);
+  dfree(b->d_errs);
+  if (b->h_errs) cudaFreeHost(b->h_errs);
+  for (auto e : {b->ev0, b->ev1, b->ev_blk[0], b->ev_blk[1]})
+    if (e) cudaEventDestroy(e);
+  for (auto e : b->ev_sim)
+    if (e) cudaEventDestroy(e);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return ZC_OK;
+}
+
+zc_status zc_batch_step(zc_batch *b, int nsteps) {
+  if (!b) return fail(ZC_EINVAL, "null batch handle");
+  if (nsteps < 0) return fail(ZC_EINVAL, "nsteps must be >= 0");
+  DeviceGuard g(b->device);
+  const int n = (int)b->sims.size();
+  const int P = b->period;
+  for (zc_sim *s : b->sims) {
+    if (s->mw) return fail(ZC_ESTATE, "a member has a moving window");
+    if (block_period(s) != P) return fail(ZC_ESTATE, "a member changed its sort_every");
+    if (s->profiling) return fail(ZC_ESTATE, "a member has profiling on");
+  }
+  CK(cudaEventRecord(b->ev0, b->st));
+  for (zc_sim *s : b->sims) {
+    CK(cudaEventRecord(s->ev0, b->st));
+    CK(cudaStreamWaitEvent(s->st, s->ev0, 0));
+  }
+  // members off a block boundary step eagerly on their own streams up to
+  // it; the whole blocks every member can then take, and a common prefix of
+  // a block for the rest, run as batch graphs; what is left, eagerly
+  std::vector<int> lead(n);
+  int blocks = nsteps / P;
+  bool aligned = true;
+  for (int k = 0; k < n; ++k) {
+    zc_sim *s = b->sims[k];
+    lead[k] = std::min(nsteps, (P - s->iter % P) % P);
+    for (int i = 0; i < lead[k]; ++i) TRY(iter_impl(s));
+    blocks = std::min(blocks, (nsteps - lead[k]) / P);
+    aligned = aligned && lead[k] == 0;
+  }
+  const int rest = aligned ? nsteps - blocks * P : 0;
+  if (blocks > 0 || rest > 0) {
+    for (int k = 0; k < n; ++k) {
+      CK(cudaEventRecord(b->ev_sim[k], b->sims[k]->st));
+      CK(cudaStreamWaitEvent(b->st, b->ev_sim[k], 0));
+    }
+    for (int i = 0; i < blocks; ++i) {
+      TRY(batch_ready(b, b->blk, P));
+      CK(cudaGraphLaunch(b->blk.exec, b->st));
+      for (zc_sim *s : b->sims) account_steps(s, s->blk);
+      const int slot = i & 1;
+      CK(launch_gather_words(b->d_errp, n, b->d_errs + (size_t)slot * n, b->st));
+      CK(cudaMemcpyAsync(b->h_errs + (size_t)slot * n, b->d_errs + (size_t)slot * n, sizeof(int) * n,
+                         cudaMemcpyDeviceToHost, b->st));
+      CK(cudaEventRecord(b->ev_blk[slot], b->st));
+      if (i > 0) {
+        // the previous block's error words, read while this block runs
+        CK(cudaEventSynchronize(b->ev_blk[1 - slot]));
+        bool any = false;
+        for (int k = 0; k < n; ++k) any |= b->h_errs[(size_t)(1 - slot) * n + k] != 0;
+        if (any) {
+          CK(cudaStreamSynchronize(b->st));
+          std::memset(b->h_errs, 0, 2 * sizeof(int) * n);
+          for (int k = 0; k < n; ++k) {
+            zc_sim *s = b->sims[k];
+            TRY(check_errors(s, true));  // a spill re-lays a member out
+            CK(cudaEventRecord(b->ev_sim[k], s->st));
+            CK(cudaStreamWaitEvent(b->st, b->ev_sim[k], 0));
+          }
+        }
+      }
+    }
+    if (rest > 0) {
+      TRY(batch_ready(b, b->tail, rest));
+      CK(cudaGraphLaunch(b->tail.exec, b->st));
+      for (zc_sim *s : b->sims) account_steps(s, s->tail);
+    }
+    CK(cudaEventRecord(b->ev_blk[0], b->st));
+    for (zc_sim *s : b->sims) CK(cudaStreamWaitEvent(s->st, b->ev_blk[0], 0));
+  }
+  for (int k = 0; k < n; ++k) {
+    zc_sim *s = b->sims[k];
+    const int m = nsteps - lead[k] - blocks * P - rest;
+    for (int i = 0; i < m; ++i) TRY(iter_impl(s));
+  }
+  for (zc_sim *s : b->sims) {
+    CK(cudaEventRecord(s->ev1, s->st));
+    CK(cudaStreamWaitEvent(b->st, s->ev1, 0));
+  }
+  CK(cudaEventRecord(b->ev1, b->st));
+  CK(cudaEventSynchronize(b->ev1));
+  cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+  for (zc_sim *s : b->sims) TRY(check_errors(s, true));
+  return ZC_OK;
+}
+
+zc_status zc_batch_last_ms(zc_batch *b, float *ms) {
+  if (!b || !ms) return fail(ZC_EINVAL, "null argument");
+  *ms = b->last_ms;
   return ZC_OK;
 }
 

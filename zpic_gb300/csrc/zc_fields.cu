@@ -552,6 +552,45 @@ cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, i
   return cudaGetLastError();
 }
 
+// one history row: the field energy from the partials (the sum of
+// k_emf_energy_final) and the kinetic energy of every species; the row index
+// is a device counter, so a captured step appends where it runs
+__global__ void k_energy_history_row(const double *partial, int nblocks, float dx, float dy,
+                                     double *const *ekin, int nsp, double *hist, int *hist_n, int cap, int cols) {
+  const int n = *hist_n;
+  __syncthreads();
+  if (n >= cap) return;
+  double *row = hist + (size_t)n * cols;
+  const int t = threadIdx.x;
+  if (t < 6) {
+    double s = 0;
+    for (int b = 0; b < nblocks; ++b) s += partial[b * 6 + t];
+    row[t] = s * (0.5 * dx * dy);
+  } else if (t - 6 < nsp) {
+    row[t] = *ekin[t - 6];
+  }
+  __syncthreads();
+  if (t == 0) *hist_n = n + 1;
+}
+
+cudaError_t launch_energy_history(const float *EB, const Grid &G, double *partial, int nblocks, double *hist,
+                                  int *hist_n, int cap, int cols, double *const *ekin, int nsp, float dx, float dy,
+                                  cudaStream_t st) {
+  if (nsp + 6 > 64) return cudaErrorInvalidValue;
+  k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);
+  k_energy_history_row<<<1, 64, 0, st>>>(partial, nblocks, dx, dy, ekin, nsp, hist, hist_n, cap, cols);
+  return cudaGetLastError();
+}
+
+__global__ void k_gather_words(int *const *src, int n, int *dst) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) dst[k] = *src[k];
+}
+
+cudaError_t launch_gather_words(int *const *src, int n, int *dst, cudaStream_t st) {
+  k_gather_words<<<(n + 255) / 256, 256, 0, st>>>(src, n, dst);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_laser(float *EB, const Grid &G, const LaserConst &L, cudaStream_t st) {
   dim3 grid((G.nx + 127) / 128, G.ny);
   k_laser_fields<<<grid, 128, 0, st>>>(EB, G, L);

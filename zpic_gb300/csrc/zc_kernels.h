@@ -138,6 +138,13 @@ cudaError_t launch_ext_add(const float *EB, float *EBp, const float *extE, const
 cudaError_t launch_window_shift(const float *EBin, float *EBout, const Grid &G, cudaStream_t st);
 cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, int nblocks, double *out, float dx,
                               float dy, cudaStream_t st);
+// appends one row (6 field-energy components, then each species' kinetic
+// energy) at hist[*hist_n] and increments *hist_n, unless cap rows exist
+cudaError_t launch_energy_history(const float *EB, const Grid &G, double *partial, int nblocks, double *hist,
+                                  int *hist_n, int cap, int cols, double *const *ekin, int nsp, float dx, float dy,
+                                  cudaStream_t st);
+// dst[k] = *src[k] for k < n (error words of a batch)
+cudaError_t launch_gather_words(int *const *src, int n, int *dst, cudaStream_t st);
 struct LaserConst {
   int type;
   float start, rise, flat, fall, a0, omega0, polarization, W0, focus, axis;

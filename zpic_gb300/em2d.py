@@ -111,9 +111,11 @@ def _load():
     P = C.c_void_p
     sigs = {
         "set_rand_seed": (None, [C.c_uint32, C.c_uint32]),
+        "rand_seed_fresh": (None, [C.c_uint32, C.c_uint32]),
         "spec_new": (None, [C.POINTER(t_species), C.c_char_p, C.c_float, P, P, P, P, P, C.c_float,
                             C.POINTER(t_density)]),
         "spec_grow_buffer": (None, [C.POINTER(t_species), C.c_int]),
+        "spec_delete": (None, [C.POINTER(t_species)]),
         "sim_new": (None, [C.POINTER(t_simulation), P, P, C.c_float, C.c_float, C.c_int,
                            C.POINTER(t_species), C.c_int]),
         "sim_delete": (None, [C.POINTER(t_simulation)]),
@@ -236,6 +238,40 @@ class Density:
 # ---------------------------------------------------------------------------
 # Species (em2d.pyx:171-458)
 # ---------------------------------------------------------------------------
+def load_particles(m_q, ppc, nx, box, dt, *, ufl=(0.0, 0.0, 0.0), uth=(0.0, 0.0, 0.0), density=None,
+                   name="species"):
+    """Loads one species on the host exactly as spec_new does
+    (em2d/particles.c:535-612), from the current state of the global random
+    generator (set_rand_seed), and returns (particles, q): the records as a
+    structured array and the charge of one simulation particle."""
+    lib = _load()
+    sp = t_species()
+    nx_a, box_a = _arr(nx, np.int32), _arr(box, np.float32)
+    ppc_a, ufl_a, uth_a = _arr(ppc, np.int32), _arr(ufl, np.float32), _arr(uth, np.float32)
+    dens = density if density is not None else Density()
+    lib.spec_new(C.byref(sp), name.encode(), float(m_q), _ptr(ppc_a), _ptr(ufl_a), _ptr(uth_a), _ptr(nx_a),
+                 _ptr(box_a), float(dt), C.byref(dens._d))
+    try:
+        if sp.np > 0:
+            buf = (t_part * sp.np).from_address(C.addressof(sp.part.contents))
+            parts = np.frombuffer(buf, dtype=PART_DTYPE).copy()
+        else:
+            parts = np.zeros(0, dtype=PART_DTYPE)
+        return parts, float(sp.q)
+    finally:
+        lib.spec_delete(C.byref(sp))
+
+
+def set_rand_seed(w, z, fresh=False):
+    """Seeds the generator used by species loading (em2d/random.c:48-53).
+    The generator is per host thread.  ``fresh`` also drops the cached
+    normal deviate, giving the state of a newly started process."""
+    if fresh:
+        _load().rand_seed_fresh(int(w), int(z))
+    else:
+        _load().set_rand_seed(int(w), int(z))
+
+
 class Species:
     """Species(name, m_q, ppc=[1,1], ufl=[0,0,0], uth=[0,0,0], density=None, n_sort=16)
 
