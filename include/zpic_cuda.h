@@ -244,6 +244,51 @@ ZC_API zc_status zc_batch_step(zc_batch *batch, int nsteps);
 ZC_API zc_status zc_batch_last_ms(zc_batch *batch, float *ms);
 ZC_API zc_status zc_batch_destroy(zc_batch *batch);
 
+/* --- differentiable step (adjoint) --------------------------------------- */
+/* A forward engine of the periodic em2d step (no smoothing, no moving
+ * window) with a charge weight per particle, and its hand-written reverse:
+ * the gradient of the total field energy after the last step (the sum of
+ * emf_get_energy's components, em2d/emf.c:729-750) with respect to every
+ * particle's weight, initial position and momentum, and the initial E and B.
+ * The reverse sweep recomputes the forward run from checkpoints kept every
+ * `checkpoint_every` steps.  Float32 (the reference's arithmetic) or float64
+ * (for finite-difference checks).  No counterpart in the reference, whose
+ * charge is species-wide (em2d/particles.c:557,576). */
+typedef struct zc_adj zc_adj;
+typedef struct {
+    int nx[2];
+    double box[2];
+    double dt;
+    double q;               /* charge of a particle of weight 1 (spec->q) */
+    double m_q;
+    int np;                 /* particles */
+    int checkpoint_every;
+    int precision;          /* 0 float32, 1 float64 */
+    int device;
+} zc_adj_desc;
+ZC_API zc_status zc_adj_create(const zc_adj_desc *desc, zc_adj **out);
+ZC_API zc_status zc_adj_destroy(zc_adj *adj);
+/* initial state: particle cells and in-cell positions (as t_part), momenta,
+ * weights (np each); E and B as 3 planes [component][iy][ix] of nx*ny cells
+ * (NULL: zero) */
+ZC_API zc_status zc_adj_set_state(zc_adj *adj, const int *ix, const int *iy, const double *x, const double *y,
+                                  const double *ux, const double *uy, const double *uz, const double *w,
+                                  const double *E, const double *B);
+/* runs nsteps from the current state, keeping checkpoints; returns the
+ * objective (field energy after the last step) and the kinetic energy of the
+ * last step's particles (NULL to skip either) */
+ZC_API zc_status zc_adj_forward(zc_adj *adj, int nsteps, double *objective, double *kinetic);
+/* gradient of the objective of the last forward run with respect to the
+ * initial state (any pointer may be NULL); the engine's state returns to the
+ * start of that run */
+ZC_API zc_status zc_adj_backward(zc_adj *adj, double *d_w, double *d_x, double *d_y, double *d_ux, double *d_uy,
+                                 double *d_uz, double *d_E, double *d_B);
+/* current state (after a forward run: its end) */
+ZC_API zc_status zc_adj_get_state(zc_adj *adj, int *ix, int *iy, double *x, double *y, double *ux, double *uy,
+                                  double *uz, double *E, double *B);
+/* device time (ms) of the last forward and backward calls, CUDA events */
+ZC_API zc_status zc_adj_times(zc_adj *adj, float *forward_ms, float *backward_ms);
+
 /* --- field energy without device allocation ----------------------------- */
 /* No counterpart in the reference.  Computes the six field-energy components
  * (the first output of zc_energy) of caller-owned device grids -- E and B

@@ -1,0 +1,48 @@
+"""A C input deck compiled against the em2d drop-in headers and linked to
+libzpic_em2d (as a reference deck is linked to the reference's objects):
+it builds here without a GPU, and on a GPU its energies after 10 steps match
+the oracle's run of the same deck."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from decks import build_cpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "zpic_gb300", "lib")
+
+
+def _build(tmp_path):
+    from zpic_gb300 import build
+
+    build.build()
+    exe = str(tmp_path / "deck_weibel")
+    subprocess.run(["gcc", "-O2", "-std=c99", "-I", os.path.join(ROOT, "include", "em2d"),
+                    os.path.join(ROOT, "tests", "c_deck", "deck_weibel.c"), "-L", LIB, "-lzpic_em2d",
+                    f"-Wl,-rpath,{LIB}", "-lm", "-o", exe], check=True)
+    return exe
+
+
+def test_c_deck_compiles_and_links(tmp_path):
+    exe = _build(tmp_path)
+    assert os.path.exists(exe)
+
+
+@pytest.mark.gpu
+def test_c_deck_matches_oracle(tmp_path):
+    exe = _build(tmp_path)
+    r = subprocess.run([exe, "10"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    vals = {"emf": [], "kin": [], "np": []}
+    for line in r.stdout.splitlines():
+        key, v = line.split()
+        vals[key].append(float(v))
+    cpu = build_cpu("weibel_smooth")
+    cpu.iter(10)
+    emf_c = cpu.emf_energy()
+    assert np.all(np.abs(np.array(vals["emf"]) - emf_c) <= 1e-5 * np.abs(emf_c).max())
+    for k in range(2):
+        assert abs(vals["kin"][k] - cpu.energy(k)) <= 1e-5 * abs(cpu.energy(k))
+        assert int(vals["np"][k]) == cpu.np_(k)

@@ -37,6 +37,8 @@ EXPORTS = [
     "zc_last_error", "zc_status_string", "zc_set_profiling", "zc_get_profile", "zc_reset_profile",
     "zc_phase_name", "zc_field_energy_static", "zc_set_graphs", "zc_history_enable", "zc_history_get",
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
+    "zc_adj_create", "zc_adj_destroy", "zc_adj_set_state", "zc_adj_forward", "zc_adj_backward",
+    "zc_adj_get_state", "zc_adj_times",
 ]
 NPHASE = 13
 
@@ -51,6 +53,12 @@ class SimDesc(C.Structure):
     _fields_ = [("nx", C.c_int * 2), ("box", C.c_float * 2), ("dt", C.c_float), ("device", C.c_int),
                 ("tile", C.c_int * 2), ("deterministic", C.c_int), ("tile_slack", C.c_float),
                 ("fast_math", C.c_int), ("sort_every", C.c_int)]
+
+
+class AdjDesc(C.Structure):
+    _fields_ = [("nx", C.c_int * 2), ("box", C.c_double * 2), ("dt", C.c_double), ("q", C.c_double),
+                ("m_q", C.c_double), ("np", C.c_int), ("checkpoint_every", C.c_int), ("precision", C.c_int),
+                ("device", C.c_int)]
 
 
 class SpeciesDesc(C.Structure):
@@ -133,6 +141,13 @@ def load(path: str = LIB_PATH):
         "zc_batch_step": [P, I],
         "zc_batch_last_ms": [P, C.POINTER(C.c_float)],
         "zc_batch_destroy": [P],
+        "zc_adj_create": [C.POINTER(AdjDesc), C.POINTER(P)],
+        "zc_adj_destroy": [P],
+        "zc_adj_set_state": [P] + [P] * 10,
+        "zc_adj_forward": [P, I, P, P],
+        "zc_adj_backward": [P] + [P] * 8,
+        "zc_adj_get_state": [P] + [P] * 9,
+        "zc_adj_times": [P, C.POINTER(C.c_float), C.POINTER(C.c_float)],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

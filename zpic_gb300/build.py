@@ -26,10 +26,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("zc_push_exact.cu", ["--fmad=false"]),
     ("zc_push_fast.cu", ["--fmad=true", "--prec-div=false", "--prec-sqrt=false"]),
+    ("zc_push_exact_det.cu", ["--fmad=false"]),
+    ("zc_push_fast_det.cu", ["--fmad=true", "--prec-div=false", "--prec-sqrt=false"]),
     ("zc_particles.cu", ["--fmad=false"]),
     ("zc_fields.cu", ["--fmad=false"]),
     ("zc_api.cu", []),
     ("zc_noalloc.cu", []),
+    ("zc_adjoint.cu", ["--fmad=false"]),
 ]
 
 

@@ -1,0 +1,1034 @@
+// zc_adjoint.cu -- the differentiable em2d step: a forward engine with
+// per-particle charge weights and its hand-written reverse (adjoint), with
+// checkpointed recomputation, in float32 or float64.
+//
+// The physics is em2d's periodic step (sim_iter, em2d/simulation.c:45-56)
+// without smoothing or moving window: staggered bilinear gather
+// (interpolate_fld, em2d/particles.c:1029-1071), relativistic Boris push and
+// move (particles.c:1145-1207), zigzag current deposit (dep_current_zamb,
+// particles.c:773-924) scaled by the particle's weight, Yee b/2, e, b/2
+// (yee_b / yee_e, em2d/emf.c:500-562).  Fields are periodic nx x ny planes
+// without guard cells; the deposit wraps directly, which is what the
+// guard-cell fold of current_update_gc (em2d/current.c:118-159) computes.
+//
+// The objective is the total field energy after the last step,
+// L = sum over E, B components of 0.5 dx dy sum f^2 (emf_get_energy,
+// em2d/emf.c:729-750).  Its gradient with respect to the initial state --
+// every particle's weight, momenta and position, and the initial E and B --
+// comes from one reverse sweep:
+//   Yee: the transposed curls (forward differences transpose to negative
+//        backward ones on the periodic grid and vice versa);
+//   deposit: the transpose of the deposit is a gather of the current's
+//        adjoint along the same zigzag segments; its derivative with respect
+//        to the start position, the displacement and v_z comes from running
+//        the deposit code on 5-way forward-mode dual numbers;
+//   push: Boris + move on 9-way dual numbers (momentum, E_p, B_p);
+//   gather: its transpose scatters the adjoint of E_p, B_p onto the grid
+//        with the same weights; the derivative of the weights with respect
+//        to the position comes from 2-way dual numbers.
+// The deposit and the gather are piecewise polynomial in the position: the
+// gradient is that of the piece the trajectory lies in (kinks where a
+// trajectory crosses a cell edge or the half-cell of the staggered gather).
+//
+// Checkpoints: the state (particles, E, B) is kept every K steps of the
+// forward run; the reverse sweep recomputes each segment of K steps from its
+// checkpoint, keeping the pre-step states of that segment, and then walks
+// it backwards.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/zpic_cuda.h"
+#include "zc_internal.cuh"
+#include "zc_kernels.h"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// forward-mode dual numbers
+// ---------------------------------------------------------------------------
+template <class R, int N>
+struct Dual {
+  R v;
+  R d[N];
+  __device__ Dual() {}
+  __device__ Dual(R x) : v(x) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = R(0);
+  }
+};
+
+template <class R, int N>
+__device__ __forceinline__ Dual<R, N> seed(R x, int k) {
+  Dual<R, N> r(x);
+  r.d[k] = R(1);
+  return r;
+}
+
+#define DUAL_T template <class R, int N>
+DUAL_T __device__ __forceinline__ Dual<R, N> operator+(const Dual<R, N> &a, const Dual<R, N> &b) {
+  Dual<R, N> r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator-(const Dual<R, N> &a, const Dual<R, N> &b) {
+  Dual<R, N> r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator-(const Dual<R, N> &a) {
+  Dual<R, N> r;
+  r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator*(const Dual<R, N> &a, const Dual<R, N> &b) {
+  Dual<R, N> r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator/(const Dual<R, N> &a, const Dual<R, N> &b) {
+  Dual<R, N> r;
+  r.v = a.v / b.v;
+  const R ib = R(1) / b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator+(const Dual<R, N> &a, R b) {
+  Dual<R, N> r = a;
+  r.v += b;
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator+(R a, const Dual<R, N> &b) { return b + a; }
+DUAL_T __device__ __forceinline__ Dual<R, N> operator-(const Dual<R, N> &a, R b) {
+  Dual<R, N> r = a;
+  r.v -= b;
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator-(R a, const Dual<R, N> &b) {
+  Dual<R, N> r;
+  r.v = a - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -b.d[i];
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator*(const Dual<R, N> &a, R b) {
+  Dual<R, N> r;
+  r.v = a.v * b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b;
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator*(R a, const Dual<R, N> &b) { return b * a; }
+DUAL_T __device__ __forceinline__ Dual<R, N> operator/(const Dual<R, N> &a, R b) {
+  Dual<R, N> r;
+  r.v = a.v / b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / b;
+  return r;
+}
+DUAL_T __device__ __forceinline__ Dual<R, N> operator/(R a, const Dual<R, N> &b) { return Dual<R, N>(a) / b; }
+DUAL_T __device__ __forceinline__ Dual<R, N> sqrt_(const Dual<R, N> &a) {
+  Dual<R, N> r;
+  r.v = sqrt(a.v);
+  const R h = R(0.5) / r.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * h;
+  return r;
+}
+#undef DUAL_T
+
+__device__ __forceinline__ float sqrt_(float a) { return sqrtf(a); }
+__device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
+__device__ __forceinline__ float value(float a) { return a; }
+__device__ __forceinline__ double value(double a) { return a; }
+template <class R, int N>
+__device__ __forceinline__ R value(const Dual<R, N> &a) {
+  return a.v;
+}
+
+// ---------------------------------------------------------------------------
+// state and grids
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+template <class R>
+struct Planes {  // 3 periodic planes [c][j][i], no guard cells
+  R *f;
+  int nx, ny;
+  __device__ __forceinline__ size_t at(int c, int i, int j) const {
+    return (size_t)c * nx * ny + (size_t)wrap(j, ny) * nx + wrap(i, nx);
+  }
+  __device__ __forceinline__ R operator()(int c, int i, int j) const { return f[at(c, i, j)]; }
+};
+
+template <class R>
+struct State {
+  int *ix, *iy;
+  R *x, *y, *ux, *uy, *uz;
+};
+
+template <class R>
+struct Params {
+  int nx, ny, np;
+  R tem, dt_dx, dt_dy, q, qnx, qny;  // qnx = q dx / dt (per unit weight)
+};
+
+// staggered bilinear gather (interpolate_fld): weights of type T, field
+// samples of type R
+template <class R, class T>
+__device__ __forceinline__ T lerp2(const Planes<R> &g, int c, int a, int b, const T &wa, const T &wb) {
+  return (g(c, a, b) * (R(1) - wa) + g(c, a + 1, b) * wa) * (R(1) - wb) +
+         (g(c, a, b + 1) * (R(1) - wa) + g(c, a + 1, b + 1) * wa) * wb;
+}
+
+template <class R, class T>
+__device__ __forceinline__ void gather(const Planes<R> &E, const Planes<R> &B, int i, int j, const T &x, const T &y,
+                                       T f[6]) {
+  const bool lx = value(x) < R(0.5), ly = value(y) < R(0.5);
+  const int ih = i + (lx ? -1 : 0), jh = j + (ly ? -1 : 0);
+  const T w1h = x + (lx ? R(0.5) : R(-0.5));
+  const T w2h = y + (ly ? R(0.5) : R(-0.5));
+  f[0] = lerp2(E, 0, ih, j, w1h, y);
+  f[1] = lerp2(E, 1, i, jh, x, w2h);
+  f[2] = lerp2(E, 2, i, j, x, y);
+  f[3] = lerp2(B, 0, i, jh, x, w2h);
+  f[4] = lerp2(B, 1, ih, j, w1h, y);
+  f[5] = lerp2(B, 2, ih, jh, w1h, w2h);
+}
+
+// transpose of the gather: adds a[c] times the weights of sample c to the
+// grids (ga for E, gb for B)
+template <class R>
+__device__ __forceinline__ void scatter_add(R *ga, R *gb, const Planes<R> &shape, int i, int j, R x, R y,
+                                            const R a[6]) {
+  const bool lx = x < R(0.5), ly = y < R(0.5);
+  const int ih = i + (lx ? -1 : 0), jh = j + (ly ? -1 : 0);
+  const R w1h = x + (lx ? R(0.5) : R(-0.5));
+  const R w2h = y + (ly ? R(0.5) : R(-0.5));
+  auto put = [&](R *g, int c, int a0, int b0, R wa, R wb, R v) {
+    if (v == R(0)) return;
+    atomicAdd(&g[shape.at(c, a0, b0)], v * (R(1) - wa) * (R(1) - wb));
+    atomicAdd(&g[shape.at(c, a0 + 1, b0)], v * wa * (R(1) - wb));
+    atomicAdd(&g[shape.at(c, a0, b0 + 1)], v * (R(1) - wa) * wb);
+    atomicAdd(&g[shape.at(c, a0 + 1, b0 + 1)], v * wa * wb);
+  };
+  put(ga, 0, ih, j, w1h, y, a[0]);
+  put(ga, 1, i, jh, x, w2h, a[1]);
+  put(ga, 2, i, j, x, y, a[2]);
+  put(gb, 0, i, jh, x, w2h, a[3]);
+  put(gb, 1, ih, j, w1h, y, a[4]);
+  put(gb, 2, ih, jh, w1h, w2h, a[5]);
+}
+
+// Boris push and move (particles.c:1145-1207): momentum, E_p, B_p in;
+// new momentum, displacement (cells) and q v_z per unit weight out
+template <class R, class T>
+__device__ __forceinline__ void boris(const T u[3], const T e_in[3], const T b_in[3], const Params<R> &P, T uo[3],
+                                      T &mx, T &my, T &qvz) {
+  const T ex = e_in[0] * P.tem, ey = e_in[1] * P.tem, ez = e_in[2] * P.tem;
+  T tx = u[0] + ex, ty = u[1] + ey, tz = u[2] + ez;
+  const T u2 = tx * tx + ty * ty + tz * tz;
+  const T g = sqrt_(R(1) + u2);
+  const T tg = P.tem / g;
+  T bx = b_in[0] * tg, by = b_in[1] * tg, bz = b_in[2] * tg;
+  const T s2 = R(2) / (R(1) + bx * bx + by * by + bz * bz);
+  const T vx = tx + ty * bz - tz * by;
+  const T vy = ty + tz * bx - tx * bz;
+  const T vz = tz + tx * by - ty * bx;
+  bx = bx * s2;
+  by = by * s2;
+  bz = bz * s2;
+  tx = tx + (vy * bz - vz * by);
+  ty = ty + (vz * bx - vx * bz);
+  tz = tz + (vx * by - vy * bx);
+  uo[0] = tx + ex;
+  uo[1] = ty + ey;
+  uo[2] = tz + ez;
+  const T rg = R(1) / sqrt_(R(1) + uo[0] * uo[0] + uo[1] * uo[1] + uo[2] * uo[2]);
+  mx = P.dt_dx * rg * uo[0];
+  my = P.dt_dy * rg * uo[1];
+  qvz = P.q * uo[2] * rg;
+}
+
+// kinetic-energy term utsq / (gamma + 1) of the time-centred momentum
+template <class R>
+__device__ __forceinline__ R kinetic(const R u[3], const R e_in[3], const Params<R> &P) {
+  const R tx = u[0] + e_in[0] * P.tem, ty = u[1] + e_in[1] * P.tem, tz = u[2] + e_in[2] * P.tem;
+  const R u2 = tx * tx + ty * ty + tz * tz;
+  return u2 / (sqrt_(R(1) + u2) + R(1));
+}
+
+// the 8 contributions of one straight segment inside one cell
+// (particles.c:886-922), per unit weight
+template <class R, class T, class Sink>
+__device__ __forceinline__ void segment(Sink &sink, int ix, int iy, const T &x0, const T &x1, const T &y0,
+                                        const T &y1, const T &dx, const T &dy, const T &qvz, const Params<R> &P) {
+  const T s0x0 = R(1) - x0, s0x1 = x0, s1x0 = R(1) - x1, s1x1 = x1;
+  const T s0y0 = R(1) - y0, s0y1 = y0, s1y0 = R(1) - y1, s1y1 = y1;
+  const T jx = dx * P.qnx, jy = dy * P.qny;
+  sink.add(0, ix, iy, jx * (R(0.5) * (s0y0 + s1y0)));
+  sink.add(0, ix, iy + 1, jx * (R(0.5) * (s0y1 + s1y1)));
+  sink.add(1, ix, iy, jy * (R(0.5) * (s0x0 + s1x0)));
+  sink.add(1, ix + 1, iy, jy * (R(0.5) * (s0x1 + s1x1)));
+  sink.add(2, ix, iy, qvz * (s0x0 * s0y0 + s1x0 * s1y0 + (s0x0 * s1y0 - s1x0 * s0y0) / R(2)));
+  sink.add(2, ix + 1, iy, qvz * (s0x1 * s0y0 + s1x1 * s1y0 + (s0x1 * s1y0 - s1x1 * s0y0) / R(2)));
+  sink.add(2, ix, iy + 1, qvz * (s0x0 * s0y1 + s1x0 * s1y1 + (s0x0 * s1y1 - s1x0 * s0y1) / R(2)));
+  sink.add(2, ix + 1, iy + 1, qvz * (s0x1 * s0y1 + s1x1 * s1y1 + (s0x1 * s1y1 - s1x1 * s0y1) / R(2)));
+}
+
+template <class T>
+struct SegT {
+  T x0, x1, y0, y1, dx, dy, qvz;
+  int ix, iy;
+};
+
+// splits segment a at its y cell edge: a keeps the part before the edge, the
+// returned segment holds the rest (particles.c:842-871)
+template <class R, class T>
+__device__ __forceinline__ SegT<T> split_y(SegT<T> &a, int dj) {
+  const R yb = (dj == 1) ? R(1) : R(0);
+  const T f = (a.y1 - yb) / a.dy;
+  const T xc = a.x0 + a.dx * (R(1) - f);
+  SegT<T> n;
+  n.y0 = T(R(1) - yb);
+  n.y1 = a.y1 - R(dj);
+  n.dy = a.dy * f;
+  n.iy = a.iy + dj;
+  n.x0 = xc;
+  n.x1 = a.x1;
+  n.dx = a.dx * f;
+  n.ix = a.ix;
+  n.qvz = a.qvz * f;
+  a.y1 = T(yb);
+  a.dy = a.dy * (R(1) - f);
+  a.dx = a.dx * (R(1) - f);
+  a.x1 = xc;
+  a.qvz = a.qvz * (R(1) - f);
+  return n;
+}
+
+template <class R, class T, class Sink>
+__device__ __forceinline__ void deposit_seg(Sink &sink, const SegT<T> &s, const Params<R> &P) {
+  segment(sink, s.ix, s.iy, s.x0, s.x1, s.y0, s.y1, s.dx, s.dy, s.qvz, P);
+}
+
+// zigzag split of a motion into at most 3 segments (particles.c:773-879)
+template <class R, class T, class Sink>
+__device__ __forceinline__ void zigzag(Sink &sink, int ix, int iy, const T &x0, const T &y0, const T &dx,
+                                       const T &dy, const T &qvz, const Params<R> &P) {
+  SegT<T> a;
+  a.x0 = x0;
+  a.y0 = y0;
+  a.dx = dx;
+  a.dy = dy;
+  a.x1 = x0 + dx;
+  a.y1 = y0 + dy;
+  a.qvz = qvz * R(0.5);
+  a.ix = ix;
+  a.iy = iy;
+  const int di = (value(a.x1) >= R(1)) - (value(a.x1) < R(0));
+  const int dj = (value(a.y1) >= R(1)) - (value(a.y1) < R(0));
+  if (di != 0) {
+    const R xb = (di == 1) ? R(1) : R(0);
+    const T f = (a.x1 - xb) / dx;
+    const T yc = y0 + dy * (R(1) - f);
+    SegT<T> b;
+    b.x0 = T(R(1) - xb);
+    b.x1 = a.x1 - R(di);
+    b.dx = dx * f;
+    b.ix = ix + di;
+    b.y0 = yc;
+    b.y1 = a.y1;
+    b.dy = dy * f;
+    b.iy = iy;
+    b.qvz = a.qvz * f;
+    a.x1 = T(xb);
+    a.dx = a.dx * (R(1) - f);
+    a.dy = a.dy * (R(1) - f);
+    a.y1 = yc;
+    a.qvz = a.qvz * (R(1) - f);
+    if (dj != 0) {
+      if (value(a.y1) < R(0) || value(a.y1) >= R(1)) {
+        // the first piece crosses the y edge; the x tail lies past it
+        const SegT<T> c = split_y<R, T>(a, dj);
+        b.y0 = b.y0 - R(dj);
+        b.y1 = b.y1 - R(dj);
+        b.iy += dj;
+        deposit_seg(sink, c, P);
+      } else {
+        const SegT<T> c = split_y<R, T>(b, dj);
+        deposit_seg(sink, c, P);
+      }
+    }
+    deposit_seg(sink, b, P);
+  } else if (dj != 0) {
+    const SegT<T> c = split_y<R, T>(a, dj);
+    deposit_seg(sink, c, P);
+  }
+  deposit_seg(sink, a, P);
+}
+
+// ---------------------------------------------------------------------------
+// sinks of the deposit
+// ---------------------------------------------------------------------------
+template <class R>
+struct DepositSink {  // forward: J += w * contribution
+  Planes<R> J;
+  R w;
+  __device__ __forceinline__ void add(int c, int i, int j, R v) const { atomicAdd(&J.f[J.at(c, i, j)], w * v); }
+};
+
+template <class R, int N>
+struct AdjointSink {  // reverse: sum of lambda_J * contribution (per unit weight)
+  Planes<R> lamJ;
+  Dual<R, N> acc;
+  __device__ __forceinline__ void add(int c, int i, int j, const Dual<R, N> &v) {
+    const R l = lamJ(c, i, j);
+    acc.v += l * v.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc.d[k] += l * v.d[k];
+  }
+};
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void k_adj_push(State<R> s, State<R> o, const R *w, Planes<R> E, Planes<R> B, Planes<R> J,
+                           double *ekin, Params<R> P) {
+  double ek = 0;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.np; p += gridDim.x * blockDim.x) {
+    const int ix = s.ix[p], iy = s.iy[p];
+    const R x = s.x[p], y = s.y[p];
+    const R u[3] = {s.ux[p], s.uy[p], s.uz[p]};
+    R f[6];
+    gather<R, R>(E, B, ix, iy, x, y, f);
+    ek += (double)w[p] * (double)kinetic(u, f, P);
+    R uo[3], mx, my, qvz;
+    boris<R, R>(u, f, f + 3, P, uo, mx, my, qvz);
+    DepositSink<R> sink{J, w[p]};
+    zigzag<R, R>(sink, ix, iy, x, y, mx, my, qvz, P);
+    R x1 = x + mx, y1 = y + my;
+    const int di = (x1 >= R(1)) - (x1 < R(0)), dj = (y1 >= R(1)) - (y1 < R(0));
+    x1 -= R(di);
+    y1 -= R(dj);
+    o.ix[p] = wrap(ix + di, P.nx);
+    o.iy[p] = wrap(iy + dj, P.ny);
+    o.x[p] = x1;
+    o.y[p] = y1;
+    o.ux[p] = uo[0];
+    o.uy[p] = uo[1];
+    o.uz[p] = uo[2];
+  }
+  if (ekin && ek != 0.0) atomicAdd(ekin, ek);
+}
+
+// reverse of one particle step: lam (x, y, ux, uy, uz) of the particle after
+// the step in, before the step out (in place); lamE / lamB receive the
+// transpose of the gather; dw the weight's derivative
+template <class R>
+__global__ void __launch_bounds__(128) k_adj_push_rev(State<R> s, const R *w, Planes<R> E, Planes<R> B,
+                                                      Planes<R> lamJ, State<R> lam, R *lamE, R *lamB, R *dw,
+                                                      Params<R> P) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.np; p += gridDim.x * blockDim.x) {
+    const int ix = s.ix[p], iy = s.iy[p];
+    const R x = s.x[p], y = s.y[p];
+    const R wp = w[p];
+    // 1. gather with d/dx, d/dy
+    Dual<R, 2> fd[6];
+    gather<R, Dual<R, 2>>(E, B, ix, iy, seed<R, 2>(x, 0), seed<R, 2>(y, 1), fd);
+    // 2. Boris + move with d/d(u, E_p, B_p)
+    Dual<R, 9> u9[3], e9[3], b9[3];
+    u9[0] = seed<R, 9>(s.ux[p], 0);
+    u9[1] = seed<R, 9>(s.uy[p], 1);
+    u9[2] = seed<R, 9>(s.uz[p], 2);
+    for (int c = 0; c < 3; ++c) {
+      e9[c] = seed<R, 9>(fd[c].v, 3 + c);
+      b9[c] = seed<R, 9>(fd[3 + c].v, 6 + c);
+    }
+    Dual<R, 9> uo[3], mx, my, qvz;
+    boris<R, Dual<R, 9>>(u9, e9, b9, P, uo, mx, my, qvz);
+    // 3. deposit with d/d(x, y, mx, my, qvz)
+    AdjointSink<R, 5> sink{lamJ, Dual<R, 5>(R(0))};
+    zigzag<R, Dual<R, 5>>(sink, ix, iy, seed<R, 5>(x, 0), seed<R, 5>(y, 1), seed<R, 5>(mx.v, 2),
+                          seed<R, 5>(my.v, 3), seed<R, 5>(qvz.v, 4), P);
+    dw[p] += sink.acc.v;
+    // 4. cotangents of the Boris outputs
+    const R lx1 = lam.x[p], ly1 = lam.y[p];
+    const R lo[6] = {lam.ux[p], lam.uy[p], lam.uz[p], lx1 + wp * sink.acc.d[2], ly1 + wp * sink.acc.d[3],
+                     wp * sink.acc.d[4]};
+    const Dual<R, 9> *outs[6] = {&uo[0], &uo[1], &uo[2], &mx, &my, &qvz};
+    R l9[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      R a = 0;
+#pragma unroll
+      for (int m = 0; m < 6; ++m) a += lo[m] * outs[m]->d[k];
+      l9[k] = a;
+    }
+    // 5. position: direct (x1 = x + mx - di), deposit, and the gather weights
+    R lx = lx1 + wp * sink.acc.d[0], ly = ly1 + wp * sink.acc.d[1];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      lx += l9[3 + c] * fd[c].d[0];
+      ly += l9[3 + c] * fd[c].d[1];
+    }
+    lam.x[p] = lx;
+    lam.y[p] = ly;
+    lam.ux[p] = l9[0];
+    lam.uy[p] = l9[1];
+    lam.uz[p] = l9[2];
+    // 6. transpose of the gather
+    scatter_add(lamE, lamB, E, ix, iy, x, y, l9 + 3);
+  }
+}
+
+// B -= c curl E  (yee_b with c = dt/2)
+template <class R>
+__global__ void k_adj_yee_b(const R *E, R *B, int nx, int ny, R cx, R cy) {
+  const size_t pl = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k % nx), j = (int)(k / nx);
+    const int ip = wrap(i + 1, nx), jp = wrap(j + 1, ny);
+    const R *Ex = E, *Ey = E + pl, *Ez = E + 2 * pl;
+    B[k] += -cy * (Ez[(size_t)jp * nx + i] - Ez[k]);
+    B[pl + k] += cx * (Ez[(size_t)j * nx + ip] - Ez[k]);
+    B[2 * pl + k] += -cx * (Ey[(size_t)j * nx + ip] - Ey[k]) + cy * (Ex[(size_t)jp * nx + i] - Ex[k]);
+  }
+}
+
+// E += dt curl B - dt J  (yee_e)
+template <class R>
+__global__ void k_adj_yee_e(R *E, const R *B, const R *J, int nx, int ny, R cx, R cy, R dt) {
+  const size_t pl = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k % nx), j = (int)(k / nx);
+    const int im = wrap(i - 1, nx), jm = wrap(j - 1, ny);
+    const R *Bx = B, *By = B + pl, *Bz = B + 2 * pl;
+    E[k] += cy * (Bz[k] - Bz[(size_t)jm * nx + i]) - dt * J[k];
+    E[pl + k] += -cx * (Bz[k] - Bz[(size_t)j * nx + im]) - dt * J[pl + k];
+    E[2 * pl + k] += cx * (By[k] - By[(size_t)j * nx + im]) - cy * (Bx[k] - Bx[(size_t)jm * nx + i]) - dt * J[2 * pl + k];
+  }
+}
+
+// transpose of k_adj_yee_b: lamE += transpose(-c curl) lamB
+template <class R>
+__global__ void k_adj_yee_b_T(const R *lB, R *lE, int nx, int ny, R cx, R cy) {
+  const size_t pl = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k % nx), j = (int)(k / nx);
+    const int im = wrap(i - 1, nx), jm = wrap(j - 1, ny);
+    const R *ax = lB, *ay = lB + pl, *az = lB + 2 * pl;
+    // B.x(i,j) -= cy (Ez(i,j+1) - Ez(i,j)); B.y += cx (Ez(i+1,j) - Ez(i,j));
+    // B.z += -cx (Ey(i+1,j) - Ey(i,j)) + cy (Ex(i,j+1) - Ex(i,j))
+    lE[k] += cy * (az[(size_t)jm * nx + i] - az[k]);
+    lE[pl + k] += -cx * (az[(size_t)j * nx + im] - az[k]);
+    lE[2 * pl + k] += -cy * (ax[(size_t)jm * nx + i] - ax[k]) + cx * (ay[(size_t)j * nx + im] - ay[k]);
+  }
+}
+
+// transpose of k_adj_yee_e: lamB += transpose(dt curl) lamE, lamJ = -dt lamE
+template <class R>
+__global__ void k_adj_yee_e_T(const R *lE, R *lB, R *lJ, int nx, int ny, R cx, R cy, R dt) {
+  const size_t pl = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k % nx), j = (int)(k / nx);
+    const int ip = wrap(i + 1, nx), jp = wrap(j + 1, ny);
+    const R *ax = lE, *ay = lE + pl, *az = lE + 2 * pl;
+    // E.x += cy (Bz(i,j) - Bz(i,j-1)); E.y += -cx (Bz(i,j) - Bz(i-1,j));
+    // E.z += cx (By(i,j) - By(i-1,j)) - cy (Bx(i,j) - Bx(i,j-1))
+    lB[k] += -cy * (az[k] - az[(size_t)jp * nx + i]);
+    lB[pl + k] += cx * (az[k] - az[(size_t)j * nx + ip]);
+    lB[2 * pl + k] += cy * (ax[k] - ax[(size_t)jp * nx + i]) - cx * (ay[k] - ay[(size_t)j * nx + ip]);
+    lJ[k] = -dt * ax[k];
+    lJ[pl + k] = -dt * ay[k];
+    lJ[2 * pl + k] = -dt * az[k];
+  }
+}
+
+// sum of squares of n values (field energy), double accumulation
+template <class R>
+__global__ void k_adj_sumsq(const R *f, size_t n, double *out) {
+  __shared__ double sred[8];
+  double s = 0;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    s += (double)f[k] * (double)f[k];
+  s = zc::block_sum_double<256>(s, sred);
+  if (threadIdx.x == 0) atomicAdd(out, s);
+}
+
+template <class R>
+__global__ void k_adj_scale(const R *src, R *dst, size_t n, R a) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    dst[k] = a * src[k];
+}
+
+template <class R>
+__global__ void k_to_double(const R *src, double *dst, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    dst[k] = (double)src[k];
+}
+
+template <class R>
+__global__ void k_from_double(const double *src, R *dst, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    dst[k] = (R)src[k];
+}
+
+int grid_for(size_t n, int per = 256) { return (int)std::max<size_t>(1, std::min<size_t>((n + per - 1) / per, 152 * 8)); }
+
+zc_status afail(zc_status s, const char *msg) {
+  zc::set_error_message(msg);
+  return s;
+}
+
+#define ACK(call)                                                                                   \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) {                                                                        \
+      char b_[256];                                                                                 \
+      snprintf(b_, sizeof b_, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return afail(ZC_ECUDA, b_);                                                                   \
+    }                                                                                               \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// host engine
+// ---------------------------------------------------------------------------
+#define TRY_(c)                   \
+  do {                            \
+    zc_status s_ = (c);           \
+    if (s_ != ZC_OK) return s_;   \
+  } while (0)
+
+struct EngineBase {
+  virtual ~EngineBase() {}
+  virtual zc_status set_state(const int *ix, const int *iy, const double *x, const double *y, const double *ux,
+                              const double *uy, const double *uz, const double *w, const double *E,
+                              const double *B) = 0;
+  virtual zc_status forward(int nsteps, double *objective, double *kin) = 0;
+  virtual zc_status backward(double *dw, double *dx, double *dy, double *dux, double *duy, double *duz, double *dE,
+                             double *dB) = 0;
+  virtual zc_status get_state(int *ix, int *iy, double *x, double *y, double *ux, double *uy, double *uz,
+                              double *E, double *B) = 0;
+  float fwd_ms = 0, bwd_ms = 0;
+};
+
+template <class R>
+struct DevState {
+  int *ix = nullptr, *iy = nullptr;
+  R *v = nullptr;  // x, y, ux, uy, uz: 5 arrays of np
+  State<R> view(int np) const { return State<R>{ix, iy, v, v + np, v + 2 * (size_t)np, v + 3 * (size_t)np, v + 4 * (size_t)np}; }
+};
+
+template <class R>
+struct Engine : EngineBase {
+  int dev, nx, ny, np, K;
+  double dx, dy, dt, q, m_q;
+  size_t pl = 0;  // cells per plane
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  R *w = nullptr;
+  DevState<R> cur, nxt;
+  R *E = nullptr, *B = nullptr, *J = nullptr;
+  // checkpoints (state + E + B) every K steps, and one segment of pre-step states
+  std::vector<DevState<R>> ck_s;
+  std::vector<R *> ck_f;  // 6 planes each
+  int nck = 0;            // checkpoints of the last forward run (slots are reused)
+  std::vector<DevState<R>> seg_s;
+  std::vector<R *> seg_f;
+  int steps_done = 0;
+  bool have_state = false;
+  // reverse
+  R *lamE = nullptr, *lamB = nullptr, *lamJ = nullptr, *dwv = nullptr;
+  DevState<R> lam;
+  double *d_scr = nullptr;  // scratch doubles
+  std::vector<void *> owned;
+
+  template <class T>
+  zc_status alloc(T **p, size_t n) {
+    if (cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+      return afail(ZC_ENOMEM, "adjoint engine: device allocation failed");
+    owned.push_back(*p);
+    return ZC_OK;
+  }
+  zc_status alloc_state(DevState<R> &s) {
+    TRY_(alloc(&s.ix, np));
+    TRY_(alloc(&s.iy, np));
+    TRY_(alloc(&s.v, 5 * (size_t)np));
+    return ZC_OK;
+  }
+
+  Params<R> params() const {
+    Params<R> P;
+    P.nx = nx;
+    P.ny = ny;
+    P.np = np;
+    P.tem = (R)(0.5 * dt / m_q);
+    P.dt_dx = (R)(dt / dx);
+    P.dt_dy = (R)(dt / dy);
+    P.q = (R)q;
+    P.qnx = (R)(q * dx / dt);
+    P.qny = (R)(q * dy / dt);
+    return P;
+  }
+  Planes<R> planes(R *f) const { return Planes<R>{f, nx, ny}; }
+
+  zc_status init(int dev_, int nx_, int ny_, int np_, int K_, double dx_, double dy_, double dt_, double q_,
+                 double m_q_) {
+    dev = dev_;
+    nx = nx_;
+    ny = ny_;
+    np = np_;
+    K = K_;
+    dx = dx_;
+    dy = dy_;
+    dt = dt_;
+    q = q_;
+    m_q = m_q_;
+    pl = (size_t)nx * ny;
+    ACK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    ACK(cudaEventCreate(&e0));
+    ACK(cudaEventCreate(&e1));
+    TRY_(alloc(&w, np));
+    TRY_(alloc_state(cur));
+    TRY_(alloc_state(nxt));
+    TRY_(alloc_state(lam));
+    TRY_(alloc(&E, 3 * pl));
+    TRY_(alloc(&B, 3 * pl));
+    TRY_(alloc(&J, 3 * pl));
+    TRY_(alloc(&lamE, 3 * pl));
+    TRY_(alloc(&lamB, 3 * pl));
+    TRY_(alloc(&lamJ, 3 * pl));
+    TRY_(alloc(&dwv, np));
+    TRY_(alloc(&d_scr, 16));
+    seg_s.resize(K);
+    seg_f.resize(K);
+    for (int k = 0; k < K; ++k) {
+      TRY_(alloc_state(seg_s[k]));
+      TRY_(alloc(&seg_f[k], 6 * pl));
+    }
+    return ZC_OK;
+  }
+
+  ~Engine() override {
+    if (st) cudaStreamSynchronize(st);
+    for (void *p : owned) cudaFree(p);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  zc_status upload(R *dst, const double *src, size_t n) {
+    if (!src) return ZC_OK;
+    double *tmp = nullptr;
+    ACK(cudaMallocAsync((void **)&tmp, n * sizeof(double), st));
+    ACK(cudaMemcpyAsync(tmp, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_from_double<R><<<grid_for(n), 256, 0, st>>>(tmp, dst, n);
+    ACK(cudaGetLastError());
+    ACK(cudaFreeAsync(tmp, st));
+    return ZC_OK;
+  }
+  zc_status download(double *dst, const R *src, size_t n) {
+    if (!dst) return ZC_OK;
+    double *tmp = nullptr;
+    ACK(cudaMallocAsync((void **)&tmp, n * sizeof(double), st));
+    k_to_double<R><<<grid_for(n), 256, 0, st>>>(src, tmp, n);
+    ACK(cudaGetLastError());
+    ACK(cudaMemcpyAsync(dst, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ACK(cudaFreeAsync(tmp, st));
+    return ZC_OK;
+  }
+
+  zc_status set_state(const int *ix, const int *iy, const double *x, const double *y, const double *ux,
+                      const double *uy, const double *uz, const double *wt, const double *Eh,
+                      const double *Bh) override {
+    ACK(cudaMemcpyAsync(cur.ix, ix, sizeof(int) * np, cudaMemcpyHostToDevice, st));
+    ACK(cudaMemcpyAsync(cur.iy, iy, sizeof(int) * np, cudaMemcpyHostToDevice, st));
+    const State<R> v = cur.view(np);
+    TRY_(upload(v.x, x, np));
+    TRY_(upload(v.y, y, np));
+    TRY_(upload(v.ux, ux, np));
+    TRY_(upload(v.uy, uy, np));
+    TRY_(upload(v.uz, uz, np));
+    TRY_(upload(w, wt, np));
+    if (Eh) TRY_(upload(E, Eh, 3 * pl));
+    else ACK(cudaMemsetAsync(E, 0, sizeof(R) * 3 * pl, st));
+    if (Bh) TRY_(upload(B, Bh, 3 * pl));
+    else ACK(cudaMemsetAsync(B, 0, sizeof(R) * 3 * pl, st));
+    ACK(cudaStreamSynchronize(st));
+    nck = 0;
+    steps_done = 0;
+    have_state = true;
+    return ZC_OK;
+  }
+
+  zc_status copy_state(DevState<R> &dst, const DevState<R> &src) {
+    ACK(cudaMemcpyAsync(dst.ix, src.ix, sizeof(int) * np, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(dst.iy, src.iy, sizeof(int) * np, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(dst.v, src.v, sizeof(R) * 5 * (size_t)np, cudaMemcpyDeviceToDevice, st));
+    return ZC_OK;
+  }
+
+  // one step of the forward engine: cur -> nxt, E, B advanced
+  zc_status step(double *ekin) {
+    const Params<R> P = params();
+    ACK(cudaMemsetAsync(J, 0, sizeof(R) * 3 * pl, st));
+    k_adj_push<R><<<grid_for(np, 256), 256, 0, st>>>(cur.view(np), nxt.view(np), w, planes(E), planes(B),
+                                                      planes(J), ekin, P);
+    ACK(cudaGetLastError());
+    const R hx = (R)(0.5 * dt / dx), hy = (R)(0.5 * dt / dy);
+    const R cx = (R)(dt / dx), cy = (R)(dt / dy);
+    k_adj_yee_b<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
+    k_adj_yee_e<R><<<grid_for(pl), 256, 0, st>>>(E, B, J, nx, ny, cx, cy, (R)dt);
+    k_adj_yee_b<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
+    ACK(cudaGetLastError());
+    std::swap(cur, nxt);
+    return ZC_OK;
+  }
+
+  zc_status save_checkpoint() {
+    if (nck == (int)ck_s.size()) {
+      DevState<R> s;
+      R *f = nullptr;
+      TRY_(alloc_state(s));
+      TRY_(alloc(&f, 6 * pl));
+      ck_s.push_back(s);
+      ck_f.push_back(f);
+    }
+    TRY_(copy_state(ck_s[nck], cur));
+    ACK(cudaMemcpyAsync(ck_f[nck], E, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(ck_f[nck] + 3 * pl, B, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+    ++nck;
+    return ZC_OK;
+  }
+
+  zc_status restore_checkpoint(int k) {
+    TRY_(copy_state(cur, ck_s[k]));
+    ACK(cudaMemcpyAsync(E, ck_f[k], sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(B, ck_f[k] + 3 * pl, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+    return ZC_OK;
+  }
+
+  zc_status objective(double *out) {
+    ACK(cudaMemsetAsync(d_scr, 0, sizeof(double), st));
+    k_adj_sumsq<R><<<grid_for(3 * pl), 256, 0, st>>>(E, 3 * pl, d_scr);
+    k_adj_sumsq<R><<<grid_for(3 * pl), 256, 0, st>>>(B, 3 * pl, d_scr);
+    ACK(cudaGetLastError());
+    double v = 0;
+    ACK(cudaMemcpyAsync(&v, d_scr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    *out = 0.5 * dx * dy * v;
+    return ZC_OK;
+  }
+
+  zc_status forward(int nsteps, double *obj, double *kin) override {
+    if (!have_state) return afail(ZC_ESTATE, "adjoint engine: no initial state");
+    if (nsteps <= 0) return afail(ZC_EINVAL, "adjoint engine: nsteps must be > 0");
+    ACK(cudaEventRecord(e0, st));
+    nck = 0;
+    ACK(cudaMemsetAsync(d_scr + 1, 0, sizeof(double), st));
+    for (int n = 0; n < nsteps; ++n) {
+      if (n % K == 0) TRY_(save_checkpoint());
+      TRY_(step(n == nsteps - 1 ? d_scr + 1 : nullptr));
+    }
+    steps_done = nsteps;
+    ACK(cudaEventRecord(e1, st));
+    if (obj) TRY_(objective(obj));
+    if (kin) {
+      // q m_q dx dy sum w utsq/(gamma+1) of the last step (particles.c:1231)
+      double v = 0;
+      ACK(cudaMemcpyAsync(&v, d_scr + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+      ACK(cudaStreamSynchronize(st));
+      *kin = q * m_q * v * dx * dy;
+    }
+    ACK(cudaEventSynchronize(e1));
+    cudaEventElapsedTime(&fwd_ms, e0, e1);
+    return ZC_OK;
+  }
+
+  zc_status backward(double *dwh, double *dxh, double *dyh, double *duxh, double *duyh, double *duzh, double *dEh,
+                     double *dBh) override {
+    if (steps_done <= 0) return afail(ZC_ESTATE, "adjoint engine: run forward first");
+    // the particles and fields at the end are needed again below: the last
+    // step's state is the current one
+    ACK(cudaEventRecord(e0, st));
+    const Params<R> P = params();
+    const R a = (R)(dx * dy);
+    k_adj_scale<R><<<grid_for(3 * pl), 256, 0, st>>>(E, lamE, 3 * pl, a);
+    k_adj_scale<R><<<grid_for(3 * pl), 256, 0, st>>>(B, lamB, 3 * pl, a);
+    ACK(cudaMemsetAsync(lam.v, 0, sizeof(R) * 5 * (size_t)np, st));
+    ACK(cudaMemsetAsync(dwv, 0, sizeof(R) * np, st));
+    const R hx = (R)(0.5 * dt / dx), hy = (R)(0.5 * dt / dy);
+    const R cx = (R)(dt / dx), cy = (R)(dt / dy);
+    for (int sgi = nck - 1; sgi >= 0; --sgi) {
+      const int n0 = sgi * K, n1 = std::min(steps_done, n0 + K);
+      // recompute the segment from its checkpoint, keeping pre-step states
+      TRY_(restore_checkpoint(sgi));
+      for (int n = n0; n < n1; ++n) {
+        const int k = n - n0;
+        TRY_(copy_state(seg_s[k], cur));
+        ACK(cudaMemcpyAsync(seg_f[k], E, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+        ACK(cudaMemcpyAsync(seg_f[k] + 3 * pl, B, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+        if (n + 1 < n1) TRY_(step(nullptr));
+      }
+      // walk the segment backwards
+      for (int n = n1 - 1; n >= n0; --n) {
+        const int k = n - n0;
+        k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+        k_adj_yee_e_T<R><<<grid_for(pl), 256, 0, st>>>(lamE, lamB, lamJ, nx, ny, cx, cy, (R)dt);
+        k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+        k_adj_push_rev<R><<<grid_for(np, 128), 128, 0, st>>>(seg_s[k].view(np), w, planes(seg_f[k]),
+                                                              planes(seg_f[k] + 3 * pl), planes(lamJ), lam.view(np),
+                                                              lamE, lamB, dwv, P);
+        ACK(cudaGetLastError());
+      }
+    }
+    ACK(cudaEventRecord(e1, st));
+    const State<R> l = lam.view(np);
+    TRY_(download(dwh, dwv, np));
+    TRY_(download(dxh, l.x, np));
+    TRY_(download(dyh, l.y, np));
+    TRY_(download(duxh, l.ux, np));
+    TRY_(download(duyh, l.uy, np));
+    TRY_(download(duzh, l.uz, np));
+    TRY_(download(dEh, lamE, 3 * pl));
+    TRY_(download(dBh, lamB, 3 * pl));
+    // the engine's state goes back to the start of the run
+    TRY_(restore_checkpoint(0));
+    ACK(cudaStreamSynchronize(st));
+    cudaEventElapsedTime(&bwd_ms, e0, e1);
+    steps_done = 0;
+    return ZC_OK;
+  }
+
+  zc_status get_state(int *ix, int *iy, double *x, double *y, double *ux, double *uy, double *uz, double *Eh,
+                      double *Bh) override {
+    if (ix) ACK(cudaMemcpyAsync(ix, cur.ix, sizeof(int) * np, cudaMemcpyDeviceToHost, st));
+    if (iy) ACK(cudaMemcpyAsync(iy, cur.iy, sizeof(int) * np, cudaMemcpyDeviceToHost, st));
+    const State<R> v = cur.view(np);
+    TRY_(download(x, v.x, np));
+    TRY_(download(y, v.y, np));
+    TRY_(download(ux, v.ux, np));
+    TRY_(download(uy, v.uy, np));
+    TRY_(download(uz, v.uz, np));
+    TRY_(download(Eh, E, 3 * pl));
+    TRY_(download(Bh, B, 3 * pl));
+    ACK(cudaStreamSynchronize(st));
+    return ZC_OK;
+  }
+};
+#undef TRY_
+
+}  // namespace
+
+struct zc_adj {
+  int device = 0;
+  std::unique_ptr<EngineBase> eng;
+};
+
+namespace {
+struct AdjDevice {
+  int prev = -1;
+  explicit AdjDevice(int d) {
+    cudaGetDevice(&prev);
+    if (prev != d) cudaSetDevice(d);
+  }
+  ~AdjDevice() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+}  // namespace
+
+extern "C" {
+
+zc_status zc_adj_create(const zc_adj_desc *d, zc_adj **out) {
+  if (!d || !out) return afail(ZC_EINVAL, "null argument");
+  *out = nullptr;
+  if (d->nx[0] < 2 || d->nx[1] < 2 || d->np < 0 || d->checkpoint_every <= 0)
+    return afail(ZC_EINVAL, "adjoint engine: invalid sizes");
+  if (!(d->box[0] > 0) || !(d->box[1] > 0) || !(d->dt > 0) || d->m_q == 0)
+    return afail(ZC_EINVAL, "adjoint engine: box, dt must be > 0 and m_q non-zero");
+  const double dx = d->box[0] / d->nx[0], dy = d->box[1] / d->nx[1];
+  const double cour = std::sqrt(1.0 / (1.0 / (dx * dx) + 1.0 / (dy * dy)));
+  if (d->dt >= cour) return afail(ZC_EINVAL, "Invalid timestep, courant condition violation");
+  if (d->precision != 0 && d->precision != 1) return afail(ZC_EINVAL, "precision must be 0 (float) or 1 (double)");
+  AdjDevice g(d->device);
+  zc_adj *h = new zc_adj();
+  h->device = d->device;
+  zc_status st;
+  if (d->precision == 0) {
+    auto *e = new Engine<float>();
+    h->eng.reset(e);
+    st = e->init(d->device, d->nx[0], d->nx[1], d->np, d->checkpoint_every, dx, dy, d->dt, d->q, d->m_q);
+  } else {
+    auto *e = new Engine<double>();
+    h->eng.reset(e);
+    st = e->init(d->device, d->nx[0], d->nx[1], d->np, d->checkpoint_every, dx, dy, d->dt, d->q, d->m_q);
+  }
+  if (st != ZC_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return ZC_OK;
+}
+
+zc_status zc_adj_destroy(zc_adj *h) {
+  if (!h) return ZC_OK;
+  AdjDevice g(h->device);
+  delete h;
+  return ZC_OK;
+}
+
+zc_status zc_adj_set_state(zc_adj *h, const int *ix, const int *iy, const double *x, const double *y,
+                           const double *ux, const double *uy, const double *uz, const double *w, const double *E,
+                           const double *B) {
+  if (!h) return afail(ZC_EINVAL, "null handle");
+  if (!ix || !iy || !x || !y || !ux || !uy || !uz || !w) return afail(ZC_EINVAL, "null particle array");
+  AdjDevice g(h->device);
+  return h->eng->set_state(ix, iy, x, y, ux, uy, uz, w, E, B);
+}
+
+zc_status zc_adj_forward(zc_adj *h, int nsteps, double *objective, double *kinetic) {
+  if (!h) return afail(ZC_EINVAL, "null handle");
+  AdjDevice g(h->device);
+  return h->eng->forward(nsteps, objective, kinetic);
+}
+
+zc_status zc_adj_backward(zc_adj *h, double *dw, double *dx, double *dy, double *dux, double *duy, double *duz,
+                          double *dE, double *dB) {
+  if (!h) return afail(ZC_EINVAL, "null handle");
+  AdjDevice g(h->device);
+  return h->eng->backward(dw, dx, dy, dux, duy, duz, dE, dB);
+}
+
+zc_status zc_adj_get_state(zc_adj *h, int *ix, int *iy, double *x, double *y, double *ux, double *uy, double *uz,
+                           double *E, double *B) {
+  if (!h) return afail(ZC_EINVAL, "null handle");
+  AdjDevice g(h->device);
+  return h->eng->get_state(ix, iy, x, y, ux, uy, uz, E, B);
+}
+
+zc_status zc_adj_times(zc_adj *h, float *forward_ms, float *backward_ms) {
+  if (!h) return afail(ZC_EINVAL, "null handle");
+  if (forward_ms) *forward_ms = h->eng->fwd_ms;
+  if (backward_ms) *backward_ms = h->eng->bwd_ms;
+  return ZC_OK;
+}
+
+}  // extern "C"

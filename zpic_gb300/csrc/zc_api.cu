@@ -161,6 +161,7 @@ struct zc_sim {
   float3 ext_E0{0, 0, 0}, ext_B0{0, 0, 0};
   float *J[2] = {nullptr, nullptr};
   int j_cur = 0;
+  unsigned long long *Jfix = nullptr;   // deterministic mode: fixed-point J planes
   CUtensorMap tmK_EB[2], tmK_EBp, tmK_J;
   CUtensorMap tmY_EB[2], tmY_J[2];
   int TX = 16, TY = 16, ntx = 0, nty = 0, ntiles = 0;
@@ -264,6 +265,8 @@ LayoutConst layout(const zc_sim *s) { return LayoutConst{s->TX, s->TY, s->ntx, s
 TileSet tiles(SpeciesState &p, int ntiles) { return TileSet{p.d_off, p.d_cap, p.d_np, ntiles}; }
 
 Spill spill_of(SpeciesState &p, int k) { return Spill{p.spill[k], p.d_spill_cnt + k, p.spill_cap}; }
+
+FixedJ fixed_j(const zc_sim *s) { return FixedJ{s->Jfix, s->G.pitch, s->G.plane}; }
 
 // outbox slots per tile: room for a moving-window column plus crossers
 // (more leavers than slots go to the spill list)
@@ -472,7 +475,7 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   {
     Phase ph(s, ZC_PHASE_SPILL, 0);
     CK(cudaMemsetAsync(p.d_spill_cnt + out, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(p.d_ekin_extra, 0, sizeof(double), st));
+    CK(cudaMemsetAsync(p.d_ekin_extra, 0, 2 * sizeof(double), st));
   }
   PushLaunch a;
   a.tm_eb = s->EBp ? &s->tmK_EBp : &s->tmK_EB[s->eb_cur];
@@ -490,6 +493,8 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   a.TX = s->TX;
   a.TY = s->TY;
   a.fast = s->fast;
+  a.det = s->deterministic;
+  a.fj = fixed_j(s);
   if (s->sort_every > 0 && p.iter % s->sort_every == 0) {
     // keep the tiles sorted by cell (the push warps then share cells)
     Phase ph(s, ZC_PHASE_SORT, 1);
@@ -505,8 +510,13 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   const float *EBpart = s->EBp ? s->EBp : s->EB[s->eb_cur];
   {
     Phase ph(s, ZC_PHASE_SPILL, 1);
-    CK(launch_push_spill(EBpart, s->J[0], s->G, p.spill[in], p.d_spill_cnt + in, p.spill_cap, spill_of(p, out),
-                         p.d_ekin_extra, s->d_err, C, 152, s->fast, st));
+    CK(launch_push_spill(EBpart, s->J[0], fixed_j(s), s->G, p.spill[in], p.d_spill_cnt + in, p.spill_cap,
+                         spill_of(p, out), p.d_ekin_extra, s->d_err, C, 152, s->fast, s->deterministic, st));
+  }
+  if (s->deterministic) {
+    // the float J the rest of the step reads: the fixed-point sum so far
+    Phase ph(s, ZC_PHASE_ZERO, 1);
+    CK(launch_fixed_to_float(s->Jfix, s->J[0], 3 * s->G.plane, st));
   }
   p.ob_in = 1 - p.ob_in;
   p.pending = true;
@@ -515,7 +525,7 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   {
     Phase ph(s, ZC_PHASE_KIN_ENERGY, 1);
     CK(launch_sum_energy(p.d_ekin_tile, s->ntiles, p.d_ekin_extra, p.d_ekin, p.q * p.m_q, s->dx[0], s->dx[1],
-                         st));
+                         s->deterministic, st));
   }
   p.iter += 1;
   if (shift) {
@@ -640,6 +650,7 @@ zc_status emf_advance_impl(zc_sim *s) {
 zc_status current_zero_impl(zc_sim *s) {
   Phase ph(s, ZC_PHASE_ZERO, 0);
   CK(cudaMemsetAsync(s->J[0], 0, sizeof(float) * 3 * s->G.plane, s->st));
+  if (s->deterministic) CK(cudaMemsetAsync(s->Jfix, 0, sizeof(unsigned long long) * 3 * s->G.plane, s->st));
   s->j_cur = 0;
   return ZC_OK;
 }
@@ -928,6 +939,14 @@ zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
     cudaMemsetAsync(s->EB[b], 0, sizeof(float) * 6 * G.plane, s->st);
     cudaMemsetAsync(s->J[b], 0, sizeof(float) * 3 * G.plane, s->st);
   }
+  if (s->deterministic) {
+    TRYC(dalloc(&s->Jfix, 3 * G.plane));
+    cudaMemsetAsync(s->Jfix, 0, sizeof(unsigned long long) * 3 * G.plane, s->st);
+    if ((s->fast ? prepare_push_tiles_fast_det(TX, TY) : prepare_push_tiles_exact_det(TX, TY)) != cudaSuccess) {
+      st = fail(ZC_ECUDA, "deterministic push kernels: shared-memory limit not set");
+      goto bad;
+    }
+  }
   TRYC(dalloc(&s->d_err, 1));
   cudaMemsetAsync(s->d_err, 0, sizeof(int), s->st);
   if (cudaMallocHost((void **)&s->h_pinned, 64 * sizeof(int)) != cudaSuccess) {
@@ -995,6 +1014,7 @@ zc_status zc_sim_destroy(zc_sim *s) {
     dfree(s->EB[b]);
     dfree(s->J[b]);
   }
+  dfree(s->Jfix);
   dfree(s->EBp);
   dfree(s->extE);
   dfree(s->extB);
@@ -1050,10 +1070,10 @@ zc_status zc_species_create(zc_sim *s, const zc_species_desc *d, const zc_part *
   TRY(alloc_particles(p.spill[0], p.spill_cap));
   TRY(alloc_particles(p.spill[1], p.spill_cap));
   TRY(dalloc(&p.d_ekin_tile, nt));
-  TRY(dalloc(&p.d_ekin_extra, 1));
+  TRY(dalloc(&p.d_ekin_extra, 2));  // deterministic mode: two fixed-point words
   TRY(dalloc(&p.d_ekin, 1));
   CK(cudaMemsetAsync(p.d_ekin, 0, sizeof(double), s->st));
-  CK(cudaMemsetAsync(p.d_ekin_extra, 0, sizeof(double), s->st));
+  CK(cudaMemsetAsync(p.d_ekin_extra, 0, 2 * sizeof(double), s->st));
   TRY(zc_species_set_particles(s, k, parts, np));
   if (id) *id = k;
   return ZC_OK;
@@ -1343,6 +1363,10 @@ zc_status zc_set_current(zc_sim *s, const float *J) {
   DeviceGuard g(s->device);
   TRY(grid_up(s, J, s->J[0]));
   s->j_cur = 0;
+  if (s->deterministic) {
+    CK(launch_float_to_fixed(s->J[0], s->Jfix, 3 * s->G.plane, s->st));
+    CK(cudaStreamSynchronize(s->st));
+  }
   return ZC_OK;
 }
 

@@ -37,6 +37,31 @@ struct LayoutConst {
   int TX, TY, ntx, nty, nx, ny;
 };
 
+// Deterministic mode: the current is accumulated as 64-bit fixed point,
+// every contribution rounded once to a multiple of 2^-40.  Integer sums are
+// exact, so the result does not depend on the order of the additions (warp
+// order, atomics, tiles, spill list): runs are bit-reproducible.  Range:
+// |J| < 2^23 per cell and component.  Kinetic-energy terms are split into a
+// multiple of 2^-30 and a remainder counted in units of 2^-62, each summed
+// as a 64-bit integer (range 2^33, resolution 2^-62).
+struct FixedJ {
+  unsigned long long *p;  // 3 planes laid out as the float J planes
+  int pitch;
+  size_t plane;
+};
+constexpr double kJFixScale = 1099511627776.0;         // 2^40
+constexpr double kEFixHi = 1073741824.0;                 // 2^30
+constexpr double kEFixLo = 4611686018427387904.0;        // 2^62
+
+// a kinetic-energy term as two integers (hi in units of 2^-30, lo of 2^-62)
+__device__ __forceinline__ void efix_split(double v, long long &hi, long long &lo) {
+  hi = __double2ll_rn(v * kEFixHi);
+  lo = __double2ll_rn((v - (double)hi / kEFixHi) * kEFixLo);
+}
+__host__ __device__ __forceinline__ double efix_join(long long hi, long long lo) {
+  return (double)hi / kEFixHi + (double)lo / kEFixLo;
+}
+
 struct PushLaunch {
   const CUtensorMap *tm_eb, *tm_j;
   Particles pin, pout;
@@ -48,6 +73,8 @@ struct PushLaunch {
   PushConst C;
   int ntiles, TX, TY;
   int fast;                               // 1: FMA build of the push kernels
+  int det;                                // 1: fixed-point currents into fj
+  FixedJ fj;
 };
 
 #ifdef __CUDACC__
@@ -71,15 +98,28 @@ bool tile_supported(int TX, int TY);
 cudaError_t launch_push_tiles(const PushLaunch &a, cudaStream_t st);
 cudaError_t launch_push_tiles_exact(const PushLaunch &a, cudaStream_t st);
 cudaError_t launch_push_tiles_fast(const PushLaunch &a, cudaStream_t st);
-cudaError_t launch_push_spill(const float *EB, float *J, const Grid &G, const Particles &sin, const int *sin_cnt,
-                              int sin_cap, const Spill &S, double *ekin, int *err, const PushConst &C,
-                              int nblocks, int fast, cudaStream_t st);
-cudaError_t launch_push_spill_exact(const float *EB, float *J, const Grid &G, const Particles &sin,
-                                    const int *sin_cnt, int sin_cap, const Spill &S, double *ekin, int *err,
-                                    const PushConst &C, int nblocks, cudaStream_t st);
-cudaError_t launch_push_spill_fast(const float *EB, float *J, const Grid &G, const Particles &sin,
-                                   const int *sin_cnt, int sin_cap, const Spill &S, double *ekin, int *err,
-                                   const PushConst &C, int nblocks, cudaStream_t st);
+cudaError_t launch_push_tiles_exact_det(const PushLaunch &a, cudaStream_t st);
+cudaError_t launch_push_tiles_fast_det(const PushLaunch &a, cudaStream_t st);
+// sets the shared-memory limit of the deterministic push kernels of one
+// tile shape on the current device (outside any stream capture)
+cudaError_t prepare_push_tiles_exact_det(int TX, int TY);
+cudaError_t prepare_push_tiles_fast_det(int TX, int TY);
+// spill push; with det, currents go to fj and the kinetic energy to ekin[0..1]
+// read as the two 64-bit fixed-point words of efix_join
+cudaError_t launch_push_spill(const float *EB, float *J, const FixedJ &fj, const Grid &G, const Particles &sin,
+                              const int *sin_cnt, int sin_cap, const Spill &S, double *ekin, int *err,
+                              const PushConst &C, int nblocks, int fast, int det, cudaStream_t st);
+#define ZC_SPILL_LAUNCHER(name)                                                                              \
+  cudaError_t name(const float *EB, float *J, const FixedJ &fj, const Grid &G, const Particles &sin,          \
+                   const int *sin_cnt, int sin_cap, const Spill &S, double *ekin, int *err, const PushConst &C, \
+                   int nblocks, cudaStream_t st)
+ZC_SPILL_LAUNCHER(launch_push_spill_exact);
+ZC_SPILL_LAUNCHER(launch_push_spill_fast);
+ZC_SPILL_LAUNCHER(launch_push_spill_exact_det);
+ZC_SPILL_LAUNCHER(launch_push_spill_fast_det);
+// fixed-point current planes <-> float planes (n values)
+cudaError_t launch_fixed_to_float(const unsigned long long *src, float *dst, size_t n, cudaStream_t st);
+cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, size_t n, cudaStream_t st);
 // stable counting sort of every tile by cell (src -> dst, same layout)
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, const int *np,
                             const LayoutConst &L, int ntiles, cudaStream_t st);
@@ -106,8 +146,10 @@ cudaError_t launch_list_to_aos(const Particles &list, const int *n_ptr, int n_ca
 cudaError_t launch_charge(const Particles &buf, const int *off, const int *np, int ntiles, const Particles &spill,
                           const int *spill_cnt, int spill_cap, float *rho, int nx, int ny, float q, int mw,
                           cudaStream_t st);
+// with det, extra[0..1] are the two 64-bit fixed-point words of a kinetic
+// energy (efix_join)
 cudaError_t launch_sum_energy(const double *tiles, int ntiles, const double *extra, double *out, float q_mq,
-                              float dx, float dy, cudaStream_t st);
+                              float dx, float dy, int det, cudaStream_t st);
 
 // fields
 struct YeeConst {

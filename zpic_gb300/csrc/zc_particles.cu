@@ -11,6 +11,8 @@
 //   k_cellsort    one CTA per tile: counting sort of the tile by cell, so
 //                 that the lanes of a push warp share cells.
 //   re-layout     upload, moving-window injection and capacity changes.
+#include <algorithm>
+
 #include "zc_internal.cuh"
 #include "zc_kernels.h"
 
@@ -343,13 +345,18 @@ __global__ void k_charge_fold(float *rho, int nx, int ny, int mw) {
 
 // sum of the per-tile kinetic-energy partials in a fixed order
 __global__ void k_sum_energy(const double *tiles, int ntiles, const double *extra, double *out, float scale_q_mq,
-                             float dx, float dy) {
+                             float dx, float dy, int det) {
   __shared__ double sred[8];
   double s = 0;
   for (int t = threadIdx.x; t < ntiles; t += 256) s += tiles[t];
   s = block_sum_double<256>(s, sred);
   if (threadIdx.x == 0) {
-    s += *extra;
+    if (det) {
+      const long long *w = reinterpret_cast<const long long *>(extra);
+      s += efix_join(w[0], w[1]);
+    } else {
+      s += *extra;
+    }
     // spec->energy = q * m_q * energy * dx * dy  (particles.c:1231)
     *out = scale_q_mq * s * dx * dy;
   }
@@ -364,14 +371,38 @@ bool tile_supported(int TX, int TY) {
 }
 
 cudaError_t launch_push_tiles(const PushLaunch &a, cudaStream_t st) {
+  if (a.det) return a.fast ? launch_push_tiles_fast_det(a, st) : launch_push_tiles_exact_det(a, st);
   return a.fast ? launch_push_tiles_fast(a, st) : launch_push_tiles_exact(a, st);
 }
 
-cudaError_t launch_push_spill(const float *EB, float *J, const Grid &G, const Particles &sin, const int *sin_cnt,
-                              int sin_cap, const Spill &S, double *ekin, int *err, const PushConst &C,
-                              int nblocks, int fast, cudaStream_t st) {
-  return fast ? launch_push_spill_fast(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C, nblocks, st)
-              : launch_push_spill_exact(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C, nblocks, st);
+cudaError_t launch_push_spill(const float *EB, float *J, const FixedJ &fj, const Grid &G, const Particles &sin,
+                              const int *sin_cnt, int sin_cap, const Spill &S, double *ekin, int *err,
+                              const PushConst &C, int nblocks, int fast, int det, cudaStream_t st) {
+  auto f = det ? (fast ? launch_push_spill_fast_det : launch_push_spill_exact_det)
+               : (fast ? launch_push_spill_fast : launch_push_spill_exact);
+  return f(EB, J, fj, G, sin, sin_cnt, sin_cap, S, ekin, err, C, nblocks, st);
+}
+
+__global__ void k_fixed_to_float(const unsigned long long *src, float *dst, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    dst[k] = (float)((double)(long long)src[k] / kJFixScale);
+}
+
+__global__ void k_float_to_fixed(const float *src, unsigned long long *dst, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    dst[k] = (unsigned long long)__double2ll_rn((double)src[k] * kJFixScale);
+}
+
+cudaError_t launch_fixed_to_float(const unsigned long long *src, float *dst, size_t n, cudaStream_t st) {
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  k_fixed_to_float<<<blocks, 256, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, size_t n, cudaStream_t st) {
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  k_float_to_fixed<<<blocks, 256, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, const int *np,
@@ -454,8 +485,8 @@ cudaError_t launch_charge(const Particles &buf, const int *off, const int *np, i
 }
 
 cudaError_t launch_sum_energy(const double *tiles, int ntiles, const double *extra, double *out, float q_mq,
-                              float dx, float dy, cudaStream_t st) {
-  k_sum_energy<<<1, 256, 0, st>>>(tiles, ntiles, extra, out, q_mq, dx, dy);
+                              float dx, float dy, int det, cudaStream_t st) {
+  k_sum_energy<<<1, 256, 0, st>>>(tiles, ntiles, extra, out, q_mq, dx, dy, det);
   return cudaGetLastError();
 }
 

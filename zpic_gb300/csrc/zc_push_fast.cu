@@ -1,7 +1,7 @@
 // zc_push_fast.cu -- the fast build of the push + deposit kernels
 // (zc_push_impl.cuh).  Compiled with FMA contraction and approximate float32 division / square
 // root: same algorithm, results within a few float32 ulps per operation of
-// the exact build.
+// the exact build.  The deterministic-mode variants are in zc_push_fast_det.cu.
 #include "zc_internal.cuh"
 #include "zc_kernels.h"
 
@@ -11,13 +11,11 @@ namespace fast {
 }  // namespace fast
 
 cudaError_t launch_push_tiles_fast(const PushLaunch &a, cudaStream_t st) {
-  return fast::launch_push_tiles_variant(a, st);
+  return fast::launch_push_tiles_variant<false>(a, st);
 }
 
-cudaError_t launch_push_spill_fast(const float *EB, float *J, const Grid &G, const Particles &sin, const int *sin_cnt,
-                                 int sin_cap, const Spill &S, double *ekin, int *err, const PushConst &C,
-                                 int nblocks, cudaStream_t st) {
-  return fast::launch_push_spill_variant(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C, nblocks, st);
+ZC_SPILL_LAUNCHER(launch_push_spill_fast) {
+  return fast::launch_push_spill_variant<false>(EB, J, fj, G, sin, sin_cnt, sin_cap, S, ekin, err, C, nblocks, st);
 }
 
 }  // namespace zc

@@ -66,6 +66,31 @@ struct GlobalCurrent {
   }
 };
 
+// deterministic mode: every contribution rounded once to 64-bit fixed point
+// and summed as integers (exact, so the order of the sums does not matter)
+__device__ __forceinline__ long long to_fixed(float v) { return __double2ll_rn((double)v * kJFixScale); }
+
+template <int BW, int PL>
+struct TileCurrentFixed {
+  unsigned long long *s;
+  __device__ __forceinline__ void add(int c, int i, int j, float v) const { addi(c, i, j, to_fixed(v)); }
+  __device__ __forceinline__ void addi(int c, int i, int j, long long v) const {
+    atomicAdd(&s[c * PL + (j + 1) * BW + (i + 1)], (unsigned long long)v);
+  }
+};
+struct GlobalCurrentFixed {
+  unsigned long long *g;
+  int pitch;
+  size_t plane;
+  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
+    atomicAdd(&g[c * plane + (size_t)(j + 1) * pitch + (i + 1)], (unsigned long long)to_fixed(v));
+  }
+};
+
+// the J tile of a deterministic push (3 planes of 64-bit fixed point) lives
+// in dynamic shared memory
+extern __shared__ __align__(128) unsigned long long zc_push_dyn_smem[];
+
 // ---------------------------------------------------------------------------
 // per-particle physics (restates em2d/particles.c:773-924, 1029-1226)
 // ---------------------------------------------------------------------------
@@ -290,17 +315,19 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 // order of the warps' runs follows their timing.  The main loop has no
 // block-wide barrier.
 // ---------------------------------------------------------------------------
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, bool DET>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
                                                    const __grid_constant__ CUtensorMap tm_j, Particles pin,
                                                    Particles pout, TileSet T, Outbox Oin, Outbox O, Spill S,
-                                                   double *ekin_tile, int *err, PushConst C) {
+                                                   double *ekin_tile, int *err, PushConst C, FixedJ fj) {
   constexpr int BW = (TX + 3 + 3) & ~3;  // halo box width, multiple of 4 floats
   constexpr int BH = TY + 3;
   constexpr int PL = BW * BH;
   constexpr int NW = NT / 32;
   __shared__ __align__(128) float sEB[6 * PL];
-  __shared__ __align__(128) float sJ[3 * PL];
+  __shared__ __align__(128) float sJ[DET ? 4 : 3 * PL];  // float J tile (the fixed one is dynamic)
+  unsigned long long *const sJd = zc_push_dyn_smem;
+  __shared__ unsigned long long s_ekin[2];                // fixed-point kinetic energy (DET)
   __shared__ __align__(8) uint64_t bar;
   __shared__ double sred[NW];
   // per-warp queue of cell-crossing motions, deposited 32 at a time so that
@@ -342,19 +369,30 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     s_nnb = c;
     s_stay = 0;
     s_leave = 0;
+    s_ekin[0] = 0;
+    s_ekin[1] = 0;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     mbar_expect_tx(&bar, 6 * PL * 4);
     tma_load_3d(sEB, &tm_eb, cx0, cy0, 0, &bar);
   }
-  for (int k = threadIdx.x; k < 3 * PL; k += NT) sJ[k] = 0.f;
+  if constexpr (DET) {
+    for (int k = threadIdx.x; k < 3 * PL; k += NT) sJd[k] = 0ull;
+  } else {
+    for (int k = threadIdx.x; k < 3 * PL; k += NT) sJ[k] = 0.f;
+  }
   const bool loaded = mbar_wait_bounded(&bar, 0);
   if (!loaded) errbits |= ERR_TIMEOUT;
   __syncthreads();
 
   const TileFields<BW, PL> fld{sEB};
-  const TileCurrent<BW, PL> dep{sJ};
+  const auto dep = [&] {
+    if constexpr (DET)
+      return TileCurrentFixed<BW, PL>{sJd};
+    else
+      return TileCurrent<BW, PL>{sJ};
+  }();
   const PushConst Cl = C;
   const long long base = T.off[t];
   const int cap = T.cap[t];
@@ -362,6 +400,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   const long long obase = (long long)t * O.cap;
   const int nnb = s_nnb;
   float ks = 0.f, kc = 0.f;
+  long long khi = 0, klo = 0;  // DET: fixed-point kinetic energy of this thread's particles
 
   // deposits queued motion e of this warp (all segments, direct atomics)
   auto deposit_queued = [&](int e) {
@@ -387,7 +426,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     int di, dj;
     bool bad;
     const float kin = push_particle(fld, li, lj, x, y, ux, uy, uz, mx, my, x1, y1, di, dj, qvz, bad, Cl);
-    kahan_add(ks, kc, valid ? kin : 0.f);
+    if constexpr (DET) {
+      long long h, l;
+      efix_split(valid ? (double)kin : 0.0, h, l);
+      khi += h;
+      klo += l;
+    } else {
+      kahan_add(ks, kc, valid ? kin : 0.f);
+    }
     errbits |= (valid && bad) ? ERR_ESCAPE : 0;
     const bool split = valid && ((di != 0) || (dj != 0));
     // the whole motion inside the cell: one segment (particles.c:781-797);
@@ -425,18 +471,46 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       const unsigned lastmask = __ballot_sync(0xffffffffu, lane == 31 || knext != key);
       const int run_last = __ffs(lastmask & (0xffffffffu << lane)) - 1;
       const unsigned maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(run_last - lane + 1));
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        if ((unsigned)off >= maxlen) break;
-        const bool take = lane + off <= run_last;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float o = __shfl_down_sync(0xffffffffu, cur.v[q], off);
-          if (take) cur.v[q] += o;
-        }
-      }
       const bool head = valid && (lane == 0 || kprev != key);
-      if (head) add_current(dep, li, lj, cur);
+      if constexpr (DET) {
+        // each lane's contributions rounded to fixed point, then summed as
+        // integers: the same total whatever lanes hold which particles
+        long long iv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) iv[q] = to_fixed(cur.v[q]);
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          if ((unsigned)off >= maxlen) break;
+          const bool take = lane + off <= run_last;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const long long o = __shfl_down_sync(0xffffffffu, iv[q], off);
+            if (take) iv[q] += o;
+          }
+        }
+        if (head) {
+          dep.addi(0, li, lj, iv[0]);
+          dep.addi(0, li, lj + 1, iv[1]);
+          dep.addi(1, li, lj, iv[2]);
+          dep.addi(1, li + 1, lj, iv[3]);
+          dep.addi(2, li, lj, iv[4]);
+          dep.addi(2, li + 1, lj, iv[5]);
+          dep.addi(2, li, lj + 1, iv[6]);
+          dep.addi(2, li + 1, lj + 1, iv[7]);
+        }
+      } else {
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          if ((unsigned)off >= maxlen) break;
+          const bool take = lane + off <= run_last;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float o = __shfl_down_sync(0xffffffffu, cur.v[q], off);
+            if (take) cur.v[q] += o;
+          }
+        }
+        if (head) add_current(dep, li, lj, cur);
+      }
     }
 
     // queue the cell-crossing motions; deposit them once a full warp's worth
@@ -552,19 +626,46 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     T.np[t] = min(s_stay, cap);
     O.cnt[t] = min(s_leave, O.cap);
   }
-  const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
-  if (threadIdx.x == 0) ekin_tile[t] = e;
-
-  // all shared-memory atomics done: hand the J tile to the TMA unit
-  fence_proxy_async_smem();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (loaded) {
-      tma_reduce_add_3d(&tm_j, sJ, cx0, cy0, 0);
-      bulk_commit();
-      bulk_wait_read0();
-    } else if (!mbar_wait_bounded(&bar, 0)) {
+  if constexpr (DET) {
+    // integer sums: exact in any order
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      khi += __shfl_down_sync(0xffffffffu, khi, off);
+      klo += __shfl_down_sync(0xffffffffu, klo, off);
+    }
+    if (lane == 0) {
+      if (khi) atomicAdd(&s_ekin[0], (unsigned long long)khi);
+      if (klo) atomicAdd(&s_ekin[1], (unsigned long long)klo);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) ekin_tile[t] = efix_join((long long)s_ekin[0], (long long)s_ekin[1]);
+    // the fixed-point J tile goes to the global fixed-point planes with
+    // integer atomics (cells outside the buffer hold no deposits)
+    for (int k = threadIdx.x; k < 3 * PL; k += NT) {
+      const unsigned long long v = sJd[k];
+      if (!v) continue;
+      const int c = k / PL, r = (k % PL) / BW, col = k % BW;
+      const int gy = cy0 + r, gx = cx0 + col;
+      if (gx < fj.pitch && (size_t)gy * fj.pitch < fj.plane)
+        atomicAdd(&fj.p[c * fj.plane + (size_t)gy * fj.pitch + gx], v);
+    }
+    if (threadIdx.x == 0 && !loaded && !mbar_wait_bounded(&bar, 0))
       errbits |= ERR_TIMEOUT;  // second bounded wait for the load still in flight
+  } else {
+    const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
+    if (threadIdx.x == 0) ekin_tile[t] = e;
+
+    // all shared-memory atomics done: hand the J tile to the TMA unit
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (loaded) {
+        tma_reduce_add_3d(&tm_j, sJ, cx0, cy0, 0);
+        bulk_commit();
+        bulk_wait_read0();
+      } else if (!mbar_wait_bounded(&bar, 0)) {
+        errbits |= ERR_TIMEOUT;  // second bounded wait for the load still in flight
+      }
     }
   }
   if (errbits) atomicOr(err, errbits);
@@ -573,16 +674,22 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
 // ---------------------------------------------------------------------------
 // spill push: same physics from global memory (rarely non-empty)
 // ---------------------------------------------------------------------------
-template <int NT>
-__global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Grid G, Particles sin,
+template <int NT, bool DET>
+__global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, FixedJ fj, Grid G, Particles sin,
                                                    const int *sin_cnt, int sin_cap, Spill S, double *ekin,
                                                    int *err, PushConst C) {
   __shared__ double sred[NT / 32];
   const int n = min(*sin_cnt, sin_cap);
   const GlobalFields fld{EB, G.pitch, G.plane};
-  const GlobalCurrent dep{J, G.pitch, G.plane};
+  const auto dep = [&] {
+    if constexpr (DET)
+      return GlobalCurrentFixed{fj.p, fj.pitch, fj.plane};
+    else
+      return GlobalCurrent{J, G.pitch, G.plane};
+  }();
   int errbits = 0;
   float ks = 0.f, kc = 0.f;
+  long long khi = 0, klo = 0;
   for (int k = blockIdx.x * NT + threadIdx.x; k < n; k += gridDim.x * NT) {
     const PRec r = load_particle(sin, k);
     int ix = r.ix, iy = r.iy;
@@ -597,33 +704,58 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Gr
     bool bad;
     const float kin = push_particle(fld, ix, iy, x, y, ux, uy, uz, mx, my, x1, y1, di, dj, qvz, bad, C);
     if (bad) errbits |= ERR_ESCAPE;
-    kahan_add(ks, kc, kin);
+    if constexpr (DET) {
+      long long h, l;
+      efix_split((double)kin, h, l);
+      khi += h;
+      klo += l;
+    } else {
+      kahan_add(ks, kc, kin);
+    }
     const Seg a = zigzag_first(dep, ix, iy, di, dj, x, y, mx, my, C.qnx, C.qny, qvz);
     add_current(dep, ix, iy, segment_current(a, C.qnx, C.qny));
     x = x1;
     y = y1;
     if (apply_boundary(ix, iy, di, dj, C)) spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
   }
-  const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
-  if (threadIdx.x == 0 && e != 0.0) atomicAdd(ekin, e);
+  if constexpr (DET) {
+    if (khi) atomicAdd(reinterpret_cast<unsigned long long *>(ekin), (unsigned long long)khi);
+    if (klo) atomicAdd(reinterpret_cast<unsigned long long *>(ekin) + 1, (unsigned long long)klo);
+  } else {
+    const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
+    if (threadIdx.x == 0 && e != 0.0) atomicAdd(ekin, e);
+  }
   if (errbits) atomicOr(err, errbits);
 }
 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-template <int TX, int TY>
+template <int TX, int TY, bool DET>
 static cudaError_t launch_push_t(const PushLaunch &a, cudaStream_t st) {
   constexpr int NT = (TX * TY >= 256) ? 256 : 128;
-  k_push_tiles<TX, TY, NT><<<a.ntiles, NT, 0, st>>>(*a.tm_eb, *a.tm_j, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
-                                                     a.ekin_tile, a.err, a.C);
+  constexpr int PL = ((TX + 3 + 3) & ~3) * (TY + 3);
+  const int dyn = DET ? 3 * PL * (int)sizeof(unsigned long long) : 0;
+  k_push_tiles<TX, TY, NT, DET><<<a.ntiles, NT, dyn, st>>>(*a.tm_eb, *a.tm_j, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
+                                                           a.ekin_tile, a.err, a.C, a.fj);
   return cudaGetLastError();
 }
 
-static cudaError_t launch_push_tiles_variant(const PushLaunch &a, cudaStream_t st) {
-  const int TX = a.TX, TY = a.TY;
+// raises the dynamic shared-memory limit of the deterministic kernels (once
+// per device, outside any stream capture)
+template <int TX, int TY, bool DET>
+static cudaError_t prepare_push_t() {
+  constexpr int NT = (TX * TY >= 256) ? 256 : 128;
+  constexpr int PL = ((TX + 3 + 3) & ~3) * (TY + 3);
+  if (!DET) return cudaSuccess;
+  return cudaFuncSetAttribute(k_push_tiles<TX, TY, NT, DET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              3 * PL * (int)sizeof(unsigned long long));
+}
+
+template <bool DET>
+static cudaError_t prepare_push_variant(int TX, int TY) {
 #define ZC_TILE(X, Y) \
-  if (TX == X && TY == Y) return launch_push_t<X, Y>(a, st);
+  if (TX == X && TY == Y) return prepare_push_t<X, Y, DET>();
   ZC_TILE(16, 16)
   ZC_TILE(8, 8)
   ZC_TILE(16, 8)
@@ -635,9 +767,27 @@ static cudaError_t launch_push_tiles_variant(const PushLaunch &a, cudaStream_t s
   return cudaErrorInvalidValue;
 }
 
-static cudaError_t launch_push_spill_variant(const float *EB, float *J, const Grid &G, const Particles &sin,
-                                             const int *sin_cnt, int sin_cap, const Spill &S, double *ekin,
-                                             int *err, const PushConst &C, int nblocks, cudaStream_t st) {
-  k_push_spill<256><<<nblocks, 256, 0, st>>>(EB, J, G, sin, sin_cnt, sin_cap, S, ekin, err, C);
+template <bool DET>
+static cudaError_t launch_push_tiles_variant(const PushLaunch &a, cudaStream_t st) {
+  const int TX = a.TX, TY = a.TY;
+#define ZC_TILE(X, Y) \
+  if (TX == X && TY == Y) return launch_push_t<X, Y, DET>(a, st);
+  ZC_TILE(16, 16)
+  ZC_TILE(8, 8)
+  ZC_TILE(16, 8)
+  ZC_TILE(32, 16)
+  ZC_TILE(32, 32)
+  ZC_TILE(8, 16)
+  ZC_TILE(16, 32)
+#undef ZC_TILE
+  return cudaErrorInvalidValue;
+}
+
+template <bool DET>
+static cudaError_t launch_push_spill_variant(const float *EB, float *J, const FixedJ &fj, const Grid &G,
+                                             const Particles &sin, const int *sin_cnt, int sin_cap, const Spill &S,
+                                             double *ekin, int *err, const PushConst &C, int nblocks,
+                                             cudaStream_t st) {
+  k_push_spill<256, DET><<<nblocks, 256, 0, st>>>(EB, J, fj, G, sin, sin_cnt, sin_cap, S, ekin, err, C);
   return cudaGetLastError();
 }
