@@ -293,6 +293,113 @@ def run_scan(args):
 
 
 # ---------------------------------------------------------------------------
+# differentiable step: gradient of the final field energy
+# ---------------------------------------------------------------------------
+def run_adjoint(args):
+    """256 x 256 cells, dx = dy = 0.1, dt = 0.06, 200 steps, checkpoints every
+    20 steps, one electron species 4 x 4 ppc (1,048,576 particles), uth 0.05,
+    weights n(x) = 1 + 0.3 sum of 8 seeded sinusoids: the float32 adjoint's
+    cost against its forward run and against the plain forward step, and its
+    gradients (8 profile amplitudes, x drift) against float64 central
+    differences (eps 1e-4) of the same engine."""
+    from zpic_gb300 import adjoint
+    from zpic_gb300._zc import CudaSim, PART_DTYPE
+
+    nx, dt, steps, K = (256, 256), 0.06, (args.steps if args.steps_given else 200), 20
+    st, amps, kk, q = adjoint.profile_setup(nx=nx, dx=0.1, ppc=(4, 4), uth=0.05, seed=7, drift=0.0)
+    n = st["ix"].size
+    box = (nx[0] * 0.1, nx[1] * 0.1)
+    sim = adjoint.AdjointSim(nx, box, dt, n, q, checkpoint_every=K, precision="float32")
+
+    def load(s, w, drift=0.0):
+        s.set_state(st["ix"], st["iy"], st["x"], st["y"], st["ux"] + drift, st["uy"], st["uz"], w)
+
+    # warm-up, then timed forward + backward
+    for _ in range(max(args.warmup, 1)):
+        load(sim, st["w"])
+        sim.forward(min(steps, 2 * K))
+        sim.backward()
+    clk = ClockSampler(0)
+    clk.start()
+    load(sim, st["w"])
+    L, _ = sim.forward(steps)
+    g = sim.backward()
+    fwd_ms, bwd_ms = sim.times()
+    clocks = clk.stop()
+    ga = adjoint.amplitude_gradient(g["w"], st["X"], kk)
+    gd = float(g["ux"].sum())
+
+    # the plain step on the same particles (weights 1: it has no weights)
+    parts = np.zeros(n, dtype=PART_DTYPE)
+    for f in ("ix", "iy", "x", "y", "ux", "uy", "uz"):
+        parts[f] = st[f]
+    plain = CudaSim(nx, box, dt, tile=(16, 16), fast_math=False)
+    plain.add_species(-1.0, q, (4, 4), parts)
+    plain.step(5)
+    plain.step(steps)
+    plain_ms = plain.last_ms()
+    plain.close()
+
+    # float64: the adjoint's own gradient and central differences of the engine
+    sim64 = adjoint.AdjointSim(nx, box, dt, n, q, checkpoint_every=K, precision="float64")
+    load(sim64, st["w"])
+    sim64.forward(steps)
+    g64 = sim64.backward()
+    f64_ms = sim64.times()
+    ga64 = adjoint.amplitude_gradient(g64["w"], st["X"], kk)
+    gd64 = float(g64["ux"].sum())
+
+    def Lf(a, drift=0.0):
+        load(sim64, adjoint.weights(st["X"], a, kk), drift)
+        return sim64.forward(steps)[0]
+
+    # central differences at shrinking steps: the objective is piecewise smooth
+    # (kinks where trajectories cross cell edges and the staggered half-cell),
+    # so a larger step averages slopes across the kinks it straddles
+    fds = {}
+    for eps in (1e-4, 1e-5, 1e-6):
+        fa = np.array([(Lf(amps + eps * e) - Lf(amps - eps * e)) / (2 * eps) for e in np.eye(len(amps))])
+        fds[eps] = (fa, (Lf(amps, eps) - Lf(amps, -eps)) / (2 * eps))
+    eps = 1e-6
+    fd, fdd = fds[eps]
+    rel_a = float(np.linalg.norm(ga - fd) / np.linalg.norm(fd))
+    rel_d = float(abs(gd - fdd) / abs(fdd))
+    rel_a64 = float(np.linalg.norm(ga64 - fd) / np.linalg.norm(fd))
+    rel_d64 = float(abs(gd64 - fdd) / abs(fdd))
+    fd_steps = {f"{e:g}": {"amplitudes_rel_err_adjoint64": float(np.linalg.norm(ga64 - v[0]) / np.linalg.norm(v[0])),
+                           "drift_rel_err_adjoint64": float(abs(gd64 - v[1]) / abs(v[1])),
+                           "fd_drift": v[1]} for e, v in fds.items()}
+    sim.close()
+    sim64.close()
+    grad_ms = fwd_ms + bwd_ms
+    line = {
+        "metric": METRIC, "value": n * steps / (grad_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": grad_ms / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice, thermal momenta, profile weights)",
+        "config": {"workload": "adjoint: 256x256 cells, dx=dy=0.1, dt=0.06, 200 steps, checkpoint every 20, "
+                               "4x4 ppc (1,048,576 particles), uth 0.05, weights 1+0.3*sum of 8 sinusoids, "
+                               "objective = total field energy at the last step",
+                   "checkpoint_every": K, "particles": n},
+        "how": "value = particle-steps of the forward run / (forward + backward device time)",
+        "adjoint": {"forward_ms": fwd_ms, "backward_ms": bwd_ms,
+                    "gradient_over_forward": grad_ms / fwd_ms,
+                    "gradient_over_plain_forward": grad_ms / plain_ms, "plain_forward_ms": plain_ms,
+                    "objective": L},
+        "gradient_check": {"float64_adjoint": {"amplitudes_rel_err_vs_fd64": rel_a64,
+                                               "drift_rel_err_vs_fd64": rel_d64,
+                                               "forward_ms": f64_ms[0], "backward_ms": f64_ms[1],
+                                               "gradient_over_forward": (f64_ms[0] + f64_ms[1]) / f64_ms[0]},
+                           "float32_adjoint": {"amplitudes_rel_err_vs_fd64": rel_a, "drift_rel_err_vs_fd64": rel_d},
+                           "eps": eps, "fd_by_step": fd_steps, "fd_amplitudes": fd.tolist(), "adjoint64_amplitudes": ga64.tolist(),
+                           "adjoint32_amplitudes": ga.tolist(), "fd_drift": fdd, "adjoint64_drift": gd64,
+                           "adjoint32_drift": gd},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def main():
@@ -308,7 +415,7 @@ def main():
                     help="bit-exact push build (every float32 op rounded as the reference C)")
     ap.add_argument("--sort-every", type=int, default=0)
     ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
-    ap.add_argument("--workload", default="plain", choices=["plain", "scan"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint"])
     ap.add_argument("--scan-runs", type=int, default=256)
     ap.add_argument("--scan-group", type=int, default=0, help="runs per batch graph (0: all)")
     args = ap.parse_args()
@@ -317,6 +424,8 @@ def main():
         return run_reference(args)
     if args.workload == "scan":
         return run_scan(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -272,6 +272,80 @@ __device__ __forceinline__ R kinetic(const R u[3], const R e_in[3], const Params
   return u2 / (sqrt_(R(1) + u2) + R(1));
 }
 
+// reverse of boris(): cotangents of (new momentum, mx, my, q v_z) in, of
+// (momentum, E_p, B_p) out; the forward intermediates are recomputed
+template <class R>
+struct V3 {
+  R x, y, z;
+};
+template <class R>
+__device__ __forceinline__ V3<R> cross(const V3<R> &a, const V3<R> &b) {
+  return V3<R>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class R>
+__device__ __forceinline__ R dot(const V3<R> &a, const V3<R> &b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <class R>
+__device__ __forceinline__ V3<R> axpy(R a, const V3<R> &x, const V3<R> &y) {  // a x + y
+  return V3<R>{a * x.x + y.x, a * x.y + y.y, a * x.z + y.z};
+}
+
+template <class R>
+__device__ __forceinline__ void boris_vjp(const R u_in[3], const R e_in[3], const R b_in[3], const Params<R> &P,
+                                          const R lu_out[3], R lmx, R lmy, R lqvz, R lu[3], R le[3], R lb[3]) {
+  // forward
+  const V3<R> e{e_in[0] * P.tem, e_in[1] * P.tem, e_in[2] * P.tem};
+  const V3<R> t0{u_in[0] + e.x, u_in[1] + e.y, u_in[2] + e.z};
+  const R u2 = dot(t0, t0);
+  const R g = sqrt_(R(1) + u2);
+  const R tg = P.tem / g;
+  const V3<R> B{b_in[0], b_in[1], b_in[2]};
+  const V3<R> b{B.x * tg, B.y * tg, B.z * tg};
+  const R s2 = R(2) / (R(1) + dot(b, b));
+  const V3<R> v = axpy(R(1), t0, cross(t0, b));
+  const V3<R> b2{b.x * s2, b.y * s2, b.z * s2};
+  const V3<R> t1 = axpy(R(1), t0, cross(v, b2));
+  const V3<R> uo = axpy(R(1), t1, e);
+  const R rg = R(1) / sqrt_(R(1) + dot(uo, uo));
+  // reverse
+  V3<R> luo{lu_out[0] + P.dt_dx * rg * lmx, lu_out[1] + P.dt_dy * rg * lmy, lu_out[2] + P.q * rg * lqvz};
+  const R lrg = P.dt_dx * uo.x * lmx + P.dt_dy * uo.y * lmy + P.q * uo.z * lqvz;
+  luo = axpy(-rg * rg * rg * lrg, uo, luo);
+  // uo = t1 + e ; t1 = t0 + v x b2
+  V3<R> le_ = luo;
+  V3<R> lt0 = luo;
+  const V3<R> lv = cross(b2, luo);
+  const V3<R> lb2 = cross(luo, v);
+  // b2 = b s2
+  V3<R> lbv{s2 * lb2.x, s2 * lb2.y, s2 * lb2.z};
+  const R ls2 = dot(b, lb2);
+  // v = t0 + t0 x b
+  lt0 = axpy(R(1), lv, lt0);
+  lt0 = axpy(R(1), cross(b, lv), lt0);
+  lbv = axpy(R(1), cross(lv, t0), lbv);
+  // s2 = 2 / (1 + |b|^2)
+  lbv = axpy(-s2 * s2 * ls2, b, lbv);
+  // b = B tg
+  const V3<R> lB{tg * lbv.x, tg * lbv.y, tg * lbv.z};
+  const R ltg = dot(B, lbv);
+  // tg = tem / g ; g = sqrt(1 + u2) ; u2 = |t0|^2
+  const R lg = -tg / g * ltg;
+  const R lu2 = lg / (R(2) * g);
+  lt0 = axpy(R(2) * lu2, t0, lt0);
+  // t0 = u + e ; e = E tem
+  le_ = axpy(R(1), lt0, le_);
+  lu[0] = lt0.x;
+  lu[1] = lt0.y;
+  lu[2] = lt0.z;
+  le[0] = P.tem * le_.x;
+  le[1] = P.tem * le_.y;
+  le[2] = P.tem * le_.z;
+  lb[0] = lB.x;
+  lb[1] = lB.y;
+  lb[2] = lB.z;
+}
+
 // the 8 contributions of one straight segment inside one cell
 // (particles.c:886-922), per unit weight
 template <class R, class T, class Sink>
@@ -392,15 +466,19 @@ struct DepositSink {  // forward: J += w * contribution
   __device__ __forceinline__ void add(int c, int i, int j, R v) const { atomicAdd(&J.f[J.at(c, i, j)], w * v); }
 };
 
+// reverse: sums of lambda_J times the contributions (per unit weight), the
+// x and y components apart from z (the deposit runs with q v_z = 1: the z
+// contributions are linear in it)
 template <class R, int N>
-struct AdjointSink {  // reverse: sum of lambda_J * contribution (per unit weight)
+struct AdjointSink {
   Planes<R> lamJ;
-  Dual<R, N> acc;
+  Dual<R, N> axy, az;
   __device__ __forceinline__ void add(int c, int i, int j, const Dual<R, N> &v) {
     const R l = lamJ(c, i, j);
-    acc.v += l * v.v;
+    Dual<R, N> &a = (c == 2) ? az : axy;
+    a.v += l * v.v;
 #pragma unroll
-    for (int k = 0; k < N; ++k) acc.d[k] += l * v.d[k];
+    for (int k = 0; k < N; ++k) a.d[k] += l * v.d[k];
   }
 };
 
@@ -437,64 +515,91 @@ __global__ void k_adj_push(State<R> s, State<R> o, const R *w, Planes<R> E, Plan
   if (ekin && ek != 0.0) atomicAdd(ekin, ek);
 }
 
-// reverse of one particle step: lam (x, y, ux, uy, uz) of the particle after
+// the contributions of a motion that stays in its cell: one segment
+template <class R, class T, class Sink>
+__device__ __forceinline__ void single_segment(Sink &sink, int ix, int iy, const T &x0, const T &y0, const T &dx,
+                                               const T &dy, const T &qvz, const Params<R> &P) {
+  segment(sink, ix, iy, x0, x0 + dx, y0, y0 + dy, dx, dy, qvz * R(0.5), P);
+}
+
+// Reverse of one particle step: lam (x, y, ux, uy, uz) of the particle after
 // the step in, before the step out (in place); lamE / lamB receive the
-// transpose of the gather; dw the weight's derivative
+// transpose of the gather; dw the weight's derivative.  FULL handles any
+// motion (up to three zigzag segments); the light variant only motions
+// that stay in their cell and returns false for the others untouched.
+template <class R, bool FULL>
+__device__ __forceinline__ bool reverse_particle(int p, const State<R> &s, const R *w, const Planes<R> &E,
+                                                 const Planes<R> &B, const Planes<R> &lamJ, const State<R> &lam,
+                                                 R *lamE, R *lamB, R *dw, const Params<R> &P) {
+  const int ix = s.ix[p], iy = s.iy[p];
+  const R x = s.x[p], y = s.y[p];
+  const R u[3] = {s.ux[p], s.uy[p], s.uz[p]};
+  // 1. gather with d/dx, d/dy
+  Dual<R, 2> fd[6];
+  gather<R, Dual<R, 2>>(E, B, ix, iy, seed<R, 2>(x, 0), seed<R, 2>(y, 1), fd);
+  R f[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) f[c] = fd[c].v;
+  // 2. Boris + move (values)
+  R uo[3], mx, my, qvz;
+  boris<R, R>(u, f, f + 3, P, uo, mx, my, qvz);
+  // 3. deposit with d/d(x, y, mx, my); linear in q v_z
+  AdjointSink<R, 4> sink{lamJ, Dual<R, 4>(R(0)), Dual<R, 4>(R(0))};
+  if constexpr (FULL) {
+    zigzag<R, Dual<R, 4>>(sink, ix, iy, seed<R, 4>(x, 0), seed<R, 4>(y, 1), seed<R, 4>(mx, 2), seed<R, 4>(my, 3),
+                          Dual<R, 4>(R(1)), P);
+  } else {
+    const R x1 = x + mx, y1 = y + my;
+    if (x1 >= R(1) || x1 < R(0) || y1 >= R(1) || y1 < R(0)) return false;
+    single_segment<R, Dual<R, 4>>(sink, ix, iy, seed<R, 4>(x, 0), seed<R, 4>(y, 1), seed<R, 4>(mx, 2),
+                                  seed<R, 4>(my, 3), Dual<R, 4>(R(1)), P);
+  }
+  const R wp = w[p];
+  dw[p] += sink.axy.v + qvz * sink.az.v;
+  R gdep[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) gdep[k] = wp * (sink.axy.d[k] + qvz * sink.az.d[k]);
+  // 4. cotangents of the Boris outputs, then its reverse
+  const R lx1 = lam.x[p], ly1 = lam.y[p];
+  const R lu1[3] = {lam.ux[p], lam.uy[p], lam.uz[p]};
+  R lu0[3], lef[3], lbf[3];
+  boris_vjp<R>(u, f, f + 3, P, lu1, lx1 + gdep[2], ly1 + gdep[3], wp * sink.az.v, lu0, lef, lbf);
+  // 5. position: direct (x1 = x + mx - di), deposit, and the gather weights
+  const R l6[6] = {lef[0], lef[1], lef[2], lbf[0], lbf[1], lbf[2]};
+  R lx = lx1 + gdep[0], ly = ly1 + gdep[1];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    lx += l6[c] * fd[c].d[0];
+    ly += l6[c] * fd[c].d[1];
+  }
+  lam.x[p] = lx;
+  lam.y[p] = ly;
+  lam.ux[p] = lu0[0];
+  lam.uy[p] = lu0[1];
+  lam.uz[p] = lu0[2];
+  // 6. transpose of the gather
+  scatter_add(lamE, lamB, E, ix, iy, x, y, l6);
+  return true;
+}
+
+// the particles whose motion stays in its cell (most of them); the others
+// are listed for k_adj_push_rev_cross
 template <class R>
 __global__ void __launch_bounds__(128) k_adj_push_rev(State<R> s, const R *w, Planes<R> E, Planes<R> B,
                                                       Planes<R> lamJ, State<R> lam, R *lamE, R *lamB, R *dw,
-                                                      Params<R> P) {
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.np; p += gridDim.x * blockDim.x) {
-    const int ix = s.ix[p], iy = s.iy[p];
-    const R x = s.x[p], y = s.y[p];
-    const R wp = w[p];
-    // 1. gather with d/dx, d/dy
-    Dual<R, 2> fd[6];
-    gather<R, Dual<R, 2>>(E, B, ix, iy, seed<R, 2>(x, 0), seed<R, 2>(y, 1), fd);
-    // 2. Boris + move with d/d(u, E_p, B_p)
-    Dual<R, 9> u9[3], e9[3], b9[3];
-    u9[0] = seed<R, 9>(s.ux[p], 0);
-    u9[1] = seed<R, 9>(s.uy[p], 1);
-    u9[2] = seed<R, 9>(s.uz[p], 2);
-    for (int c = 0; c < 3; ++c) {
-      e9[c] = seed<R, 9>(fd[c].v, 3 + c);
-      b9[c] = seed<R, 9>(fd[3 + c].v, 6 + c);
-    }
-    Dual<R, 9> uo[3], mx, my, qvz;
-    boris<R, Dual<R, 9>>(u9, e9, b9, P, uo, mx, my, qvz);
-    // 3. deposit with d/d(x, y, mx, my, qvz)
-    AdjointSink<R, 5> sink{lamJ, Dual<R, 5>(R(0))};
-    zigzag<R, Dual<R, 5>>(sink, ix, iy, seed<R, 5>(x, 0), seed<R, 5>(y, 1), seed<R, 5>(mx.v, 2),
-                          seed<R, 5>(my.v, 3), seed<R, 5>(qvz.v, 4), P);
-    dw[p] += sink.acc.v;
-    // 4. cotangents of the Boris outputs
-    const R lx1 = lam.x[p], ly1 = lam.y[p];
-    const R lo[6] = {lam.ux[p], lam.uy[p], lam.uz[p], lx1 + wp * sink.acc.d[2], ly1 + wp * sink.acc.d[3],
-                     wp * sink.acc.d[4]};
-    const Dual<R, 9> *outs[6] = {&uo[0], &uo[1], &uo[2], &mx, &my, &qvz};
-    R l9[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      R a = 0;
-#pragma unroll
-      for (int m = 0; m < 6; ++m) a += lo[m] * outs[m]->d[k];
-      l9[k] = a;
-    }
-    // 5. position: direct (x1 = x + mx - di), deposit, and the gather weights
-    R lx = lx1 + wp * sink.acc.d[0], ly = ly1 + wp * sink.acc.d[1];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      lx += l9[3 + c] * fd[c].d[0];
-      ly += l9[3 + c] * fd[c].d[1];
-    }
-    lam.x[p] = lx;
-    lam.y[p] = ly;
-    lam.ux[p] = l9[0];
-    lam.uy[p] = l9[1];
-    lam.uz[p] = l9[2];
-    // 6. transpose of the gather
-    scatter_add(lamE, lamB, E, ix, iy, x, y, l9 + 3);
-  }
+                                                      int *cross, int *ncross, Params<R> P) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.np; p += gridDim.x * blockDim.x)
+    if (!reverse_particle<R, false>(p, s, w, E, B, lamJ, lam, lamE, lamB, dw, P)) cross[atomicAdd(ncross, 1)] = p;
+}
+
+// the listed cell-crossing particles
+template <class R>
+__global__ void __launch_bounds__(128) k_adj_push_rev_cross(State<R> s, const R *w, Planes<R> E, Planes<R> B,
+                                                            Planes<R> lamJ, State<R> lam, R *lamE, R *lamB, R *dw,
+                                                            const int *cross, const int *ncross, Params<R> P) {
+  const int n = *ncross;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    reverse_particle<R, true>(cross[k], s, w, E, B, lamJ, lam, lamE, lamB, dw, P);
 }
 
 // B -= c curl E  (yee_b with c = dt/2)
@@ -655,6 +760,7 @@ struct Engine : EngineBase {
   bool have_state = false;
   // reverse
   R *lamE = nullptr, *lamB = nullptr, *lamJ = nullptr, *dwv = nullptr;
+  int *d_cross = nullptr, *d_ncross = nullptr;  // cell-crossing particles of a reverse step
   DevState<R> lam;
   double *d_scr = nullptr;  // scratch doubles
   std::vector<void *> owned;
@@ -666,10 +772,14 @@ struct Engine : EngineBase {
     owned.push_back(*p);
     return ZC_OK;
   }
+  // one block per state: cells (2 x np ints), then the 5 real arrays
+  size_t state_bytes() const { return 2 * sizeof(int) * (size_t)np + 5 * sizeof(R) * (size_t)np; }
   zc_status alloc_state(DevState<R> &s) {
-    TRY_(alloc(&s.ix, np));
-    TRY_(alloc(&s.iy, np));
-    TRY_(alloc(&s.v, 5 * (size_t)np));
+    char *b = nullptr;
+    TRY_(alloc(&b, state_bytes()));
+    s.ix = reinterpret_cast<int *>(b);
+    s.iy = s.ix + np;
+    s.v = reinterpret_cast<R *>(b + 2 * sizeof(int) * (size_t)np);
     return ZC_OK;
   }
 
@@ -715,6 +825,8 @@ struct Engine : EngineBase {
     TRY_(alloc(&lamB, 3 * pl));
     TRY_(alloc(&lamJ, 3 * pl));
     TRY_(alloc(&dwv, np));
+    TRY_(alloc(&d_cross, np));
+    TRY_(alloc(&d_ncross, 1));
     TRY_(alloc(&d_scr, 16));
     seg_s.resize(K);
     seg_f.resize(K);
@@ -778,9 +890,15 @@ struct Engine : EngineBase {
   }
 
   zc_status copy_state(DevState<R> &dst, const DevState<R> &src) {
-    ACK(cudaMemcpyAsync(dst.ix, src.ix, sizeof(int) * np, cudaMemcpyDeviceToDevice, st));
-    ACK(cudaMemcpyAsync(dst.iy, src.iy, sizeof(int) * np, cudaMemcpyDeviceToDevice, st));
-    ACK(cudaMemcpyAsync(dst.v, src.v, sizeof(R) * 5 * (size_t)np, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(dst.ix, src.ix, state_bytes(), cudaMemcpyDeviceToDevice, st));
+    return ZC_OK;
+  }
+
+  // keeps the pre-step state of step n of a segment in slot k
+  zc_status keep_pre_step(int k) {
+    TRY_(copy_state(seg_s[k], cur));
+    ACK(cudaMemcpyAsync(seg_f[k], E, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(seg_f[k] + 3 * pl, B, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
     return ZC_OK;
   }
 
@@ -842,8 +960,12 @@ struct Engine : EngineBase {
     ACK(cudaEventRecord(e0, st));
     nck = 0;
     ACK(cudaMemsetAsync(d_scr + 1, 0, sizeof(double), st));
+    // the last segment's pre-step states are kept on the way: the reverse
+    // sweep starts with them and need not recompute that segment
+    const int last0 = ((nsteps - 1) / K) * K;
     for (int n = 0; n < nsteps; ++n) {
       if (n % K == 0) TRY_(save_checkpoint());
+      if (n >= last0) TRY_(keep_pre_step(n - last0));
       TRY_(step(n == nsteps - 1 ? d_scr + 1 : nullptr));
     }
     steps_done = nsteps;
@@ -878,13 +1000,13 @@ struct Engine : EngineBase {
     for (int sgi = nck - 1; sgi >= 0; --sgi) {
       const int n0 = sgi * K, n1 = std::min(steps_done, n0 + K);
       // recompute the segment from its checkpoint, keeping pre-step states
-      TRY_(restore_checkpoint(sgi));
-      for (int n = n0; n < n1; ++n) {
-        const int k = n - n0;
-        TRY_(copy_state(seg_s[k], cur));
-        ACK(cudaMemcpyAsync(seg_f[k], E, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
-        ACK(cudaMemcpyAsync(seg_f[k] + 3 * pl, B, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
-        if (n + 1 < n1) TRY_(step(nullptr));
+      // (the last one was kept by the forward run)
+      if (sgi != nck - 1) {
+        TRY_(restore_checkpoint(sgi));
+        for (int n = n0; n < n1; ++n) {
+          TRY_(keep_pre_step(n - n0));
+          if (n + 1 < n1) TRY_(step(nullptr));
+        }
       }
       // walk the segment backwards
       for (int n = n1 - 1; n >= n0; --n) {
@@ -892,9 +1014,13 @@ struct Engine : EngineBase {
         k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
         k_adj_yee_e_T<R><<<grid_for(pl), 256, 0, st>>>(lamE, lamB, lamJ, nx, ny, cx, cy, (R)dt);
         k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+        ACK(cudaMemsetAsync(d_ncross, 0, sizeof(int), st));
         k_adj_push_rev<R><<<grid_for(np, 128), 128, 0, st>>>(seg_s[k].view(np), w, planes(seg_f[k]),
                                                               planes(seg_f[k] + 3 * pl), planes(lamJ), lam.view(np),
-                                                              lamE, lamB, dwv, P);
+                                                              lamE, lamB, dwv, d_cross, d_ncross, P);
+        k_adj_push_rev_cross<R><<<grid_for(np / 4, 128), 128, 0, st>>>(
+            seg_s[k].view(np), w, planes(seg_f[k]), planes(seg_f[k] + 3 * pl), planes(lamJ), lam.view(np), lamE,
+            lamB, dwv, d_cross, d_ncross, P);
         ACK(cudaGetLastError());
       }
     }
@@ -938,6 +1064,7 @@ struct Engine : EngineBase {
 
 struct zc_adj {
   int device = 0;
+  int nx = 0, ny = 0, np = 0;
   std::unique_ptr<EngineBase> eng;
 };
 
@@ -970,6 +1097,9 @@ zc_status zc_adj_create(const zc_adj_desc *d, zc_adj **out) {
   AdjDevice g(d->device);
   zc_adj *h = new zc_adj();
   h->device = d->device;
+  h->nx = d->nx[0];
+  h->ny = d->nx[1];
+  h->np = d->np;
   zc_status st;
   if (d->precision == 0) {
     auto *e = new Engine<float>();
@@ -1000,6 +1130,11 @@ zc_status zc_adj_set_state(zc_adj *h, const int *ix, const int *iy, const double
                            const double *B) {
   if (!h) return afail(ZC_EINVAL, "null handle");
   if (!ix || !iy || !x || !y || !ux || !uy || !uz || !w) return afail(ZC_EINVAL, "null particle array");
+  // every particle inside the grid, with an in-cell position in [0, 1]
+  for (int p = 0; p < h->np; ++p)
+    if (ix[p] < 0 || ix[p] >= h->nx || iy[p] < 0 || iy[p] >= h->ny || !(x[p] >= 0.0 && x[p] <= 1.0) ||
+        !(y[p] >= 0.0 && y[p] <= 1.0))
+      return afail(ZC_EINVAL, "adjoint engine: particle outside the grid or its cell");
   AdjDevice g(h->device);
   return h->eng->set_state(ix, iy, x, y, ux, uy, uz, w, E, B);
 }
