@@ -293,6 +293,70 @@ def run_scan(args):
 
 
 # ---------------------------------------------------------------------------
+# moving-window laser wakefield
+# ---------------------------------------------------------------------------
+def run_lwfa(args):
+    """2000 x 256 cells, box 40 x 51.2 (dx 0.02, dy 0.2), dt 0.014, 3000
+    steps, moving window; Gaussian laser a0 2, omega0 10, W0 4, FWHM 2,
+    start 17, focus 20, axis 25.6, polarisation along y (polarization 0);
+    cold electrons of density 1 from x = 20, 4 x 2 ppc; binomial smoothing
+    along x, level 4.  The particles are loaded as spec_new does; the column
+    the window uncovers is injected from the host, as
+    spec_move_window does."""
+    from zpic_gb300 import em2d
+    from zpic_gb300._zc import PART_DTYPE, CudaSim
+
+    nx, box, dt = (2000, 256), (40.0, 51.2), 0.014
+    steps = args.steps if args.steps_given else 3000
+    ppc = (4, 2)
+    em2d.set_rand_seed(12345, 67890, fresh=True)
+    parts, q = em2d.load_particles(-1.0, ppc, nx, box, dt, density=em2d.Density(type="step", start=20.0))
+    # the column injected at every window move: the ppc lattice of cells
+    # (nx-1, j), cold (the plasma extends past the window's right edge)
+    hx, hy = np.float32(1.0) / np.float32(ppc[0]), np.float32(1.0) / np.float32(ppc[1])
+    col = np.zeros(nx[1] * ppc[0] * ppc[1], dtype=PART_DTYPE)
+    k = 0
+    for j in range(nx[1]):
+        for b in range(ppc[1]):
+            for a in range(ppc[0]):
+                col[k] = (nx[0] - 1, j, hx * np.float32(a + 0.5), hy * np.float32(b + 0.5), 0, 0, 0)
+                k += 1
+    sim = CudaSim(nx, box, dt, tile=(32, 16), fast_math=not args.exact)
+    sim.add_species(-1.0, q, ppc, parts)
+    sim.add_laser(type="gaussian", start=17.0, fwhm=2.0, a0=2.0, omega0=10.0, W0=4.0, focus=20.0, axis=25.6,
+                  polarization=0.0)
+    sim.set_moving_window()
+    sim.set_injector(lambda species, n_move: col)
+    sim.set_smooth("binomial", 4, "none", 0)
+    n0 = sim.count(0)
+    clk = ClockSampler(0)
+    clk.start()
+    sim.step(steps)
+    ms = sim.last_ms()
+    clocks = clk.stop()
+    n1 = sim.count(0)
+    info = sim.info()
+    Ex = sim.E()[nx[1] // 2 + 1, 1:nx[0] + 1, 0]
+    sim.close()
+    nps = 0.5 * (n0 + n1) * steps
+    line = {
+        "metric": METRIC, "value": nps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 0,
+        "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (reference loading, step density)",
+        "config": {"workload": "moving-window laser wakefield: 2000x256 cells, box 40x51.2, dt 0.014, 3000 steps, "
+                               "Gaussian laser a0 2 omega0 10 W0 4 FWHM 2 start 17 focus 20 pol y, density 1 "
+                               "from x=20, 4x2 ppc cold, binomial x smoothing level 4",
+                   "particles_start": int(n0), "particles_end": int(n1), "window_moves": info["n_move"],
+                   "push_build": "exact" if args.exact else "fast"},
+        "how": "value = mean particle count x steps / device time of zc_step(3000) (host injection included)",
+        "wake": {"on_axis_Ex_max_abs": float(np.abs(Ex).max()), "on_axis_Ex_rms": float(np.sqrt(np.mean(Ex ** 2)))},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # differentiable step: gradient of the final field energy
 # ---------------------------------------------------------------------------
 def run_adjoint(args):
@@ -415,7 +479,8 @@ def main():
                     help="bit-exact push build (every float32 op rounded as the reference C)")
     ap.add_argument("--sort-every", type=int, default=0)
     ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
-    ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint", "lwfa"])
+    ap.add_argument("--deterministic", action="store_true", help="fixed-point (bit-reproducible) deposition")
     ap.add_argument("--scan-runs", type=int, default=256)
     ap.add_argument("--scan-group", type=int, default=0, help="runs per batch graph (0: all)")
     args = ap.parse_args()
@@ -426,6 +491,8 @@ def main():
         return run_scan(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "lwfa":
+        return run_lwfa(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -464,7 +531,7 @@ def main():
     N = parts.size
     q = np.float32(-1.0) / np.float32(W["ppc"][0] * W["ppc"][1])
     sim = CudaSim(W["nx"], W["box"], W["dt"], device=local, tile=tile, fast_math=not args.exact,
-                  sort_every=args.sort_every)
+                  sort_every=args.sort_every, deterministic=args.deterministic)
     sim.add_species(W["m_q"], float(q), W["ppc"], parts)
     sm = W["smooth"]
     sim.set_smooth(sm[0], sm[1], sm[2], sm[3])
@@ -536,6 +603,7 @@ def main():
                    "particles_per_gpu": int(N), "uth": W["uth"],
                    "smoothing": "compensated level 1, x and y", "tile": list(tile),
                    "push_build": "exact (no FMA contraction)" if args.exact else "fast (FMA contraction)",
+                   "deposition": "64-bit fixed point (bit-reproducible)" if args.deterministic else "float32",
                    "cell_sort_every": args.sort_every or 8,
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (1.88 GB of particles read and written per step)"},
