@@ -171,6 +171,12 @@ ZC_API zc_status zc_energy(zc_sim *sim, double emf_energy[6], double *kin_energy
 /* charge density of one species on an (nx+1)*(ny+1) grid
  * (spec_deposit_charge, em2d/particles.c:1289-1324) */
 ZC_API zc_status zc_species_charge(zc_sim *sim, int species, float *charge);
+/* phase-space density of one species added to `buf` (pha_nx[0]*pha_nx[1]
+ * floats, host memory): quantities 1 x1, 2 x2, 4 u1, 5 u2, 6 u3 as the
+ * reference's rep_type nibbles; pha_range = {x1min, x1max, x2min, x2max}
+ * (spec_deposit_pha, em2d/particles.c:1569-1632) */
+ZC_API zc_status zc_species_phasespace(zc_sim *sim, int species, int quant1, int quant2, const int pha_nx[2],
+                                       const float pha_range[4], float *buf);
 ZC_API zc_status zc_get_info(zc_sim *sim, zc_info *info);
 ZC_API zc_status zc_grid_view_get(zc_sim *sim, zc_grid_view *view);
 ZC_API zc_status zc_synchronize(zc_sim *sim);

@@ -118,6 +118,7 @@ def _load(backend: str, fast: bool):
         "set_E": (None, [P, P]), "set_B": (None, [P, P]), "set_J": (None, [P, P]),
         "emf_energy": (None, [P, P]),
         "spec_charge": (None, [P, C.c_int, P]),
+        "spec_pha": (None, [P, C.c_int, C.c_int, C.c_int, P, P, P]),
     }
     fns = {}
     for name, (res, args) in sig.items():
@@ -352,6 +353,15 @@ class CpuSim:
     def charge(self, k) -> np.ndarray:
         out = np.zeros((self.nx[1] + 1, self.nx[0] + 1), dtype=np.float32)
         self.f["spec_charge"](self.h, k, _ptr(out))
+        return out
+
+    PHA = {"x1": 1, "x2": 2, "u1": 4, "u2": 5, "u3": 6}
+
+    def phasespace(self, k, quants, pha_nx, pha_range) -> np.ndarray:
+        n = np.ascontiguousarray(pha_nx, dtype=np.int32)
+        r = np.ascontiguousarray(np.asarray(pha_range, dtype=np.float32).reshape(4))
+        out = np.zeros((int(n[1]), int(n[0])), dtype=np.float32)
+        self.f["spec_pha"](self.h, k, self.PHA[quants[0]], self.PHA[quants[1]], _ptr(n), _ptr(r), _ptr(out))
         return out
 
 

@@ -212,6 +212,11 @@ void zr_set_B(zr_sim *s, const float *b) { memcpy(s->sim.emf.B_buf, b, nbytes(s)
 void zr_set_J(zr_sim *s, const float *b) { memcpy(s->sim.current.J_buf, b, nbytes(s)); }
 void zr_emf_energy(const zr_sim *s, double en[6]) { emf_get_energy(&s->sim.emf, en); }
 void zr_spec_charge(const zr_sim *s, int k, float *rho) { spec_deposit_charge(&s->spec[k], rho); }
+void zr_spec_pha(const zr_sim *s, int k, int q1, int q2, const int pha_nx[2], const float range[4], float *buf)
+{
+    const float r[2][2] = {{range[0], range[1]}, {range[2], range[3]}};
+    spec_deposit_pha(&s->spec[k], q1 + 16 * q2, pha_nx, r, buf);
+}
 
 /* cumulative particle-advance time and pushes (em2d/particles.c:36-59) */
 double zr_spec_time(void) { return spec_time(); }

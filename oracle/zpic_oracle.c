@@ -1100,3 +1100,43 @@ void zo_spec_charge(const zo_sim *s, int k, float *rho)                    /* pa
         for (int j = 0; j < sp->nx[1] + 1; j++) rho[j * nrow] += rho[sp->nx[0] + j * nrow];
     for (int i = 0; i < sp->nx[0] + 1; i++) rho[i] += rho[i + sp->nx[1] * nrow];
 }
+
+/* phase-space density (spec_deposit_pha, particles.c:1569-1632) with the
+ * axis quantities of spec_pha_axis (particles.c:1510-1536): quantity codes
+ * 1 x1, 2 x2, 4 u1, 5 u2, 6 u3; range = {x1min, x1max, x2min, x2max} */
+static float zo_pha_quant(const zo_spec *sp, int n, int q)
+{
+    switch (q) {
+    case 1: return (sp->p[n].x + sp->p[n].ix) * sp->dx[0];
+    case 2: return (sp->p[n].y + sp->p[n].iy) * sp->dx[1];
+    case 4: return sp->p[n].ux;
+    case 5: return sp->p[n].uy;
+    default: return sp->p[n].uz;
+    }
+}
+
+void zo_spec_pha(const zo_sim *s, int k, int q1, int q2, const int pha_nx[2], const float range[4], float *buf)
+{
+    const zo_spec *sp = &s->spec[k];
+    const int nrow = pha_nx[0];
+    const float x1min = range[0], x2min = range[2];
+    const float rdx1 = pha_nx[0] / (range[1] - range[0]);
+    const float rdx2 = pha_nx[1] / (range[3] - range[2]);
+    for (int n = 0; n < sp->np; n++) {
+        const float nx1 = (zo_pha_quant(sp, n, q1) - x1min) * rdx1;
+        const float nx2 = (zo_pha_quant(sp, n, q2) - x2min) * rdx2;
+        const int i1 = (int)(nx1 + 0.5f), i2 = (int)(nx2 + 0.5f);
+        const float w1 = nx1 - i1 + 0.5f, w2 = nx2 - i2 + 0.5f;
+        int idx = i1 + nrow * i2;
+        if (i2 >= 0 && i2 < pha_nx[1]) {
+            if (i1 >= 0 && i1 < pha_nx[0]) buf[idx] += (1.0f - w1) * (1.0f - w2) * sp->q;
+            if (i1 + 1 >= 0 && i1 + 1 < pha_nx[0]) buf[idx + 1] += w1 * (1.0f - w2) * sp->q;
+        }
+        idx += nrow;
+        if (i2 + 1 >= 0 && i2 + 1 < pha_nx[1]) {
+            if (i1 >= 0 && i1 < pha_nx[0]) buf[idx] += (1.0f - w1) * w2 * sp->q;
+            if (i1 + 1 >= 0 && i1 + 1 < pha_nx[0]) buf[idx + 1] += w1 * w2 * sp->q;
+        }
+    }
+}
+

@@ -137,6 +137,9 @@ void zo_set_J(zo_sim *s, const float *buf);
 void zo_emf_energy(const zo_sim *s, double energy[6]);
 /* spec_deposit_charge (em2d/particles.c:1289-1324): charge grid (nx+1)*(ny+1) */
 void zo_spec_charge(const zo_sim *s, int sp, float *charge);
+/* spec_deposit_pha (em2d/particles.c:1569-1632): quantities 1 x1, 2 x2,
+ * 4 u1, 5 u2, 6 u3; range {x1min, x1max, x2min, x2max}; adds into buf */
+void zo_spec_pha(const zo_sim *s, int sp, int q1, int q2, const int pha_nx[2], const float range[4], float *buf);
 
 #ifdef __cplusplus
 }

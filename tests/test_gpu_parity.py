@@ -147,6 +147,17 @@ def test_charge_density():
     assert np.allclose(g.charge(0), cpu.charge(0), rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("name", ["custom_ext", "lwfa_window"])
+def test_phasespace_density(name):
+    cpu, g = mirror(name)
+    g.step(4)
+    cpu.iter(4)
+    for qs, rg in ((("x1", "u1"), ((0.0, 6.0), (-0.5, 0.5))), (("x2", "u3"), ((0.0, 5.0), (-1.0, 1.0))),
+                   (("u1", "u2"), ((-0.3, 0.3), (-0.3, 0.3)))):
+        a, b = g.phasespace(0, qs, (40, 24), rg), cpu.phasespace(0, qs, (40, 24), rg)
+        assert np.allclose(a, b, rtol=1e-5, atol=1e-6 * max(np.abs(b).max(), 1e-30)), qs
+
+
 def _tile_runs(parts, tile, nx):
     """Tile index and local cell of every particle, in buffer order."""
     tx, ty = tile

@@ -69,6 +69,9 @@ for step in range(d["steps"] + 10):
     assert a.n_move() == b.n_move()
 for k in range(ns):
     assert np.array_equal(a.charge(k), b.charge(k))
+    for qs, rg in ((("x1", "u1"), ((0.0, 4.0), (-0.5, 0.5))), (("x2", "u3"), ((0.0, 3.0), (-1.0, 1.0))),
+                   (("u1", "u2"), ((-0.3, 0.3), (-0.3, 0.3)))):
+        assert np.array_equal(a.phasespace(k, qs, (32, 24), rg), b.phasespace(k, qs, (32, 24), rg))
 print("OK")
 """
 

@@ -38,7 +38,7 @@ EXPORTS = [
     "zc_phase_name", "zc_field_energy_static", "zc_set_graphs", "zc_history_enable", "zc_history_get",
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
     "zc_adj_create", "zc_adj_destroy", "zc_adj_set_state", "zc_adj_forward", "zc_adj_backward",
-    "zc_adj_get_state", "zc_adj_times",
+    "zc_adj_get_state", "zc_adj_times", "zc_species_phasespace",
 ]
 NPHASE = 13
 
@@ -148,6 +148,7 @@ def load(path: str = LIB_PATH):
         "zc_adj_backward": [P] + [P] * 8,
         "zc_adj_get_state": [P] + [P] * 9,
         "zc_adj_times": [P, C.POINTER(C.c_float), C.POINTER(C.c_float)],
+        "zc_species_phasespace": [P, I, I, I, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -354,6 +355,18 @@ class CudaSim:
         rho = np.zeros((self.nx[1] + 1, self.nx[0] + 1), dtype=np.float32) if out is None else out
         _ck(self.lib.zc_species_charge(self.h, int(k), _p(rho)))
         return rho
+
+    PHA = {"x1": 1, "x2": 2, "u1": 4, "u2": 5, "u3": 6}
+
+    def phasespace(self, k, quants, pha_nx, pha_range, out=None):
+        """Phase-space density [pha_nx[1], pha_nx[0]] of species k
+        (quants e.g. ("x1", "u1"), pha_range ((x1min, x1max), (x2min, x2max)))."""
+        n = np.ascontiguousarray(pha_nx, dtype=np.int32)
+        r = np.ascontiguousarray(np.asarray(pha_range, dtype=np.float32).reshape(4))
+        buf = np.zeros((int(n[1]), int(n[0])), dtype=np.float32) if out is None else out
+        _ck(self.lib.zc_species_phasespace(self.h, int(k), self.PHA[quants[0]], self.PHA[quants[1]], _p(n), _p(r),
+                                           _p(buf)))
+        return buf
 
     def info(self):
         i = Info()

@@ -958,7 +958,13 @@ EXPORT void spec_deposit_pha(const t_species *spec, const int rep_type, const in
 {
     int k = 0;
     entry_t *e = reg_by_species(spec, &k);
-    if (e) pull_species(e, k);
+    if (e) {  /* a species of a GPU simulation: deposited on the device */
+        const float rg[4] = {pha_range[0][0], pha_range[0][1], pha_range[1][0], pha_range[1][1]};
+        zc_check(zc_species_phasespace(e->gpu, k, rep_type & 0x000F, (rep_type & 0x00F0) >> 4, pha_nx, rg, buf),
+                 "spec_deposit_pha");
+        return;
+    }
+    /* a stand-alone species (no device state): on the host */
     const int nrow = pha_nx[0];
     const int q1 = rep_type & 0x000F, q2 = (rep_type & 0x00F0) >> 4;
     const float x1min = pha_range[0][0], x2min = pha_range[1][0];

@@ -1402,6 +1402,41 @@ zc_status zc_species_charge(zc_sim *s, int k, float *charge) {
   return ZC_OK;
 }
 
+zc_status zc_species_phasespace(zc_sim *s, int k, int quant1, int quant2, const int pha_nx[2],
+                                const float pha_range[4], float *buf) {
+  TRY(check_species(s, k));
+  if (!pha_nx || !pha_range || !buf) return fail(ZC_EINVAL, "null argument");
+  auto valid_q = [](int q) { return q == 1 || q == 2 || q == 4 || q == 5 || q == 6; };
+  if (!valid_q(quant1) || !valid_q(quant2)) return fail(ZC_EINVAL, "invalid phase-space quantity");
+  if (pha_nx[0] <= 0 || pha_nx[1] <= 0 || !(pha_range[1] != pha_range[0]) || !(pha_range[3] != pha_range[2]))
+    return fail(ZC_EINVAL, "invalid phase-space grid");
+  DeviceGuard g(s->device);
+  SpeciesState &p = s->sp[k];
+  TRY(settle(s, p));
+  PhaConst P;
+  P.q1 = quant1;
+  P.q2 = quant2;
+  P.n1 = pha_nx[0];
+  P.n2 = pha_nx[1];
+  P.x1min = pha_range[0];
+  P.x2min = pha_range[2];
+  P.rdx1 = pha_nx[0] / (pha_range[1] - pha_range[0]);
+  P.rdx2 = pha_nx[1] / (pha_range[3] - pha_range[2]);
+  P.dx = s->dx[0];
+  P.dy = s->dx[1];
+  P.q = p.q;
+  const size_t n = (size_t)pha_nx[0] * pha_nx[1];
+  float *d = nullptr;
+  TRY(dalloc(&d, n));
+  CK(cudaMemcpyAsync(d, buf, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
+  CK(launch_phasespace(p.buf[p.cur], p.d_off, p.d_np, s->ntiles, p.spill[p.spill_cur], p.d_spill_cnt + p.spill_cur,
+                       p.spill_cap, d, P, s->st));
+  CK(cudaMemcpyAsync(buf, d, n * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  dfree(d);
+  return ZC_OK;
+}
+
 zc_status zc_get_info(zc_sim *s, zc_info *info) {
   if (!s || !info) return fail(ZC_EINVAL, "null argument");
   info->iter = s->iter;

@@ -143,6 +143,14 @@ cudaError_t launch_gather_aos(const Particles &buf, const int *off, const int *n
                               int *aos, int ntiles, cudaStream_t st);
 cudaError_t launch_list_to_aos(const Particles &list, const int *n_ptr, int n_cap, int *aos, long long d0,
                                cudaStream_t st);
+// phase-space density of one species (quantity codes 1 x1, 2 x2, 4 u1,
+// 5 u2, 6 u3), added to pha[n1 * n2]
+struct PhaConst {
+  int q1, q2, n1, n2;
+  float x1min, x2min, rdx1, rdx2, dx, dy, q;
+};
+cudaError_t launch_phasespace(const Particles &buf, const int *off, const int *np, int ntiles, const Particles &spill,
+                              const int *spill_cnt, int spill_cap, float *pha, const PhaConst &P, cudaStream_t st);
 cudaError_t launch_charge(const Particles &buf, const int *off, const int *np, int ntiles, const Particles &spill,
                           const int *spill_cnt, int spill_cap, float *rho, int nx, int ny, float q, int mw,
                           cudaStream_t st);

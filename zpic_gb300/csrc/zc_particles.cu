@@ -331,6 +331,57 @@ __global__ void k_charge_list(Particles list, const int *n_ptr, int n_cap, float
   }
 }
 
+// phase-space density (spec_deposit_pha, particles.c:1569-1632): the two
+// axis quantities of spec_pha_axis (particles.c:1510-1536), linear weights
+// onto an n1 x n2 grid, out-of-range cells dropped
+__device__ __forceinline__ float pha_quant(const PRec &r, int q, const PhaConst &P) {
+  switch (q) {
+    case 1: return (r.x + r.ix) * P.dx;
+    case 2: return (r.y + r.iy) * P.dy;
+    case 4: return r.ux;
+    case 5: return r.uy;
+    default: return r.uz;
+  }
+}
+
+__device__ __forceinline__ void pha_add(float *buf, const PRec &r, const PhaConst &P) {
+  const float nx1 = (pha_quant(r, P.q1, P) - P.x1min) * P.rdx1;
+  const float nx2 = (pha_quant(r, P.q2, P) - P.x2min) * P.rdx2;
+  const int i1 = (int)(nx1 + 0.5f), i2 = (int)(nx2 + 0.5f);
+  const float w1 = nx1 - i1 + 0.5f, w2 = nx2 - i2 + 0.5f;
+  const int idx = i1 + P.n1 * i2;
+  const bool a0 = i1 >= 0 && i1 < P.n1, a1 = i1 + 1 >= 0 && i1 + 1 < P.n1;
+  if (i2 >= 0 && i2 < P.n2) {
+    if (a0) atomicAdd(&buf[idx], (1.0f - w1) * (1.0f - w2) * P.q);
+    if (a1) atomicAdd(&buf[idx + 1], w1 * (1.0f - w2) * P.q);
+  }
+  if (i2 + 1 >= 0 && i2 + 1 < P.n2) {
+    if (a0) atomicAdd(&buf[idx + P.n1], (1.0f - w1) * w2 * P.q);
+    if (a1) atomicAdd(&buf[idx + P.n1 + 1], w1 * w2 * P.q);
+  }
+}
+
+__global__ void k_pha_tiles(Particles buf, const int *off, const int *np, int ntiles, float *pha, PhaConst P) {
+  const int t = blockIdx.x;
+  if (t >= ntiles) return;
+  const int n = np[t];
+  const long long a = off[t];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) pha_add(pha, load_particle(buf, a + k), P);
+}
+
+__global__ void k_pha_list(Particles list, const int *n_ptr, int n_cap, float *pha, PhaConst P) {
+  const int n = min(*n_ptr, n_cap);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    pha_add(pha, load_particle(list, k), P);
+}
+
+cudaError_t launch_phasespace(const Particles &buf, const int *off, const int *np, int ntiles, const Particles &spill,
+                              const int *spill_cnt, int spill_cap, float *pha, const PhaConst &P, cudaStream_t st) {
+  k_pha_tiles<<<ntiles, 256, 0, st>>>(buf, off, np, ntiles, pha, P);
+  k_pha_list<<<64, 256, 0, st>>>(spill, spill_cnt, spill_cap, pha, P);
+  return cudaGetLastError();
+}
+
 // boundary corrections of the charge grid (particles.c:1311-1321)
 __global__ void k_charge_fold(float *rho, int nx, int ny, int mw) {
   const int nrow = nx + 1;
