@@ -123,6 +123,24 @@ ZC_API zc_status zc_sim_destroy(zc_sim *sim);
  * spec_new (em2d/particles.c:535-612) and uploads them */
 ZC_API zc_status zc_species_create(zc_sim *sim, const zc_species_desc *desc, const zc_part *parts,
                             int np, int *species_id);
+/* density profile of a species loaded on the device (t_density,
+ * em2d/particles.h:60-83): type 0 uniform, 1 empty, 2 step (from start),
+ * 3 slab (start..end); n the density */
+typedef struct {
+    int type;
+    float n;
+    float start, end;
+} zc_density;
+/* loads a species on the device (spec_set_x / spec_set_u,
+ * em2d/particles.c:85-354): the ppc lattice of every cell inside the profile
+ * (the positions spec_new gives), thermal momenta uth * N(0,1) from a
+ * counter-based generator (Philox4x32-10 keyed by `seed`), the mean momentum
+ * of each cell removed and the drift ufl added; written straight into the
+ * tile layout in cell order.  Momenta are statistically, not bitwise, those
+ * of the reference's generator.  ppc[0] <= 32. */
+ZC_API zc_status zc_species_create_device(zc_sim *sim, float m_q, const int ppc[2], const zc_density *density,
+                                          const float ufl[3], const float uth[3], unsigned long long seed,
+                                          int *species_id);
 /* replaces the device particles of a species (host edits between steps,
  * Species.add / Species.particles writes, python/source/em2d.pyx:238-312) */
 ZC_API zc_status zc_species_set_particles(zc_sim *sim, int species, const zc_part *parts, int np);

@@ -38,7 +38,7 @@ EXPORTS = [
     "zc_phase_name", "zc_field_energy_static", "zc_set_graphs", "zc_history_enable", "zc_history_get",
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
     "zc_adj_create", "zc_adj_destroy", "zc_adj_set_state", "zc_adj_forward", "zc_adj_backward",
-    "zc_adj_get_state", "zc_adj_times", "zc_species_phasespace",
+    "zc_adj_get_state", "zc_adj_times", "zc_species_phasespace", "zc_species_create_device",
 ]
 NPHASE = 13
 
@@ -59,6 +59,13 @@ class AdjDesc(C.Structure):
     _fields_ = [("nx", C.c_int * 2), ("box", C.c_double * 2), ("dt", C.c_double), ("q", C.c_double),
                 ("m_q", C.c_double), ("np", C.c_int), ("checkpoint_every", C.c_int), ("precision", C.c_int),
                 ("device", C.c_int)]
+
+
+class Density(C.Structure):
+    _fields_ = [("type", C.c_int), ("n", C.c_float), ("start", C.c_float), ("end", C.c_float)]
+
+
+DENSITY = {"uniform": 0, "empty": 1, "step": 2, "slab": 3}
 
 
 class SpeciesDesc(C.Structure):
@@ -149,6 +156,7 @@ def load(path: str = LIB_PATH):
         "zc_adj_get_state": [P] + [P] * 9,
         "zc_adj_times": [P, C.POINTER(C.c_float), C.POINTER(C.c_float)],
         "zc_species_phasespace": [P, I, I, I, P, P, P],
+        "zc_species_create_device": [P, C.c_float, P, C.POINTER(Density), P, P, C.c_ulonglong, C.POINTER(I)],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -215,6 +223,20 @@ class CudaSim:
         d = SpeciesDesc(float(m_q), float(q), (C.c_int * 2)(int(ppc[0]), int(ppc[1])))
         k = C.c_int()
         _ck(self.lib.zc_species_create(self.h, C.byref(d), _p(parts), int(parts.size), C.byref(k)))
+        self.n_species += 1
+        return k.value
+
+    def add_species_device(self, m_q, ppc, density="uniform", start=0.0, end=0.0, n=1.0, ufl=(0, 0, 0),
+                           uth=(0, 0, 0), seed=0) -> int:
+        """Loads a species on the device: the ppc lattice inside the density
+        profile, thermal momenta from a counter-based generator."""
+        d = Density(DENSITY[density], float(n), float(start), float(end))
+        pp = np.ascontiguousarray(ppc, dtype=np.int32)
+        uf = np.ascontiguousarray(ufl, dtype=np.float32)
+        ut = np.ascontiguousarray(uth, dtype=np.float32)
+        k = C.c_int()
+        _ck(self.lib.zc_species_create_device(self.h, float(m_q), _p(pp), C.byref(d), _p(uf), _p(ut), int(seed),
+                                              C.byref(k)))
         self.n_species += 1
         return k.value
 

@@ -1079,6 +1079,86 @@ zc_status zc_species_create(zc_sim *s, const zc_species_desc *d, const zc_part *
   return ZC_OK;
 }
 
+zc_status zc_species_create_device(zc_sim *s, float m_q, const int ppc[2], const zc_density *dens, const float ufl[3],
+                                   const float uth[3], unsigned long long seed, int *id) {
+  if (!s || !ppc) return fail(ZC_EINVAL, "null argument");
+  if (m_q == 0.0f) return fail(ZC_EINVAL, "m_q must be non-zero");
+  if (ppc[0] < 1 || ppc[1] < 1 || ppc[0] > 32) return fail(ZC_EINVAL, "ppc must be 1..32 along x and >= 1 along y");
+  const int type = dens ? dens->type : 0;
+  if (type != 0 && type != 1 && type != 2 && type != 3)
+    return fail(ZC_EINVAL, "device loading supports uniform, empty, step and slab densities");
+  DeviceGuard g(s->device);
+  // charge of one particle (spec_new, particles.c:557,576)
+  float n = dens ? dens->n : 1.0f;
+  if (n == 0.0f) n = 1.0f;
+  zc_species_desc d;
+  d.m_q = m_q;
+  d.q = copysignf(1.0f, m_q) / (ppc[0] * ppc[1]) * fabsf(n);
+  d.ppc[0] = ppc[0];
+  d.ppc[1] = ppc[1];
+  int k = -1;
+  TRY(zc_species_create(s, &d, nullptr, 0, &k));
+  if (id) *id = k;
+  if (type == 1) return ZC_OK;  // empty
+  SpeciesState &p = s->sp[k];
+  // lattice points of every column inside the profile, tested as spec_set_x
+  // tests them (particles.c:187-224): xp = i + lattice x against start/dx,
+  // end/dx (floats)
+  const float hx = 1.0f / ppc[0], hy = 1.0f / ppc[1];
+  std::vector<float> latx(ppc[0]);
+  for (int a = 0; a < ppc[0]; ++a) latx[a] = (float)(hx * (a + 0.5));
+  const float lo = (type == 2 || type == 3) ? dens->start / s->dx[0] : 0.0f;
+  const float hi = (type == 3) ? dens->end / s->dx[0] : 0.0f;
+  std::vector<int> colpts(s->nx);
+  std::vector<unsigned> colmask(s->nx);
+  for (int i = 0; i < s->nx; ++i) {
+    unsigned m = 0;
+    for (int a = 0; a < ppc[0]; ++a) {
+      const float xp = i + latx[a];
+      const bool in = (type == 0) || (xp > lo && (type != 3 || xp < hi));
+      if (in) m |= 1u << a;
+    }
+    colmask[i] = m;
+    colpts[i] = __builtin_popcount(m);
+  }
+  const LayoutConst L = layout(s);
+  std::vector<int> cnt(s->ntiles);
+  for (int t = 0; t < s->ntiles; ++t) {
+    const int tx = t % s->ntx, ty = t / s->ntx;
+    const int cx0 = tx * s->TX, cy0 = ty * s->TY;
+    const int wx = std::min(s->TX, s->nx - cx0), wy = std::min(s->TY, s->ny - cy0);
+    long long c = 0;
+    for (int li = 0; li < wx; ++li) c += colpts[cx0 + li];
+    c *= (long long)ppc[1] * wy;
+    if (c > p.h_cap[t]) return fail(ZC_ESTATE, "device loading: tile capacity below the lattice count");
+    cnt[t] = (int)c;
+  }
+  int *d_colpts = nullptr;
+  unsigned *d_colmask = nullptr;
+  TRY(dalloc(&d_colpts, s->nx));
+  TRY(dalloc(&d_colmask, s->nx));
+  CK(cudaMemcpyAsync(d_colpts, colpts.data(), sizeof(int) * s->nx, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(d_colmask, colmask.data(), sizeof(unsigned) * s->nx, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(p.d_np, cnt.data(), sizeof(int) * s->ntiles, cudaMemcpyHostToDevice, s->st));
+  InitConst I;
+  I.ppcx = ppc[0];
+  I.ppcy = ppc[1];
+  I.hx = hx;
+  I.hy = hy;
+  for (int c = 0; c < 3; ++c) {
+    I.uth[c] = uth ? uth[c] : 0.0f;
+    I.ufl[c] = ufl ? ufl[c] : 0.0f;
+  }
+  I.seed_lo = (unsigned)seed;
+  I.seed_hi = (unsigned)(seed >> 32);
+  CK(launch_init_tiles(p.buf[p.cur], p.d_off, d_colpts, d_colmask, I, L, s->ntiles, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  dfree(d_colpts);
+  dfree(d_colmask);
+  invalidate_graph(s);
+  return check_errors(s, false);
+}
+
 zc_status zc_species_set_particles(zc_sim *s, int k, const zc_part *parts, int np) {
   TRY(check_species(s, k));
   if (np < 0 || (np > 0 && !parts)) return fail(ZC_EINVAL, "invalid particle buffer");

@@ -143,6 +143,17 @@ cudaError_t launch_gather_aos(const Particles &buf, const int *off, const int *n
                               int *aos, int ntiles, cudaStream_t st);
 cudaError_t launch_list_to_aos(const Particles &list, const int *n_ptr, int n_cap, int *aos, long long d0,
                                cudaStream_t st);
+// device-side loading: lattice spacing, per-column inclusion masks (bit a
+// of colmask[i]: lattice point a of column i is inside the profile),
+// thermal spread and drift, generator key
+struct InitConst {
+  int ppcx, ppcy;
+  float hx, hy;
+  float uth[3], ufl[3];
+  unsigned seed_lo, seed_hi;
+};
+cudaError_t launch_init_tiles(const Particles &buf, const int *off, const int *colpts, const unsigned *colmask,
+                              const InitConst &I, const LayoutConst &L, int ntiles, cudaStream_t st);
 // phase-space density of one species (quantity codes 1 x1, 2 x2, 4 u1,
 // 5 u2, 6 u3), added to pha[n1 * n2]
 struct PhaConst {

@@ -331,6 +331,111 @@ __global__ void k_charge_list(Particles list, const int *n_ptr, int n_cap, float
   }
 }
 
+// ---------------------------------------------------------------------------
+// device-side loading (spec_set_x / spec_set_u, particles.c:85-354): the
+// ppc lattice of every cell, kept where the density profile includes it
+// (uniform, step, slab as spec_set_x tests the lattice points), thermal
+// momenta from a counter-based generator, each cell's mean momentum
+// removed and the fluid drift added; written straight into the tiles in
+// cell order.  One thread per cell: the cell's particles and its mean stay
+// in that thread.
+// ---------------------------------------------------------------------------
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011): 10 rounds of the 4x32 multiply-xor bijection
+// keyed by a 64-bit key, on a 128-bit counter
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+  constexpr unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  constexpr unsigned W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const unsigned hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += W0;
+    k.y += W1;
+  }
+  return c;
+}
+
+// uniform in (0, 1) from 32 random bits
+__device__ __forceinline__ float u01(unsigned v) { return ((v >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+
+// three standard normal deviates (Box-Muller on two pairs of uniforms)
+__device__ __forceinline__ void normal3(uint4 r, float &a, float &b, float &c) {
+  const float r0 = sqrtf(-2.0f * logf(u01(r.x))), r1 = sqrtf(-2.0f * logf(u01(r.z)));
+  float s0, c0, s1, c1;
+  sincospif(2.0f * u01(r.y), &s0, &c0);
+  sincospif(2.0f * u01(r.w), &s1, &c1);
+  a = r0 * c0;
+  b = r0 * s0;
+  c = r1 * c1;
+}
+
+__global__ void __launch_bounds__(256) k_init_tiles(Particles buf, const int *off, const int *colpts,
+                                                    const unsigned *colmask, InitConst I, LayoutConst L) {
+  const int t = blockIdx.x;
+  const int tx = t % L.ntx, ty = t / L.ntx;
+  const int cx0 = tx * L.TX, cy0 = ty * L.TY;
+  const int wx = min(L.TX, L.nx - cx0), wy = min(L.TY, L.ny - cy0);  // cells of this (maybe partial) tile
+  // particles per cell column of the tile, and their prefix
+  __shared__ int spre[65];
+  if (threadIdx.x == 0) {
+    int a = 0;
+    for (int li = 0; li < wx; ++li) {
+      spre[li] = a;
+      a += colpts[cx0 + li] * I.ppcy;
+    }
+    spre[wx] = a;
+  }
+  __syncthreads();
+  const int row = spre[wx];  // particles in one row of cells of the tile
+  const long long base = off[t];
+  for (int cell = threadIdx.x; cell < L.TX * L.TY; cell += blockDim.x) {
+    const int li = cell % L.TX, lj = cell / L.TX;
+    if (li >= wx || lj >= wy) continue;
+    const int i = cx0 + li, j = cy0 + lj;
+    const int nc = colpts[i] * I.ppcy;
+    if (nc == 0) continue;
+    // cell order inside the tile: local index li + lj * TX
+    const long long o = base + (long long)lj * row + spre[li];
+    const unsigned mask = colmask[i];
+    float mx = 0.f, my = 0.f, mz = 0.f;
+    int m = 0;
+    const unsigned long long cid = (unsigned long long)j * L.nx + i;
+    for (int b = 0; b < I.ppcy; ++b)
+      for (int a = 0; a < I.ppcx; ++a) {
+        if (!(mask >> a & 1)) continue;
+        const uint4 r = philox4x32_10(make_uint4((unsigned)cid, (unsigned)(cid >> 32), (unsigned)(b * I.ppcx + a), 0u),
+                                      make_uint2(I.seed_lo, I.seed_hi));
+        float n0, n1, n2;
+        normal3(r, n0, n1, n2);
+        const float ux = I.uth[0] * n0, uy = I.uth[1] * n1, uz = I.uth[2] * n2;
+        mx += ux;
+        my += uy;
+        mz += uz;
+        store_particle(buf, o + m, i, j, I.hx * (a + 0.5f), I.hy * (b + 0.5f), ux, uy, uz);
+        ++m;
+      }
+    // remove the cell's mean momentum, add the fluid drift (particles.c:102-146)
+    const float inv = 1.0f / m;
+    mx *= inv;
+    my *= inv;
+    mz *= inv;
+    for (int k = 0; k < m; ++k) {
+      PRec r = load_particle(buf, o + k);
+      store_particle(buf, o + k, r.ix, r.iy, r.x, r.y, r.ux - mx + I.ufl[0], r.uy - my + I.ufl[1],
+                     r.uz - mz + I.ufl[2]);
+    }
+  }
+}
+
+cudaError_t launch_init_tiles(const Particles &buf, const int *off, const int *colpts, const unsigned *colmask,
+                              const InitConst &I, const LayoutConst &L, int ntiles, cudaStream_t st) {
+  k_init_tiles<<<ntiles, 256, 0, st>>>(buf, off, colpts, colmask, I, L);
+  return cudaGetLastError();
+}
+
 // phase-space density (spec_deposit_pha, particles.c:1569-1632): the two
 // axis quantities of spec_pha_axis (particles.c:1510-1536), linear weights
 // onto an n1 x n2 grid, out-of-range cells dropped
