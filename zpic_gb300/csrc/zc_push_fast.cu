@@ -2,6 +2,7 @@
 // (zc_push_impl.cuh).  Compiled with FMA contraction and approximate float32 division / square
 // root: same algorithm, results within a few float32 ulps per operation of
 // the exact build.  The deterministic-mode variants are in zc_push_fast_det.cu.
+#define ZC_FAST_ALGEBRA 1  // re-associated current weights (zc_push_impl.cuh)
 #include "zc_internal.cuh"
 #include "zc_kernels.h"
 

@@ -2,6 +2,7 @@
 // deterministic mode (zc_push_impl.cuh with DET = true: currents and
 // kinetic energy accumulated as 64-bit fixed point).  Compiled with the
 // flags of zc_push_fast.cu.
+#define ZC_FAST_ALGEBRA 1  // re-associated current weights (zc_push_impl.cuh)
 #include "zc_internal.cuh"
 #include "zc_kernels.h"
 

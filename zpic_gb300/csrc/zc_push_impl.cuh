@@ -113,6 +113,28 @@ struct SegCurrent {
 };
 
 __device__ __forceinline__ SegCurrent segment_current(const Seg &s, float qnx, float qny) {
+#ifdef ZC_FAST_ALGEBRA
+  // the same weights, re-associated (fast build only): Jx, Jy from the
+  // segment's mid-point; each Jz corner q (a (c + d/2) + b (d - c/2)) with
+  // a, b its start / end x weights and c, d its start / end y weights
+  SegCurrent r;
+  const float jx = qnx * s.dx, jy = qny * s.dy;
+  const float ym = 0.5f * (s.y0 + s.y1), xm = 0.5f * (s.x0 + s.x1);
+  r.v[1] = jx * ym;
+  r.v[0] = jx - r.v[1];
+  r.v[3] = jy * xm;
+  r.v[2] = jy - r.v[3];
+  const float c0 = 1.0f - s.y0, d0 = 1.0f - s.y1;
+  const float p0 = c0 + 0.5f * d0, m0 = d0 - 0.5f * c0;
+  const float p1 = s.y0 + 0.5f * s.y1, m1 = s.y1 - 0.5f * s.y0;
+  const float a0 = 1.0f - s.x0, b0 = 1.0f - s.x1;
+  const float q = s.qvz;
+  r.v[4] = q * (a0 * p0 + b0 * m0);
+  r.v[5] = q * (s.x0 * p0 + s.x1 * m0);
+  r.v[6] = q * (a0 * p1 + b0 * m1);
+  r.v[7] = q * (s.x0 * p1 + s.x1 * m1);
+  return r;
+#else
   const float s0x0 = 1.0f - s.x0, s0x1 = s.x0;
   const float s1x0 = 1.0f - s.x1, s1x1 = s.x1;
   const float s0y0 = 1.0f - s.y0, s0y1 = s.y0;
@@ -132,6 +154,7 @@ __device__ __forceinline__ SegCurrent segment_current(const Seg &s, float qnx, f
   r.v[6] = q * (s0x0 * s0y1 + s1x0 * s1y1 + (s0x0 * s1y1 - s1x0 * s0y1) / 2.0f);
   r.v[7] = q * (s0x1 * s0y1 + s1x1 * s1y1 + (s0x1 * s1y1 - s1x1 * s0y1) / 2.0f);
   return r;
+#endif
 }
 
 template <class D>
