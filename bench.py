@@ -188,25 +188,51 @@ def cpu_run(nx, ny, steps, warmup, fast=True):
     return n * steps / t, kind, n
 
 
+def _cpu_worker(a):
+    """one host process of the parallel CPU baseline (spawned)"""
+    nx, ny, steps, warmup = a
+    return cpu_run(nx, ny, steps, warmup)
+
+
+def cpu_run_parallel(nx, ny, steps, warmup, procs):
+    """`procs` concurrent single-threaded runs of the reference algorithm on
+    the same sub-box (the reference's fan-out of independent runs); returns
+    (aggregate particle-steps/s, kind, particles per run)."""
+    import multiprocessing as mp
+
+    from oracle import pyoracle
+
+    pyoracle.build()
+    with mp.get_context("spawn").Pool(procs) as pool:
+        res = pool.map(_cpu_worker, [(nx, ny, steps, warmup)] * procs)
+    return sum(r[0] for r in res), res[0][1], res[0][2]
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    nx, ny = 1024, 512
-    v, kind, n = cpu_run(nx, ny, args.steps, args.warmup)
+    procs = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    # one core on a 512 x 512 sub-box, then every core at once on 256 x 256
+    # sub-boxes (the reference is single-threaded: its host-wide throughput
+    # is that of independent processes)
+    v1, kind, n1 = cpu_run(512, 512, min(args.steps, 10), min(args.warmup, 2))
+    vp, kind, npr = cpu_run_parallel(256, 256, args.steps, args.warmup, procs)
     W = WORKLOAD
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / v * 1e3,
+        "impl": "reference", "metric": METRIC, "value": vp, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": npr * procs / vp * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": {"workload": W["name"], "nx": list(W["nx"]), "ppc": list(W["ppc"]),
                                         "dt": W["dt"], "dx": 0.1, "smoothing": "compensated level 1, x and y"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
-                         "sample": f"{nx}x{ny}-cell sub-box of the workload ({n} particles), "
-                                   f"{args.steps} timed steps after {args.warmup} warm-up steps, "
-                                   f"single-threaded C (the reference em2d is single-threaded), "
-                                   f"host {platform.machine()}"},
-        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": {"value": vp, "unit": UNIT, "cores": procs, "kind": kind,
+                         "sample": f"{procs} concurrent single-threaded runs, each a 256x256-cell sub-box of the "
+                                   f"workload ({npr} particles), {args.steps} timed steps after {args.warmup} "
+                                   f"warm-up steps; host {platform.machine()}",
+                         "single_core": {"value": v1, "cores": 1,
+                                         "sample": f"512x512-cell sub-box ({n1} particles), "
+                                                   f"{min(args.steps, 10)} timed steps"}},
+        "e2e": {"value": vp, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
