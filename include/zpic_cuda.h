@@ -269,11 +269,15 @@ ZC_API zc_status zc_batch_last_ms(zc_batch *batch, float *ms);
 ZC_API zc_status zc_batch_destroy(zc_batch *batch);
 
 /* --- differentiable step (adjoint) --------------------------------------- */
-/* A forward engine of the periodic em2d step (no smoothing, no moving
- * window) with a charge weight per particle, and its hand-written reverse:
- * the gradient of the total field energy after the last step (the sum of
- * emf_get_energy's components, em2d/emf.c:729-750) with respect to every
- * particle's weight, initial position and momentum, and the initial E and B.
+/* A forward engine of the em2d step with a charge weight per particle, and
+ * its hand-written reverse: the gradient of an objective of the fields after
+ * the last step with respect to every particle's weight, initial position
+ * and momentum, and the initial E and B.  Periodic, or with a moving window
+ * (absorbing x edges, x guard cells with the reference's Yee ranges, the
+ * window shift, particles entering at their birth step); current filter
+ * passes along x.  Objectives: 0 the total field energy (the sum of
+ * emf_get_energy's components, em2d/emf.c:729-750); 1 dx sum Ex^2 along one
+ * row of cells (an on-axis wake amplitude).
  * The reverse sweep recomputes the forward run from checkpoints kept every
  * `checkpoint_every` steps.  Float32 (the reference's arithmetic) or float64
  * (for finite-difference checks).  No counterpart in the reference, whose
@@ -289,11 +293,15 @@ typedef struct {
     int checkpoint_every;
     int precision;          /* 0 float32, 1 float64 */
     int device;
+    int moving_window;      /* 1: moving window (fields [3][ny][nx+3], cells -1 .. nx+1) */
+    int objective;          /* 0 field energy, 1 on-axis Ex (row objective_row) */
+    int objective_row;
 } zc_adj_desc;
 ZC_API zc_status zc_adj_create(const zc_adj_desc *desc, zc_adj **out);
 ZC_API zc_status zc_adj_destroy(zc_adj *adj);
 /* initial state: particle cells and in-cell positions (as t_part), momenta,
- * weights (np each); E and B as 3 planes [component][iy][ix] of nx*ny cells
+ * weights (np each); E and B as 3 planes [component][iy][column] of
+ * nx (periodic) or nx+3 (moving window, cell i at column i+1) columns
  * (NULL: zero) */
 ZC_API zc_status zc_adj_set_state(zc_adj *adj, const int *ix, const int *iy, const double *x, const double *y,
                                   const double *ux, const double *uy, const double *uz, const double *w,
@@ -307,9 +315,16 @@ ZC_API zc_status zc_adj_forward(zc_adj *adj, int nsteps, double *objective, doub
  * start of that run */
 ZC_API zc_status zc_adj_backward(zc_adj *adj, double *d_w, double *d_x, double *d_y, double *d_ux, double *d_uy,
                                  double *d_uz, double *d_E, double *d_B);
-/* current state (after a forward run: its end) */
-ZC_API zc_status zc_adj_get_state(zc_adj *adj, int *ix, int *iy, double *x, double *y, double *ux, double *uy,
-                                  double *uz, double *E, double *B);
+/* current state (after a forward run: its end); alive = 0 for particles that
+ * left through an absorbing x edge */
+ZC_API zc_status zc_adj_get_state(zc_adj *adj, int *ix, int *iy, int *alive, double *x, double *y, double *ux,
+                                  double *uy, double *uz, double *E, double *B);
+/* step at which each particle starts (moving-window injection: the step
+ * after the window move that uncovers its column); NULL: all at step 0 */
+ZC_API zc_status zc_adj_set_birth(zc_adj *adj, const int *birth);
+/* current filter passes along x, each [sa, sb, sa] (kernel_x,
+ * em2d/current.c:316-354; binomial sa = 1/4, sb = 1/2) */
+ZC_API zc_status zc_adj_set_smooth(zc_adj *adj, int npasses, const double *sa, const double *sb);
 /* device time (ms) of the last forward and backward calls, CUDA events */
 ZC_API zc_status zc_adj_times(zc_adj *adj, float *forward_ms, float *backward_ms);
 

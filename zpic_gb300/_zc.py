@@ -39,6 +39,7 @@ EXPORTS = [
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
     "zc_adj_create", "zc_adj_destroy", "zc_adj_set_state", "zc_adj_forward", "zc_adj_backward",
     "zc_adj_get_state", "zc_adj_times", "zc_species_phasespace", "zc_species_create_device",
+    "zc_adj_set_birth", "zc_adj_set_smooth",
 ]
 NPHASE = 13
 
@@ -58,7 +59,7 @@ class SimDesc(C.Structure):
 class AdjDesc(C.Structure):
     _fields_ = [("nx", C.c_int * 2), ("box", C.c_double * 2), ("dt", C.c_double), ("q", C.c_double),
                 ("m_q", C.c_double), ("np", C.c_int), ("checkpoint_every", C.c_int), ("precision", C.c_int),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("moving_window", C.c_int), ("objective", C.c_int), ("objective_row", C.c_int)]
 
 
 class Density(C.Structure):
@@ -153,7 +154,9 @@ def load(path: str = LIB_PATH):
         "zc_adj_set_state": [P] + [P] * 10,
         "zc_adj_forward": [P, I, P, P],
         "zc_adj_backward": [P] + [P] * 8,
-        "zc_adj_get_state": [P] + [P] * 9,
+        "zc_adj_get_state": [P] + [P] * 10,
+        "zc_adj_set_birth": [P, P],
+        "zc_adj_set_smooth": [P, I, P, P],
         "zc_adj_times": [P, C.POINTER(C.c_float), C.POINTER(C.c_float)],
         "zc_species_phasespace": [P, I, I, I, P, P, P],
         "zc_species_create_device": [P, C.c_float, P, C.POINTER(Density), P, P, C.c_ulonglong, C.POINTER(I)],

@@ -165,19 +165,24 @@ __device__ __forceinline__ R value(const Dual<R, N> &a) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+// 3 planes [c][j][i], periodic in y.  Periodic runs: nx columns, periodic
+// in x.  Moving window: nx + 3 columns holding cells -1 .. nx+1 (the
+// reference's x guard cells, em2d/emf.c:59-89), not periodic in x.
 template <class R>
-struct Planes {  // 3 periodic planes [c][j][i], no guard cells
+struct Planes {
   R *f;
-  int nx, ny;
+  int nx, ny, mw;
+  __device__ __forceinline__ int pitch() const { return mw ? nx + 3 : nx; }
   __device__ __forceinline__ size_t at(int c, int i, int j) const {
-    return (size_t)c * nx * ny + (size_t)wrap(j, ny) * nx + wrap(i, nx);
+    const int pt = pitch();
+    return (size_t)c * pt * ny + (size_t)wrap(j, ny) * pt + (mw ? i + 1 : wrap(i, nx));
   }
   __device__ __forceinline__ R operator()(int c, int i, int j) const { return f[at(c, i, j)]; }
 };
 
 template <class R>
 struct State {
-  int *ix, *iy;
+  int *ix, *iy, *alive;  // alive: 0 once the particle left through an absorbing x edge
   R *x, *y, *ux, *uy, *uz;
 };
 
@@ -185,7 +190,16 @@ template <class R>
 struct Params {
   int nx, ny, np;
   R tem, dt_dx, dt_dy, q, qnx, qny;  // qnx = q dx / dt (per unit weight)
+  int mw;                             // moving window: absorbing x edges, window shifts
+  int shift;                          // this step shifts the window
+  int n;                              // step index (particles are born at their birth step)
 };
+
+// a particle takes part in step P.n
+template <class R>
+__device__ __forceinline__ bool active(const State<R> &s, const int *birth, int p, const Params<R> &P) {
+  return s.alive[p] && (!birth || birth[p] <= P.n);
+}
 
 // staggered bilinear gather (interpolate_fld): weights of type T, field
 // samples of type R
@@ -486,10 +500,21 @@ struct AdjointSink {
 // kernels
 // ---------------------------------------------------------------------------
 template <class R>
-__global__ void k_adj_push(State<R> s, State<R> o, const R *w, Planes<R> E, Planes<R> B, Planes<R> J,
-                           double *ekin, Params<R> P) {
+__global__ void k_adj_push(State<R> s, State<R> o, const R *w, const int *birth, Planes<R> E, Planes<R> B,
+                           Planes<R> J, double *ekin, Params<R> P) {
   double ek = 0;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.np; p += gridDim.x * blockDim.x) {
+    if (!active(s, birth, p, P)) {  // not born yet or gone: carried over unchanged
+      o.ix[p] = s.ix[p];
+      o.iy[p] = s.iy[p];
+      o.alive[p] = s.alive[p];
+      o.x[p] = s.x[p];
+      o.y[p] = s.y[p];
+      o.ux[p] = s.ux[p];
+      o.uy[p] = s.uy[p];
+      o.uz[p] = s.uz[p];
+      continue;
+    }
     const int ix = s.ix[p], iy = s.iy[p];
     const R x = s.x[p], y = s.y[p];
     const R u[3] = {s.ux[p], s.uy[p], s.uz[p]};
@@ -504,7 +529,11 @@ __global__ void k_adj_push(State<R> s, State<R> o, const R *w, Planes<R> E, Plan
     const int di = (x1 >= R(1)) - (x1 < R(0)), dj = (y1 >= R(1)) - (y1 < R(0));
     x1 -= R(di);
     y1 -= R(dj);
-    o.ix[p] = wrap(ix + di, P.nx);
+    // periodic, or (moving window) the shift and the absorbing x edges
+    // (particles.c:1234-1259, spec_move_window particles.c:619-640)
+    const int nix = P.mw ? ix + di - P.shift : wrap(ix + di, P.nx);
+    o.ix[p] = nix;
+    o.alive[p] = P.mw ? (nix >= 0 && nix < P.nx) : 1;
     o.iy[p] = wrap(iy + dj, P.ny);
     o.x[p] = x1;
     o.y[p] = y1;
@@ -528,9 +557,10 @@ __device__ __forceinline__ void single_segment(Sink &sink, int ix, int iy, const
 // motion (up to three zigzag segments); the light variant only motions
 // that stay in their cell and returns false for the others untouched.
 template <class R, bool FULL>
-__device__ __forceinline__ bool reverse_particle(int p, const State<R> &s, const R *w, const Planes<R> &E,
-                                                 const Planes<R> &B, const Planes<R> &lamJ, const State<R> &lam,
-                                                 R *lamE, R *lamB, R *dw, const Params<R> &P) {
+__device__ __forceinline__ bool reverse_particle(int p, const State<R> &s, const R *w, const int *birth,
+                                                 const Planes<R> &E, const Planes<R> &B, const Planes<R> &lamJ,
+                                                 const State<R> &lam, R *lamE, R *lamB, R *dw, const Params<R> &P) {
+  if (!active(s, birth, p, P)) return true;  // took no part in this step
   const int ix = s.ix[p], iy = s.iy[p];
   const R x = s.x[p], y = s.y[p];
   const R u[3] = {s.ux[p], s.uy[p], s.uz[p]};
@@ -585,21 +615,23 @@ __device__ __forceinline__ bool reverse_particle(int p, const State<R> &s, const
 // the particles whose motion stays in its cell (most of them); the others
 // are listed for k_adj_push_rev_cross
 template <class R>
-__global__ void __launch_bounds__(128) k_adj_push_rev(State<R> s, const R *w, Planes<R> E, Planes<R> B,
-                                                      Planes<R> lamJ, State<R> lam, R *lamE, R *lamB, R *dw,
-                                                      int *cross, int *ncross, Params<R> P) {
+__global__ void __launch_bounds__(128) k_adj_push_rev(State<R> s, const R *w, const int *birth, Planes<R> E,
+                                                      Planes<R> B, Planes<R> lamJ, State<R> lam, R *lamE, R *lamB,
+                                                      R *dw, int *cross, int *ncross, Params<R> P) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.np; p += gridDim.x * blockDim.x)
-    if (!reverse_particle<R, false>(p, s, w, E, B, lamJ, lam, lamE, lamB, dw, P)) cross[atomicAdd(ncross, 1)] = p;
+    if (!reverse_particle<R, false>(p, s, w, birth, E, B, lamJ, lam, lamE, lamB, dw, P))
+      cross[atomicAdd(ncross, 1)] = p;
 }
 
 // the listed cell-crossing particles
 template <class R>
-__global__ void __launch_bounds__(128) k_adj_push_rev_cross(State<R> s, const R *w, Planes<R> E, Planes<R> B,
-                                                            Planes<R> lamJ, State<R> lam, R *lamE, R *lamB, R *dw,
-                                                            const int *cross, const int *ncross, Params<R> P) {
+__global__ void __launch_bounds__(128) k_adj_push_rev_cross(State<R> s, const R *w, const int *birth, Planes<R> E,
+                                                            Planes<R> B, Planes<R> lamJ, State<R> lam, R *lamE,
+                                                            R *lamB, R *dw, const int *cross, const int *ncross,
+                                                            Params<R> P) {
   const int n = *ncross;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-    reverse_particle<R, true>(cross[k], s, w, E, B, lamJ, lam, lamE, lamB, dw, P);
+    reverse_particle<R, true>(cross[k], s, w, birth, E, B, lamJ, lam, lamE, lamB, dw, P);
 }
 
 // B -= c curl E  (yee_b with c = dt/2)
@@ -665,6 +697,180 @@ __global__ void k_adj_yee_e_T(const R *lE, R *lB, R *lJ, int nx, int ny, R cx, R
   }
 }
 
+// ---------------------------------------------------------------------------
+// moving window: planes of nx + 3 columns (cells -1 .. nx+1), periodic in y
+// ---------------------------------------------------------------------------
+// yee_b over the reference's range, cells -1 .. nx (em2d/emf.c:500-522)
+template <class R>
+__global__ void k_adj_yee_b_mw(const R *E, R *B, int nx, int ny, R cx, R cy) {
+  const int pt = nx + 3;
+  const size_t pl = (size_t)pt * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt), j = (int)(k / pt);  // buffer column b = cell b - 1
+    if (b > nx + 1) continue;
+    const size_t kp = (size_t)wrap(j + 1, ny) * pt + b, kr = k + 1;
+    const R *Ex = E, *Ey = E + pl, *Ez = E + 2 * pl;
+    B[k] += -cy * (Ez[kp] - Ez[k]);
+    B[pl + k] += cx * (Ez[kr] - Ez[k]);
+    B[2 * pl + k] += -cx * (Ey[kr] - Ey[k]) + cy * (Ex[kp] - Ex[k]);
+  }
+}
+
+// yee_e over the reference's range, cells 0 .. nx+1 (em2d/emf.c:531-562)
+template <class R>
+__global__ void k_adj_yee_e_mw(R *E, const R *B, const R *J, int nx, int ny, R cx, R cy, R dt) {
+  const int pt = nx + 3;
+  const size_t pl = (size_t)pt * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt), j = (int)(k / pt);
+    if (b < 1) continue;
+    const size_t km = (size_t)wrap(j - 1, ny) * pt + b, kl = k - 1;
+    const R *Bx = B, *By = B + pl, *Bz = B + 2 * pl;
+    E[k] += cy * (Bz[k] - Bz[km]) - dt * J[k];
+    E[pl + k] += -cx * (Bz[k] - Bz[kl]) - dt * J[pl + k];
+    E[2 * pl + k] += cx * (By[k] - By[kl]) - cy * (Bx[k] - Bx[km]) - dt * J[2 * pl + k];
+  }
+}
+
+// transpose of k_adj_yee_b_mw: lamE += transpose(-c curl) lamB
+template <class R>
+__global__ void k_adj_yee_b_T_mw(const R *lB, R *lE, int nx, int ny, R cx, R cy) {
+  const int pt = nx + 3;
+  const size_t pl = (size_t)pt * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt), j = (int)(k / pt);
+    const bool in = b <= nx + 1, inl = b >= 1 && b - 1 <= nx + 1;  // cell and its left neighbour updated
+    const size_t km = (size_t)wrap(j - 1, ny) * pt + b;
+    const R *ax = lB, *ay = lB + pl, *az = lB + 2 * pl;
+    R ex = 0, ey = 0, ez = 0;
+    if (in) {
+      ex += cy * (az[km] - az[k]);
+      ey += cx * az[k];
+      ez += cy * (ax[k] - ax[km]) - cx * ay[k];
+    }
+    if (inl) {
+      ey += -cx * az[k - 1];
+      ez += cx * ay[k - 1];
+    }
+    lE[k] += ex;
+    lE[pl + k] += ey;
+    lE[2 * pl + k] += ez;
+  }
+}
+
+// transpose of k_adj_yee_e_mw: lamB += transpose(dt curl) lamE, lamJ = -dt lamE
+template <class R>
+__global__ void k_adj_yee_e_T_mw(const R *lE, R *lB, R *lJ, int nx, int ny, R cx, R cy, R dt) {
+  const int pt = nx + 3;
+  const size_t pl = (size_t)pt * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt), j = (int)(k / pt);
+    const bool in = b >= 1, inr = b + 1 <= nx + 2;  // cell and its right neighbour updated
+    const size_t kp = (size_t)wrap(j + 1, ny) * pt + b;
+    const R *ax = lE, *ay = lE + pl, *az = lE + 2 * pl;
+    R bx = 0, by = 0, bz = 0;
+    if (in) {
+      bz += cy * (ax[k] - ax[kp]) - cx * ay[k];
+      by += cx * az[k];
+      bx += -cy * (az[k] - az[kp]);
+    }
+    if (inr) {
+      bz += cx * ay[k + 1];
+      by += -cx * az[k + 1];
+    }
+    lB[k] += bx;
+    lB[pl + k] += by;
+    lB[2 * pl + k] += bz;
+    lJ[k] = in ? -dt * ax[k] : R(0);
+    lJ[pl + k] = in ? -dt * ay[k] : R(0);
+    lJ[2 * pl + k] = in ? -dt * az[k] : R(0);
+  }
+}
+
+// window shift (emf_move_window, em2d/emf.c:648-675): cells -1 .. nx-2 take
+// their right neighbour, cells nx-1 .. nx+1 are zeroed; out of place
+template <class R>
+__global__ void k_adj_shift(const R *in, R *out, int nx, size_t n) {
+  const int pt = nx + 3;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt);
+    out[k] = (b < nx) ? in[k + 1] : R(0);
+  }
+}
+
+// its transpose
+template <class R>
+__global__ void k_adj_shift_T(const R *lout, R *lin, int nx, size_t n) {
+  const int pt = nx + 3;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt);
+    lin[k] = (b >= 1 && b - 1 < nx) ? lout[k - 1] : R(0);
+  }
+}
+
+// one [sa, sb, sa] filter pass along x (kernel_x, em2d/current.c:316-354),
+// out of place: periodic runs filter every cell periodically; with a moving
+// window the interior cells 0 .. nx-1 are filtered and the guard cells kept
+template <class R>
+__global__ void k_adj_smooth_x(const R *in, R *out, int nx, int ny, int mw, R sa, R sb) {
+  const int pt = mw ? nx + 3 : nx;
+  const size_t n = (size_t)3 * pt * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt);
+    const size_t row = k - b;
+    if (mw) {
+      out[k] = (b >= 1 && b <= nx) ? sa * in[k - 1] + sb * in[k] + sa * in[k + 1] : in[k];
+    } else {
+      out[k] = sa * in[row + wrap(b - 1, nx)] + sb * in[k] + sa * in[row + wrap(b + 1, nx)];
+    }
+  }
+}
+
+// its transpose
+template <class R>
+__global__ void k_adj_smooth_x_T(const R *lout, R *lin, int nx, int ny, int mw, R sa, R sb) {
+  const int pt = mw ? nx + 3 : nx;
+  const size_t n = (size_t)3 * pt * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(k % pt);
+    const size_t row = k - b;
+    if (mw) {
+      auto inner = [&](int c) { return c >= 1 && c <= nx; };
+      R v = inner(b) ? sb * lout[k] : lout[k];
+      if (b >= 1 && inner(b - 1)) v += sa * lout[k - 1];
+      if (b + 1 < pt && inner(b + 1)) v += sa * lout[k + 1];
+      lin[k] = v;
+    } else {
+      lin[k] = sa * lout[row + wrap(b - 1, nx)] + sb * lout[k] + sa * lout[row + wrap(b + 1, nx)];
+    }
+  }
+}
+
+// objective terms of the interior cells: 1 = Ex on row `row` (sum Ex^2 dx),
+// 0 = every component (the field energy); writes the adjoint seed and adds
+// the objective's sum of squares to *acc
+template <class R>
+__global__ void k_adj_objective(const R *E, const R *B, R *lE, R *lB, int nx, int ny, int mw, int kind, int row,
+                                R seed, double *acc) {
+  const int pt = mw ? nx + 3 : nx;
+  const size_t pl = (size_t)pt * ny;
+  __shared__ double sred[8];
+  double s = 0;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < 6 * pl; k += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(k / pl);
+    const size_t kk = k - (size_t)c * pl;
+    const int b = (int)(kk % pt), j = (int)(kk / pt);
+    const bool interior = !mw || (b >= 1 && b <= nx);
+    const bool used = interior && (kind == 0 || (c == 0 && j == row));
+    const R f = (c < 3) ? E[k] : B[k - 3 * pl];
+    if (used) s += (double)f * (double)f;
+    R *l = (c < 3) ? lE + k : lB + (k - 3 * pl);
+    if (lE) *l = used ? seed * f : R(0);
+  }
+  s = zc::block_sum_double<256>(s, sred);
+  if (threadIdx.x == 0 && acc) atomicAdd(acc, s);
+}
+
 // sum of squares of n values (field energy), double accumulation
 template <class R>
 __global__ void k_adj_sumsq(const R *f, size_t n, double *out) {
@@ -725,31 +931,40 @@ struct EngineBase {
   virtual zc_status set_state(const int *ix, const int *iy, const double *x, const double *y, const double *ux,
                               const double *uy, const double *uz, const double *w, const double *E,
                               const double *B) = 0;
+  virtual zc_status set_birth(const int *birth) = 0;
+  virtual zc_status set_smooth(int n, const double *sa, const double *sb) = 0;
   virtual zc_status forward(int nsteps, double *objective, double *kin) = 0;
   virtual zc_status backward(double *dw, double *dx, double *dy, double *dux, double *duy, double *duz, double *dE,
                              double *dB) = 0;
-  virtual zc_status get_state(int *ix, int *iy, double *x, double *y, double *ux, double *uy, double *uz,
-                              double *E, double *B) = 0;
+  virtual zc_status get_state(int *ix, int *iy, int *alive, double *x, double *y, double *ux, double *uy,
+                              double *uz, double *E, double *B) = 0;
   float fwd_ms = 0, bwd_ms = 0;
 };
 
 template <class R>
 struct DevState {
-  int *ix = nullptr, *iy = nullptr;
+  int *ix = nullptr, *iy = nullptr, *alive = nullptr;
   R *v = nullptr;  // x, y, ux, uy, uz: 5 arrays of np
-  State<R> view(int np) const { return State<R>{ix, iy, v, v + np, v + 2 * (size_t)np, v + 3 * (size_t)np, v + 4 * (size_t)np}; }
+  State<R> view(int np) const {
+    return State<R>{ix, iy, alive, v, v + np, v + 2 * (size_t)np, v + 3 * (size_t)np, v + 4 * (size_t)np};
+  }
 };
 
 template <class R>
 struct Engine : EngineBase {
   int dev, nx, ny, np, K;
+  int mw = 0, obj_kind = 0, obj_row = 0;
   double dx, dy, dt, q, m_q;
-  size_t pl = 0;  // cells per plane
+  float dtf = 0, dxf = 0;  // the float step and cell size the window-move test uses
+  size_t pl = 0;           // cells per plane
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   R *w = nullptr;
+  int *birth = nullptr;    // step at which each particle starts (null: all at 0)
   DevState<R> cur, nxt;
-  R *E = nullptr, *B = nullptr, *J = nullptr;
+  R *E = nullptr, *B = nullptr, *J = nullptr, *tmp = nullptr;
+  std::vector<std::pair<R, R>> passes;  // current filter passes along x
+  std::vector<char> shifts;             // window moves of the last forward run, per step
   // checkpoints (state + E + B) every K steps, and one segment of pre-step states
   std::vector<DevState<R>> ck_s;
   std::vector<R *> ck_f;  // 6 planes each
@@ -772,18 +987,21 @@ struct Engine : EngineBase {
     owned.push_back(*p);
     return ZC_OK;
   }
-  // one block per state: cells (2 x np ints), then the 5 real arrays
-  size_t state_bytes() const { return 2 * sizeof(int) * (size_t)np + 5 * sizeof(R) * (size_t)np; }
+  // one block per state: cells and alive flags (3 x np ints), then the 5 real arrays
+  size_t state_bytes() const { return 3 * sizeof(int) * (size_t)np + 5 * sizeof(R) * (size_t)np; }
   zc_status alloc_state(DevState<R> &s) {
     char *b = nullptr;
-    TRY_(alloc(&b, state_bytes()));
+    TRY_(alloc(&b, state_bytes() + 16));
     s.ix = reinterpret_cast<int *>(b);
     s.iy = s.ix + np;
-    s.v = reinterpret_cast<R *>(b + 2 * sizeof(int) * (size_t)np);
+    s.alive = s.iy + np;
+    const size_t off = (3 * sizeof(int) * (size_t)np + 15) / 16 * 16;
+    s.v = reinterpret_cast<R *>(b + off);
     return ZC_OK;
   }
+  size_t state_span() const { return (3 * sizeof(int) * (size_t)np + 15) / 16 * 16 + 5 * sizeof(R) * (size_t)np; }
 
-  Params<R> params() const {
+  Params<R> params(int n, int shift) const {
     Params<R> P;
     P.nx = nx;
     P.ny = ny;
@@ -794,23 +1012,30 @@ struct Engine : EngineBase {
     P.q = (R)q;
     P.qnx = (R)(q * dx / dt);
     P.qny = (R)(q * dy / dt);
+    P.mw = mw;
+    P.shift = shift;
+    P.n = n;
     return P;
   }
-  Planes<R> planes(R *f) const { return Planes<R>{f, nx, ny}; }
+  Planes<R> planes(R *f) const { return Planes<R>{f, nx, ny, mw}; }
 
-  zc_status init(int dev_, int nx_, int ny_, int np_, int K_, double dx_, double dy_, double dt_, double q_,
-                 double m_q_) {
-    dev = dev_;
-    nx = nx_;
-    ny = ny_;
-    np = np_;
-    K = K_;
+  zc_status init(const zc_adj_desc *d, double dx_, double dy_) {
+    dev = d->device;
+    nx = d->nx[0];
+    ny = d->nx[1];
+    np = d->np;
+    K = d->checkpoint_every;
+    mw = d->moving_window ? 1 : 0;
+    obj_kind = d->objective;
+    obj_row = d->objective_row;
     dx = dx_;
     dy = dy_;
-    dt = dt_;
-    q = q_;
-    m_q = m_q_;
-    pl = (size_t)nx * ny;
+    dt = d->dt;
+    q = d->q;
+    m_q = d->m_q;
+    dtf = (float)d->dt;
+    dxf = (float)d->box[0] / (float)d->nx[0];
+    pl = (size_t)(mw ? nx + 3 : nx) * ny;
     ACK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     ACK(cudaEventCreate(&e0));
     ACK(cudaEventCreate(&e1));
@@ -821,6 +1046,7 @@ struct Engine : EngineBase {
     TRY_(alloc(&E, 3 * pl));
     TRY_(alloc(&B, 3 * pl));
     TRY_(alloc(&J, 3 * pl));
+    TRY_(alloc(&tmp, 3 * pl));
     TRY_(alloc(&lamE, 3 * pl));
     TRY_(alloc(&lamB, 3 * pl));
     TRY_(alloc(&lamJ, 3 * pl));
@@ -847,22 +1073,22 @@ struct Engine : EngineBase {
 
   zc_status upload(R *dst, const double *src, size_t n) {
     if (!src) return ZC_OK;
-    double *tmp = nullptr;
-    ACK(cudaMallocAsync((void **)&tmp, n * sizeof(double), st));
-    ACK(cudaMemcpyAsync(tmp, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
-    k_from_double<R><<<grid_for(n), 256, 0, st>>>(tmp, dst, n);
+    double *t = nullptr;
+    ACK(cudaMallocAsync((void **)&t, n * sizeof(double), st));
+    ACK(cudaMemcpyAsync(t, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_from_double<R><<<grid_for(n), 256, 0, st>>>(t, dst, n);
     ACK(cudaGetLastError());
-    ACK(cudaFreeAsync(tmp, st));
+    ACK(cudaFreeAsync(t, st));
     return ZC_OK;
   }
   zc_status download(double *dst, const R *src, size_t n) {
     if (!dst) return ZC_OK;
-    double *tmp = nullptr;
-    ACK(cudaMallocAsync((void **)&tmp, n * sizeof(double), st));
-    k_to_double<R><<<grid_for(n), 256, 0, st>>>(src, tmp, n);
+    double *t = nullptr;
+    ACK(cudaMallocAsync((void **)&t, n * sizeof(double), st));
+    k_to_double<R><<<grid_for(n), 256, 0, st>>>(src, t, n);
     ACK(cudaGetLastError());
-    ACK(cudaMemcpyAsync(dst, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    ACK(cudaFreeAsync(tmp, st));
+    ACK(cudaMemcpyAsync(dst, t, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ACK(cudaFreeAsync(t, st));
     return ZC_OK;
   }
 
@@ -871,6 +1097,8 @@ struct Engine : EngineBase {
                       const double *Bh) override {
     ACK(cudaMemcpyAsync(cur.ix, ix, sizeof(int) * np, cudaMemcpyHostToDevice, st));
     ACK(cudaMemcpyAsync(cur.iy, iy, sizeof(int) * np, cudaMemcpyHostToDevice, st));
+    std::vector<int> ones(np, 1);
+    ACK(cudaMemcpyAsync(cur.alive, ones.data(), sizeof(int) * np, cudaMemcpyHostToDevice, st));
     const State<R> v = cur.view(np);
     TRY_(upload(v.x, x, np));
     TRY_(upload(v.y, y, np));
@@ -889,8 +1117,29 @@ struct Engine : EngineBase {
     return ZC_OK;
   }
 
+  zc_status set_birth(const int *bh) override {
+    if (!bh) {
+      birth = nullptr;
+      return ZC_OK;
+    }
+    if (!birth) {
+      int *b = nullptr;
+      TRY_(alloc(&b, np));
+      birth = b;
+    }
+    ACK(cudaMemcpyAsync(birth, bh, sizeof(int) * np, cudaMemcpyHostToDevice, st));
+    ACK(cudaStreamSynchronize(st));
+    return ZC_OK;
+  }
+
+  zc_status set_smooth(int n, const double *sa, const double *sb) override {
+    passes.clear();
+    for (int k = 0; k < n; ++k) passes.push_back({(R)sa[k], (R)sb[k]});
+    return ZC_OK;
+  }
+
   zc_status copy_state(DevState<R> &dst, const DevState<R> &src) {
-    ACK(cudaMemcpyAsync(dst.ix, src.ix, state_bytes(), cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(dst.ix, src.ix, state_span(), cudaMemcpyDeviceToDevice, st));
     return ZC_OK;
   }
 
@@ -902,18 +1151,50 @@ struct Engine : EngineBase {
     return ZC_OK;
   }
 
+  // the window moves at step n when (n+1) dt passes the next cell edge
+  // (spec_move_window / emf_move_window, particles.c:621, emf.c:650)
+  void plan_shifts(int nsteps) {
+    shifts.assign(nsteps, 0);
+    if (!mw) return;
+    int nm = 0;
+    for (int n = 0; n < nsteps; ++n) {
+      const int it = n + 1;
+      if ((it * dtf) > (dxf * (nm + 1))) {
+        shifts[n] = 1;
+        ++nm;
+      }
+    }
+  }
+
   // one step of the forward engine: cur -> nxt, E, B advanced
-  zc_status step(double *ekin) {
-    const Params<R> P = params();
+  zc_status step(int n, double *ekin) {
+    const Params<R> P = params(n, shifts[n]);
     ACK(cudaMemsetAsync(J, 0, sizeof(R) * 3 * pl, st));
-    k_adj_push<R><<<grid_for(np, 256), 256, 0, st>>>(cur.view(np), nxt.view(np), w, planes(E), planes(B),
+    k_adj_push<R><<<grid_for(np, 256), 256, 0, st>>>(cur.view(np), nxt.view(np), w, birth, planes(E), planes(B),
                                                       planes(J), ekin, P);
     ACK(cudaGetLastError());
+    // current filter passes along x (current_smooth, em2d/current.c:427-459)
+    for (const auto &ps : passes) {
+      k_adj_smooth_x<R><<<grid_for(3 * pl), 256, 0, st>>>(J, tmp, nx, ny, mw, ps.first, ps.second);
+      std::swap(J, tmp);
+    }
     const R hx = (R)(0.5 * dt / dx), hy = (R)(0.5 * dt / dy);
     const R cx = (R)(dt / dx), cy = (R)(dt / dy);
-    k_adj_yee_b<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
-    k_adj_yee_e<R><<<grid_for(pl), 256, 0, st>>>(E, B, J, nx, ny, cx, cy, (R)dt);
-    k_adj_yee_b<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
+    if (mw) {
+      k_adj_yee_b_mw<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
+      k_adj_yee_e_mw<R><<<grid_for(pl), 256, 0, st>>>(E, B, J, nx, ny, cx, cy, (R)dt);
+      k_adj_yee_b_mw<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
+      if (P.shift) {
+        k_adj_shift<R><<<grid_for(3 * pl), 256, 0, st>>>(E, tmp, nx, 3 * pl);
+        ACK(cudaMemcpyAsync(E, tmp, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+        k_adj_shift<R><<<grid_for(3 * pl), 256, 0, st>>>(B, tmp, nx, 3 * pl);
+        ACK(cudaMemcpyAsync(B, tmp, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+      }
+    } else {
+      k_adj_yee_b<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
+      k_adj_yee_e<R><<<grid_for(pl), 256, 0, st>>>(E, B, J, nx, ny, cx, cy, (R)dt);
+      k_adj_yee_b<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
+    }
     ACK(cudaGetLastError());
     std::swap(cur, nxt);
     return ZC_OK;
@@ -942,21 +1223,28 @@ struct Engine : EngineBase {
     return ZC_OK;
   }
 
-  zc_status objective(double *out) {
+  // the objective of the current fields; with seed, the adjoint of its
+  // fields goes to lamE / lamB
+  R obj_seed() const { return obj_kind == 0 ? (R)(dx * dy) : (R)(2.0 * dx); }
+  double obj_scale() const { return obj_kind == 0 ? 0.5 * dx * dy : dx; }
+  zc_status objective(double *out, bool seed) {
     ACK(cudaMemsetAsync(d_scr, 0, sizeof(double), st));
-    k_adj_sumsq<R><<<grid_for(3 * pl), 256, 0, st>>>(E, 3 * pl, d_scr);
-    k_adj_sumsq<R><<<grid_for(3 * pl), 256, 0, st>>>(B, 3 * pl, d_scr);
+    k_adj_objective<R><<<grid_for(6 * pl), 256, 0, st>>>(E, B, seed ? lamE : nullptr, seed ? lamB : nullptr, nx, ny,
+                                                          mw, obj_kind, obj_row, obj_seed(), d_scr);
     ACK(cudaGetLastError());
-    double v = 0;
-    ACK(cudaMemcpyAsync(&v, d_scr, sizeof(double), cudaMemcpyDeviceToHost, st));
-    ACK(cudaStreamSynchronize(st));
-    *out = 0.5 * dx * dy * v;
+    if (out) {
+      double v = 0;
+      ACK(cudaMemcpyAsync(&v, d_scr, sizeof(double), cudaMemcpyDeviceToHost, st));
+      ACK(cudaStreamSynchronize(st));
+      *out = obj_scale() * v;
+    }
     return ZC_OK;
   }
 
   zc_status forward(int nsteps, double *obj, double *kin) override {
     if (!have_state) return afail(ZC_ESTATE, "adjoint engine: no initial state");
     if (nsteps <= 0) return afail(ZC_EINVAL, "adjoint engine: nsteps must be > 0");
+    plan_shifts(nsteps);
     ACK(cudaEventRecord(e0, st));
     nck = 0;
     ACK(cudaMemsetAsync(d_scr + 1, 0, sizeof(double), st));
@@ -966,11 +1254,11 @@ struct Engine : EngineBase {
     for (int n = 0; n < nsteps; ++n) {
       if (n % K == 0) TRY_(save_checkpoint());
       if (n >= last0) TRY_(keep_pre_step(n - last0));
-      TRY_(step(n == nsteps - 1 ? d_scr + 1 : nullptr));
+      TRY_(step(n, n == nsteps - 1 ? d_scr + 1 : nullptr));
     }
     steps_done = nsteps;
     ACK(cudaEventRecord(e1, st));
-    if (obj) TRY_(objective(obj));
+    if (obj) TRY_(objective(obj, false));
     if (kin) {
       // q m_q dx dy sum w utsq/(gamma+1) of the last step (particles.c:1231)
       double v = 0;
@@ -983,20 +1271,43 @@ struct Engine : EngineBase {
     return ZC_OK;
   }
 
+  // reverse of the field part of step n: lamE, lamB after the step in,
+  // before the step out; lamJ receives the current's adjoint (before the
+  // filter passes)
+  zc_status field_reverse(int n) {
+    const R hx = (R)(0.5 * dt / dx), hy = (R)(0.5 * dt / dy);
+    const R cx = (R)(dt / dx), cy = (R)(dt / dy);
+    if (mw) {
+      if (shifts[n]) {
+        k_adj_shift_T<R><<<grid_for(3 * pl), 256, 0, st>>>(lamE, tmp, nx, 3 * pl);
+        ACK(cudaMemcpyAsync(lamE, tmp, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+        k_adj_shift_T<R><<<grid_for(3 * pl), 256, 0, st>>>(lamB, tmp, nx, 3 * pl);
+        ACK(cudaMemcpyAsync(lamB, tmp, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
+      }
+      k_adj_yee_b_T_mw<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+      k_adj_yee_e_T_mw<R><<<grid_for(pl), 256, 0, st>>>(lamE, lamB, lamJ, nx, ny, cx, cy, (R)dt);
+      k_adj_yee_b_T_mw<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+    } else {
+      k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+      k_adj_yee_e_T<R><<<grid_for(pl), 256, 0, st>>>(lamE, lamB, lamJ, nx, ny, cx, cy, (R)dt);
+      k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+    }
+    for (int k = (int)passes.size() - 1; k >= 0; --k) {
+      k_adj_smooth_x_T<R><<<grid_for(3 * pl), 256, 0, st>>>(lamJ, tmp, nx, ny, mw, passes[k].first, passes[k].second);
+      std::swap(lamJ, tmp);
+    }
+    ACK(cudaGetLastError());
+    return ZC_OK;
+  }
+
   zc_status backward(double *dwh, double *dxh, double *dyh, double *duxh, double *duyh, double *duzh, double *dEh,
                      double *dBh) override {
     if (steps_done <= 0) return afail(ZC_ESTATE, "adjoint engine: run forward first");
-    // the particles and fields at the end are needed again below: the last
-    // step's state is the current one
     ACK(cudaEventRecord(e0, st));
-    const Params<R> P = params();
-    const R a = (R)(dx * dy);
-    k_adj_scale<R><<<grid_for(3 * pl), 256, 0, st>>>(E, lamE, 3 * pl, a);
-    k_adj_scale<R><<<grid_for(3 * pl), 256, 0, st>>>(B, lamB, 3 * pl, a);
+    // the adjoint of the final fields (the forward run left them in E, B)
+    TRY_(objective(nullptr, true));
     ACK(cudaMemsetAsync(lam.v, 0, sizeof(R) * 5 * (size_t)np, st));
     ACK(cudaMemsetAsync(dwv, 0, sizeof(R) * np, st));
-    const R hx = (R)(0.5 * dt / dx), hy = (R)(0.5 * dt / dy);
-    const R cx = (R)(dt / dx), cy = (R)(dt / dy);
     for (int sgi = nck - 1; sgi >= 0; --sgi) {
       const int n0 = sgi * K, n1 = std::min(steps_done, n0 + K);
       // recompute the segment from its checkpoint, keeping pre-step states
@@ -1005,22 +1316,21 @@ struct Engine : EngineBase {
         TRY_(restore_checkpoint(sgi));
         for (int n = n0; n < n1; ++n) {
           TRY_(keep_pre_step(n - n0));
-          if (n + 1 < n1) TRY_(step(nullptr));
+          if (n + 1 < n1) TRY_(step(n, nullptr));
         }
       }
       // walk the segment backwards
       for (int n = n1 - 1; n >= n0; --n) {
         const int k = n - n0;
-        k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
-        k_adj_yee_e_T<R><<<grid_for(pl), 256, 0, st>>>(lamE, lamB, lamJ, nx, ny, cx, cy, (R)dt);
-        k_adj_yee_b_T<R><<<grid_for(pl), 256, 0, st>>>(lamB, lamE, nx, ny, hx, hy);
+        TRY_(field_reverse(n));
+        const Params<R> P = params(n, shifts[n]);
         ACK(cudaMemsetAsync(d_ncross, 0, sizeof(int), st));
-        k_adj_push_rev<R><<<grid_for(np, 128), 128, 0, st>>>(seg_s[k].view(np), w, planes(seg_f[k]),
+        k_adj_push_rev<R><<<grid_for(np, 128), 128, 0, st>>>(seg_s[k].view(np), w, birth, planes(seg_f[k]),
                                                               planes(seg_f[k] + 3 * pl), planes(lamJ), lam.view(np),
                                                               lamE, lamB, dwv, d_cross, d_ncross, P);
         k_adj_push_rev_cross<R><<<grid_for(np / 4, 128), 128, 0, st>>>(
-            seg_s[k].view(np), w, planes(seg_f[k]), planes(seg_f[k] + 3 * pl), planes(lamJ), lam.view(np), lamE,
-            lamB, dwv, d_cross, d_ncross, P);
+            seg_s[k].view(np), w, birth, planes(seg_f[k]), planes(seg_f[k] + 3 * pl), planes(lamJ), lam.view(np),
+            lamE, lamB, dwv, d_cross, d_ncross, P);
         ACK(cudaGetLastError());
       }
     }
@@ -1042,10 +1352,11 @@ struct Engine : EngineBase {
     return ZC_OK;
   }
 
-  zc_status get_state(int *ix, int *iy, double *x, double *y, double *ux, double *uy, double *uz, double *Eh,
-                      double *Bh) override {
+  zc_status get_state(int *ix, int *iy, int *alive, double *x, double *y, double *ux, double *uy, double *uz,
+                      double *Eh, double *Bh) override {
     if (ix) ACK(cudaMemcpyAsync(ix, cur.ix, sizeof(int) * np, cudaMemcpyDeviceToHost, st));
     if (iy) ACK(cudaMemcpyAsync(iy, cur.iy, sizeof(int) * np, cudaMemcpyDeviceToHost, st));
+    if (alive) ACK(cudaMemcpyAsync(alive, cur.alive, sizeof(int) * np, cudaMemcpyDeviceToHost, st));
     const State<R> v = cur.view(np);
     TRY_(download(x, v.x, np));
     TRY_(download(y, v.y, np));
@@ -1094,6 +1405,9 @@ zc_status zc_adj_create(const zc_adj_desc *d, zc_adj **out) {
   const double cour = std::sqrt(1.0 / (1.0 / (dx * dx) + 1.0 / (dy * dy)));
   if (d->dt >= cour) return afail(ZC_EINVAL, "Invalid timestep, courant condition violation");
   if (d->precision != 0 && d->precision != 1) return afail(ZC_EINVAL, "precision must be 0 (float) or 1 (double)");
+  if (d->objective != 0 && d->objective != 1) return afail(ZC_EINVAL, "objective must be 0 or 1");
+  if (d->objective == 1 && (d->objective_row < 0 || d->objective_row >= d->nx[1]))
+    return afail(ZC_EINVAL, "objective row outside the grid");
   AdjDevice g(d->device);
   zc_adj *h = new zc_adj();
   h->device = d->device;
@@ -1104,11 +1418,11 @@ zc_status zc_adj_create(const zc_adj_desc *d, zc_adj **out) {
   if (d->precision == 0) {
     auto *e = new Engine<float>();
     h->eng.reset(e);
-    st = e->init(d->device, d->nx[0], d->nx[1], d->np, d->checkpoint_every, dx, dy, d->dt, d->q, d->m_q);
+    st = e->init(d, dx, dy);
   } else {
     auto *e = new Engine<double>();
     h->eng.reset(e);
-    st = e->init(d->device, d->nx[0], d->nx[1], d->np, d->checkpoint_every, dx, dy, d->dt, d->q, d->m_q);
+    st = e->init(d, dx, dy);
   }
   if (st != ZC_OK) {
     delete h;
@@ -1152,11 +1466,23 @@ zc_status zc_adj_backward(zc_adj *h, double *dw, double *dx, double *dy, double 
   return h->eng->backward(dw, dx, dy, dux, duy, duz, dE, dB);
 }
 
-zc_status zc_adj_get_state(zc_adj *h, int *ix, int *iy, double *x, double *y, double *ux, double *uy, double *uz,
-                           double *E, double *B) {
+zc_status zc_adj_get_state(zc_adj *h, int *ix, int *iy, int *alive, double *x, double *y, double *ux, double *uy,
+                           double *uz, double *E, double *B) {
   if (!h) return afail(ZC_EINVAL, "null handle");
   AdjDevice g(h->device);
-  return h->eng->get_state(ix, iy, x, y, ux, uy, uz, E, B);
+  return h->eng->get_state(ix, iy, alive, x, y, ux, uy, uz, E, B);
+}
+
+zc_status zc_adj_set_birth(zc_adj *h, const int *birth) {
+  if (!h) return afail(ZC_EINVAL, "null handle");
+  AdjDevice g(h->device);
+  return h->eng->set_birth(birth);
+}
+
+zc_status zc_adj_set_smooth(zc_adj *h, int npasses, const double *sa, const double *sb) {
+  if (!h) return afail(ZC_EINVAL, "null handle");
+  if (npasses < 0 || (npasses > 0 && (!sa || !sb))) return afail(ZC_EINVAL, "invalid filter passes");
+  return h->eng->set_smooth(npasses, sa, sb);
 }
 
 zc_status zc_adj_times(zc_adj *h, float *forward_ms, float *backward_ms) {
