@@ -277,7 +277,7 @@ ZC_API zc_status zc_batch_destroy(zc_batch *batch);
  * window shift, particles entering at their birth step); current filter
  * passes along x.  Objectives: 0 the total field energy (the sum of
  * emf_get_energy's components, em2d/emf.c:729-750); 1 dx sum Ex^2 along one
- * row of cells (an on-axis wake amplitude).
+ * row of cells, over a range of columns (an on-axis wake amplitude).
  * The reverse sweep recomputes the forward run from checkpoints kept every
  * `checkpoint_every` steps.  Float32 (the reference's arithmetic) or float64
  * (for finite-difference checks).  No counterpart in the reference, whose
@@ -296,6 +296,7 @@ typedef struct {
     int moving_window;      /* 1: moving window (fields [3][ny][nx+3], cells -1 .. nx+1) */
     int objective;          /* 0 field energy, 1 on-axis Ex (row objective_row) */
     int objective_row;
+    int objective_cells[2]; /* cells i0 .. i1-1 of the on-axis objective (i1 <= 0: to nx) */
 } zc_adj_desc;
 ZC_API zc_status zc_adj_create(const zc_adj_desc *desc, zc_adj **out);
 ZC_API zc_status zc_adj_destroy(zc_adj *adj);

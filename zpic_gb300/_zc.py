@@ -59,7 +59,8 @@ class SimDesc(C.Structure):
 class AdjDesc(C.Structure):
     _fields_ = [("nx", C.c_int * 2), ("box", C.c_double * 2), ("dt", C.c_double), ("q", C.c_double),
                 ("m_q", C.c_double), ("np", C.c_int), ("checkpoint_every", C.c_int), ("precision", C.c_int),
-                ("device", C.c_int), ("moving_window", C.c_int), ("objective", C.c_int), ("objective_row", C.c_int)]
+                ("device", C.c_int), ("moving_window", C.c_int), ("objective", C.c_int), ("objective_row", C.c_int),
+                ("objective_cells", C.c_int * 2)]
 
 
 class Density(C.Structure):

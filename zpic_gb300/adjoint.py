@@ -35,7 +35,7 @@ class AdjointSim:
     """One adjoint engine: nx x ny periodic cells, np particles."""
 
     def __init__(self, nx, box, dt, n_particles, q, m_q=-1.0, checkpoint_every=20, precision="float32", device=0,
-                 moving_window=False, objective="field_energy", objective_row=0):
+                 moving_window=False, objective="field_energy", objective_row=0, objective_cells=(0, 0)):
         self.lib = load()
         d = AdjDesc()
         d.nx[0], d.nx[1] = int(nx[0]), int(nx[1])
@@ -50,6 +50,7 @@ class AdjointSim:
         d.moving_window = int(bool(moving_window))
         d.objective = {"field_energy": 0, "axis_ex": 1}[objective]
         d.objective_row = int(objective_row)
+        d.objective_cells[0], d.objective_cells[1] = int(objective_cells[0]), int(objective_cells[1])
         h = C.c_void_p()
         _ck(self.lib.zc_adj_create(C.byref(d), C.byref(h)))
         self.h = h

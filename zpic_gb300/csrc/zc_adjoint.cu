@@ -846,12 +846,13 @@ __global__ void k_adj_smooth_x_T(const R *lout, R *lin, int nx, int ny, int mw, 
   }
 }
 
-// objective terms of the interior cells: 1 = Ex on row `row` (sum Ex^2 dx),
+// objective terms of the interior cells: 1 = Ex on row `row`, cells
+// i0 .. i1-1 (sum Ex^2 dx),
 // 0 = every component (the field energy); writes the adjoint seed and adds
 // the objective's sum of squares to *acc
 template <class R>
 __global__ void k_adj_objective(const R *E, const R *B, R *lE, R *lB, int nx, int ny, int mw, int kind, int row,
-                                R seed, double *acc) {
+                                int i0, int i1, R seed, double *acc) {
   const int pt = mw ? nx + 3 : nx;
   const size_t pl = (size_t)pt * ny;
   __shared__ double sred[8];
@@ -861,7 +862,8 @@ __global__ void k_adj_objective(const R *E, const R *B, R *lE, R *lB, int nx, in
     const size_t kk = k - (size_t)c * pl;
     const int b = (int)(kk % pt), j = (int)(kk / pt);
     const bool interior = !mw || (b >= 1 && b <= nx);
-    const bool used = interior && (kind == 0 || (c == 0 && j == row));
+    const int i = mw ? b - 1 : b;  // cell index
+    const bool used = interior && (kind == 0 || (c == 0 && j == row && i >= i0 && i < i1));
     const R f = (c < 3) ? E[k] : B[k - 3 * pl];
     if (used) s += (double)f * (double)f;
     R *l = (c < 3) ? lE + k : lB + (k - 3 * pl);
@@ -953,7 +955,7 @@ struct DevState {
 template <class R>
 struct Engine : EngineBase {
   int dev, nx, ny, np, K;
-  int mw = 0, obj_kind = 0, obj_row = 0;
+  int mw = 0, obj_kind = 0, obj_row = 0, obj_i0 = 0, obj_i1 = 0;
   double dx, dy, dt, q, m_q;
   float dtf = 0, dxf = 0;  // the float step and cell size the window-move test uses
   size_t pl = 0;           // cells per plane
@@ -1028,6 +1030,8 @@ struct Engine : EngineBase {
     mw = d->moving_window ? 1 : 0;
     obj_kind = d->objective;
     obj_row = d->objective_row;
+    obj_i0 = std::max(0, d->objective_cells[0]);
+    obj_i1 = d->objective_cells[1] > 0 ? std::min(d->objective_cells[1], d->nx[0]) : d->nx[0];
     dx = dx_;
     dy = dy_;
     dt = d->dt;
@@ -1230,7 +1234,7 @@ struct Engine : EngineBase {
   zc_status objective(double *out, bool seed) {
     ACK(cudaMemsetAsync(d_scr, 0, sizeof(double), st));
     k_adj_objective<R><<<grid_for(6 * pl), 256, 0, st>>>(E, B, seed ? lamE : nullptr, seed ? lamB : nullptr, nx, ny,
-                                                          mw, obj_kind, obj_row, obj_seed(), d_scr);
+                                                          mw, obj_kind, obj_row, obj_i0, obj_i1, obj_seed(), d_scr);
     ACK(cudaGetLastError());
     if (out) {
       double v = 0;
