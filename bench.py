@@ -489,6 +489,36 @@ def run_adjoint(args):
     return 0
 
 
+def wakefield_fd_study(W, make, load, steps):
+    """Central differences of the float64 engine at shrinking steps, for a0
+    and ramp knot 3, with the wake-region objective and with the whole axis,
+    beside the float64 adjoint of each."""
+    from zpic_gb300 import adjoint
+
+    out = {}
+    for label, cells in (("wake_cells_200_899", (200, 900)), ("whole_axis", (0, 0))):
+        s_ = make("float64", cells)
+        kn = W["knots_n"]
+
+        def Lf(scale, knots):
+            load(s_, scale, knots)
+            return s_.forward(steps)[0]
+
+        Lf(1.0, kn)
+        g = s_.backward()
+        r = {"adjoint_a0": float((g["E"] * W["E"]).sum() + (g["B"] * W["B"]).sum()) / W["a0"],
+             "adjoint_knot3": float(adjoint.ramp_gradient(g["w"], W["X"], W["knots_x"])[3])}
+        for eps in (1e-5, 1e-6, 1e-7, 1e-8):
+            e = np.zeros_like(kn)
+            e[3] = eps
+            r[f"fd_a0_eps{eps:g}"] = (Lf(1 + eps, kn) - Lf(1 - eps, kn)) / (2 * eps * W["a0"])
+            r[f"fd_knot3_eps{eps:g}"] = (Lf(1.0, kn + e) - Lf(1.0, kn - e)) / (2 * eps)
+        out[label] = r
+        s_.close()
+    print(json.dumps({"workload": "wakefield adjoint, finite-difference step study (float64)", **out}), flush=True)
+    return 0
+
+
 def run_wakefield_adjoint(args):
     """The moving-window laser wakefield (2000 x 256, 3000 steps) through
     the adjoint engine: gradient of the final on-axis Ex wake (dx sum Ex^2
@@ -508,9 +538,9 @@ def run_wakefield_adjoint(args):
     n = st["ix"].size
     row = nx[1] // 2
 
-    def make(prec):
+    def make(prec, cells=(200, 900)):
         s_ = adjoint.AdjointSim(nx, box, dt, n, W["q"], checkpoint_every=K, precision=prec, moving_window=True,
-                                objective="axis_ex", objective_row=row, objective_cells=(200, 900))
+                                objective="axis_ex", objective_row=row, objective_cells=cells)
         s_.set_birth(W["birth"])
         s_.set_smooth(W["passes"])
         return s_
@@ -520,6 +550,8 @@ def run_wakefield_adjoint(args):
         s_.set_state(st["ix"], st["iy"], st["x"], st["y"], st["ux"], st["uy"], st["uz"], w, scale * W["E"],
                      scale * W["B"])
 
+    if args.fd_study:
+        return wakefield_fd_study(W, make, load, steps)
     sim = make("float32")
     clk = ClockSampler(0)
     clk.start()
@@ -602,6 +634,7 @@ def main():
     ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
     ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint", "lwfa", "wakefield_adjoint"])
     ap.add_argument("--deterministic", action="store_true", help="fixed-point (bit-reproducible) deposition")
+    ap.add_argument("--fd-study", action="store_true", help="wakefield adjoint: finite differences at shrinking steps")
     ap.add_argument("--scan-runs", type=int, default=256)
     ap.add_argument("--scan-group", type=int, default=0, help="runs per batch graph (0: all)")
     args = ap.parse_args()
