@@ -405,8 +405,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
 }
 
 // host AoS -> device SoA list (temporary), returns the list
-zc_status upload_list(zc_sim *s, const zc_part *parts, int n, Particles &list, int **d_cnt_unused) {
-  (void)d_cnt_unused;
+zc_status upload_list(zc_sim *s, const zc_part *parts, int n, Particles &list) {
   TRY(alloc_particles(list, std::max(n, 1)));
   if (n <= 0) return ZC_OK;
   void *d_aos = nullptr;
@@ -555,14 +554,14 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
       CK(cudaMallocAsync(&d_aos, sizeof(zc_part) * (size_t)n, st));
       CK(cudaMemcpyAsync(d_aos, s->h_inj, sizeof(zc_part) * (size_t)n, cudaMemcpyHostToDevice, st));
       CK(cudaEventRecord(s->inj_done, st));
-      int *d_dummy = nullptr;
-      CK(cudaMallocAsync((void **)&d_dummy, sizeof(int) * s->ntiles, st));
-      CK(cudaMemsetAsync(d_dummy, 0, sizeof(int) * s->ntiles, st));
-      CK(launch_stage_to_list(d_aos, n, s->inj_list, d_dummy, layout(s), s->d_err, st));
+      int *d_tile_cnt = nullptr;  // per-tile counts of the staging kernel (not needed here)
+      CK(cudaMallocAsync((void **)&d_tile_cnt, sizeof(int) * s->ntiles, st));
+      CK(cudaMemsetAsync(d_tile_cnt, 0, sizeof(int) * s->ntiles, st));
+      CK(launch_stage_to_list(d_aos, n, s->inj_list, d_tile_cnt, layout(s), s->d_err, st));
       CK(launch_append_list(s->inj_list, n, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur),
                             layout(s), s->d_err, st));
       CK(cudaFreeAsync(d_aos, st));
-      CK(cudaFreeAsync(d_dummy, st));
+      CK(cudaFreeAsync(d_tile_cnt, st));
     }
   }
   return ZC_OK;
@@ -958,8 +957,6 @@ zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
   TRYC(dalloc(&s->d_emf, 6));
   TRYC(dalloc(&s->stage, (size_t)(s->nx + 3) * (s->ny + 3) * 3));
   {
-    constexpr int dummy = 0;
-    (void)dummy;
     const int BW = (TX + 6) & ~3, BH = TY + 3;
     for (int b = 0; b < 2; ++b) {
       TRYC(make_map(&s->tmK_EB[b], s->EB[b], G, 6, BW, BH));
@@ -1170,7 +1167,7 @@ zc_status zc_species_set_particles(zc_sim *s, int k, const zc_part *parts, int n
     if (p.ob[b].cnt) CK(cudaMemsetAsync(p.ob[b].cnt, 0, sizeof(int) * s->ntiles, s->st));
   p.pending = false;
   Particles list{};
-  TRY(upload_list(s, parts, np, list, nullptr));
+  TRY(upload_list(s, parts, np, list));
   zc_status r = relayout(s, k, &list, np);
   free_particles(list);
   if (r != ZC_OK) return r;
@@ -1185,7 +1182,7 @@ zc_status zc_species_inject(zc_sim *s, int k, const zc_part *parts, int np) {
   SpeciesState &p = s->sp[k];
   TRY(settle(s, p));
   Particles list{};
-  TRY(upload_list(s, parts, np, list, nullptr));
+  TRY(upload_list(s, parts, np, list));
   CK(launch_append_list(list, np, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur), layout(s), s->d_err,
                         s->st));
   CK(cudaStreamSynchronize(s->st));

@@ -66,51 +66,10 @@ __global__ void k_fold_y(float *J, Grid G) {
 }
 
 // ---------------------------------------------------------------------------
-// one [sa, sb, sa] filter pass, out of place (kernel_x / kernel_y,
-// em2d/current.c:316-413).  Every buffer cell is written: the filtered
-// interior, the guard cells the reference refreshes, and untouched copies.
+// one [sa, sb, sa] filter tap (kernel_x / kernel_y, em2d/current.c:316-413)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float f3pt(float sa, float sb, float l, float m, float u) {
   return sa * l + sb * m + sa * u;
-}
-
-__global__ void k_smooth_x(const float *Jin, float *Jout, Grid G, float sa, float sb, int mw) {
-  const int gx = G.nx + 3, gy = G.ny + 3;
-  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int by = blockIdx.y;
-  if (bx >= gx || by >= gy) return;
-  const int i = bx - 1, j = by - 1;
-  int src = -1;  // interior column whose filtered value lands here
-  if (j >= 0 && j < G.ny) {
-    if (i >= 0 && i < G.nx) src = bx;
-    else if (!mw) src = (i < 0) ? G.nx : bx - G.nx;  // -1 <- nx-1, nx <- 0, nx+1 <- 1
-  }
-  for (int c = 0; c < 3; ++c) {
-    float v;
-    if (src >= 0) {
-      const size_t s = gidx(G, c, src, by);
-      v = f3pt(sa, sb, Jin[s - 1], Jin[s], Jin[s + 1]);
-    } else {
-      v = Jin[gidx(G, c, bx, by)];
-    }
-    Jout[gidx(G, c, bx, by)] = v;
-  }
-}
-
-__global__ void k_smooth_y(const float *Jin, float *Jout, Grid G, float sa, float sb) {
-  const int gx = G.nx + 3, gy = G.ny + 3;
-  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int by = blockIdx.y;
-  if (bx >= gx || by >= gy) return;
-  const int i = bx - 1, j = by - 1;
-  // the row whose (new) value this cell holds after the y guard refresh
-  const int srow = (j >= 0 && j < G.ny) ? by : ((j < 0) ? G.ny : by - G.ny);
-  const bool filt = (i >= 0 && i < G.nx);  // only interior columns are filtered
-  for (int c = 0; c < 3; ++c) {
-    const size_t s = gidx(G, c, bx, srow);
-    const float v = filt ? f3pt(sa, sb, Jin[s - G.pitch], Jin[s], Jin[s + G.pitch]) : Jin[s];
-    Jout[gidx(G, c, bx, by)] = v;
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -486,17 +445,6 @@ cudaError_t launch_planes_to_aos(const float *planes, float *aos, const Grid &G,
 cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
   if (!mw) k_fold_x<<<(G.ny + 3 + 127) / 128, 128, 0, st>>>(J, G);
   k_fold_y<<<(G.nx + 3 + 127) / 128, 128, 0, st>>>(J, G);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_smooth_x(const float *Jin, float *Jout, const Grid &G, float sa, float sb, int mw,
-                            cudaStream_t st) {
-  k_smooth_x<<<grid_rows(G, 256), 256, 0, st>>>(Jin, Jout, G, sa, sb, mw);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_smooth_y(const float *Jin, float *Jout, const Grid &G, float sa, float sb, cudaStream_t st) {
-  k_smooth_y<<<grid_rows(G, 256), 256, 0, st>>>(Jin, Jout, G, sa, sb);
   return cudaGetLastError();
 }
 

@@ -179,9 +179,6 @@ struct YeeConst {
 cudaError_t launch_aos_to_planes(const float *aos, float *planes, const Grid &G, int ncomp, cudaStream_t st);
 cudaError_t launch_planes_to_aos(const float *planes, float *aos, const Grid &G, int ncomp, cudaStream_t st);
 cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st);
-cudaError_t launch_smooth_x(const float *Jin, float *Jout, const Grid &G, float sa, float sb, int mw,
-                            cudaStream_t st);
-cudaError_t launch_smooth_y(const float *Jin, float *Jout, const Grid &G, float sa, float sb, cudaStream_t st);
 // all filter passes along one axis in one launch
 constexpr int kMaxSmoothPasses = 16;
 struct SmoothPasses {
