@@ -2,7 +2,7 @@
 GB300, in particle-steps/s.
 
 Workload (one GPU): uniform thermal plasma, 2048 x 2048 cells, dx = dy = 0.1,
-dt = 0.05, periodic, one electron species (m_q = -1), 4 x 4 particles per
+dt = 0.05, 200 steps, periodic, one electron species (m_q = -1), 4 x 4 particles per
 cell (67,108,864 particles), isotropic thermal momentum 0.05, compensated
 level-1 binomial current smoothing along x and y.  Initial particles are
 seeded synthetic data with the reference's loading (ppc lattice, Gaussian
@@ -622,7 +622,7 @@ def run_wakefield_adjoint(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--tile", default="32x16")

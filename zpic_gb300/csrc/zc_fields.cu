@@ -327,15 +327,19 @@ __global__ void k_window_shift(const float *EBin, float *EBout, Grid G) {
 __global__ void __launch_bounds__(256) k_emf_energy_partial(const float *EB, Grid G, double *partial) {
   __shared__ double sred[8];
   float s[6] = {0, 0, 0, 0, 0, 0}, cc[6] = {0, 0, 0, 0, 0, 0};
-  const int n = G.nx * G.ny;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int bx = k % G.nx + 1, by = k / G.nx + 1;
-    for (int c = 0; c < 6; ++c) {
-      const float f = EB[gidx(G, c, bx, by)];
-      const float y = f * f - cc[c];
-      const float t = s[c] + y;
-      cc[c] = (t - s[c]) - y;
-      s[c] = t;
+  // interior rows over the blocks, interior columns over the threads: no
+  // index division, coalesced rows
+  for (int by = blockIdx.x + 1; by <= G.ny; by += gridDim.x) {
+    const size_t row = (size_t)by * G.pitch;
+    for (int bx = threadIdx.x + 1; bx <= G.nx; bx += blockDim.x) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const float f = EB[c * G.plane + row + bx];
+        const float y = f * f - cc[c];
+        const float t = s[c] + y;
+        cc[c] = (t - s[c]) - y;
+        s[c] = t;
+      }
     }
   }
   for (int c = 0; c < 6; ++c) {
