@@ -650,30 +650,11 @@ def main():
     if args.workload == "wakefield_adjoint":
         return run_wakefield_adjoint(args)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist_mod
+    from zpic_gb300.replicas import Replicas
 
-        torch.cuda.set_device(local)
-        dist_mod.init_process_group("nccl")
-        dist = dist_mod
-
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def allmax(v):
-        if not dist:
-            return v
-        import torch
-
-        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    rep = Replicas()  # torchrun: one independent replica per GPU, no data-path collective
+    rank, world, local = rep.rank, rep.world, rep.local
+    barrier, allmax = rep.barrier, rep.allmax
 
     from zpic_gb300._zc import CudaSim
 
@@ -783,8 +764,7 @@ def main():
     if rank == 0:
         print(json.dumps(line), flush=True)
     sim.close()
-    if dist:
-        dist.destroy_process_group()
+    rep.close()
     return 0
 
 
