@@ -107,3 +107,22 @@ def test_rand_norm_sequence_matches_reference():
 def test_courant_violation_is_rejected():
     with pytest.raises(ValueError, match="courant"):
         pyoracle.CpuSim([16, 16], [1.6, 1.6], 0.2)
+
+
+def test_oracle_deposit_conserves_charge():
+    """The oracle's deposit satisfies discrete continuity (the property the
+    full-size GPU test checks at 67M particles)."""
+    import continuity
+    from decks import DECKS, build_cpu
+
+    d = dict(DECKS["thermal"])
+    d.pop("smooth")
+    cpu = build_cpu("thermal", deck=d)
+    nx, ny = d["nx"]
+    dx = np.float32(d["box"][0]) / np.float32(nx)
+    dy = np.float32(d["box"][1]) / np.float32(ny)
+    rho0 = cpu.charge(0)
+    cpu.current_zero()
+    cpu.spec_advance(0)
+    res, dmax = continuity.residual(rho0, cpu.charge(0), cpu.J(), nx, ny, dx, dy, np.float32(d["dt"]))
+    assert dmax > 1e-3 and res < 2e-6, (res, dmax)
