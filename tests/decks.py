@@ -81,6 +81,16 @@ DECKS = {
         laser=dict(type="plane", start=0.9, fwhm=0.3, a0=0.5, omega0=8.0),
         moving_window=True,
         steps=60),
+    # moving window with current smoothing along both axes (the window keeps
+    # the x guard columns out of the x passes)
+    "window_smooth_xy": dict(
+        nx=[96, 24], box=[1.92, 4.8], dt=0.014,
+        species=[dict(name="e", m_q=-1.0, ppc=[2, 2], density=dict(type="step", start=1.0))],
+        laser=dict(type="gaussian", start=1.3, fwhm=0.4, a0=1.5, omega0=10.0, W0=1.2,
+                   focus=1.5, axis=2.4, polarization=0.0),
+        moving_window=True,
+        smooth=dict(xtype="binomial", xlevel=2, ytype="compensated", ylevel=2),
+        steps=50),
 }
 
 

@@ -11,7 +11,7 @@ every deck of ``tests/decks.py`` and stores, per deck:
 
 Usage (where the reference tree and a C compiler are present)::
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [deck ...]   # default: every deck
 
 The reference's ``spec_sort`` is disabled (``n_sort=0``) so that particle
 buffer order is comparable; sorting only permutes the buffer.
@@ -57,7 +57,8 @@ def main():
     pyoracle.build()
     if not pyoracle.ref_available():
         sys.exit("reference build not available (oracle/_ref missing)")
-    for name in DECKS:
+    names = sys.argv[1:] or list(DECKS)
+    for name in names:
         # the reference keeps its generator in process globals: one fresh
         # process per deck
         if os.fork() == 0:

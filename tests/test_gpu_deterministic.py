@@ -51,7 +51,7 @@ def test_tile_shape_and_graphs_do_not_change_bits():
             _same(ref, st)
 
 
-@pytest.mark.parametrize("name", ["weibel_smooth", "thermal", "custom_ext", "lwfa_window"])
+@pytest.mark.parametrize("name", ["weibel_smooth", "thermal", "custom_ext", "lwfa_window", "window_smooth_xy"])
 def test_deterministic_matches_oracle(name):
     cpu, g = mirror(name, deterministic=True)
     for step in range(10):

@@ -271,7 +271,8 @@ FixedJ fixed_j(const zc_sim *s) { return FixedJ{s->Jfix, s->G.pitch, s->G.plane}
 // outbox slots per tile: room for a moving-window column plus crossers
 // (more leavers than slots go to the spill list)
 zc_status ensure_outbox(zc_sim *s, SpeciesState &p, int max_cap) {
-  int per = std::max(128, ((max_cap / 8) + 31) / 32 * 32);
+  // (at most 2^26 slots: the push lists incoming slots in 28-bit fields)
+  int per = std::min(1 << 26, std::max(128, ((max_cap / 8) + 31) / 32 * 32));
   long long need = (long long)per * s->ntiles;
   if (per <= p.ob[0].cap && need <= p.ob_alloc) return ZC_OK;
   for (int b = 0; b < 2; ++b) {
@@ -600,14 +601,21 @@ zc_status current_update_impl(zc_sim *s) {
     }
   }
   int c = 0;
-  if (px.n > 0) {
+  if (px.n > 0 && py.n > 0 && px.n <= 8 && py.n <= 8) {
+    // both axes in one pass over J
     Phase ph(s, ZC_PHASE_SMOOTH, 1);
-    CK(launch_smooth_x_all(s->J[0], s->G, px, s->mw, st));
-  }
-  if (py.n > 0) {
-    Phase ph(s, ZC_PHASE_SMOOTH, 1);
-    CK(launch_smooth_y_all(s->J[0], s->J[1], s->G, py, st));
+    CK(launch_smooth_xy_all(s->J[0], s->J[1], s->G, px, py, s->mw, st));
     c = 1;
+  } else {
+    if (px.n > 0) {
+      Phase ph(s, ZC_PHASE_SMOOTH, 1);
+      CK(launch_smooth_x_all(s->J[0], s->G, px, s->mw, st));
+    }
+    if (py.n > 0) {
+      Phase ph(s, ZC_PHASE_SMOOTH, 1);
+      CK(launch_smooth_y_all(s->J[0], s->J[1], s->G, py, st));
+      c = 1;
+    }
   }
   s->j_cur = c;
   return ZC_OK;
@@ -1258,6 +1266,8 @@ zc_status zc_set_smooth(zc_sim *s, int xtype, int xlevel, int ytype, int ylevel)
   if (ytype != 0 && ylevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along y direction");
   if ((xtype != 0 && xlevel >= kMaxSmoothPasses) || (ytype != 0 && xlevel >= kMaxSmoothPasses))
     return fail(ZC_EINVAL, "smoothing level above %d is not supported", kMaxSmoothPasses - 1);
+  if (xtype != 0 && smooth_x_smem(s->G) > 200 * 1024)
+    return fail(ZC_EINVAL, "smoothing along x supports grids of up to 25600 cells along x");
   invalidate_graph(s);
   s->xtype = xtype;
   s->xlevel = xlevel;

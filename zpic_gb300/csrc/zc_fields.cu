@@ -87,68 +87,70 @@ __device__ __forceinline__ float f3pt(float sa, float sb, float l, float m, floa
 // operations in the same order as with one kernel per pass.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_smooth_x_all(float *J, Grid G, SmoothPasses P, int mw) {
-  extern __shared__ float srow[];  // [2][3][gx]
+  extern __shared__ float srow[];  // [2][gx]: one component of one row
   const int gx = G.nx + 3;
   const int by = blockIdx.x + 1;   // interior row
-  for (int c = 0; c < 3; ++c)
-    for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) srow[c * gx + bx] = J[gidx(G, c, bx, by)];
+  const int c = blockIdx.y;        // component
+  // asynchronous copies: every load of the row in flight at once
+  for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) cp_async4_zfill(srow + bx, J + gidx(G, c, bx, by), true);
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   int cur = 0;
   for (int p = 0; p < P.n; ++p) {
     const float sa = P.sa[p], sb = P.sb[p];
-    for (int c = 0; c < 3; ++c) {
-      const float *r = srow + (cur * 3 + c) * gx;
-      float *o = srow + ((1 - cur) * 3 + c) * gx;
-      for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) {
-        float v;
-        if (bx >= 1 && bx <= G.nx) v = f3pt(sa, sb, r[bx - 1], r[bx], r[bx + 1]);
-        else if (mw) v = r[bx];
-        else {
-          const int s = (bx == 0) ? G.nx : bx - G.nx;  // guard <- filtered interior value
-          v = f3pt(sa, sb, r[s - 1], r[s], r[s + 1]);
-        }
-        o[bx] = v;
+    const float *r = srow + cur * gx;
+    float *o = srow + (1 - cur) * gx;
+    for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) {
+      float v;
+      if (bx >= 1 && bx <= G.nx) v = f3pt(sa, sb, r[bx - 1], r[bx], r[bx + 1]);
+      else if (mw) v = r[bx];
+      else {
+        const int s = (bx == 0) ? G.nx : bx - G.nx;  // guard <- filtered interior value
+        v = f3pt(sa, sb, r[s - 1], r[s], r[s + 1]);
       }
+      o[bx] = v;
     }
     __syncthreads();
     cur = 1 - cur;
   }
-  for (int c = 0; c < 3; ++c)
-    for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) J[gidx(G, c, bx, by)] = srow[(cur * 3 + c) * gx + bx];
+  for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) J[gidx(G, c, bx, by)] = srow[cur * gx + bx];
 }
 
 constexpr int kSmoothYRows = 64;   // interior rows per CTA
 constexpr int kSmoothYCols = 32;   // columns per CTA (one warp across)
 
 __global__ void __launch_bounds__(256) k_smooth_y_all(const float *Jin, float *Jout, Grid G, SmoothPasses P) {
-  extern __shared__ float sbuf[];  // [2][3][ROWS + 2H][COLS], then guard rows [2][3][COLS]
+  extern __shared__ float sbuf[];  // [2][ROWS + 2H][COLS], then guard rows [2][COLS]; one component
   const int H = P.n;
   const int R = kSmoothYRows + 2 * H;
   constexpr int W = kSmoothYCols;
   const int gx = G.nx + 3;
+  const int c = blockIdx.z;                                  // component
   const int cc = threadIdx.x & 31, r0 = threadIdx.x >> 5;   // column, first row of this thread
   const int bx = blockIdx.x * W + cc;
   const bool col_ok = bx < gx;
   const bool filt = bx >= 1 && bx <= G.nx;                   // only interior columns are filtered
   const int j0 = blockIdx.y * kSmoothYRows;                  // first interior row of the strip
-  float *glo = sbuf + 6 * R * W, *ghi = glo + 3 * W;         // y guard rows -1 and ny as stored
-  if (r0 == 0)
-    for (int c = 0; c < 3; ++c) {
-      glo[c * W + cc] = col_ok ? Jin[gidx(G, c, bx, 0)] : 0.f;
-      ghi[c * W + cc] = col_ok ? Jin[gidx(G, c, bx, G.ny + 1)] : 0.f;
-    }
+  float *glo = sbuf + 2 * R * W, *ghi = glo + W;             // y guard rows -1 and ny as stored
+  if (r0 == 0) {
+    cp_async4_zfill(glo + cc, col_ok ? Jin + gidx(G, c, bx, 0) : Jin, col_ok);
+    cp_async4_zfill(ghi + cc, col_ok ? Jin + gidx(G, c, bx, G.ny + 1) : Jin, col_ok);
+  }
   // rows j0-H .. j0+ROWS+H-1, wrapped periodically over the interior rows
   for (int rr = r0; rr < R; rr += 8) {
     int j = (j0 - H + rr) % G.ny;
     if (j < 0) j += G.ny;
-    for (int c = 0; c < 3; ++c) sbuf[(c * R + rr) * W + cc] = col_ok ? Jin[gidx(G, c, bx, j + 1)] : 0.f;
+    cp_async4_zfill(sbuf + rr * W + cc, col_ok ? Jin + gidx(G, c, bx, j + 1) : Jin, col_ok);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   int cur = 0;
   for (int p = 0; p < P.n; ++p) {
     const float sa = P.sa[p], sb = P.sb[p];
-    const float *in = sbuf + cur * 3 * R * W;
-    float *out = sbuf + (1 - cur) * 3 * R * W;
+    const float *in = sbuf + cur * R * W;
+    float *out = sbuf + (1 - cur) * R * W;
     for (int rr = r0; rr < R; rr += 8) {
       bool lo_guard = false, hi_guard = false;
       if (p == 0) {
@@ -158,32 +160,137 @@ __global__ void __launch_bounds__(256) k_smooth_y_all(const float *Jin, float *J
         hi_guard = (jm == G.ny - 1);
       }
       const bool inside = rr > p && rr < R - 1 - p;
-      for (int c = 0; c < 3; ++c) {
-        const int k = (c * R + rr) * W + cc;
-        float v = in[k];
-        if (inside && filt) {
-          const float lo = lo_guard ? glo[c * W + cc] : in[k - W];
-          const float hi = hi_guard ? ghi[c * W + cc] : in[k + W];
-          v = f3pt(sa, sb, lo, in[k], hi);
-        }
-        out[k] = v;
+      const int k = rr * W + cc;
+      float v = in[k];
+      if (inside && filt) {
+        const float lo = lo_guard ? glo[cc] : in[k - W];
+        const float hi = hi_guard ? ghi[cc] : in[k + W];
+        v = f3pt(sa, sb, lo, in[k], hi);
       }
+      out[k] = v;
     }
     __syncthreads();
     cur = 1 - cur;
   }
   if (!col_ok) return;
-  const float *res = sbuf + cur * 3 * R * W;
+  const float *res = sbuf + cur * R * W;
   for (int rr = r0; rr < kSmoothYRows; rr += 8) {
     const int j = j0 + rr;
     if (j >= G.ny) break;
-    for (int c = 0; c < 3; ++c) {
-      const float v = res[(c * R + rr + H) * W + cc];
-      Jout[gidx(G, c, bx, j + 1)] = v;
-      // y guard rows are periodic copies of the filtered interior rows
-      if (j == G.ny - 1) Jout[gidx(G, c, bx, 0)] = v;
-      if (j < 2) Jout[gidx(G, c, bx, G.ny + 1 + j)] = v;
+    const float v = res[(rr + H) * W + cc];
+    Jout[gidx(G, c, bx, j + 1)] = v;
+    // y guard rows are periodic copies of the filtered interior rows
+    if (j == G.ny - 1) Jout[gidx(G, c, bx, 0)] = v;
+    if (j < 2) Jout[gidx(G, c, bx, G.ny + 1 + j)] = v;
+  }
+}
+
+// Both axes in one pass over J (the x passes of every row of the strip, its
+// halo rows included, then the y passes), for the common case of filtering
+// along both: the rows are filtered along x in shared memory with a halo of
+// one column per x pass -- periodic images of the interior columns, or with a
+// moving window the fixed guard columns -- so that each cell sees exactly the
+// float operations of k_smooth_x_all followed by k_smooth_y_all.
+__global__ void __launch_bounds__(256, 6) k_smooth_xy_all(const float *Jin, float *Jout, Grid G, SmoothPasses PX,
+                                                       SmoothPasses P, int mw) {
+  // rows [2][R][XW] (x halo of HX columns each side), guard rows [2][W],
+  // interior row index of each tile row (periodic)
+  extern __shared__ float sbuf[];
+  const int H = P.n, HX = PX.n;
+  const int R = kSmoothYRows + 2 * H;
+  constexpr int W = kSmoothYCols;
+  const int XW = W + 2 * HX;
+  const int gx = G.nx + 3;
+  const int c = blockIdx.z;
+  const int bx0 = blockIdx.x * W;
+  const int j0 = blockIdx.y * kSmoothYRows;
+  float *glo = sbuf + 2 * R * XW, *ghi = glo + W;
+  int *rowj = reinterpret_cast<int *>(ghi + W);
+  const int tid = threadIdx.x;
+  if (tid < W) {
+    const int b = bx0 + tid;
+    cp_async4_zfill(glo + tid, b < gx ? Jin + gidx(G, c, b, 0) : Jin, b < gx);
+    cp_async4_zfill(ghi + tid, b < gx ? Jin + gidx(G, c, b, G.ny + 1) : Jin, b < gx);
+  }
+  for (int rr = tid; rr < R; rr += blockDim.x) {
+    int jm = (j0 - H + rr) % G.ny;
+    rowj[rr] = jm < 0 ? jm + G.ny : jm;
+  }
+  __syncthreads();
+  // k = rr * XW + q walks the tile in steps of the block size
+  const int step_r = blockDim.x / XW, step_q = blockDim.x % XW;
+  const int n = R * XW;
+  {
+    int rr = tid / XW, q = tid % XW;
+    for (int k = tid; k < n; k += blockDim.x) {
+      // buffer column of strip column q: with a moving window the column
+      // itself (zero outside the buffer), else its periodic image over the
+      // interior columns
+      int b = bx0 - HX + q;
+      if (!mw && (b < 1 || b > G.nx)) b = ((b - 1) % G.nx + G.nx) % G.nx + 1;
+      const bool ok = b >= 0 && b < gx;
+      cp_async4_zfill(sbuf + k, ok ? Jin + gidx(G, c, b, rowj[rr] + 1) : Jin, ok);
+      q += step_q;
+      rr += step_r;
+      if (q >= XW) { q -= XW; ++rr; }
     }
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  // x passes (kernel_x): every strip column filtered from its neighbours,
+  // except the guard columns of a moving window, which stay as they are;
+  // after p passes the columns p .. XW-1-p hold the filtered values
+  int cur = 0;
+  for (int p = 0; p < HX; ++p) {
+    const float sa = PX.sa[p], sb = PX.sb[p];
+    const float *in = sbuf + cur * R * XW;
+    float *out = sbuf + (1 - cur) * R * XW;
+    int q = tid % XW;
+    for (int k = tid; k < n; k += blockDim.x) {
+      const int b = bx0 - HX + q;
+      float v = in[k];
+      if (q > 0 && q < XW - 1 && (!mw || (b >= 1 && b <= G.nx))) v = f3pt(sa, sb, in[k - 1], in[k], in[k + 1]);
+      out[k] = v;
+      q += step_q;
+      if (q >= XW) q -= XW;
+    }
+    __syncthreads();
+    cur = 1 - cur;
+  }
+  // y passes (kernel_y) on the strip's own columns, as k_smooth_y_all
+  const int cc = tid & 31, r0 = tid >> 5;
+  const int bx = bx0 + cc;
+  const bool filt = bx >= 1 && bx <= G.nx;
+  for (int p = 0; p < H; ++p) {
+    const float sa = P.sa[p], sb = P.sb[p];
+    const float *in = sbuf + cur * R * XW + HX;
+    float *out = sbuf + (1 - cur) * R * XW + HX;
+    for (int rr = r0; rr < R; rr += 8) {
+      // the first pass reads the y guard rows as stored
+      const int jm = p == 0 ? rowj[rr] : -1;
+      const bool inside = rr > p && rr < R - 1 - p;
+      const int k = rr * XW + cc;
+      float v = in[k];
+      if (inside && filt) {
+        const float lo = jm == 0 ? glo[cc] : in[k - XW];
+        const float hi = jm == G.ny - 1 ? ghi[cc] : in[k + XW];
+        v = f3pt(sa, sb, lo, in[k], hi);
+      }
+      out[k] = v;
+    }
+    __syncthreads();
+    cur = 1 - cur;
+  }
+  if (bx >= gx) return;
+  const float *res = sbuf + cur * R * XW + HX;
+  for (int rr = r0; rr < kSmoothYRows; rr += 8) {
+    const int j = j0 + rr;
+    if (j >= G.ny) break;
+    const float v = res[(rr + H) * XW + cc];
+    Jout[gidx(G, c, bx, j + 1)] = v;
+    if (j == G.ny - 1) Jout[gidx(G, c, bx, 0)] = v;
+    if (j < 2) Jout[gidx(G, c, bx, G.ny + 1 + j)] = v;
   }
 }
 
@@ -452,25 +559,34 @@ cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// shared memory of one x-filter CTA (a component of a row, double buffered)
+size_t smooth_x_smem(const Grid &G) { return sizeof(float) * 2 * (size_t)(G.nx + 3); }
+
 cudaError_t launch_smooth_x_all(float *J, const Grid &G, const SmoothPasses &P, int mw, cudaStream_t st) {
-  const size_t sh = sizeof(float) * 6 * (size_t)(G.nx + 3);
+  const size_t sh = smooth_x_smem(G);
   if (sh > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_smooth_x_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
     if (e != cudaSuccess) return e;
   }
-  k_smooth_x_all<<<G.ny, 256, sh, st>>>(J, G, P, mw);
+  k_smooth_x_all<<<dim3(G.ny, 3), 256, sh, st>>>(J, G, P, mw);
   return cudaGetLastError();
 }
 
 cudaError_t launch_smooth_y_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &P,
                                 cudaStream_t st) {
-  const size_t sh = sizeof(float) * 6 * ((size_t)(kSmoothYRows + 2 * P.n) + 1) * kSmoothYCols;
-  if (sh > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_smooth_y_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
-    if (e != cudaSuccess) return e;
-  }
-  dim3 grid((G.nx + 3 + kSmoothYCols - 1) / kSmoothYCols, (G.ny + kSmoothYRows - 1) / kSmoothYRows);
+  const size_t sh = sizeof(float) * 2 * ((size_t)(kSmoothYRows + 2 * P.n) + 1) * kSmoothYCols;
+  dim3 grid((G.nx + 3 + kSmoothYCols - 1) / kSmoothYCols, (G.ny + kSmoothYRows - 1) / kSmoothYRows, 3);
   k_smooth_y_all<<<grid, 256, sh, st>>>(Jin, Jout, G, P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth_xy_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
+                                 const SmoothPasses &P, int mw, cudaStream_t st) {
+  const size_t R = kSmoothYRows + 2 * P.n, XW = kSmoothYCols + 2 * PX.n;
+  const size_t sh = sizeof(float) * (2 * R * XW + 2 * kSmoothYCols) + sizeof(int) * R;
+  if (sh > 48 * 1024) return cudaErrorInvalidValue;  // more than 8 passes along an axis
+  dim3 grid((G.nx + 3 + kSmoothYCols - 1) / kSmoothYCols, (G.ny + kSmoothYRows - 1) / kSmoothYRows, 3);
+  k_smooth_xy_all<<<grid, 256, sh, st>>>(Jin, Jout, G, PX, P, mw);
   return cudaGetLastError();
 }
 

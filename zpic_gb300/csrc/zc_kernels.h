@@ -186,6 +186,11 @@ struct SmoothPasses {
   float sa[kMaxSmoothPasses], sb[kMaxSmoothPasses];
 };
 cudaError_t launch_smooth_x_all(float *J, const Grid &G, const SmoothPasses &P, int mw, cudaStream_t st);
+// both axes in one pass (x passes PX, then y passes P), out of place
+cudaError_t launch_smooth_xy_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
+                                 const SmoothPasses &P, int mw, cudaStream_t st);
+// shared memory an x-filter CTA needs (one component of one row)
+size_t smooth_x_smem(const Grid &G);
 cudaError_t launch_smooth_y_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &P,
                                 cudaStream_t st);
 cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,

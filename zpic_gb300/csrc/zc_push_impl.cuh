@@ -335,8 +335,10 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 // go to this tile's slot of `O`.  Stayers are compacted into the tile's
 // segment of `pout`: every warp reserves its slots with one shared-memory
 // atomic, so the lanes of a warp keep their (cell-sorted) order while the
-// order of the warps' runs follows their timing.  The main loop has no
-// block-wide barrier.
+// order of the warps' runs follows their timing.  The particles bound for
+// the tile are first listed from the neighbours' outboxes (one warp per
+// neighbour) and pushed in full warps after the own particles.  The main
+// loop has no block-wide barrier.
 // ---------------------------------------------------------------------------
 template <int TX, int TY, int NT, bool DET>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
@@ -361,6 +363,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   __shared__ __align__(16) float4 pf_u[NW][2][32];   // prefetched particles, per warp, double buffered
   __shared__ __align__(16) float2 pf_xy[NW][2][32];
   __shared__ int nb[8], s_nnb;        // distinct neighbour tiles
+  // incoming particles bound for this tile, listed as (outbox slot << 4 |
+  // neighbour) so that they are pushed in full warps
+  constexpr int INCAP = 512;
+  __shared__ int s_in[INCAP];
+  __shared__ int s_nin;
   __shared__ int s_stay, s_leave;     // output counters (warp-aggregated atomics)
 
   const int t = blockIdx.x;
@@ -390,6 +397,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
         if (!dup) nb[c++] = id;
       }
     s_nnb = c;
+    s_nin = 0;
     s_stay = 0;
     s_leave = 0;
     s_ekin[0] = 0;
@@ -587,6 +595,32 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     }
   };
 
+  // incoming particles: warp w scans the outboxes of neighbours w, w + NW,
+  // ... for the slots bound for this tile and lists them; a full list
+  // leaves the rest to be pushed right here
+  for (int m = warp; m < nnb; m += NW) {
+    const int src = nb[m];
+    const int n = Oin.cnt[src];
+    const long long ob = (long long)src * Oin.cap;
+    for (int e0 = 0; e0 < n; e0 += 32) {
+      const int e = e0 + lane;
+      const bool bound = e < n && Oin.dst[ob + e] == t;
+      const unsigned bm = __ballot_sync(0xffffffffu, bound);
+      if (!bm) continue;
+      int slot = 0;
+      if (lane == 0) slot = atomicAdd(&s_nin, __popc(bm));
+      slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(bm & ((1u << lane) - 1));
+      if (bound && slot < INCAP) s_in[slot] = (e << 4) | m;
+      const bool over = bound && slot >= INCAP;
+      if (__any_sync(0xffffffffu, over)) {
+        PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (over) r = load_particle(Oin.p, ob + e);
+        process(over, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
+      }
+    }
+  }
+  __syncthreads();
+
   // own particles: warp w takes chunks w, w + NW, ... of 32; the next
   // chunk is copied into shared memory while this one is pushed
   {
@@ -626,18 +660,19 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     cp_async_wait<0>();
   }
 
-  // incoming particles: the warps walk the neighbours' outboxes in chunks of
-  // 32 slots and push the ones bound for this tile
-  for (int m = 0; m < nnb; ++m) {
-    const int src = nb[m];
-    const int n = Oin.cnt[src];
-    const long long ob = (long long)src * Oin.cap;
-    for (int e0 = warp * 32; e0 < n; e0 += NT) {
-      const int e = e0 + lane;
-      const bool valid = e < n && Oin.dst[ob + e] == t;
-      if (!__any_sync(0xffffffffu, valid)) continue;
+  // the listed incoming particles, in chunks of 32 that continue the own
+  // chunks' round robin over the warps
+  {
+    const int nin = min(s_nin, INCAP);
+    const int own_chunks = (n_own + 31) / 32;
+    for (int i = (warp + NW - own_chunks % NW) % NW; i * 32 < nin; i += NW) {
+      const int k = i * 32 + lane;
+      const bool valid = k < nin;
       PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if (valid) r = load_particle(Oin.p, ob + e);
+      if (valid) {
+        const int v = s_in[k];
+        r = load_particle(Oin.p, (long long)nb[v & 15] * Oin.cap + (v >> 4));
+      }
       process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
     }
   }
