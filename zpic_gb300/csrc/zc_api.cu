@@ -4,6 +4,7 @@
 // error message.
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -112,6 +113,7 @@ struct SpeciesState {
   Particles spill[2] = {};
   int *d_spill_cnt = nullptr;  // [2]
   int spill_cap = 0;
+  int max_cap = 0;             // largest tile capacity
   int spill_cur = 0;
   // outboxes: leavers posted by one push, pulled by the next (ob[ob_in]
   // holds the pending ones; its counts are all zero when nothing is pending)
@@ -348,6 +350,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   }
   if (tot >= (1LL << 31)) return fail(ZC_ENOMEM, "species too large for 32-bit tile offsets");
   TRY(ensure_outbox(s, p, max_cap));
+  p.max_cap = max_cap;
 
   Particles nbuf[2] = {};
   const bool grow = tot > p.alloc;
@@ -448,6 +451,41 @@ zc_status check_errors(zc_sim *s, bool relayout_spill) {
   return ZC_OK;
 }
 
+// Scale of the push's integer current tile (jsplit).  Every contribution
+// is below vmax = 1.5 |q| in magnitude: a segment's Jx is qnx dx' with |dx'|
+// <= |mx| = (dt/dx) |ux| / gamma < dt/dx, so |Jx| < |q| (Jy alike), and its Jz
+// corner weights times qvz/2 stay below 1.25 |q| (the margin covers the
+// fast build's approximate square roots); a warp adds at most 32 of them at
+// once.  A tile takes at most n = 3 (largest tile + 8 outboxes)
+// contributions per node (three segments per particle).  With 2^cl >= n, L =
+// min(22, 31 - cl) keeps the sums of the |m|, |l| <= 2^(L-1) below 2^30; js
+// = 2^k with k = 40 (the unit of the deterministic sums) unless n vmax js
+// 2^-2L <= 2^30 (the sum of the |h| below 2^31) or 32 vmax js 2^-2L < 2^22
+// (the shifter's range) need less.  Deterministic runs require k = 40, so
+// that their sums do not depend on the tile layout.
+zc_status set_current_scale(zc_sim *s, const SpeciesState &p, PushConst &C) {
+  const double vmax = std::max(1.5 * std::fabs((double)p.q), 1e-30);
+  const long long n = 3LL * ((long long)p.max_cap + 8LL * p.ob[0].cap) + 1;
+  int cl = 0;
+  while ((1LL << cl) < n) ++cl;
+  if (cl > 28) return fail(ZC_ENOMEM, "tile capacity too large for the integer current tile");
+  const int L = std::min(22, 31 - cl);
+  const double k1 = std::floor(std::log2(std::ldexp(1.0, 30 + 2 * L) / ((double)n * vmax)));
+  const double k2 = std::floor(std::log2(std::ldexp(1.0, 16 + 2 * L) / vmax));
+  const int kx = (int)std::max(-60.0, std::min(40.0, std::min(k1, k2)));
+  if (s->deterministic && kx < 40)
+    return fail(ZC_EINVAL, "charge or tile capacity too large for deterministic (fixed-point) deposition");
+  C.js = (float)std::ldexp(1.0, kx);
+  C.js_invl = (float)std::ldexp(1.0, -L);
+  C.js_twol = (float)std::ldexp(1.0, L);
+  C.js_inv2l = (float)std::ldexp(1.0, -2 * L);
+  C.js_two2l = (float)std::ldexp(1.0, 2 * L);
+  C.js_lo = (float)std::ldexp(1.0, -kx);
+  C.js_l = L;
+  C.js_det = s->deterministic ? 1LL : 0LL;  // 2^(40 - k), k = 40
+  return ZC_OK;
+}
+
 zc_status spec_advance_impl(zc_sim *s, int k) {
   SpeciesState &p = s->sp[k];
   cudaStream_t st = s->st;
@@ -471,6 +509,7 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   C.nty = s->nty;
   C.shift = shift;
   C.mw = s->mw;
+  TRY(set_current_scale(s, p, C));
   const int in = p.spill_cur, out = 1 - p.spill_cur;
   {
     Phase ph(s, ZC_PHASE_SPILL, 0);

@@ -13,6 +13,13 @@ struct PushConst {
   int nx, ny, ntx, nty;
   int shift;                              // moving-window shift applied this step (0/1)
   int mw;                                 // absorbing boundaries along x
+  // tile current as integers (see jsplit): a contribution v counts as
+  // rint(v js) = h 2^2L + m 2^L + l; js_invl = 2^-L, js_twol = 2^L,
+  // js_inv2l = 2^-2L, js_two2l = 2^2L, js_lo = 1 / js; deterministic global
+  // sums in units of 2^-40 take each integer times js_det (2^40 / js)
+  float js, js_invl, js_twol, js_inv2l, js_two2l, js_lo;
+  int js_l;
+  long long js_det;
 };
 
 struct TileSet {

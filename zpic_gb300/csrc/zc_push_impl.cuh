@@ -42,13 +42,75 @@ struct TileFields {
     return s[c * PL + (j + 1) * BW + (i + 1)];
   }
 };
-template <int BW, int PL>
-struct TileCurrent {
-  float *s;
-  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
-    atomicAdd(&s[c * PL + (j + 1) * BW + (i + 1)], v);
+// The tile current is kept as three planes of 32-bit integers: a
+// contribution v counts as the integer rint(v js) = h 2^2L + m 2^L + l (js a
+// power of two, |m|, |l| <= 2^(L-1)), each part added to its plane with a
+// 32-bit integer atomic (float atomic adds on shared memory run as
+// compare-and-swap loops, integer ones are single instructions).  The host
+// picks L so that no plane can overflow with the most contributions a tile
+// can take, and js = 2^40 (the unit of the deterministic mode) unless the
+// largest contribution needs a smaller one.  The parts are rounded with the
+// 1.5 2^23 shifter (exact for |t| < 2^22) instead of conversion instructions.
+constexpr float kShifter = 12582912.0f;  // 1.5 * 2^23
+constexpr int kShifterBits = 0x4B400000;
+
+__device__ __forceinline__ void jsplit(float v, const PushConst &C, int &h, int &m, int &l) {
+  const float x = __fmul_rn(v, C.js);                  // exact: js is a power of two
+  const float th = __fmaf_rn(x, C.js_inv2l, kShifter);  // rint(x 2^-2L) + shifter
+  h = __float_as_int(th) - kShifterBits;
+  const float r1 = __fmaf_rn(-__fsub_rn(th, kShifter), C.js_two2l, x);  // exact remainder
+  const float tm = __fmaf_rn(r1, C.js_invl, kShifter);
+  m = __float_as_int(tm) - kShifterBits;
+  const float r2 = __fmaf_rn(-__fsub_rn(tm, kShifter), C.js_twol, r1);  // exact remainder
+  l = __float_as_int(__fadd_rn(r2, kShifter)) - kShifterBits;
+}
+
+// node offsets of the integer J tile, per component: Jx takes columns
+// -1..TX, Jy rows -1..TY, Jz both one more (the halo each can receive)
+template <int TX, int TY>
+struct JTileLayout {
+  static constexpr int WX = TX + 2, HX = TY + 3;
+  static constexpr int WY = TX + 3, HY = TY + 2;
+  static constexpr int WZ = TX + 3, HZ = TY + 3;
+  static constexpr int OX = 0, OY = WX * HX, OZ = OY + WY * HY;
+  static constexpr int N = OZ + WZ * HZ;  // nodes per plane
+  // component, row and column (halo included) of node k
+  __device__ __forceinline__ static void where(int k, int &c, int &r, int &col) {
+    if (k < OY) {
+      c = 0, r = k / WX, col = k % WX;
+    } else if (k < OZ) {
+      c = 1, r = (k - OY) / WY, col = (k - OY) % WY;
+    } else {
+      c = 2, r = (k - OZ) / WZ, col = (k - OZ) % WZ;
+    }
+  }
+  __device__ __forceinline__ static int node(int c, int i, int j) {
+    return c == 0 ? OX + (j + 1) * WX + (i + 1) : (c == 1 ? OY + (j + 1) * WY + (i + 1) : OZ + (j + 1) * WZ + (i + 1));
   }
 };
+
+// the integer a node of the tile holds: h 2^2L + m 2^L + l
+__device__ __forceinline__ long long tile_node_sum(const int *p, int n, int k, int L) {
+  return (long long)p[k] * (1LL << (2 * L)) + (long long)p[n + k] * (1LL << L) + p[2 * n + k];
+}
+
+template <class LAY>
+struct TileCurrentSplit {
+  int *p;  // planes h, m, l of LAY::N nodes each
+  const PushConst *C;
+  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
+    int h, m, l;
+    jsplit(v, *C, h, m, l);
+    addi(c, i, j, h, m, l);
+  }
+  __device__ __forceinline__ void addi(int c, int i, int j, int h, int m, int l) const {
+    const int k = LAY::node(c, i, j);
+    atomicAdd(&p[k], h);
+    atomicAdd(&p[LAY::N + k], m);
+    atomicAdd(&p[2 * LAY::N + k], l);
+  }
+};
+
 struct GlobalFields {
   const float *g;
   int pitch;
@@ -66,30 +128,21 @@ struct GlobalCurrent {
   }
 };
 
-// deterministic mode: every contribution rounded once to 64-bit fixed point
-// and summed as integers (exact, so the order of the sums does not matter)
-__device__ __forceinline__ long long to_fixed(float v) { return __double2ll_rn((double)v * kJFixScale); }
+// deterministic mode: every contribution rounded once to the integer
+// rint(v js) (as the tile current rounds it) and summed in units of 2^-40
+__device__ __forceinline__ long long to_fixed(float v, const PushConst &C) {
+  return __float2ll_rn(v * C.js) * C.js_det;
+}
 
-template <int BW, int PL>
-struct TileCurrentFixed {
-  unsigned long long *s;
-  __device__ __forceinline__ void add(int c, int i, int j, float v) const { addi(c, i, j, to_fixed(v)); }
-  __device__ __forceinline__ void addi(int c, int i, int j, long long v) const {
-    atomicAdd(&s[c * PL + (j + 1) * BW + (i + 1)], (unsigned long long)v);
-  }
-};
 struct GlobalCurrentFixed {
   unsigned long long *g;
   int pitch;
   size_t plane;
+  const PushConst *C;
   __device__ __forceinline__ void add(int c, int i, int j, float v) const {
-    atomicAdd(&g[c * plane + (size_t)(j + 1) * pitch + (i + 1)], (unsigned long long)to_fixed(v));
+    atomicAdd(&g[c * plane + (size_t)(j + 1) * pitch + (i + 1)], (unsigned long long)to_fixed(v, *C));
   }
 };
-
-// the J tile of a deterministic push (3 planes of 64-bit fixed point) lives
-// in dynamic shared memory
-extern __shared__ __align__(128) unsigned long long zc_push_dyn_smem[];
 
 // ---------------------------------------------------------------------------
 // per-particle physics (restates em2d/particles.c:773-924, 1029-1226)
@@ -349,23 +402,29 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   constexpr int BH = TY + 3;
   constexpr int PL = BW * BH;
   constexpr int NW = NT / 32;
+  using LAY = JTileLayout<TX, TY>;
+  // E/B tile; once every particle is pushed it stages the float J tile for
+  // the TMA reduce-add
   __shared__ __align__(128) float sEB[6 * PL];
-  __shared__ __align__(128) float sJ[DET ? 4 : 3 * PL];  // float J tile (the fixed one is dynamic)
-  unsigned long long *const sJd = zc_push_dyn_smem;
+  __shared__ __align__(16) int sJi[3 * LAY::N];  // J tile, integer parts h, m, l (jsplit)
   __shared__ unsigned long long s_ekin[2];                // fixed-point kinetic energy (DET)
   __shared__ __align__(8) uint64_t bar;
   __shared__ double sred[NW];
   // per-warp queue of cell-crossing motions, deposited 32 at a time so that
-  // the split code runs with full warps (QCAP = 2 x 32)
-  constexpr int QCAP = 64;
+  // the split code runs with (nearly) full warps: flushed from QFLUSH
+  // waiting motions on, so at most QFLUSH - 1 + 32 are held
+  constexpr int QFLUSH = 24;
+  constexpr int QCAP = QFLUSH - 1 + 32;
   __shared__ float qf[NW][5][QCAP];  // x0, y0, dx, dy, qvz
   __shared__ int qi[NW][QCAP];       // local cell and shifts, packed
-  __shared__ __align__(16) float4 pf_u[NW][2][32];   // prefetched particles, per warp, double buffered
-  __shared__ __align__(16) float2 pf_xy[NW][2][32];
+  // prefetched particles, one chunk per warp: each lane reads its slot into
+  // registers before it copies the next chunk's particle into the slot
+  __shared__ __align__(16) float4 pf_u[NW][32];
+  __shared__ __align__(16) float2 pf_xy[NW][32];
   __shared__ int nb[8], s_nnb;        // distinct neighbour tiles
   // incoming particles bound for this tile, listed as (outbox slot << 4 |
   // neighbour) so that they are pushed in full warps
-  constexpr int INCAP = 512;
+  constexpr int INCAP = 64;
   __shared__ int s_in[INCAP];
   __shared__ int s_nin;
   __shared__ int s_stay, s_leave;     // output counters (warp-aggregated atomics)
@@ -408,23 +467,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     mbar_expect_tx(&bar, 6 * PL * 4);
     tma_load_3d(sEB, &tm_eb, cx0, cy0, 0, &bar);
   }
-  if constexpr (DET) {
-    for (int k = threadIdx.x; k < 3 * PL; k += NT) sJd[k] = 0ull;
-  } else {
-    for (int k = threadIdx.x; k < 3 * PL; k += NT) sJ[k] = 0.f;
-  }
+  for (int k = threadIdx.x; k < 3 * LAY::N; k += NT) sJi[k] = 0;
   const bool loaded = mbar_wait_bounded(&bar, 0);
   if (!loaded) errbits |= ERR_TIMEOUT;
   __syncthreads();
 
   const TileFields<BW, PL> fld{sEB};
-  const auto dep = [&] {
-    if constexpr (DET)
-      return TileCurrentFixed<BW, PL>{sJd};
-    else
-      return TileCurrent<BW, PL>{sJ};
-  }();
   const PushConst Cl = C;
+  const TileCurrentSplit<LAY> dep{sJi, &Cl};
   const long long base = T.off[t];
   const int cap = T.cap[t];
   const int n_own = T.np[t];
@@ -506,28 +556,34 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       if constexpr (DET) {
         // each lane's contributions rounded to fixed point, then summed as
         // integers: the same total whatever lanes hold which particles
-        long long iv[8];
+        int ih[8], im[8], il[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) iv[q] = to_fixed(cur.v[q]);
+        for (int q = 0; q < 8; ++q) jsplit(cur.v[q], Cl, ih[q], im[q], il[q]);
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
           if ((unsigned)off >= maxlen) break;
           const bool take = lane + off <= run_last;
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
-            const long long o = __shfl_down_sync(0xffffffffu, iv[q], off);
-            if (take) iv[q] += o;
+            const int oh = __shfl_down_sync(0xffffffffu, ih[q], off);
+            const int om = __shfl_down_sync(0xffffffffu, im[q], off);
+            const int ol = __shfl_down_sync(0xffffffffu, il[q], off);
+            if (take) {
+              ih[q] += oh;
+              im[q] += om;
+              il[q] += ol;
+            }
           }
         }
         if (head) {
-          dep.addi(0, li, lj, iv[0]);
-          dep.addi(0, li, lj + 1, iv[1]);
-          dep.addi(1, li, lj, iv[2]);
-          dep.addi(1, li + 1, lj, iv[3]);
-          dep.addi(2, li, lj, iv[4]);
-          dep.addi(2, li + 1, lj, iv[5]);
-          dep.addi(2, li, lj + 1, iv[6]);
-          dep.addi(2, li + 1, lj + 1, iv[7]);
+          dep.addi(0, li, lj, ih[0], im[0], il[0]);
+          dep.addi(0, li, lj + 1, ih[1], im[1], il[1]);
+          dep.addi(1, li, lj, ih[2], im[2], il[2]);
+          dep.addi(1, li + 1, lj, ih[3], im[3], il[3]);
+          dep.addi(2, li, lj, ih[4], im[4], il[4]);
+          dep.addi(2, li + 1, lj, ih[5], im[5], il[5]);
+          dep.addi(2, li, lj + 1, ih[6], im[6], il[6]);
+          dep.addi(2, li + 1, lj + 1, ih[7], im[7], il[7]);
         }
       } else {
 #pragma unroll
@@ -544,8 +600,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       }
     }
 
-    // queue the cell-crossing motions; deposit them once a full warp's worth
-    // is waiting
+    // queue the cell-crossing motions; deposit them once QFLUSH are waiting
     {
       const unsigned sm = __ballot_sync(0xffffffffu, split);
       if (sm) {
@@ -560,9 +615,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
         }
         qcount += __popc(sm);
         __syncwarp();
-        if (qcount >= 32) {
-          qcount -= 32;
-          deposit_queued(qcount + lane);
+        if (qcount >= QFLUSH) {
+          const int nq = min(qcount, 32);
+          qcount -= nq;
+          if (lane < nq) deposit_queued(qcount + lane);
           __syncwarp();
         }
       }
@@ -624,26 +680,19 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   // own particles: warp w takes chunks w, w + NW, ... of 32; the next
   // chunk is copied into shared memory while this one is pushed
   {
-    int b = 0;
     if (warp * 32 + lane < n_own) {
-      cp_async16(&pf_u[warp][0][lane], &pin.u[base + warp * 32 + lane]);
-      cp_async8(&pf_xy[warp][0][lane], &pin.xy[base + warp * 32 + lane]);
+      cp_async16(&pf_u[warp][lane], &pin.u[base + warp * 32 + lane]);
+      cp_async8(&pf_xy[warp][lane], &pin.xy[base + warp * 32 + lane]);
     }
     cp_async_commit();
     for (int k0 = warp * 32; k0 < n_own; k0 += NT) {
-      const int kn = k0 + NT + lane;
-      if (kn < n_own) {
-        cp_async16(&pf_u[warp][b ^ 1][lane], &pin.u[base + kn]);
-        cp_async8(&pf_xy[warp][b ^ 1][lane], &pin.xy[base + kn]);
-      }
-      cp_async_commit();
-      cp_async_wait<1>();  // this chunk's copies are in
+      cp_async_wait<0>();  // this chunk's copies (each lane its own slot) are in
       const int k = k0 + lane;
       const bool valid = k < n_own;
       PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (valid) {
-        const float4 u = pf_u[warp][b][lane];
-        const float2 xy = pf_xy[warp][b][lane];
+        const float4 u = pf_u[warp][lane];
+        const float2 xy = pf_xy[warp][lane];
         const unsigned c = (unsigned)__float_as_int(u.w);
         r.ix = (int)(c & 0xffffu);
         r.iy = (int)(c >> 16);
@@ -653,9 +702,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
         r.uy = u.y;
         r.uz = u.z;
       }
-      __syncwarp();
+      const int kn = k0 + NT + lane;
+      if (kn < n_own) {
+        cp_async16(&pf_u[warp][lane], &pin.u[base + kn]);
+        cp_async8(&pf_xy[warp][lane], &pin.xy[base + kn]);
+      }
+      cp_async_commit();
       process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
-      b ^= 1;
     }
     cp_async_wait<0>();
   }
@@ -697,15 +750,17 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     }
     __syncthreads();
     if (threadIdx.x == 0) ekin_tile[t] = efix_join((long long)s_ekin[0], (long long)s_ekin[1]);
-    // the fixed-point J tile goes to the global fixed-point planes with
-    // integer atomics (cells outside the buffer hold no deposits)
-    for (int k = threadIdx.x; k < 3 * PL; k += NT) {
-      const unsigned long long v = sJd[k];
+    // the integer J tile goes to the global fixed-point planes (units of
+    // 2^-40) with 64-bit integer atomics (cells outside the buffer hold no
+    // deposits)
+    for (int k = threadIdx.x; k < LAY::N; k += NT) {
+      const long long v = tile_node_sum(sJi, LAY::N, k, Cl.js_l);
       if (!v) continue;
-      const int c = k / PL, r = (k % PL) / BW, col = k % BW;
+      int c, r, col;
+      LAY::where(k, c, r, col);
       const int gy = cy0 + r, gx = cx0 + col;
       if (gx < fj.pitch && (size_t)gy * fj.pitch < fj.plane)
-        atomicAdd(&fj.p[c * fj.plane + (size_t)gy * fj.pitch + gx], v);
+        atomicAdd(&fj.p[c * fj.plane + (size_t)gy * fj.pitch + gx], (unsigned long long)(v * Cl.js_det));
     }
     if (threadIdx.x == 0 && !loaded && !mbar_wait_bounded(&bar, 0))
       errbits |= ERR_TIMEOUT;  // second bounded wait for the load still in flight
@@ -713,12 +768,22 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
     if (threadIdx.x == 0) ekin_tile[t] = e;
 
-    // all shared-memory atomics done: hand the J tile to the TMA unit
+    // every particle is pushed (the barrier in block_sum_double): the E/B
+    // tile becomes the float J tile, in the layout of the TMA box
+    float *sJf = sEB;
+    for (int k = threadIdx.x; k < 3 * PL; k += NT) sJf[k] = 0.f;
+    __syncthreads();
+    for (int k = threadIdx.x; k < LAY::N; k += NT) {
+      int c, r, col;
+      LAY::where(k, c, r, col);
+      // one rounding: the exact integer sum, then the power-of-two scale
+      sJf[c * PL + r * BW + col] = __ll2float_rn(tile_node_sum(sJi, LAY::N, k, Cl.js_l)) * Cl.js_lo;
+    }
     fence_proxy_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
       if (loaded) {
-        tma_reduce_add_3d(&tm_j, sJ, cx0, cy0, 0);
+        tma_reduce_add_3d(&tm_j, sJf, cx0, cy0, 0);
         bulk_commit();
         bulk_wait_read0();
       } else if (!mbar_wait_bounded(&bar, 0)) {
@@ -741,7 +806,7 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Fi
   const GlobalFields fld{EB, G.pitch, G.plane};
   const auto dep = [&] {
     if constexpr (DET)
-      return GlobalCurrentFixed{fj.p, fj.pitch, fj.plane};
+      return GlobalCurrentFixed{fj.p, fj.pitch, fj.plane, &C};
     else
       return GlobalCurrent{J, G.pitch, G.plane};
   }();
@@ -792,22 +857,15 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Fi
 template <int TX, int TY, bool DET>
 static cudaError_t launch_push_t(const PushLaunch &a, cudaStream_t st) {
   constexpr int NT = (TX * TY >= 256) ? 256 : 128;
-  constexpr int PL = ((TX + 3 + 3) & ~3) * (TY + 3);
-  const int dyn = DET ? 3 * PL * (int)sizeof(unsigned long long) : 0;
-  k_push_tiles<TX, TY, NT, DET><<<a.ntiles, NT, dyn, st>>>(*a.tm_eb, *a.tm_j, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
+  k_push_tiles<TX, TY, NT, DET><<<a.ntiles, NT, 0, st>>>(*a.tm_eb, *a.tm_j, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
                                                            a.ekin_tile, a.err, a.C, a.fj);
   return cudaGetLastError();
 }
 
-// raises the dynamic shared-memory limit of the deterministic kernels (once
-// per device, outside any stream capture)
+// nothing to prepare: every variant runs with static shared memory only
 template <int TX, int TY, bool DET>
 static cudaError_t prepare_push_t() {
-  constexpr int NT = (TX * TY >= 256) ? 256 : 128;
-  constexpr int PL = ((TX + 3 + 3) & ~3) * (TY + 3);
-  if (!DET) return cudaSuccess;
-  return cudaFuncSetAttribute(k_push_tiles<TX, TY, NT, DET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              3 * PL * (int)sizeof(unsigned long long));
+  return cudaSuccess;
 }
 
 template <bool DET>
