@@ -268,7 +268,7 @@ TileSet tiles(SpeciesState &p, int ntiles) { return TileSet{p.d_off, p.d_cap, p.
 
 Spill spill_of(SpeciesState &p, int k) { return Spill{p.spill[k], p.d_spill_cnt + k, p.spill_cap}; }
 
-FixedJ fixed_j(const zc_sim *s) { return FixedJ{s->Jfix, s->G.pitch, s->G.plane}; }
+FixedJ fixed_j(const zc_sim *s) { return FixedJ{s->Jfix, s->G.pitch, s->G.plane, s->J[0]}; }
 
 // outbox slots per tile: room for a moving-window column plus crossers
 // (more leavers than slots go to the spill list)
@@ -518,7 +518,6 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   }
   PushLaunch a;
   a.tm_eb = s->EBp ? &s->tmK_EBp : &s->tmK_EB[s->eb_cur];
-  a.tm_j = &s->tmK_J;
   a.pin = p.buf[p.cur];
   a.pout = p.buf[1 - p.cur];
   a.T = tiles(p, s->ntiles);

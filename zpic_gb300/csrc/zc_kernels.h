@@ -55,6 +55,7 @@ struct FixedJ {
   unsigned long long *p;  // 3 planes laid out as the float J planes
   int pitch;
   size_t plane;
+  float *f;               // the float J planes (the push's direct deposits)
 };
 constexpr double kJFixScale = 1099511627776.0;         // 2^40
 constexpr double kEFixHi = 1073741824.0;                 // 2^30
@@ -70,7 +71,7 @@ __host__ __device__ __forceinline__ double efix_join(long long hi, long long lo)
 }
 
 struct PushLaunch {
-  const CUtensorMap *tm_eb, *tm_j;
+  const CUtensorMap *tm_eb;
   Particles pin, pout;
   TileSet T;
   Outbox Oin, O;                          // pending incoming (previous step), leavers (this step)

@@ -12,20 +12,23 @@
 //                 with a 1-lower / 2-upper cell halo arrive in shared memory
 //                 by one 3-D TMA box; every particle of the tile is pushed
 //                 (staggered bilinear gather, relativistic Boris, move) and
-//                 its current deposited with the zigzag scheme into a shared
-//                 J tile; the J tile is added to global J with one TMA
-//                 reduce-add.  Tiles are kept sorted by cell, so the lanes of
-//                 a warp mostly share a cell: their gathers are broadcasts,
-//                 and the current of the segment every particle starts with
-//                 (it lies in the particle's own cell) is summed across the
-//                 lanes of a cell with a segmented warp-shuffle reduction
-//                 before one lane per cell issues the shared-memory atomics.
-//                 Cell-crossing motions (a few per cent) wait in a per-warp
-//                 shared-memory queue and are split and deposited 32 at a
-//                 time, so the split code runs with full warps.  Particles
-//                 that stay are compacted in order; particles that leave go
-//                 to the tile's outbox, from which the destination tile pulls
-//                 them at the start of the next step's push.
+//                 its current deposited with the zigzag scheme.  Tiles are
+//                 kept sorted by cell, so the lanes of a warp mostly share a
+//                 cell: their gathers are broadcasts, and the current of the
+//                 segment every particle starts with (it lies in the
+//                 particle's own cell) is summed across the lanes of a cell
+//                 with a segmented warp-shuffle reduction before one lane per
+//                 cell deposits it.  The fast and exact builds deposit with
+//                 float reductions on the global J planes, which L2 performs
+//                 natively; the deterministic builds accumulate a shared
+//                 integer J tile (exact, order-independent sums) and add it
+//                 to the global fixed-point planes.  Cell-crossing motions (a
+//                 few per cent) wait in a per-warp shared-memory queue and are
+//                 split and deposited a warp's worth at a time, so the split
+//                 code runs with (nearly) full warps.  Particles that stay
+//                 are compacted in order; particles that leave go to the
+//                 tile's outbox, from which the destination tile pulls them
+//                 at the start of the next step's push.
 //   k_push_spill  the same physics for particles that did not fit a tile,
 //                 from global memory (normally empty).
 //
@@ -86,6 +89,18 @@ struct JTileLayout {
   }
   __device__ __forceinline__ static int node(int c, int i, int j) {
     return c == 0 ? OX + (j + 1) * WX + (i + 1) : (c == 1 ? OY + (j + 1) * WY + (i + 1) : OZ + (j + 1) * WZ + (i + 1));
+  }
+};
+
+// fast and exact builds: every deposit goes straight to the global J
+// planes as a float reduction, which L2 performs (no compare-and-swap loop);
+// g points at the tile's first cell, (i, j) run over -1 .. TX, -1 .. TY
+struct TileCurrentGlobal {
+  float *g;
+  int pitch;
+  size_t plane;
+  __device__ __forceinline__ void add(int c, int i, int j, float v) const {
+    atomicAdd(g + c * plane + (long long)j * pitch + i, v);
   }
 };
 
@@ -395,7 +410,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 // ---------------------------------------------------------------------------
 template <int TX, int TY, int NT, bool DET>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
-                                                   const __grid_constant__ CUtensorMap tm_j, Particles pin,
+                                                   Particles pin,
                                                    Particles pout, TileSet T, Outbox Oin, Outbox O, Spill S,
                                                    double *ekin_tile, int *err, PushConst C, FixedJ fj) {
   constexpr int BW = (TX + 3 + 3) & ~3;  // halo box width, multiple of 4 floats
@@ -403,17 +418,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   constexpr int PL = BW * BH;
   constexpr int NW = NT / 32;
   using LAY = JTileLayout<TX, TY>;
-  // E/B tile; once every particle is pushed it stages the float J tile for
-  // the TMA reduce-add
-  __shared__ __align__(128) float sEB[6 * PL];
-  __shared__ __align__(16) int sJi[3 * LAY::N];  // J tile, integer parts h, m, l (jsplit)
+  __shared__ __align__(128) float sEB[6 * PL];  // E/B tile with its halo
+  // deterministic builds: J tile, integer parts h, m, l (jsplit)
+  __shared__ __align__(16) int sJi[DET ? 3 * LAY::N : 1];
   __shared__ unsigned long long s_ekin[2];                // fixed-point kinetic energy (DET)
   __shared__ __align__(8) uint64_t bar;
   __shared__ double sred[NW];
   // per-warp queue of cell-crossing motions, deposited 32 at a time so that
   // the split code runs with (nearly) full warps: flushed from QFLUSH
   // waiting motions on, so at most QFLUSH - 1 + 32 are held
-  constexpr int QFLUSH = 24;
+  constexpr int QFLUSH = DET ? 24 : 32;
   constexpr int QCAP = QFLUSH - 1 + 32;
   __shared__ float qf[NW][5][QCAP];  // x0, y0, dx, dy, qvz
   __shared__ int qi[NW][QCAP];       // local cell and shifts, packed
@@ -467,14 +481,20 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     mbar_expect_tx(&bar, 6 * PL * 4);
     tma_load_3d(sEB, &tm_eb, cx0, cy0, 0, &bar);
   }
-  for (int k = threadIdx.x; k < 3 * LAY::N; k += NT) sJi[k] = 0;
+  if constexpr (DET)
+    for (int k = threadIdx.x; k < 3 * LAY::N; k += NT) sJi[k] = 0;
   const bool loaded = mbar_wait_bounded(&bar, 0);
   if (!loaded) errbits |= ERR_TIMEOUT;
   __syncthreads();
 
   const TileFields<BW, PL> fld{sEB};
   const PushConst Cl = C;
-  const TileCurrentSplit<LAY> dep{sJi, &Cl};
+  const auto dep = [&] {
+    if constexpr (DET)
+      return TileCurrentSplit<LAY>{sJi, &Cl};
+    else
+      return TileCurrentGlobal{fj.f + (size_t)(cy0 + 1) * fj.pitch + (cx0 + 1), fj.pitch, fj.plane};
+  }();
   const long long base = T.off[t];
   const int cap = T.cap[t];
   const int n_own = T.np[t];
@@ -768,28 +788,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     const double e = block_sum_double<NT>((double)ks - (double)kc, sred);
     if (threadIdx.x == 0) ekin_tile[t] = e;
 
-    // every particle is pushed (the barrier in block_sum_double): the E/B
-    // tile becomes the float J tile, in the layout of the TMA box
-    float *sJf = sEB;
-    for (int k = threadIdx.x; k < 3 * PL; k += NT) sJf[k] = 0.f;
-    __syncthreads();
-    for (int k = threadIdx.x; k < LAY::N; k += NT) {
-      int c, r, col;
-      LAY::where(k, c, r, col);
-      // one rounding: the exact integer sum, then the power-of-two scale
-      sJf[c * PL + r * BW + col] = __ll2float_rn(tile_node_sum(sJi, LAY::N, k, Cl.js_l)) * Cl.js_lo;
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      if (loaded) {
-        tma_reduce_add_3d(&tm_j, sJf, cx0, cy0, 0);
-        bulk_commit();
-        bulk_wait_read0();
-      } else if (!mbar_wait_bounded(&bar, 0)) {
-        errbits |= ERR_TIMEOUT;  // second bounded wait for the load still in flight
-      }
-    }
+    if (threadIdx.x == 0 && !loaded && !mbar_wait_bounded(&bar, 0))
+      errbits |= ERR_TIMEOUT;  // second bounded wait for the load still in flight
   }
   if (errbits) atomicOr(err, errbits);
 }
@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Fi
 template <int TX, int TY, bool DET>
 static cudaError_t launch_push_t(const PushLaunch &a, cudaStream_t st) {
   constexpr int NT = (TX * TY >= 256) ? 256 : 128;
-  k_push_tiles<TX, TY, NT, DET><<<a.ntiles, NT, 0, st>>>(*a.tm_eb, *a.tm_j, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
+  k_push_tiles<TX, TY, NT, DET><<<a.ntiles, NT, 0, st>>>(*a.tm_eb, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
                                                            a.ekin_tile, a.err, a.C, a.fj);
   return cudaGetLastError();
 }
