@@ -856,7 +856,9 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Fi
 // ---------------------------------------------------------------------------
 template <int TX, int TY, bool DET>
 static cudaError_t launch_push_t(const PushLaunch &a, cudaStream_t st) {
-  constexpr int NT = (TX * TY >= 256) ? 256 : 128;
+  // 4 warps per CTA (8 CTAs per SM: shorter barriers, CTAs in more phases);
+  // the deterministic build's integer J tile keeps 8 warps per CTA
+  constexpr int NT = (DET && TX * TY >= 256) ? 256 : 128;
   k_push_tiles<TX, TY, NT, DET><<<a.ntiles, NT, 0, st>>>(*a.tm_eb, a.pin, a.pout, a.T, a.Oin, a.O, a.S,
                                                            a.ekin_tile, a.err, a.C, a.fj);
   return cudaGetLastError();
