@@ -639,21 +639,10 @@ zc_status current_update_impl(zc_sim *s) {
     }
   }
   int c = 0;
-  if (px.n > 0 && py.n > 0 && px.n <= 8 && py.n <= 8) {
-    // both axes in one pass over J
+  if (px.n > 0 || py.n > 0) {
     Phase ph(s, ZC_PHASE_SMOOTH, 1);
-    CK(launch_smooth_xy_all(s->J[0], s->J[1], s->G, px, py, s->mw, st));
+    CK(launch_smooth(s->J[0], s->J[1], s->G, px, py, s->mw, st));
     c = 1;
-  } else {
-    if (px.n > 0) {
-      Phase ph(s, ZC_PHASE_SMOOTH, 1);
-      CK(launch_smooth_x_all(s->J[0], s->G, px, s->mw, st));
-    }
-    if (py.n > 0) {
-      Phase ph(s, ZC_PHASE_SMOOTH, 1);
-      CK(launch_smooth_y_all(s->J[0], s->J[1], s->G, py, st));
-      c = 1;
-    }
   }
   s->j_cur = c;
   return ZC_OK;
@@ -1302,10 +1291,10 @@ zc_status zc_set_smooth(zc_sim *s, int xtype, int xlevel, int ytype, int ylevel)
   // em2d/simulation.c:136-144
   if (xtype != 0 && xlevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along x direction");
   if (ytype != 0 && ylevel <= 0) return fail(ZC_EINVAL, "Invalid smooth level along y direction");
-  if ((xtype != 0 && xlevel >= kMaxSmoothPasses) || (ytype != 0 && xlevel >= kMaxSmoothPasses))
-    return fail(ZC_EINVAL, "smoothing level above %d is not supported", kMaxSmoothPasses - 1);
-  if (xtype != 0 && smooth_x_smem(s->G) > 200 * 1024)
-    return fail(ZC_EINVAL, "smoothing along x supports grids of up to 25600 cells along x");
+  // at most 15 passes along x (a warp of the filter keeps a halo column per
+  // pass on each side) and kMaxSmoothPasses along y
+  if ((xtype != 0 && xlevel > 14) || (ytype != 0 && xlevel > 14))
+    return fail(ZC_EINVAL, "smoothing level above 14 is not supported");
   invalidate_graph(s);
   s->xtype = xtype;
   s->xlevel = xlevel;

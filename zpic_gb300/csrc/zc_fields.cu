@@ -8,6 +8,8 @@
 // All of them are HBM-bound stencils; none is a contraction.
 #include <math.h>
 
+#include <type_traits>
+
 #include "zc_internal.cuh"
 #include "zc_kernels.h"
 
@@ -73,225 +75,143 @@ __device__ __forceinline__ float f3pt(float sa, float sb, float l, float m, floa
 }
 
 // ---------------------------------------------------------------------------
-// all filter passes along one axis in one kernel.  Passes along x act on
-// every interior row independently: a CTA loads its row (guards included)
-// into shared memory, runs the passes there -- refreshing the periodic x
-// guards after each pass unless the window moves, as kernel_x does -- and
-// writes the row back in place.  Passes along y are periodic convolutions
-// over the interior rows (kernel_y refreshes the y guards after each pass),
-// except that the first pass reads the y guard rows as they are (the x
-// passes leave them at their pre-filter values): a CTA takes a strip of 32
-// columns and ROWS rows plus one halo row per pass on each side, runs the
-// passes in shared memory and writes its rows (and the y guard rows they
-// feed) out of place.  Every cell sees the same float
-// operations in the same order as with one kernel per pass.
+// All filter passes, along x and then along y, in one sweep over J and
+// without shared memory.  A warp owns 32 consecutive buffer columns -- HX
+// halo columns on each side (periodic images of interior columns, or with a
+// moving window the columns themselves, zero outside the buffer), so that it
+// writes W = 32 - 2 HX of them -- and walks down a block of rows plus H halo
+// rows above and below (periodic over the interior rows).  Each row is read
+// once and filtered along x by HX passes across the lanes (kernel_x; after
+// p passes lanes p .. 31-p hold filtered values; a moving window's guard
+// columns stay as they are).  The rows then go through H y-pass stages held
+// in registers (kernel_y): stage p keeps the last two rows it received and,
+// given the next one, emits the filtered middle row to stage p + 1, so the
+// last stage emits rows H behind the walk.  Only interior columns are
+// filtered along y, and the first y pass reads the y guard rows as stored
+// (the x passes leave them untouched).  The y guard rows of the result are
+// periodic copies of the filtered rows, or, without y passes, the rows as
+// stored.  Every cell sees the same float operations in the same order as
+// with one kernel per pass (em2d/current.c:316-413).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_smooth_x_all(float *J, Grid G, SmoothPasses P, int mw) {
-  extern __shared__ float srow[];  // [2][gx]: one component of one row
-  const int gx = G.nx + 3;
-  const int by = blockIdx.x + 1;   // interior row
-  const int c = blockIdx.y;        // component
-  // asynchronous copies: every load of the row in flight at once
-  for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) cp_async4_zfill(srow + bx, J + gidx(G, c, bx, by), true);
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  int cur = 0;
-  for (int p = 0; p < P.n; ++p) {
-    const float sa = P.sa[p], sb = P.sb[p];
-    const float *r = srow + cur * gx;
-    float *o = srow + (1 - cur) * gx;
-    for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) {
-      float v;
-      if (bx >= 1 && bx <= G.nx) v = f3pt(sa, sb, r[bx - 1], r[bx], r[bx + 1]);
-      else if (mw) v = r[bx];
-      else {
-        const int s = (bx == 0) ? G.nx : bx - G.nx;  // guard <- filtered interior value
-        v = f3pt(sa, sb, r[s - 1], r[s], r[s + 1]);
-      }
-      o[bx] = v;
-    }
-    __syncthreads();
-    cur = 1 - cur;
-  }
-  for (int bx = threadIdx.x; bx < gx; bx += blockDim.x) J[gidx(G, c, bx, by)] = srow[cur * gx + bx];
-}
+constexpr int kSmoothRows = 32;  // interior rows per warp
+constexpr int kSmoothRing = 16;  // rows in flight per warp (asynchronous copies)
+constexpr int kSmoothWarps = 8;  // warps per CTA
 
-constexpr int kSmoothYRows = 64;   // interior rows per CTA
-constexpr int kSmoothYCols = 32;   // columns per CTA (one warp across)
-
-__global__ void __launch_bounds__(256) k_smooth_y_all(const float *Jin, float *Jout, Grid G, SmoothPasses P) {
-  extern __shared__ float sbuf[];  // [2][ROWS + 2H][COLS], then guard rows [2][COLS]; one component
-  const int H = P.n;
-  const int R = kSmoothYRows + 2 * H;
-  constexpr int W = kSmoothYCols;
+// NX, NY: the pass counts when known at compile time (exact loops, no
+// branches per row), or -1 to read them from PX, PY (up to kMaxSmoothPasses)
+template <int NX, int NY>
+__global__ void __launch_bounds__(32 * kSmoothWarps) k_smooth(const float *Jin, float *Jout, Grid G, SmoothPasses PX,
+                                                              SmoothPasses PY, int mw) {
+  constexpr int MX = NX >= 0 ? NX : kMaxSmoothPasses;  // loop bounds
+  constexpr int MY = NY >= 0 ? NY : kMaxSmoothPasses;
+  // each warp streams its rows through a private ring of row slots: a lane
+  // copies and later reads only its own column, so no synchronisation is
+  // needed beyond the copies' own completion
+  __shared__ float ring[kSmoothWarps][kSmoothRing][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int HX = NX >= 0 ? NX : PX.n, H = NY >= 0 ? NY : PY.n;
+  const int W = 32 - 2 * HX;
   const int gx = G.nx + 3;
-  const int c = blockIdx.z;                                  // component
-  const int cc = threadIdx.x & 31, r0 = threadIdx.x >> 5;   // column, first row of this thread
-  const int bx = blockIdx.x * W + cc;
-  const bool col_ok = bx < gx;
-  const bool filt = bx >= 1 && bx <= G.nx;                   // only interior columns are filtered
-  const int j0 = blockIdx.y * kSmoothYRows;                  // first interior row of the strip
-  float *glo = sbuf + 2 * R * W, *ghi = glo + W;             // y guard rows -1 and ny as stored
-  if (r0 == 0) {
-    cp_async4_zfill(glo + cc, col_ok ? Jin + gidx(G, c, bx, 0) : Jin, col_ok);
-    cp_async4_zfill(ghi + cc, col_ok ? Jin + gidx(G, c, bx, G.ny + 1) : Jin, col_ok);
+  const int nstrip = (gx + W - 1) / W;
+  const int nblk = (G.ny + kSmoothRows - 1) / kSmoothRows;
+  const int wid = blockIdx.x * kSmoothWarps + w;
+  if (wid >= nstrip * nblk) return;  // whole warps leave together
+  const int c = blockIdx.y;
+  const int strip = wid % nstrip, blk = wid / nstrip;
+  const int b = strip * W - HX + lane;  // this lane's buffer column
+  int src = b;
+  bool have = true;
+  if (mw) have = b >= 0 && b < gx;
+  else if (b < 1 || b > G.nx) src = ((b - 1) % G.nx + G.nx) % G.nx + 1;
+  const bool xfilt = (lane > 0 && lane < 31) && (!mw || (b >= 1 && b <= G.nx));
+  const bool yfilt = b >= 1 && b <= G.nx;
+  const bool writer = lane >= HX && lane < 32 - HX && b < gx;
+  const float *col = Jin + c * G.plane + (have ? src : 0);
+  float *out = Jout + c * G.plane + b;
+  const int j0 = blk * kSmoothRows;
+  const int nrows = min(kSmoothRows, G.ny - j0);
+  const int R = nrows + 2 * H;  // rows walked
+  float *slot = &ring[w][0][lane];
+  int jw = (j0 - H) % G.ny;  // interior row of walk row 0
+  if (jw < 0) jw += G.ny;
+  // the first kSmoothRing rows in flight, one copy group per row
+  int jl = jw;  // interior row of the next row to copy
+#pragma unroll 1
+  for (int d = 0; d < kSmoothRing; ++d) {
+    if (d < R) cp_async4_zfill(slot + d * 32, have ? col + (size_t)(jl + 1) * G.pitch : Jin, have);
+    cp_async_commit();
+    jl = (jl + 1 == G.ny) ? 0 : jl + 1;
   }
-  // rows j0-H .. j0+ROWS+H-1, wrapped periodically over the interior rows
-  for (int rr = r0; rr < R; rr += 8) {
-    int j = (j0 - H + rr) % G.ny;
-    if (j < 0) j += G.ny;
-    cp_async4_zfill(sbuf + rr * W + cc, col_ok ? Jin + gidx(G, c, bx, j + 1) : Jin, col_ok);
+  const float glo = have ? col[0] : 0.f;                             // guard row -1 as stored
+  const float ghi = have ? col[(size_t)(G.ny + 1) * G.pitch] : 0.f;  // guard row ny as stored
+  if (H == 0 && blk == 0 && writer) {
+    // without y passes the y guard rows keep their values
+    out[0] = glo;
+    out[(size_t)(G.ny + 1) * G.pitch] = ghi;
+    out[(size_t)(G.ny + 2) * G.pitch] = have ? col[(size_t)(G.ny + 2) * G.pitch] : 0.f;
   }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  int cur = 0;
-  for (int p = 0; p < P.n; ++p) {
-    const float sa = P.sa[p], sb = P.sb[p];
-    const float *in = sbuf + cur * R * W;
-    float *out = sbuf + (1 - cur) * R * W;
-    for (int rr = r0; rr < R; rr += 8) {
-      bool lo_guard = false, hi_guard = false;
-      if (p == 0) {
-        int jm = (j0 - H + rr) % G.ny;
-        if (jm < 0) jm += G.ny;
-        lo_guard = (jm == 0);
-        hi_guard = (jm == G.ny - 1);
-      }
-      const bool inside = rr > p && rr < R - 1 - p;
-      const int k = rr * W + cc;
-      float v = in[k];
-      if (inside && filt) {
-        const float lo = lo_guard ? glo[cc] : in[k - W];
-        const float hi = hi_guard ? ghi[cc] : in[k + W];
-        v = f3pt(sa, sb, lo, in[k], hi);
-      }
-      out[k] = v;
-    }
-    __syncthreads();
-    cur = 1 - cur;
-  }
-  if (!col_ok) return;
-  const float *res = sbuf + cur * R * W;
-  for (int rr = r0; rr < kSmoothYRows; rr += 8) {
-    const int j = j0 + rr;
-    if (j >= G.ny) break;
-    const float v = res[(rr + H) * W + cc];
-    Jout[gidx(G, c, bx, j + 1)] = v;
-    // y guard rows are periodic copies of the filtered interior rows
-    if (j == G.ny - 1) Jout[gidx(G, c, bx, 0)] = v;
-    if (j < 2) Jout[gidx(G, c, bx, G.ny + 1 + j)] = v;
-  }
-}
+  float s0[MY > 0 ? MY : 1], s1[MY > 0 ? MY : 1];  // each stage's last two rows
+  int jprev = (jw == 0) ? G.ny - 1 : jw - 1;      // interior row of walk row rr - 1
 
-// Both axes in one pass over J (the x passes of every row of the strip, its
-// halo rows included, then the y passes), for the common case of filtering
-// along both: the rows are filtered along x in shared memory with a halo of
-// one column per x pass -- periodic images of the interior columns, or with a
-// moving window the fixed guard columns -- so that each cell sees exactly the
-// float operations of k_smooth_x_all followed by k_smooth_y_all.
-__global__ void __launch_bounds__(256, 6) k_smooth_xy_all(const float *Jin, float *Jout, Grid G, SmoothPasses PX,
-                                                       SmoothPasses P, int mw) {
-  // rows [2][R][XW] (x halo of HX columns each side), guard rows [2][W],
-  // interior row index of each tile row (periodic)
-  extern __shared__ float sbuf[];
-  const int H = P.n, HX = PX.n;
-  const int R = kSmoothYRows + 2 * H;
-  constexpr int W = kSmoothYCols;
-  const int XW = W + 2 * HX;
-  const int gx = G.nx + 3;
-  const int c = blockIdx.z;
-  const int bx0 = blockIdx.x * W;
-  const int j0 = blockIdx.y * kSmoothYRows;
-  float *glo = sbuf + 2 * R * XW, *ghi = glo + W;
-  int *rowj = reinterpret_cast<int *>(ghi + W);
-  const int tid = threadIdx.x;
-  if (tid < W) {
-    const int b = bx0 + tid;
-    cp_async4_zfill(glo + tid, b < gx ? Jin + gidx(G, c, b, 0) : Jin, b < gx);
-    cp_async4_zfill(ghi + tid, b < gx ? Jin + gidx(G, c, b, G.ny + 1) : Jin, b < gx);
-  }
-  for (int rr = tid; rr < R; rr += blockDim.x) {
-    int jm = (j0 - H + rr) % G.ny;
-    rowj[rr] = jm < 0 ? jm + G.ny : jm;
-  }
-  __syncthreads();
-  // k = rr * XW + q walks the tile in steps of the block size
-  const int step_r = blockDim.x / XW, step_q = blockDim.x % XW;
-  const int n = R * XW;
-  {
-    int rr = tid / XW, q = tid % XW;
-    for (int k = tid; k < n; k += blockDim.x) {
-      // buffer column of strip column q: with a moving window the column
-      // itself (zero outside the buffer), else its periodic image over the
-      // interior columns
-      int b = bx0 - HX + q;
-      if (!mw && (b < 1 || b > G.nx)) b = ((b - 1) % G.nx + G.nx) % G.nx + 1;
-      const bool ok = b >= 0 && b < gx;
-      cp_async4_zfill(sbuf + k, ok ? Jin + gidx(G, c, b, rowj[rr] + 1) : Jin, ok);
-      q += step_q;
-      rr += step_r;
-      if (q >= XW) { q -= XW; ++rr; }
+  // one walk row; FILL: the first 2H rows, while the stages fill up
+  auto step = [&](int rr, auto fill) {
+    constexpr bool FILL = decltype(fill)::value;
+    cp_async_wait<kSmoothRing - 1>();  // row rr has arrived
+    const int k = rr & (kSmoothRing - 1);
+    float v = slot[k * 32];
+    // the slot is free again: copy row rr + kSmoothRing into it
+    if (rr + kSmoothRing < R) cp_async4_zfill(slot + k * 32, have ? col + (size_t)(jl + 1) * G.pitch : Jin, have);
+    cp_async_commit();
+    jl = (jl + 1 == G.ny) ? 0 : jl + 1;
+#pragma unroll
+    for (int p = 0; p < MX; ++p) {
+      if (NX < 0 && p >= HX) break;
+      const float l = __shfl_up_sync(0xffffffffu, v, 1);
+      const float u = __shfl_down_sync(0xffffffffu, v, 1);
+      if (xfilt) v = f3pt(PX.sa[p], PX.sb[p], l, v, u);
     }
-  }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  // x passes (kernel_x): every strip column filtered from its neighbours,
-  // except the guard columns of a moving window, which stay as they are;
-  // after p passes the columns p .. XW-1-p hold the filtered values
-  int cur = 0;
-  for (int p = 0; p < HX; ++p) {
-    const float sa = PX.sa[p], sb = PX.sb[p];
-    const float *in = sbuf + cur * R * XW;
-    float *out = sbuf + (1 - cur) * R * XW;
-    int q = tid % XW;
-    for (int k = tid; k < n; k += blockDim.x) {
-      const int b = bx0 - HX + q;
-      float v = in[k];
-      if (q > 0 && q < XW - 1 && (!mw || (b >= 1 && b <= G.nx))) v = f3pt(sa, sb, in[k - 1], in[k], in[k + 1]);
-      out[k] = v;
-      q += step_q;
-      if (q >= XW) q -= XW;
-    }
-    __syncthreads();
-    cur = 1 - cur;
-  }
-  // y passes (kernel_y) on the strip's own columns, as k_smooth_y_all
-  const int cc = tid & 31, r0 = tid >> 5;
-  const int bx = bx0 + cc;
-  const bool filt = bx >= 1 && bx <= G.nx;
-  for (int p = 0; p < H; ++p) {
-    const float sa = P.sa[p], sb = P.sb[p];
-    const float *in = sbuf + cur * R * XW + HX;
-    float *out = sbuf + (1 - cur) * R * XW + HX;
-    for (int rr = r0; rr < R; rr += 8) {
-      // the first pass reads the y guard rows as stored
-      const int jm = p == 0 ? rowj[rr] : -1;
-      const bool inside = rr > p && rr < R - 1 - p;
-      const int k = rr * XW + cc;
-      float v = in[k];
-      if (inside && filt) {
-        const float lo = jm == 0 ? glo[cc] : in[k - XW];
-        const float hi = jm == G.ny - 1 ? ghi[cc] : in[k + XW];
-        v = f3pt(sa, sb, lo, in[k], hi);
+    // stage p receives walk row rr - p (stage p - 1 emits rows p .. on) and
+    // emits the middle row once it holds the two rows below
+    bool emit = true;
+#pragma unroll
+    for (int p = 0; p < MY; ++p) {
+      if (NY < 0 && p >= H) break;
+      const bool ready = !FILL || rr - p >= p + 2;
+      float e = 0.f;
+      if (ready) {
+        float lo = s0[p], hi = v;
+        if (p == 0) {
+          // the middle row next to a y guard row reads it as stored
+          lo = (jprev == 0) ? glo : lo;
+          hi = (jprev == G.ny - 1) ? ghi : hi;
+        }
+        e = yfilt ? f3pt(PY.sa[p], PY.sb[p], lo, s1[p], hi) : s1[p];
       }
-      out[k] = v;
+      s0[p] = s1[p];
+      s1[p] = v;
+      if (FILL && !ready) {
+        emit = false;
+        break;
+      }
+      v = e;
     }
-    __syncthreads();
-    cur = 1 - cur;
-  }
-  if (bx >= gx) return;
-  const float *res = sbuf + cur * R * XW + HX;
-  for (int rr = r0; rr < kSmoothYRows; rr += 8) {
-    const int j = j0 + rr;
-    if (j >= G.ny) break;
-    const float v = res[(rr + H) * XW + cc];
-    Jout[gidx(G, c, bx, j + 1)] = v;
-    if (j == G.ny - 1) Jout[gidx(G, c, bx, 0)] = v;
-    if (j < 2) Jout[gidx(G, c, bx, G.ny + 1 + j)] = v;
-  }
+    jprev = (jprev + 1 == G.ny) ? 0 : jprev + 1;
+    // the last stage emits walk row rr - H; rows H .. R-1-H are the output
+    if ((!FILL || (emit && rr >= 2 * H)) && writer) {
+      const int j = j0 + rr - 2 * H;
+      out[(size_t)(j + 1) * G.pitch] = v;
+      if (H > 0) {
+        if (j == G.ny - 1) out[0] = v;
+        if (j < 2) out[(size_t)(G.ny + 1 + j) * G.pitch] = v;
+      }
+    }
+  };
+  const int nfill = min(2 * H, R);
+#pragma unroll 1
+  for (int rr = 0; rr < nfill; ++rr) step(rr, std::true_type{});
+#pragma unroll 2
+  for (int rr = nfill; rr < R; ++rr) step(rr, std::false_type{});
+  cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------
@@ -559,34 +479,28 @@ cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// shared memory of one x-filter CTA (a component of a row, double buffered)
-size_t smooth_x_smem(const Grid &G) { return sizeof(float) * 2 * (size_t)(G.nx + 3); }
-
-cudaError_t launch_smooth_x_all(float *J, const Grid &G, const SmoothPasses &P, int mw, cudaStream_t st) {
-  const size_t sh = smooth_x_smem(G);
-  if (sh > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_smooth_x_all, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
-    if (e != cudaSuccess) return e;
+cudaError_t launch_smooth(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
+                          const SmoothPasses &PY, int mw, cudaStream_t st) {
+  if (PX.n > kMaxSmoothPasses || PY.n > kMaxSmoothPasses || PX.n > 15) return cudaErrorInvalidValue;
+  const int W = 32 - 2 * PX.n;
+  const long long warps = (long long)((G.nx + 3 + W - 1) / W) * ((G.ny + kSmoothRows - 1) / kSmoothRows);
+  const dim3 grid((unsigned)((warps + kSmoothWarps - 1) / kSmoothWarps), 3);
+  const int block = 32 * kSmoothWarps;
+  // exact pass counts for up to 4 passes per axis, else counts read at run time
+#define ZC_SMOOTH(A, B)                                                     \
+  if (PX.n == A && PY.n == B) {                                            \
+    k_smooth<A, B><<<grid, block, 0, st>>>(Jin, Jout, G, PX, PY, mw);      \
+    return cudaGetLastError();                                             \
   }
-  k_smooth_x_all<<<dim3(G.ny, 3), 256, sh, st>>>(J, G, P, mw);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_smooth_y_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &P,
-                                cudaStream_t st) {
-  const size_t sh = sizeof(float) * 2 * ((size_t)(kSmoothYRows + 2 * P.n) + 1) * kSmoothYCols;
-  dim3 grid((G.nx + 3 + kSmoothYCols - 1) / kSmoothYCols, (G.ny + kSmoothYRows - 1) / kSmoothYRows, 3);
-  k_smooth_y_all<<<grid, 256, sh, st>>>(Jin, Jout, G, P);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_smooth_xy_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
-                                 const SmoothPasses &P, int mw, cudaStream_t st) {
-  const size_t R = kSmoothYRows + 2 * P.n, XW = kSmoothYCols + 2 * PX.n;
-  const size_t sh = sizeof(float) * (2 * R * XW + 2 * kSmoothYCols) + sizeof(int) * R;
-  if (sh > 48 * 1024) return cudaErrorInvalidValue;  // more than 8 passes along an axis
-  dim3 grid((G.nx + 3 + kSmoothYCols - 1) / kSmoothYCols, (G.ny + kSmoothYRows - 1) / kSmoothYRows, 3);
-  k_smooth_xy_all<<<grid, 256, sh, st>>>(Jin, Jout, G, PX, P, mw);
+#define ZC_SMOOTH_ROW(A) ZC_SMOOTH(A, 0) ZC_SMOOTH(A, 1) ZC_SMOOTH(A, 2) ZC_SMOOTH(A, 3) ZC_SMOOTH(A, 4)
+  ZC_SMOOTH_ROW(0)
+  ZC_SMOOTH_ROW(1)
+  ZC_SMOOTH_ROW(2)
+  ZC_SMOOTH_ROW(3)
+  ZC_SMOOTH_ROW(4)
+#undef ZC_SMOOTH_ROW
+#undef ZC_SMOOTH
+  k_smooth<-1, -1><<<grid, block, 0, st>>>(Jin, Jout, G, PX, PY, mw);
   return cudaGetLastError();
 }
 

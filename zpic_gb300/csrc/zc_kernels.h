@@ -61,10 +61,15 @@ constexpr double kJFixScale = 1099511627776.0;         // 2^40
 constexpr double kEFixHi = 1073741824.0;                 // 2^30
 constexpr double kEFixLo = 4611686018427387904.0;        // 2^62
 
-// a kinetic-energy term as two integers (hi in units of 2^-30, lo of 2^-62)
-__device__ __forceinline__ void efix_split(double v, long long &hi, long long &lo) {
-  hi = __double2ll_rn(v * kEFixHi);
-  lo = __double2ll_rn((v - (double)hi / kEFixHi) * kEFixLo);
+// a float kinetic-energy term as two integers: hi = rint(v 2^30) and lo =
+// rint((v - hi 2^-30) 2^62), without double arithmetic: t = v 2^30 is exact,
+// so are its nearest integer hf and the remainder t - hf (|.| <= 1/2), and
+// the remainder times 2^32 is lo (exact for v >= 2^-39, rounded below)
+__device__ __forceinline__ void efix_split(float v, long long &hi, long long &lo) {
+  const float t = __fmul_rn(v, 1073741824.0f);  // 2^30
+  const float hf = rintf(t);
+  hi = __float2ll_rn(hf);
+  lo = __float2ll_rn(__fmul_rn(__fsub_rn(t, hf), 4294967296.0f));  // 2^32
 }
 __host__ __device__ __forceinline__ double efix_join(long long hi, long long lo) {
   return (double)hi / kEFixHi + (double)lo / kEFixLo;
@@ -193,14 +198,9 @@ struct SmoothPasses {
   int n;
   float sa[kMaxSmoothPasses], sb[kMaxSmoothPasses];
 };
-cudaError_t launch_smooth_x_all(float *J, const Grid &G, const SmoothPasses &P, int mw, cudaStream_t st);
-// both axes in one pass (x passes PX, then y passes P), out of place
-cudaError_t launch_smooth_xy_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
-                                 const SmoothPasses &P, int mw, cudaStream_t st);
-// shared memory an x-filter CTA needs (one component of one row)
-size_t smooth_x_smem(const Grid &G);
-cudaError_t launch_smooth_y_all(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &P,
-                                cudaStream_t st);
+// every x filter pass, then every y pass, out of place (Jin -> Jout)
+cudaError_t launch_smooth(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
+                          const SmoothPasses &PY, int mw, cudaStream_t st);
 cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
                        const YeeConst &Y, int *err, cudaStream_t st);
 cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st);

@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     const float kin = push_particle(fld, li, lj, x, y, ux, uy, uz, mx, my, x1, y1, di, dj, qvz, bad, Cl);
     if constexpr (DET) {
       long long h, l;
-      efix_split(valid ? (double)kin : 0.0, h, l);
+      efix_split(valid ? kin : 0.0f, h, l);
       khi += h;
       klo += l;
     } else {
@@ -829,7 +829,7 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Fi
     if (bad) errbits |= ERR_ESCAPE;
     if constexpr (DET) {
       long long h, l;
-      efix_split((double)kin, h, l);
+      efix_split(kin, h, l);
       khi += h;
       klo += l;
     } else {
