@@ -181,6 +181,22 @@ ZC_API zc_status zc_get_fields(zc_sim *sim, float *E_buf, float *B_buf);
 /* fields seen by the particles (E_part / B_part, em2d/emf.h:96-97) */
 ZC_API zc_status zc_get_particle_fields(zc_sim *sim, float *E_buf, float *B_buf);
 ZC_API zc_status zc_get_current(zc_sim *sim, float *J_buf);
+
+/* Diagnostics without a stall: one component (0, 1, 2) of one grid's
+ * interior, nx * ny floats with x fastest (the layout of the reference's
+ * emf_report / current_report buffers, em2d/emf.c:368-482,
+ * em2d/current.c:194-281), copied into host memory after the work already
+ * on the handle's stream.  The call returns at once; `*fence` completes
+ * when `dst` holds the data (`dst` must stay valid until then, and pinned
+ * memory from zc_host_alloc keeps the copy asynchronous). */
+enum { ZC_GRID_E = 0, ZC_GRID_B = 1, ZC_GRID_EPART = 2, ZC_GRID_BPART = 3, ZC_GRID_J = 4 };
+typedef struct zc_fence zc_fence;
+ZC_API zc_status zc_copy_grid_async(zc_sim *sim, int grid, int comp, float *dst, zc_fence **fence);
+ZC_API zc_status zc_fence_wait(zc_fence *fence);  /* may be called from any thread */
+ZC_API void zc_fence_destroy(zc_fence *fence);
+/* page-locked host memory for asynchronous copies */
+ZC_API zc_status zc_host_alloc(size_t bytes, void **ptr);
+ZC_API void zc_host_free(void *ptr);
 ZC_API zc_status zc_set_current(zc_sim *sim, const float *J_buf);
 /* field energy per component (emf_get_energy, em2d/emf.c:729-750) and the
  * time-centred kinetic energy of each species after its last advance

@@ -143,7 +143,10 @@ def _load(backend: str, fast: bool):
         for name, res, args in [("sim_finalize", None, [P]),
                                 ("spec_set_n_sort", None, [P, C.c_int, C.c_int]),
                                 ("spec_time", C.c_double, []),
-                                ("spec_npush", C.c_double, [])]:
+                                ("spec_npush", C.c_double, []),
+                                ("report_emf", None, [P, C.c_int, C.c_int]),
+                                ("report_current", None, [P, C.c_int]),
+                                ("report_spec", None, [P, C.c_int, C.c_int, P, P])]:
             g = getattr(lib, "zr_" + name)
             g.restype = res
             g.argtypes = args
@@ -363,6 +366,26 @@ class CpuSim:
         out = np.zeros((int(n[1]), int(n[0])), dtype=np.float32)
         self.f["spec_pha"](self.h, k, self.PHA[quants[0]], self.PHA[quants[1]], _ptr(n), _ptr(r), _ptr(out))
         return out
+
+
+def _report_methods():
+    def report_emf(self, field, fc):
+        """The reference's emf_report (field 0..3: E, B, E_part, B_part),
+        written below the current directory (reference back end only)."""
+        self.f["report_emf"](self.h, int(field), int(fc))
+
+    def report_current(self, jc):
+        self.f["report_current"](self.h, int(jc))
+
+    def report_spec(self, k, rep_type, pha_nx=(0, 0), pha_range=((0, 0), (0, 0))):
+        n = np.ascontiguousarray(pha_nx, dtype=np.int32)
+        r = np.ascontiguousarray(np.asarray(pha_range, dtype=np.float32).reshape(4))
+        self.f["report_spec"](self.h, int(k), int(rep_type), _ptr(n), _ptr(r))
+
+    return report_emf, report_current, report_spec
+
+
+CpuSim.report_emf, CpuSim.report_current, CpuSim.report_spec = _report_methods()
 
 
 def set_rand_seed(w=12345, z=67890, backend="oracle", fast=False, fresh=False):

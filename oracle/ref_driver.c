@@ -218,6 +218,16 @@ void zr_spec_pha(const zr_sim *s, int k, int q1, int q2, const int pha_nx[2], co
     spec_deposit_pha(&s->spec[k], q1 + 16 * q2, pha_nx, r, buf);
 }
 
+/* the reference's own ZDF reports (em2d/emf.c:368, current.c:194,
+ * particles.c:1725), written below the current directory */
+void zr_report_emf(zr_sim *s, int field, int fc) { emf_report(&s->sim.emf, (char)field, fc); }
+void zr_report_current(zr_sim *s, int jc) { current_report(&s->sim.current, jc); }
+void zr_report_spec(zr_sim *s, int k, int rep_type, const int pha_nx[2], const float range[4])
+{
+    const float r[2][2] = {{range[0], range[1]}, {range[2], range[3]}};
+    spec_report(&s->spec[k], rep_type, pha_nx, r);
+}
+
 /* cumulative particle-advance time and pushes (em2d/particles.c:36-59) */
 double zr_spec_time(void) { return spec_time(); }
 double zr_spec_npush(void) { return (double)spec_npush(); }

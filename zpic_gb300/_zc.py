@@ -39,7 +39,8 @@ EXPORTS = [
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
     "zc_adj_create", "zc_adj_destroy", "zc_adj_set_state", "zc_adj_forward", "zc_adj_backward",
     "zc_adj_get_state", "zc_adj_times", "zc_species_phasespace", "zc_species_create_device",
-    "zc_adj_set_birth", "zc_adj_set_smooth",
+    "zc_adj_set_birth", "zc_adj_set_smooth", "zc_copy_grid_async", "zc_fence_wait", "zc_fence_destroy",
+    "zc_host_alloc", "zc_host_free",
 ]
 NPHASE = 13
 
@@ -161,11 +162,17 @@ def load(path: str = LIB_PATH):
         "zc_adj_times": [P, C.POINTER(C.c_float), C.POINTER(C.c_float)],
         "zc_species_phasespace": [P, I, I, I, P, P, P],
         "zc_species_create_device": [P, C.c_float, P, C.POINTER(Density), P, P, C.c_ulonglong, C.POINTER(I)],
+        "zc_copy_grid_async": [P, I, I, P, C.POINTER(P)],
+        "zc_fence_wait": [P],
+        "zc_host_alloc": [C.c_size_t, C.POINTER(P)],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
         f.argtypes = args
         f.restype = I
+    for name in ("zc_fence_destroy", "zc_host_free"):
+        getattr(lib, name).argtypes = [P]
+        getattr(lib, name).restype = None
     lib.zc_last_error.restype = C.c_char_p
     lib.zc_last_error.argtypes = []
     lib.zc_status_string.restype = C.c_char_p

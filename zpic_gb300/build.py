@@ -79,9 +79,9 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.replace(tmp, lib)
     # the em2d drop-in C API (plain C host code over the C-ABI)
     em2d = os.path.join(LIBDIR, "libzpic_em2d.so")
-    _run([os.environ.get("CC", "gcc"), "-O2", "-std=c99", "-D_DEFAULT_SOURCE", "-fPIC", "-shared",
-          "-fvisibility=hidden", os.path.join(CSRC, "em2d", "em2d_host.c"), "-o", em2d + ".tmp",
-          "-L", LIBDIR, "-lzpic_cuda", "-Wl,-rpath,$ORIGIN", "-lm"])
+    _run([os.environ.get("CC", "gcc"), "-O2", "-std=c99", "-D_DEFAULT_SOURCE", "-fPIC", "-shared", "-pthread",
+          "-fvisibility=hidden", os.path.join(CSRC, "em2d", "em2d_host.c"), os.path.join(CSRC, "em2d", "zdf_io.c"),
+          "-o", em2d + ".tmp", "-L", LIBDIR, "-lzpic_cuda", "-Wl,-rpath,$ORIGIN", "-lm"])
     os.replace(em2d + ".tmp", em2d)
     return lib
 

@@ -13,7 +13,10 @@
  *   - parameter checks with the reference's exit(-1) behaviour
  *     (em2d/simulation.c:106-110, 136-146; em2d/emf.c:246-270);
  *   - host mirrors of the device state (t_species.part, t_emf.E_buf/B_buf,
- *     t_current.J_buf), refreshed by the reporting calls and sim_sync_host.
+ *     t_current.J_buf), refreshed by sim_sync_host (and the particle mirror
+ *     by the particle report);
+ *   - the ZDF report files, gathered from the device and written on a
+ *     background thread (zdf_io.c).
  * Everything per time step (push, deposit, current update, field advance,
  * moving window) runs on the GPU via zc_step / the zc_* phase calls.
  */
@@ -25,7 +28,10 @@
 #include <sys/time.h>
 #include <time.h>
 
+#include <pthread.h>
+
 #include "../../../include/em2d/simulation.h"
+#include "../../../include/em2d/zdf.h"
 #include "../../../include/em2d/random.h"
 #include "../../../include/em2d/timer.h"
 #include "../../../include/zpic_cuda.h"
@@ -596,6 +602,7 @@ EXPORT void sim_new(t_simulation *sim, int nx[], float box[], float dt, float tm
 
 EXPORT void sim_delete(t_simulation *sim)
 {
+    zdf_flush();  /* report files still queued may wait on this simulation's copies */
     entry_t *e = reg_by_sim(sim);
     if (e) {
         zc_sim_destroy(e->gpu);
@@ -995,41 +1002,376 @@ EXPORT void spec_deposit_pha(const t_species *spec, const int rep_type, const in
     }
 }
 
-/* ZDF file output (the reference's *_report routines) is not part of this
- * library; the report calls refresh the host mirrors and say so once. */
-static void no_zdf(void)
+/* ------------------------------------------------------------------------- */
+/* ZDF reports (emf.c:368-482, current.c:194-281, particles.c:1342-1750)     */
+/* ------------------------------------------------------------------------- */
+/* A report gathers its data -- fields and current straight from the device
+ * buffers with an asynchronous copy of the one component asked for, charge,
+ * phase space and particles through their host deposits -- and queues the
+ * file for the background writer (zdf_io.c), so the simulation goes on
+ * while the file is formatted and written.  zdf_flush() waits for the files. */
+int zdf_async_submit(int (*run)(void *), void *arg);
+
+/* page-locked buffers for the asynchronous copies, reused */
+typedef struct pin_buf {
+    void *p;
+    size_t bytes;
+    struct pin_buf *next;
+} pin_buf;
+static pthread_mutex_t pin_mu = PTHREAD_MUTEX_INITIALIZER;
+static pin_buf *pin_free = NULL;
+static int pin_nfree = 0;
+
+static void *pin_get(size_t bytes, size_t *got)
 {
-    static int said = 0;
-    if (!said) fprintf(stderr, "(*warning*) ZDF diagnostic files are not written by libzpic_em2d\n");
-    said = 1;
+    pthread_mutex_lock(&pin_mu);
+    for (pin_buf **pp = &pin_free; *pp; pp = &(*pp)->next) {
+        if ((*pp)->bytes >= bytes) {
+            pin_buf *b = *pp;
+            *pp = b->next;
+            pin_nfree--;
+            pthread_mutex_unlock(&pin_mu);
+            void *p = b->p;
+            *got = b->bytes;
+            free(b);
+            return p;
+        }
+    }
+    pthread_mutex_unlock(&pin_mu);
+    void *p = NULL;
+    if (zc_host_alloc(bytes, &p) != ZC_OK) return NULL;
+    *got = bytes;
+    return p;
 }
 
-EXPORT void spec_report(const t_species *spec, const int rep_type, const int pha_nx[], const float pha_range[][2])
+static void pin_put(void *p, size_t bytes)
 {
-    (void)rep_type;
-    (void)pha_nx;
-    (void)pha_range;
-    int k = 0;
-    entry_t *e = reg_by_species(spec, &k);
-    if (e) pull_species(e, k);
-    no_zdf();
+    pin_buf *b = (pin_buf *)malloc(sizeof(pin_buf));
+    pthread_mutex_lock(&pin_mu);
+    if (!b || pin_nfree >= 8) {  /* keep a few for reuse */
+        pthread_mutex_unlock(&pin_mu);
+        free(b);
+        zc_host_free(p);
+        return;
+    }
+    b->p = p;
+    b->bytes = bytes;
+    b->next = pin_free;
+    pin_free = b;
+    pin_nfree++;
+    pthread_mutex_unlock(&pin_mu);
+}
+
+static const char *const kUnitsX = "c/\\omega_p";
+static const char *const kTimeUnits = "1/\\omega_p";
+
+typedef struct grid_job {
+    t_zdf_grid_info info;
+    t_zdf_grid_axis axis[2];
+    t_zdf_iteration iter;
+    char name[128], label[128], units[64], path[1024];
+    char ax_name[2][16], ax_label[2][16], ax_units[2][32];
+    float *data;
+    size_t bytes;  /* > 0: page-locked buffer of that size */
+    zc_fence *fence;
+} grid_job;
+
+static int run_grid_job(void *arg)
+{
+    grid_job *j = (grid_job *)arg;
+    int ok = 1;
+    if (j->fence) {
+        ok = zc_fence_wait(j->fence) == ZC_OK;
+        zc_fence_destroy(j->fence);
+    }
+    if (ok) ok = zdf_save_grid(j->data, zdf_float32, &j->info, &j->iter, j->path);
+    if (j->bytes) pin_put(j->data, j->bytes);
+    else free(j->data);
+    free(j);
+    return ok;
+}
+
+/* a 2-D grid job with the reference's metadata layout */
+static grid_job *grid_job_new(int nx, int ny, const char *units, double x0, double x1, double y0, double y1,
+                              const char *axn0, const char *axl0, const char *axu0, const char *axn1,
+                              const char *axl1, const char *axu1, int n, double t)
+{
+    grid_job *j = (grid_job *)calloc(1, sizeof(grid_job));
+    if (!j) return NULL;
+    snprintf(j->units, sizeof(j->units), "%s", units);
+    snprintf(j->ax_name[0], 16, "%s", axn0);
+    snprintf(j->ax_label[0], 16, "%s", axl0);
+    snprintf(j->ax_units[0], 32, "%s", axu0);
+    snprintf(j->ax_name[1], 16, "%s", axn1);
+    snprintf(j->ax_label[1], 16, "%s", axl1);
+    snprintf(j->ax_units[1], 32, "%s", axu1);
+    for (int a = 0; a < 2; a++) {
+        j->axis[a].name = j->ax_name[a];
+        j->axis[a].type = zdf_linear;
+        j->axis[a].label = j->ax_label[a];
+        j->axis[a].units = j->ax_units[a];
+    }
+    j->axis[0].min = x0;
+    j->axis[0].max = x1;
+    j->axis[1].min = y0;
+    j->axis[1].max = y1;
+    j->info.name = j->name;
+    j->info.ndims = 2;
+    j->info.count[0] = (uint64_t)nx;
+    j->info.count[1] = (uint64_t)ny;
+    j->info.label = j->label;
+    j->info.units = j->units;
+    j->info.axis = j->axis;
+    j->iter.name = "ITERATION";
+    j->iter.n = n;
+    j->iter.t = t;
+    j->iter.time_units = (char *)kTimeUnits;
+    return j;
+}
+
+/* the interior of component c of a host grid (float3, row stride nrow) */
+static float *pack_component(const float3 *f, int nrow, int nx, int ny, int c)
+{
+    float *buf = (float *)malloc((size_t)nx * ny * sizeof(float));
+    if (!buf) return NULL;
+    for (int jy = 0; jy < ny; jy++)
+        for (int ix = 0; ix < nx; ix++) {
+            const float3 v = f[ix + jy * nrow];
+            buf[ix + jy * nx] = (c == 0) ? v.x : (c == 1) ? v.y : v.z;
+        }
+    return buf;
+}
+
+/* fills job data: the device component when the grid belongs to a GPU
+ * simulation, else the host one */
+static int job_data(grid_job *j, entry_t *e, int grid, int comp, const float3 *host, int nrow, int nx, int ny)
+{
+    if (e) {
+        size_t got = 0;
+        j->data = (float *)pin_get((size_t)nx * ny * sizeof(float), &got);
+        if (!j->data) return 0;
+        j->bytes = got;
+        if (zc_copy_grid_async(e->gpu, grid, comp, j->data, &j->fence) != ZC_OK) {
+            pin_put(j->data, got);
+            j->data = NULL;
+            return 0;
+        }
+        return 1;
+    }
+    j->data = pack_component(host, nrow, nx, ny, comp);
+    return j->data != NULL;
+}
+
+static void report_failed(grid_job *j, const char *what)
+{
+    fprintf(stderr, "(*error*) %s: %s\n", what, zc_last_error());
+    free(j);
 }
 
 EXPORT void emf_report(const t_emf *emf, const char field, const int fc)
 {
-    (void)field;
-    (void)fc;
-    entry_t *e = reg_by_emf(emf);
-    if (e) zc_check(zc_get_fields(e->gpu, (float *)emf->E_buf, (float *)emf->B_buf), "emf_report");
-    no_zdf();
+    static const char comp[] = {'x', 'y', 'z'};
+    if (fc < 0 || fc > 2) {
+        fprintf(stderr, "(*error*) Invalid field component (fc) selected, returning\n");
+        return;
+    }
+    grid_job *j = grid_job_new(emf->nx[0], emf->nx[1], "m_e c \\omega_p e^{-1}", 0.0, emf->box[0], 0.0,
+                               emf->box[1], "x", "x", kUnitsX, "y", "y", kUnitsX, emf->iter,
+                               emf->iter * emf->dt);
+    if (!j) return;
+    int grid;
+    const float3 *host;
+    switch (field) {
+    case EFLD:
+        grid = ZC_GRID_E, host = emf->E;
+        snprintf(j->name, 16, "E%1d", fc);
+        snprintf(j->label, 16, "E_%c", comp[fc]);
+        break;
+    case BFLD:
+        grid = ZC_GRID_B, host = emf->B;
+        snprintf(j->name, 16, "B%1d", fc);
+        snprintf(j->label, 16, "B_%c", comp[fc]);
+        break;
+    case EPART:
+        grid = ZC_GRID_EPART, host = emf->E_part;
+        snprintf(j->name, 16, "E%1d-part", fc);
+        snprintf(j->label, 16, "E_{%cp}", comp[fc]);
+        break;
+    case BPART:
+        grid = ZC_GRID_BPART, host = emf->B_part;
+        snprintf(j->name, 16, "B%1d-part", fc);
+        snprintf(j->label, 16, "B_{%cp}", comp[fc]);
+        break;
+    default:
+        fprintf(stderr, "Invalid field type selected, returning\n");
+        free(j);
+        return;
+    }
+    snprintf(j->path, sizeof(j->path), "EMF");
+    if (!job_data(j, reg_by_emf(emf), grid, fc, host, emf->nrow, emf->nx[0], emf->nx[1])) {
+        report_failed(j, "emf_report");
+        return;
+    }
+    zdf_async_submit(run_grid_job, j);
 }
 
 EXPORT void current_report(const t_current *current, const int jc)
 {
-    (void)jc;
-    entry_t *e = reg_by_current(current);
-    if (e) zc_check(zc_get_current(e->gpu, (float *)current->J_buf), "current_report");
-    no_zdf();
+    static const char comp[] = {'x', 'y', 'z'};
+    if (jc < 0 || jc > 2) {
+        fprintf(stderr, "(*error*) Invalid current component (jc) selected, returning\n");
+        return;
+    }
+    grid_job *j = grid_job_new(current->nx[0], current->nx[1], "e \\omega_p^2 / c", 0.0, current->box[0], 0.0,
+                               current->box[1], "x", "x", kUnitsX, "y", "y", kUnitsX, current->iter,
+                               current->iter * current->dt);
+    if (!j) return;
+    snprintf(j->name, 3, "J%1u", (unsigned)jc);
+    snprintf(j->label, 4, "J_%c", comp[jc]);
+    snprintf(j->path, sizeof(j->path), "CURRENT");
+    if (!job_data(j, reg_by_current(current), ZC_GRID_J, jc, current->J, current->nrow, current->nx[0],
+                  current->nx[1])) {
+        report_failed(j, "current_report");
+        return;
+    }
+    zdf_async_submit(run_grid_job, j);
+}
+
+static void spec_rep_charge(const t_species *spec)
+{
+    const int nx = spec->nx[0], ny = spec->nx[1];
+    float *charge = (float *)calloc((size_t)(nx + 1) * (ny + 1), sizeof(float));
+    float *buf = (float *)malloc((size_t)nx * ny * sizeof(float));
+    grid_job *j = grid_job_new(nx, ny, "n_e", spec->n_move * spec->dx[0], spec->box[0] + spec->n_move * spec->dx[0],
+                               0.0, spec->box[1], "x", "x", kUnitsX, "y", "y", kUnitsX, spec->iter,
+                               spec->iter * spec->dt);
+    if (!charge || !buf || !j) {
+        free(charge), free(buf), free(j);
+        return;
+    }
+    spec_deposit_charge(spec, charge);
+    for (int jy = 0; jy < ny; jy++) memcpy(buf + (size_t)jy * nx, charge + (size_t)jy * (nx + 1), nx * sizeof(float));
+    free(charge);
+    snprintf(j->name, sizeof(j->name), "%s-charge", spec->name);
+    snprintf(j->label, sizeof(j->label), "%s \\rho", spec->name);
+    snprintf(j->path, sizeof(j->path), "CHARGE/%s", spec->name);
+    j->data = buf;
+    zdf_async_submit(run_grid_job, j);
+}
+
+static const char *pha_units(int quant)
+{
+    switch (quant) {
+    case X1:
+    case X2:
+        return "c/\\omega_p";
+    case U1:
+    case U2:
+    case U3:
+        return "m_e c";
+    }
+    return "";
+}
+
+static void spec_rep_pha(const t_species *spec, const int rep_type, const int pha_nx[], const float pha_range[][2])
+{
+    static const char *const ax_name[] = {"x1", "x2", "x3", "u1", "u2", "u3"};
+    static const char *const ax_label[] = {"x", "y", "z", "u_x", "u_y", "u_z"};
+    const int q1 = rep_type & 0x000F, q2 = (rep_type & 0x00F0) >> 4;
+    if (q1 < 1 || q1 > 6 || q2 < 1 || q2 > 6 || !pha_nx || !pha_range) {
+        fprintf(stderr, "(*error*) Invalid phasespace type selected, returning\n");
+        return;
+    }
+    float *buf = (float *)calloc((size_t)pha_nx[0] * pha_nx[1], sizeof(float));
+    grid_job *j = grid_job_new(pha_nx[0], pha_nx[1], "a.u.", pha_range[0][0], pha_range[0][1], pha_range[1][0],
+                               pha_range[1][1], ax_name[q1 - 1], ax_label[q1 - 1], pha_units(q1), ax_name[q2 - 1],
+                               ax_label[q2 - 1], pha_units(q2), spec->iter, spec->iter * spec->dt);
+    if (!buf || !j) {
+        free(buf), free(j);
+        return;
+    }
+    spec_deposit_pha(spec, rep_type, pha_nx, pha_range, buf);
+    snprintf(j->name, 64, "%s-%s%s", spec->name, ax_name[q1 - 1], ax_name[q2 - 1]);
+    snprintf(j->label, 64, "%s %s-%s", spec->name, ax_label[q1 - 1], ax_label[q2 - 1]);
+    snprintf(j->path, sizeof(j->path), "PHASESPACE/%s", spec->name);
+    j->data = buf;
+    zdf_async_submit(run_grid_job, j);
+}
+
+typedef struct part_job {
+    t_zdf_part_info info;
+    t_zdf_iteration iter;
+    char name[MAX_SPNAME_LEN + 1], path[1024];
+    float *data;  /* x, y, ux, uy, uz, np each */
+} part_job;
+
+static int run_part_job(void *arg)
+{
+    static const char *const quants[] = {"x", "y", "ux", "uy", "uz"};
+    part_job *j = (part_job *)arg;
+    t_zdf_file f;
+    int ok = zdf_open_part_file(&f, &j->info, &j->iter, j->path);
+    for (int q = 0; ok && q < 5; q++)
+        ok = zdf_add_quant_part_file(&f, quants[q], j->data + (size_t)q * j->info.np, j->info.np) || !j->info.np;
+    if (f.fp) ok = zdf_close_file(&f) && ok;
+    free(j->data);
+    free(j);
+    return ok;
+}
+
+static void spec_rep_particles(const t_species *spec)
+{
+    static const char *const quants[] = {"x", "y", "ux", "uy", "uz"};
+    static const char *const qlabels[] = {"x", "y", "u_x", "u_y", "u_z"};
+    static const char *const qunits[] = {"c/\\omega_p", "c/\\omega_p", "c", "c", "c"};
+    int k = 0;
+    entry_t *e = reg_by_species(spec, &k);
+    if (e) pull_species(e, k);  /* refreshes the host mirror, as the particles go to the file */
+    const size_t np = spec->np > 0 ? (size_t)spec->np : 0;
+    part_job *j = (part_job *)calloc(1, sizeof(part_job));
+    float *d = (float *)malloc(5 * (np ? np : 1) * sizeof(float));
+    if (!j || !d) {
+        free(j), free(d);
+        return;
+    }
+    for (size_t i = 0; i < np; i++) {
+        const t_part *p = &spec->part[i];
+        d[i] = (spec->n_move + p->ix + p->x) * spec->dx[0];
+        d[np + i] = (p->iy + p->y) * spec->dx[1];
+        d[2 * np + i] = p->ux;
+        d[3 * np + i] = p->uy;
+        d[4 * np + i] = p->uz;
+    }
+    snprintf(j->name, sizeof(j->name), "%s", spec->name);
+    snprintf(j->path, sizeof(j->path), "PARTICLES/%s", spec->name);
+    j->info.name = j->name;
+    j->info.label = j->name;
+    j->info.np = np;
+    j->info.nquants = 5;
+    j->info.quants = (char **)quants;
+    j->info.qlabels = (char **)qlabels;
+    j->info.qunits = (char **)qunits;
+    j->iter.name = "ITERATION";
+    j->iter.n = spec->iter;
+    j->iter.t = spec->iter * spec->dt;
+    j->iter.time_units = (char *)kTimeUnits;
+    j->data = d;
+    zdf_async_submit(run_part_job, j);
+}
+
+EXPORT void spec_report(const t_species *spec, const int rep_type, const int pha_nx[], const float pha_range[][2])
+{
+    switch (rep_type & 0xF000) {
+    case CHARGE:
+        spec_rep_charge(spec);
+        break;
+    case PHA:
+        spec_rep_pha(spec, rep_type, pha_nx, pha_range);
+        break;
+    case PARTICLES:
+        spec_rep_particles(spec);
+        break;
+    }
 }
 
 EXPORT void spec_move_window(t_species *spec)

@@ -1472,6 +1472,70 @@ zc_status zc_get_current(zc_sim *s, float *J) {
   return grid_down(s, s->J[s->j_cur], J);
 }
 
+struct zc_fence {
+  cudaEvent_t ev = nullptr;
+};
+
+zc_status zc_copy_grid_async(zc_sim *s, int grid, int comp, float *dst, zc_fence **fence) {
+  if (!s || !dst || !fence) return fail(ZC_EINVAL, "null argument");
+  *fence = nullptr;
+  if (comp < 0 || comp > 2) return fail(ZC_EINVAL, "grid component must be 0, 1 or 2");
+  DeviceGuard g(s->device);
+  const float *eb = s->EB[s->eb_cur], *ebp = s->EBp ? s->EBp : s->EB[s->eb_cur];
+  const float *base = nullptr;
+  switch (grid) {
+    case ZC_GRID_E: base = eb; break;
+    case ZC_GRID_B: base = eb + 3 * s->G.plane; break;
+    case ZC_GRID_EPART: base = ebp; break;
+    case ZC_GRID_BPART: base = ebp + 3 * s->G.plane; break;
+    case ZC_GRID_J: base = s->J[s->j_cur]; break;
+    default: return fail(ZC_EINVAL, "unknown grid %d", grid);
+  }
+  // interior cell (0, 0) sits at buffer column 1 of buffer row 1
+  const float *src = base + comp * s->G.plane + s->G.pitch + 1;
+  CK(cudaMemcpy2DAsync(dst, sizeof(float) * s->G.nx, src, sizeof(float) * s->G.pitch, sizeof(float) * s->G.nx,
+                       s->G.ny, cudaMemcpyDeviceToHost, s->st));
+  zc_fence *f = new (std::nothrow) zc_fence;
+  if (!f) return fail(ZC_ENOMEM, "fence allocation failed");
+  cudaError_t e = cudaEventCreateWithFlags(&f->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(f->ev, s->st);
+  if (e != cudaSuccess) {
+    if (f->ev) cudaEventDestroy(f->ev);
+    delete f;
+    return fail(ZC_ECUDA, "fence: %s", cudaGetErrorString(e));
+  }
+  *fence = f;
+  return ZC_OK;
+}
+
+zc_status zc_fence_wait(zc_fence *f) {
+  if (!f) return fail(ZC_EINVAL, "null fence");
+  const cudaError_t e = cudaEventSynchronize(f->ev);
+  if (e != cudaSuccess) return fail(ZC_ECUDA, "fence wait: %s", cudaGetErrorString(e));
+  return ZC_OK;
+}
+
+void zc_fence_destroy(zc_fence *f) {
+  if (!f) return;
+  if (f->ev) cudaEventDestroy(f->ev);
+  delete f;
+}
+
+zc_status zc_host_alloc(size_t bytes, void **p) {
+  if (!p) return fail(ZC_EINVAL, "null argument");
+  *p = nullptr;
+  const cudaError_t e = cudaHostAlloc(p, bytes ? bytes : 1, cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(ZC_ENOMEM, "pinned host allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  }
+  return ZC_OK;
+}
+
+void zc_host_free(void *p) {
+  if (p) cudaFreeHost(p);
+}
+
 zc_status zc_set_current(zc_sim *s, const float *J) {
   if (!s || !J) return fail(ZC_EINVAL, "null argument");
   DeviceGuard g(s->device);

@@ -134,6 +134,7 @@ def _load():
         "spec_report": (None, [C.POINTER(t_species), C.c_int, P, P]),
         "emf_report": (None, [C.POINTER(t_emf), C.c_char, C.c_int]),
         "current_report": (None, [C.POINTER(t_current), C.c_int]),
+        "zdf_flush": (C.c_int, []),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -141,6 +142,12 @@ def _load():
         f.argtypes = args
     _lib = lib
     return lib
+
+
+def zdf_flush():
+    """Waits until every report file queued so far is written (the reports
+    write ZDF files on a background thread); returns how many failed."""
+    return int(_load().zdf_flush())
 
 
 def gpu_options(device=0, tile=(16, 16), fast_math=False):
