@@ -197,6 +197,56 @@ ZC_API void zc_fence_destroy(zc_fence *fence);
 /* page-locked host memory for asynchronous copies */
 ZC_API zc_status zc_host_alloc(size_t bytes, void **ptr);
 ZC_API void zc_host_free(void *ptr);
+
+/* ------------------------------------------------------------------------- */
+/* em1d: the reference's one-dimensional electromagnetic step (em1d/*.c)     */
+/* ------------------------------------------------------------------------- */
+/* One handle = one 1-D simulation on one GPU: push + zigzag deposit
+ * (em1d/particles.c:707-1062), current update with binomial / compensated
+ * filtering (em1d/current.c:111-330), Yee advance with periodic, open (Mur)
+ * or moving-window boundaries (em1d/emf.c:379-580).  Grids are the
+ * reference's float3 buffers of nx + 3 cells (one lower, two upper guard
+ * cells); particles the reference's 20-byte record. */
+typedef struct zc1_sim zc1_sim;
+typedef struct zc1_desc {
+    int nx;
+    float box;
+    float dt;
+    int device;
+    int open_fields;     /* Mur boundaries (emf.bc_type = EMF_BC_OPEN) */
+    int open_particles;  /* particles leaving [0, nx) are removed (PART_BC_OPEN) */
+    int moving_window;   /* sim_set_moving_window: fields and current without boundary */
+    int sort_every;      /* cell sort interval of the particle buffers (0: 16) */
+} zc1_desc;
+typedef struct zc1_part {  /* em1d/particles.h:29-35 */
+    int ix;
+    float x, ux, uy, uz;
+} zc1_part;
+typedef struct zc1_species_desc {
+    float m_q, q;        /* q: the species' particle charge (spec_new, particles.c:530-545) */
+    int ppc;
+    float ufl[3], uth[3];
+    int density;         /* injection profile: 0 uniform, 1 empty, 2 step, 3 slab */
+    float start, end;
+} zc1_species_desc;
+ZC_API zc_status zc1_create(const zc1_desc *desc, zc1_sim **sim);
+ZC_API void zc1_destroy(zc1_sim *sim);
+/* particles as loaded by the caller (e.g. the reference's spec_new); a
+ * moving window injects cold particles (ufl) into column nx-1 by the profile */
+ZC_API zc_status zc1_add_species(zc1_sim *sim, const zc1_species_desc *desc, const zc1_part *parts, int np,
+                                 int *species);
+ZC_API zc_status zc1_set_smooth(zc1_sim *sim, int type, int level);  /* 0 none, 1 binomial, 2 compensated */
+ZC_API zc_status zc1_set_fields(zc1_sim *sim, const float *E_buf, const float *B_buf);
+ZC_API zc_status zc1_get_fields(zc1_sim *sim, float *E_buf, float *B_buf);
+ZC_API zc_status zc1_get_current(zc1_sim *sim, float *J_buf);
+ZC_API zc_status zc1_step(zc1_sim *sim, int nsteps);
+/* field energy per component (emf_get_energy, em1d/emf.c:590-612) and each
+ * species' time-centred kinetic energy of its last advance */
+ZC_API zc_status zc1_energy(zc1_sim *sim, double emf_energy[6], double *kin_energy);
+ZC_API zc_status zc1_species_count(zc1_sim *sim, int species, int *np);
+ZC_API zc_status zc1_get_particles(zc1_sim *sim, int species, zc1_part *out, int cap, int *np);
+ZC_API zc_status zc1_get_info(zc1_sim *sim, int *iter, int *n_move);
+ZC_API zc_status zc1_synchronize(zc1_sim *sim);
 ZC_API zc_status zc_set_current(zc_sim *sim, const float *J_buf);
 /* field energy per component (emf_get_energy, em2d/emf.c:729-750) and the
  * time-centred kinetic energy of each species after its last advance

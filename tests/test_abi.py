@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared(header):
     text = open(os.path.join(ROOT, "include", header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(zc_[a-z_0-9]+)\s*\(", text)) - {"zc_inject_fn"})
+    return sorted(set(re.findall(r"\b(zc1?_[a-z_0-9]+)\s*\(", text)) - {"zc_inject_fn"})
 
 
 @pytest.fixture(scope="module")

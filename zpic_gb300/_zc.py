@@ -40,7 +40,9 @@ EXPORTS = [
     "zc_adj_create", "zc_adj_destroy", "zc_adj_set_state", "zc_adj_forward", "zc_adj_backward",
     "zc_adj_get_state", "zc_adj_times", "zc_species_phasespace", "zc_species_create_device",
     "zc_adj_set_birth", "zc_adj_set_smooth", "zc_copy_grid_async", "zc_fence_wait", "zc_fence_destroy",
-    "zc_host_alloc", "zc_host_free",
+    "zc_host_alloc", "zc_host_free", "zc1_create", "zc1_destroy", "zc1_add_species", "zc1_set_smooth",
+    "zc1_set_fields", "zc1_get_fields", "zc1_get_current", "zc1_step", "zc1_energy", "zc1_species_count",
+    "zc1_get_particles", "zc1_get_info", "zc1_synchronize",
 ]
 NPHASE = 13
 
@@ -165,12 +167,24 @@ def load(path: str = LIB_PATH):
         "zc_copy_grid_async": [P, I, I, P, C.POINTER(P)],
         "zc_fence_wait": [P],
         "zc_host_alloc": [C.c_size_t, C.POINTER(P)],
+        "zc1_create": [P, C.POINTER(P)],
+        "zc1_add_species": [P, P, P, I, C.POINTER(I)],
+        "zc1_set_smooth": [P, I, I],
+        "zc1_set_fields": [P, P, P],
+        "zc1_get_fields": [P, P, P],
+        "zc1_get_current": [P, P],
+        "zc1_step": [P, I],
+        "zc1_energy": [P, P, P],
+        "zc1_species_count": [P, I, C.POINTER(I)],
+        "zc1_get_particles": [P, I, P, I, C.POINTER(I)],
+        "zc1_get_info": [P, C.POINTER(I), C.POINTER(I)],
+        "zc1_synchronize": [P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
         f.argtypes = args
         f.restype = I
-    for name in ("zc_fence_destroy", "zc_host_free"):
+    for name in ("zc_fence_destroy", "zc_host_free", "zc1_destroy"):
         getattr(lib, name).argtypes = [P]
         getattr(lib, name).restype = None
     lib.zc_last_error.restype = C.c_char_p

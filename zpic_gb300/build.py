@@ -33,6 +33,7 @@ UNITS = [
     ("zc_api.cu", []),
     ("zc_noalloc.cu", []),
     ("zc_adjoint.cu", ["--fmad=false"]),
+    ("zc_em1d.cu", ["--fmad=false"]),
 ]
 
 
