@@ -617,6 +617,159 @@ def run_wakefield_adjoint(args):
 
 
 # ---------------------------------------------------------------------------
+# the em1d step: the reference's own 1-D laser wakefield deck
+# ---------------------------------------------------------------------------
+# em1d/input/lwfa.c: 1000 cells, box 20, dt 0.019, tmax 22.8; electrons
+# (m_q -1) of density 1 from x = 20, 128 ppc, cold; laser start 17, FWHM 2,
+# a0 2, omega0 10, polarisation pi/2; moving window; compensated level-4
+# smoothing.  All plasma enters through the window's right edge.
+EM1D = dict(nx=1000, box=20.0, dt=0.019, tmax=22.8, ppc=128, m_q=-1.0, density=("step", 20.0, 0.0),
+            laser=dict(start=17.0, fwhm=2.0, a0=2.0, omega0=10.0, polarization=float(np.pi / 2)),
+            smooth=("compensated", 4))
+# algorithmic bytes of the push per particle: the 20-byte record read and
+# written (fields and current stay in L1/L2: 1000 cells)
+EM1D_PART_BYTES = 40
+
+
+def em1d_steps(dt, tmax):
+    """iterations of the reference's main loop, for (n=0,t=0; t<=tmax; n++,
+    t=n*dt) in float (em1d/main.c:55)"""
+    n = 0
+    while np.float32(n) * np.float32(dt) <= np.float32(tmax):
+        n += 1
+    return n
+
+
+def em1d_deck():
+    """the deck as a dict for the CPU checker (oracle/pyoracle_em1d)"""
+    W = EM1D
+    return dict(nx=W["nx"], box=W["box"], dt=W["dt"],
+                species=[dict(name="electrons", m_q=W["m_q"], ppc=W["ppc"],
+                              density=dict(type="step", start=W["density"][1]))],
+                laser=W["laser"], moving_window=True, smooth=dict(type=W["smooth"][0], level=W["smooth"][1]))
+
+
+def _em1d_sim():
+    from zpic_gb300.em1d_gpu import PART_DTYPE, CudaSim1D
+
+    W = EM1D
+    sim = CudaSim1D(W["nx"], W["box"], W["dt"], moving_window=True)
+    q = float(np.float32(np.copysign(1.0, W["m_q"]) / W["ppc"]))  # spec_new, em1d/particles.c:529
+    sim.add_species(W["m_q"], q, W["ppc"], np.zeros(0, dtype=PART_DTYPE), density=W["density"])
+    L = W["laser"]
+    sim.add_laser(L["start"], L["a0"], L["omega0"], fwhm=L["fwhm"], polarization=L["polarization"])
+    sim.set_smooth(*W["smooth"])
+    return sim
+
+
+def em1d_cpu(steps, fast=True):
+    """the deck on one host core: the reference em1d (stock -Ofast build)
+    where it is built, else the C restatement; returns (particle-steps/s,
+    kind, seconds, particle-steps)"""
+    from oracle import pyoracle, pyoracle_em1d
+
+    pyoracle.build()
+    backend = "ref" if pyoracle_em1d.available("ref", fast) else "oracle"
+    s = pyoracle_em1d.RefSim1D(em1d_deck(), stock_sort=True, backend=backend, fast=fast)
+    pushed = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pushed += s.np_(0)
+        s.iter()
+    t = time.perf_counter() - t0
+    s.close()
+    return pushed / t, ("reference" if backend == "ref" else "port"), t, pushed
+
+
+def run_em1d(args):
+    """The em1d step on the reference's 1-D wakefield deck (em1d/input/lwfa.c),
+    the whole run of 1201 steps.  A first pass with a per-step particle count
+    gives the exact particle-steps (particles pushed per step summed); a
+    profiled pass gives each kernel's device time; the timed pass is one
+    zc1_step call of the whole run (CUDA events on the simulation's stream);
+    e2e is the same run through the public API on the wall clock, from
+    creating the simulation to reading E and B back."""
+    W = EM1D
+    steps = args.steps if args.steps_given else em1d_steps(W["dt"], W["tmax"])
+    # pass 1: per-step counts (particles pushed at step s = count before it)
+    sim = _em1d_sim()
+    pushed, counts = 0, []
+    for _ in range(steps):
+        n = sim.count(0)
+        pushed += n
+        counts.append(n)
+        sim.step(1)
+    n_end = sim.count(0)
+    sim.close()
+    # pass 2: per-kernel device times (events around every launch)
+    sim = _em1d_sim()
+    sim.set_profile(True)
+    sim.step(steps)
+    prof = sim.profile()
+    sim.close()
+    # warm-up runs of the timed pass, then the timed pass
+    for _ in range(max(args.warmup, 3)):
+        sim = _em1d_sim()
+        sim.step(min(steps, 100))
+        sim.close()
+    sim = _em1d_sim()
+    clk = ClockSampler(0)
+    clk.start()
+    sim.step(steps)
+    ms = sim.last_ms()
+    clocks = clk.stop()
+    launches = sim.launches()
+    info = sim.info()
+    n_timed = sim.count(0)
+    sim.close()
+    # e2e: public API, wall clock, fields back on the host
+    t0 = time.perf_counter()
+    sim = _em1d_sim()
+    sim.step(steps)
+    E, B = sim.E(), sim.B()
+    t_e2e = time.perf_counter() - t0
+    sim.close()
+    value = pushed / (ms * 1e-3)
+    # roofline of the dominant kernel
+    dom = max(prof, key=lambda k: prof[k][0])
+    hbm, peak_kind = peaks()
+    push_ms, push_n = prof["push"]
+    push_bytes = EM1D_PART_BYTES * pushed / max(push_n, 1)
+    achieved = push_bytes / (push_ms * 1e-3 / max(push_n, 1)) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (the reference deck's cold plasma, injected by the moving window)",
+        "config": {"workload": "em1d laser wakefield (em1d/input/lwfa.c): 1000 cells, box 20, dt 0.019, "
+                               f"{steps} steps (tmax 22.8), moving window, laser a0 2 omega0 10 FWHM 2 start 17 "
+                               "pol pi/2, density 1 from x=20, 128 ppc cold, compensated smoothing level 4",
+                   "particles_end": int(n_end), "particles_end_timed_pass": int(n_timed),
+                   "particles_max": int(max(counts + [n_end])), "window_moves": info["n_move"],
+                   "l2": "working set L2-resident (under 6 MB); no flush"},
+        "how": "value = particles pushed summed over the steps / device time of one zc1_step call of the whole run",
+        "e2e": {"value": pushed / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": (E.nbytes + B.nbytes) / steps,
+                "how": "wall clock of create + laser + zc1_step(all) + E/B read; the deck's plasma is injected "
+                       "on the device, so nothing is uploaded"},
+        "gpu_launches": launches,
+        "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / max(sum(x[0] for x in prof.values()), 1e-30)}
+                    for k, v in prof.items()},
+        "roofline": {"bound": "hbm", "kernel": "k1_push", "dominant_kernel_kind": dom, "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "peak_source": peak_kind,
+                     "note": "40 B per particle; a push moves at most 5 MB, so launch latency, not HBM, bounds it"},
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        v, kind, t, n = em1d_cpu(steps)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+                                "sample": f"the whole deck ({steps} steps, {n} particle-steps, {t:.2f} s), "
+                                          "stock sort every 16 steps"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def main():
@@ -632,7 +785,8 @@ def main():
                     help="bit-exact push build (every float32 op rounded as the reference C)")
     ap.add_argument("--sort-every", type=int, default=0)
     ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
-    ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint", "lwfa", "wakefield_adjoint"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint", "lwfa", "wakefield_adjoint",
+                                                              "em1d"])
     ap.add_argument("--deterministic", action="store_true", help="fixed-point (bit-reproducible) deposition")
     ap.add_argument("--fd-study", action="store_true", help="wakefield adjoint: finite differences at shrinking steps")
     ap.add_argument("--scan-runs", type=int, default=256)
@@ -649,6 +803,8 @@ def main():
         return run_lwfa(args)
     if args.workload == "wakefield_adjoint":
         return run_wakefield_adjoint(args)
+    if args.workload == "em1d":
+        return run_em1d(args)
 
     from zpic_gb300.replicas import Replicas
 

@@ -239,7 +239,27 @@ ZC_API zc_status zc1_set_smooth(zc1_sim *sim, int type, int level);  /* 0 none, 
 ZC_API zc_status zc1_set_fields(zc1_sim *sim, const float *E_buf, const float *B_buf);
 ZC_API zc_status zc1_get_fields(zc1_sim *sim, float *E_buf, float *B_buf);
 ZC_API zc_status zc1_get_current(zc1_sim *sim, float *J_buf);
+/* adds a laser pulse to E and B (emf_add_laser, em1d/emf.c:191-260; the
+ * plane-wave fields of zc_laser, whose type, W0, focus and axis are unused).
+ * Periodic simulations then copy the guard cells, as the reference does for
+ * its default boundary; its decks add the laser before they switch to open or
+ * moving-window boundaries, where the copies are zero for a pulse inside the
+ * box. */
+ZC_API zc_status zc1_add_laser(zc1_sim *sim, const zc_laser *laser);
+/* sim_iter x nsteps (em1d/simulation.c:45-56) */
 ZC_API zc_status zc1_step(zc1_sim *sim, int nsteps);
+/* device time of the last zc1_step call (CUDA events on the simulation's stream) */
+ZC_API zc_status zc1_last_step_ms(zc1_sim *sim, float *ms);
+/* kernels the steps of this simulation have launched so far */
+ZC_API zc_status zc1_get_launches(zc1_sim *sim, long long *launches);
+/* per-kernel device time: with profiling on, every launch of a step is
+ * bracketed by CUDA events (which costs time of its own; leave it off for
+ * timing runs).  zc1_set_profile resets the sums; zc1_get_profile returns
+ * milliseconds and launches per kind since then (a "compact" or "sort" entry
+ * covers its three kernels). */
+enum { ZC1_K_PUSH = 0, ZC1_K_COMPACT, ZC1_K_INJECT, ZC1_K_SORT, ZC1_K_CURRENT, ZC1_K_EMF, ZC1_NKIND };
+ZC_API zc_status zc1_set_profile(zc1_sim *sim, int on);
+ZC_API zc_status zc1_get_profile(zc1_sim *sim, double ms[ZC1_NKIND], long long launches[ZC1_NKIND]);
 /* field energy per component (emf_get_energy, em1d/emf.c:590-612) and each
  * species' time-centred kinetic energy of its last advance */
 ZC_API zc_status zc1_energy(zc1_sim *sim, double emf_energy[6], double *kin_energy);

@@ -1,29 +1,42 @@
-"""ctypes access to the reference em1d (oracle/_ref/libzpic_ref_em1d.so,
-built by oracle/Makefile from the reference's own sources): the checker of
-the 1-D GPU step.  TEST INFRASTRUCTURE ONLY."""
+"""ctypes access to the em1d checker libraries, the checker of the 1-D GPU
+step.  TEST INFRASTRUCTURE ONLY.
+
+* ``backend="ref"``    -- oracle/_ref/libzpic_ref_em1d.so: the reference em1d
+  built by oracle/Makefile from its own sources (only where they exist);
+* ``backend="oracle"`` -- oracle/liboracle_em1d.so: our C restatement
+  (zpic_oracle_em1d.c), which builds anywhere.
+
+Both export the same zr1_* entry points.  ``fast=True`` picks the build with
+the reference's stock -Ofast flags (timing); the default strict IEEE build is
+the one that reproduces the reference's bits."""
 import ctypes as C
 import os
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB = os.path.join(HERE, "_ref", "libzpic_ref_em1d.so")
 PART_DTYPE = np.dtype([("ix", "<i4"), ("x", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4")])
 DENSITY = {"uniform": 0, "empty": 1, "step": 2, "slab": 3}
 SMOOTH = {"none": 0, "binomial": 1, "compensated": 2}
 
-_lib = None
+_libs = {}
 
 
-def available():
-    return os.path.exists(LIB)
+def lib_path(backend="ref", fast=False):
+    if backend == "ref":
+        return os.path.join(HERE, "_ref", "libzpic_ref_em1d_fast.so" if fast else "libzpic_ref_em1d.so")
+    return os.path.join(HERE, "liboracle_em1d_fast.so" if fast else "liboracle_em1d.so")
 
 
-def _load():
-    global _lib
-    if _lib is not None:
-        return _lib
-    lib = C.CDLL(LIB)
+def available(backend="ref", fast=False):
+    return os.path.exists(lib_path(backend, fast))
+
+
+def _load(backend="ref", fast=False):
+    path = lib_path(backend, fast)
+    if path in _libs:
+        return _libs[path]
+    lib = C.CDLL(path)
     P = C.c_void_p
     sig = {
         "zr1_set_rand_seed": (None, [C.c_uint32, C.c_uint32]),
@@ -52,7 +65,7 @@ def _load():
         f = getattr(lib, name)
         f.restype = res
         f.argtypes = args
-    _lib = lib
+    _libs[path] = lib
     return lib
 
 
@@ -63,8 +76,8 @@ def _p(a):
 class RefSim1D:
     """A reference em1d simulation built from a deck dict (tests/decks_em1d.py)."""
 
-    def __init__(self, deck):
-        f = self.f = _load()
+    def __init__(self, deck, stock_sort=False, backend="ref", fast=False):
+        f = self.f = _load(backend, fast)
         f.zr1_set_rand_seed(12345, 67890)
         self.nx = int(deck["nx"])
         self.h = f.zr1_sim_new(self.nx, float(deck["box"]), float(deck["dt"]))
@@ -78,8 +91,11 @@ class RefSim1D:
                               float(d.get("end", 0.0)), float(d.get("n", 1.0)))
             self.nspec += 1
         f.zr1_finalize(self.h)
-        for k in range(self.nspec):
-            f.zr1_set_n_sort(self.h, k, 0)  # sorting only permutes the buffer
+        if not stock_sort:
+            # sorting only permutes the buffer; off for bit comparisons of the
+            # particle records, on (every 16 steps, spec_new) for timing
+            for k in range(self.nspec):
+                f.zr1_set_n_sort(self.h, k, 0)
         if "laser" in deck:
             L = deck["laser"]
             f.zr1_add_laser(self.h, L["start"], L["fwhm"], L["a0"], L["omega0"], L.get("polarization", 0.0))
@@ -93,6 +109,11 @@ class RefSim1D:
 
     def iter(self):
         self.f.zr1_iter(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.f.zr1_sim_delete(self.h)
+            self.h = None
 
     def np_(self, k):
         return int(self.f.zr1_spec_np(self.h, k))

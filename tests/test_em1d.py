@@ -1,8 +1,10 @@
-"""The em1d step on the GPU (zc1_*, zpic_gb300/em1d_gpu.py) against the
+"""The em1d step on the GPU (zc1_*, zpic_gb300/em1d_gpu.py) and the C
+restatement of the em1d step (oracle/zpic_oracle_em1d.c) against the
 reference em1d: fixtures made by tests/golden/make_em1d_golden.py from the
 reference compiled here, decks in tests/decks_em1d.py (periodic two-stream,
 open boundaries with a laser and a slab, moving-window wakefield).
 
+The laser's initial fields (zc1_add_laser) within 1e-6 of the reference's.
 Per step: the particle counts equal, field and kinetic energies within
 1e-5; after each of the first 10 steps E, B, J within 1e-5 relative L2 per
 component (E and B measured on their common scale); after the last step the
@@ -72,6 +74,85 @@ print("OK")
         assert r.returncode == 0 and "OK" in r.stdout, name + r.stdout[-2000:] + r.stderr[-2000:]
 
 
+_CHILD_ORACLE = r"""
+import sys
+sys.path[:0] = [{root!r}, {tests!r}]
+import numpy as np
+from decks_em1d import DECKS_1D
+from oracle.pyoracle_em1d import RefSim1D
+g = np.load({path!r})
+d = DECKS_1D[{name!r}]
+s = RefSim1D(d, backend="oracle")
+assert s.particles(0).tobytes() == g["p0_0"].tobytes(), "loading"
+assert s.E().tobytes() == g["E0"].tobytes() and s.B().tobytes() == g["B0"].tobytes(), "laser"
+for step in range(d["steps"]):
+    s.iter()
+    if step < len(g["E_near"]):
+        for f in "EBJ":
+            assert getattr(s, f)().tobytes() == g[f + "_near"][step].tobytes(), (step, f)
+    assert np.array_equal(s.emf_energy(), g["emf_energy"][step]), step
+    for k in range(s.nspec):
+        assert s.np_(k) == g["np"][step][k] and s.energy(k) == g["kin_energy"][step][k], (step, k)
+for f in "EBJ":
+    assert getattr(s, f)().tobytes() == g[f].tobytes(), f
+print("OK")
+"""
+
+
+def _run_child(code):
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_fixtures(name):
+    """The C restatement (oracle/zpic_oracle_em1d.c, strict IEEE build)
+    reproduces the reference's fixtures bit for bit: the loaded particles,
+    the laser, E/B/J after each of the first 10 steps and after the last,
+    and the energies and particle counts of every step."""
+    from oracle import pyoracle, pyoracle_em1d
+
+    pyoracle.build()
+    assert pyoracle_em1d.available("oracle")
+    _run_child(_CHILD_ORACLE.format(root=ROOT, tests=os.path.join(ROOT, "tests"),
+                                    path=os.path.join(GOLD, name + ".npz"), name=name))
+
+
+_CHILD_SORTED = r"""
+import sys
+sys.path[:0] = [{root!r}, {tests!r}]
+import numpy as np
+from decks_em1d import DECKS_1D
+from oracle.pyoracle_em1d import RefSim1D
+d = DECKS_1D[{name!r}]
+s = RefSim1D(d, stock_sort=True, backend={backend!r})
+for _ in range(d["steps"]):
+    s.iter()
+np.savez({out!r}, E=s.E(), J=s.J(), p=s.particles(0))
+print("OK")
+"""
+
+
+def test_oracle_sort_matches_reference(tmp_path):
+    """With the reference's stock sort (every 16 steps) the restatement and
+    the reference leave the same particle order and fields (lwfa deck)."""
+    from oracle import pyoracle, pyoracle_em1d
+
+    pyoracle.build()
+    if not pyoracle_em1d.available("ref"):
+        pytest.skip("reference em1d not built here")
+    out = {}
+    for b in ("ref", "oracle"):
+        out[b] = str(tmp_path / f"{b}.npz")
+        _run_child(_CHILD_SORTED.format(root=ROOT, tests=os.path.join(ROOT, "tests"), name="lwfa", backend=b,
+                                        out=out[b]))
+    a, b = np.load(out["ref"]), np.load(out["oracle"])
+    for k in a.files:
+        assert a[k].tobytes() == b[k].tobytes(), k
+
+
 def _mirror(name, g):
     from zpic_gb300.em1d_gpu import CudaSim1D
 
@@ -83,10 +164,29 @@ def _mirror(name, g):
         sim.add_species(sp["m_q"], float(g["q"][k]), sp["ppc"], g[f"p0_{k}"], ufl=sp.get("ufl", (0, 0, 0)),
                         uth=sp.get("uth", (0, 0, 0)),
                         density=(dens.get("type", "uniform"), dens.get("start", 0.0), dens.get("end", 0.0)))
-    sim.set_fields(g["E0"], g["B0"])
+    if "laser" in d:
+        L = d["laser"]
+        sim.add_laser(L["start"], L["a0"], L["omega0"], fwhm=L["fwhm"], polarization=L.get("polarization", 0.0))
+    else:
+        sim.set_fields(g["E0"], g["B0"])
     if "smooth" in d:
         sim.set_smooth(d["smooth"]["type"], d["smooth"]["level"])
     return sim
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", [n for n in NAMES if "laser" in DECKS_1D[n]])
+def test_em1d_laser_matches_reference(name):
+    """zc1_add_laser against the reference's emf_add_laser: the fields of the
+    deck before the first step, guard cells included, within 1e-6 of the
+    field's largest value (double cos on the device against the host's)"""
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    sim = _mirror(name, g)
+    for f, ref in (("E", g["E0"]), ("B", g["B0"])):
+        got = getattr(sim, f)()
+        assert np.abs(ref).max() > 0
+        assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max(), f
+    sim.close()
 
 
 @pytest.mark.gpu

@@ -42,7 +42,8 @@ EXPORTS = [
     "zc_adj_set_birth", "zc_adj_set_smooth", "zc_copy_grid_async", "zc_fence_wait", "zc_fence_destroy",
     "zc_host_alloc", "zc_host_free", "zc1_create", "zc1_destroy", "zc1_add_species", "zc1_set_smooth",
     "zc1_set_fields", "zc1_get_fields", "zc1_get_current", "zc1_step", "zc1_energy", "zc1_species_count",
-    "zc1_get_particles", "zc1_get_info", "zc1_synchronize",
+    "zc1_get_particles", "zc1_get_info", "zc1_synchronize", "zc1_add_laser", "zc1_last_step_ms",
+    "zc1_get_launches", "zc1_set_profile", "zc1_get_profile",
 ]
 NPHASE = 13
 
@@ -179,6 +180,11 @@ def load(path: str = LIB_PATH):
         "zc1_get_particles": [P, I, P, I, C.POINTER(I)],
         "zc1_get_info": [P, C.POINTER(I), C.POINTER(I)],
         "zc1_synchronize": [P],
+        "zc1_add_laser": [P, P],
+        "zc1_last_step_ms": [P, C.POINTER(C.c_float)],
+        "zc1_get_launches": [P, C.POINTER(C.c_longlong)],
+        "zc1_set_profile": [P, I],
+        "zc1_get_profile": [P, P, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

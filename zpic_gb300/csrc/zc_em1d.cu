@@ -431,6 +431,19 @@ __device__ __forceinline__ void yee_b1(float *E, float *B, int nx, float dt_dx) 
   }
 }
 
+// periodic guard cells of E and B (emf_update_gc, emf.c:476-500): -1 <- nx-1
+// and nx <- 0 only; the second upper guard cell nx+1 keeps the value yee_e
+// gave it.  Threads 0..11 of the CTA.
+__device__ __forceinline__ void periodic_gc1(float *E, float *B, int nx) {
+  if (threadIdx.x < 12) {
+    float *F = (threadIdx.x < 6) ? E : B;
+    const int t = threadIdx.x % 6, g = t / 3, c = t % 3;
+    const int gi = (g == 0) ? -1 : nx;
+    const int src = (g == 0) ? nx - 1 : 0;
+    F[(gi + GC0) * 3 + c] = F[(src + GC0) * 3 + c];
+  }
+}
+
 __global__ void __launch_bounds__(1024) k1_emf(float *E, float *B, const float *J, float *mur, Emf1 M) {
   const int nx = M.nx;
   const float hdt = M.dt / 2.0f;
@@ -467,15 +480,7 @@ __global__ void __launch_bounds__(1024) k1_emf(float *E, float *B, const float *
   __syncthreads();
   yee_b1(E, B, nx, hdt / M.dx);
   __syncthreads();
-  if (M.bc == 1 && threadIdx.x < 12) {
-    // periodic guard cells (emf.c:476-500): -1 <- nx-1 and nx <- 0 only; the
-    // second upper guard cell nx+1 keeps the value yee_e gave it
-    float *F = (threadIdx.x < 6) ? E : B;
-    const int t = threadIdx.x % 6, g = t / 3, c = t % 3;
-    const int gi = (g == 0) ? -1 : nx;
-    const int src = (g == 0) ? nx - 1 : 0;
-    F[(gi + GC0) * 3 + c] = F[(src + GC0) * 3 + c];
-  }
+  if (M.bc == 1) periodic_gc1(E, B, nx);
   if (M.shift) {
     // shift left one cell, zero the cells nx-1 .. nx+1 (emf.c:513-540)
     __syncthreads();
@@ -500,6 +505,26 @@ __global__ void __launch_bounds__(1024) k1_emf(float *E, float *B, const float *
       B[k] = 0.f;
     }
   }
+}
+
+// laser launch (emf_add_laser, em1d/emf.c:191-260): the plane-wave pulse
+// added to Ey/Ez at the cell nodes and By/Bz half a cell ahead, with the
+// reference's float/double mix; periodic runs then refresh the guard cells
+__global__ void __launch_bounds__(1024) k1_laser(float *E, float *B, int nx, zc::LaserConst L, int periodic) {
+  const float amp = L.omega0 * L.a0;
+  const float cp = cos((double)L.polarization), sp = sin((double)L.polarization);
+  const float k = L.omega0;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+    const float z = i * L.dx, z2 = z + L.dx / 2;
+    const float a = amp * zc::laser_env(L, z), a2 = amp * zc::laser_env(L, z2);
+    const int o = (i + GC0) * 3;
+    E[o + 1] += +a * cos((double)(k * z)) * cp;
+    E[o + 2] += +a * cos((double)(k * z)) * sp;
+    B[o + 1] += -a2 * cos((double)(k * z2)) * sp;
+    B[o + 2] += +a2 * cos((double)(k * z2)) * cp;
+  }
+  __syncthreads();
+  if (periodic) periodic_gc1(E, B, nx);
 }
 
 // field energy per component (emf.c:590-612): double sums of float squares
@@ -551,6 +576,17 @@ struct zc1_sim {
   int *d_which = nullptr, *d_err = nullptr, *d_blk = nullptr, *d_cnt = nullptr;
   int blk_cap = 0;
   double *d_emf = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.f;
+  long long launches = 0;  // kernels launched by the step so far
+  // optional per-kernel timing: an event pair around every launch, summed
+  // per kind after the steps (zc1_set_profile / zc1_get_profile)
+  int profile = 0;
+  std::vector<cudaEvent_t> prof_ev;
+  std::vector<int> prof_kind;
+  size_t prof_used = 0;
+  double prof_ms[ZC1_NKIND] = {};
+  long long prof_n[ZC1_NKIND] = {};
   std::vector<Species1> sp;
 };
 
@@ -626,10 +662,14 @@ int read_np(zc1_sim *s, Species1 &p) {
   return n;
 }
 
-// room for `need` particles in both buffers, keeping the current ones
-zc_status ensure_cap(zc1_sim *s, Species1 &p, int need) {
-  if (need <= p.cap) return ZC_OK;
+// room for `extra` more particles in both buffers, keeping the current ones;
+// the device count is read (a sync) only when its upper bound no longer fits,
+// and the buffers grow only when the true count does not
+zc_status ensure_cap(zc1_sim *s, Species1 &p, int extra) {
+  if (p.np_bound + extra <= p.cap) return ZC_OK;
   const int n = read_np(s, p);
+  const int need = n + extra;
+  if (need <= p.cap) return ZC_OK;
   const int cap = std::max(need, (int)(1.25 * n) + 1024);
   Parts nb[2];
   for (int b = 0; b < 2; ++b) {
@@ -657,6 +697,43 @@ zc_status check_err(zc1_sim *s) {
   return ZC_OK;
 }
 
+// start of a profiled launch of `kind`: returns the slot of its event pair
+// (-1 when profiling is off)
+int prof_begin(zc1_sim *s, int kind) {
+  if (!s->profile) return -1;
+  const size_t slot = s->prof_used;
+  if (2 * slot + 2 > s->prof_ev.size()) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+      if (a) cudaEventDestroy(a);
+      return -1;
+    }
+    s->prof_ev.push_back(a);
+    s->prof_ev.push_back(b);
+    s->prof_kind.push_back(kind);
+  }
+  s->prof_kind[slot] = kind;
+  cudaEventRecord(s->prof_ev[2 * slot], s->st);
+  s->prof_used = slot + 1;
+  return (int)slot;
+}
+
+void prof_end(zc1_sim *s, int slot) {
+  if (slot >= 0) cudaEventRecord(s->prof_ev[2 * (size_t)slot + 1], s->st);
+}
+
+// adds the recorded launches to the per-kind sums (after a stream sync)
+void prof_collect(zc1_sim *s) {
+  for (size_t i = 0; i < s->prof_used; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, s->prof_ev[2 * i], s->prof_ev[2 * i + 1]) == cudaSuccess) {
+      s->prof_ms[s->prof_kind[i]] += ms;
+      s->prof_n[s->prof_kind[i]] += 1;
+    }
+  }
+  s->prof_used = 0;
+}
+
 zc_status compact(zc1_sim *s, Species1 &p) {
   const int nblk = (p.np_bound + kCompactPer - 1) / kCompactPer;
   if (nblk == 0) return ZC_OK;
@@ -668,20 +745,26 @@ zc_status compact(zc1_sim *s, Species1 &p) {
   }
   int *d_old = s->d_blk + nblk;  // the count before compaction
   CK1(cudaMemcpyAsync(d_old, p.d_np, sizeof(int), cudaMemcpyDeviceToDevice, s->st));
+  const int pf = prof_begin(s, ZC1_K_COMPACT);
   k1_live_count<<<nblk, kCompactBlock, 0, s->st>>>(p.buf[p.cur].ix, d_old, s->d_blk);
   k1_scan_blocks<<<1, 1024, 0, s->st>>>(s->d_blk, nblk, p.d_np);
   k1_live_scatter<<<nblk, kCompactBlock, 0, s->st>>>(p.buf[p.cur], p.buf[1 - p.cur], d_old, s->d_blk);
+  prof_end(s, pf);
   CK1(cudaGetLastError());
+  s->launches += 3;
   p.cur = 1 - p.cur;
   return ZC_OK;
 }
 
 zc_status sort_cells(zc1_sim *s, Species1 &p) {
+  const int pf = prof_begin(s, ZC1_K_SORT);
   CK1(cudaMemsetAsync(s->d_cnt, 0, sizeof(int) * s->nx, s->st));
   k1_cell_count<<<grid_blocks(), 256, 0, s->st>>>(p.buf[p.cur].ix, p.d_np, s->d_cnt);
   k1_cell_scan<<<1, 1024, 0, s->st>>>(s->d_cnt, s->nx);
   k1_cell_scatter<<<grid_blocks(), 256, 0, s->st>>>(p.buf[p.cur], p.buf[1 - p.cur], p.d_np, s->d_cnt);
+  prof_end(s, pf);
   CK1(cudaGetLastError());
+  s->launches += 3;
   p.cur = 1 - p.cur;
   return ZC_OK;
 }
@@ -704,23 +787,32 @@ zc_status step1(zc1_sim *s) {
     C.shift = shift;
     C.open = (s->mw || s->part_open) ? 1 : 0;
     CK1(cudaMemsetAsync(p.d_ekin, 0, sizeof(double), st));
+    const int pf = prof_begin(s, ZC1_K_PUSH);
     k1_push<<<grid_blocks(), 256, 0, st>>>(p.buf[p.cur], p.d_np, s->E, s->B, s->J[0], C, p.d_ekin, s->d_err);
+    prof_end(s, pf);
     CK1(cudaGetLastError());
+    s->launches += 1;
     if (C.open) TRY1(compact(s, p));
     p.iter += 1;
     if (shift) {
       p.n_move += 1;
       if (p.inj.type != 1) {
-        TRY1(ensure_cap(s, p, p.np_bound + p.inj.ppc));
+        TRY1(ensure_cap(s, p, p.inj.ppc));
+        const int pi = prof_begin(s, ZC1_K_INJECT);
         k1_inject<<<1, 32, 0, st>>>(p.buf[p.cur], p.d_np, p.cap, p.inj, s->nx, p.n_move, s->d_err);
+        prof_end(s, pi);
         CK1(cudaGetLastError());
+        s->launches += 1;
         p.np_bound += p.inj.ppc;
       }
     }
     if (s->sort_every > 0 && p.iter % s->sort_every == 0) TRY1(sort_cells(s, p));
   }
+  const int pc = prof_begin(s, ZC1_K_CURRENT);
   k1_current<<<1, 1024, 0, st>>>(s->J[0], s->J[1], s->nx, s->current_periodic, s->smooth, s->d_which);
+  prof_end(s, pc);
   CK1(cudaGetLastError());
+  s->launches += 1;
   s->j_cur = s->smooth.n % 2;  // the passes alternate buffers
   Emf1 M;
   M.nx = s->nx;
@@ -729,8 +821,11 @@ zc_status step1(zc1_sim *s) {
   M.bc = s->field_bc;
   s->iter += 1;
   M.shift = (s->mw && ((float)s->iter * s->dt) > (s->dx * (float)(s->n_move + 1))) ? 1 : 0;
+  const int pe = prof_begin(s, ZC1_K_EMF);
   k1_emf<<<1, 1024, 0, st>>>(s->E, s->B, s->J[s->j_cur], s->mur, M);
+  prof_end(s, pe);
   CK1(cudaGetLastError());
+  s->launches += 1;
   if (M.shift) s->n_move += 1;
   return ZC_OK;
 }
@@ -770,6 +865,8 @@ zc_status zc1_create(const zc1_desc *d, zc1_sim **out) {
   if (e == cudaSuccess) e = cudaMalloc(&s->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_cnt, sizeof(int) * s->nx);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_emf, sizeof(double) * 6);
+  if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
   if (e == cudaSuccess) e = cudaMemset(s->E, 0, gbytes);
   if (e == cudaSuccess) e = cudaMemset(s->B, 0, gbytes);
   if (e == cudaSuccess) e = cudaMemset(s->J[0], 0, gbytes);
@@ -804,6 +901,9 @@ void zc1_destroy(zc1_sim *s) {
   cudaFree(s->d_blk);
   cudaFree(s->d_cnt);
   cudaFree(s->d_emf);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  for (cudaEvent_t e : s->prof_ev) cudaEventDestroy(e);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
 }
@@ -883,6 +983,36 @@ zc_status zc1_set_fields(zc1_sim *s, const float *E, const float *B) {
   return ZC_OK;
 }
 
+zc_status zc1_add_laser(zc1_sim *s, const zc_laser *in) {
+  if (!s || !in) return fail1(ZC_EINVAL, "null argument");
+  zc_laser L = *in;
+  // parameter checks, em1d/emf.c:193-219
+  if (L.fwhm != 0) {
+    if (L.fwhm <= 0) return fail1(ZC_EINVAL, "Invalid laser FWHM, must be > 0");
+    L.rise = L.fwhm;
+    L.fall = L.fwhm;
+    L.flat = 0.;
+  }
+  if (L.rise <= 0) return fail1(ZC_EINVAL, "Invalid laser RISE, must be > 0");
+  if (L.flat < 0) return fail1(ZC_EINVAL, "Invalid laser FLAT, must be >= 0");
+  if (L.fall <= 0) return fail1(ZC_EINVAL, "Invalid laser FALL, must be > 0");
+  Guard1 g(s->device);
+  zc::LaserConst c{};
+  c.type = 0;
+  c.start = L.start;
+  c.rise = L.rise;
+  c.flat = L.flat;
+  c.fall = L.fall;
+  c.a0 = L.a0;
+  c.omega0 = L.omega0;
+  c.polarization = L.polarization;
+  c.dx = s->dx;
+  k1_laser<<<1, 1024, 0, s->st>>>(s->E, s->B, s->nx, c, s->field_bc == 1 ? 1 : 0);
+  CK1(cudaGetLastError());
+  CK1(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
 zc_status zc1_get_fields(zc1_sim *s, float *E, float *B) {
   if (!s) return fail1(ZC_EINVAL, "null simulation handle");
   Guard1 g(s->device);
@@ -904,10 +1034,49 @@ zc_status zc1_get_current(zc1_sim *s, float *J) {
 zc_status zc1_step(zc1_sim *s, int nsteps) {
   if (!s || nsteps < 0) return fail1(ZC_EINVAL, "invalid argument");
   Guard1 g(s->device);
+  CK1(cudaEventRecord(s->ev0, s->st));
   for (int k = 0; k < nsteps; ++k) {
     TRY1(step1(s));
-    if ((k + 1) % 16 == 0 || k + 1 == nsteps) TRY1(check_err(s));
+    if ((k + 1) % 16 == 0 && k + 1 < nsteps) {
+      TRY1(check_err(s));
+      prof_collect(s);
+    }
   }
+  CK1(cudaEventRecord(s->ev1, s->st));
+  CK1(cudaEventSynchronize(s->ev1));
+  cudaEventElapsedTime(&s->last_ms, s->ev0, s->ev1);
+  prof_collect(s);
+  return check_err(s);
+}
+
+zc_status zc1_set_profile(zc1_sim *s, int on) {
+  if (!s) return fail1(ZC_EINVAL, "null simulation handle");
+  s->profile = on ? 1 : 0;
+  for (int k = 0; k < ZC1_NKIND; ++k) {
+    s->prof_ms[k] = 0.0;
+    s->prof_n[k] = 0;
+  }
+  return ZC_OK;
+}
+
+zc_status zc1_get_profile(zc1_sim *s, double ms[ZC1_NKIND], long long launches[ZC1_NKIND]) {
+  if (!s) return fail1(ZC_EINVAL, "null simulation handle");
+  for (int k = 0; k < ZC1_NKIND; ++k) {
+    if (ms) ms[k] = s->prof_ms[k];
+    if (launches) launches[k] = s->prof_n[k];
+  }
+  return ZC_OK;
+}
+
+zc_status zc1_get_launches(zc1_sim *s, long long *n) {
+  if (!s || !n) return fail1(ZC_EINVAL, "null argument");
+  *n = s->launches;
+  return ZC_OK;
+}
+
+zc_status zc1_last_step_ms(zc1_sim *s, float *ms) {
+  if (!s || !ms) return fail1(ZC_EINVAL, "null argument");
+  *ms = s->last_ms;
   return ZC_OK;
 }
 

@@ -387,23 +387,6 @@ __global__ void k_emf_energy_final(const double *partial, int nblocks, double *o
 // laser launch (emf_add_laser, em2d/emf.c:158-350): same double-precision
 // library calls on float arguments as the reference
 // ---------------------------------------------------------------------------
-__device__ float laser_env(const LaserConst &L, float z) {
-  const double half_pi = 1.57079632679489661923132169163975144;
-  if (z > L.start) return 0.0f;
-  if (z > L.start - L.rise) {
-    float u = z - L.start;
-    float e = sin(half_pi * u / L.rise);
-    return e * e;
-  }
-  if (z > L.start - (L.rise + L.flat)) return 1.0f;
-  if (z > L.start - (L.rise + L.flat + L.fall)) {
-    float u = z - (L.start - L.rise - L.flat - L.fall);
-    float e = sin(half_pi * u / L.fall);
-    return e * e;
-  }
-  return 0.0f;
-}
-
 __device__ float laser_gauss(const LaserConst &L, float zpos, float r) {
   float z = zpos - L.focus;
   float zr = L.omega0 * (L.W0 * L.W0) / 2;

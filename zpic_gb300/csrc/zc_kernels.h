@@ -223,6 +223,28 @@ struct LaserConst {
 };
 cudaError_t launch_laser(float *EB, const Grid &G, const LaserConst &L, cudaStream_t st);
 
+#ifdef __CUDACC__
+// longitudinal envelope of a laser pulse (lon_env, em2d/emf.c:158-186 and
+// em1d/emf.c:157-180): sin^2 rise and fall around a flat top, evaluated with
+// the double-precision sin on float arguments as the reference does
+__device__ inline float laser_env(const LaserConst &L, float z) {
+  const double half_pi = 1.57079632679489661923132169163975144;
+  if (z > L.start) return 0.0f;
+  if (z > L.start - L.rise) {
+    float u = z - L.start;
+    float e = sin(half_pi * u / L.rise);
+    return e * e;
+  }
+  if (z > L.start - (L.rise + L.flat)) return 1.0f;
+  if (z > L.start - (L.rise + L.flat + L.fall)) {
+    float u = z - (L.start - L.rise - L.flat - L.fall);
+    float e = sin(half_pi * u / L.fall);
+    return e * e;
+  }
+  return 0.0f;
+}
+#endif
+
 // sets the message returned by zc_last_error() on this thread
 void set_error_message(const char *msg);
 

@@ -5,6 +5,7 @@
     sim.add_species(m_q, q, ppc, particles, ufl=..., density=("step", start, end))
     sim.set_smooth("compensated", 1)
     sim.set_fields(E, B)         # (nx + 3, 3) float32 buffers, reference layout
+    sim.add_laser(start, a0, omega0, fwhm=..., polarization=...)
     sim.step(n)
     sim.E(), sim.B(), sim.J(), sim.energy(), sim.particles(k)
 
@@ -93,8 +94,39 @@ class CudaSim1D:
         _zc._ck(self.lib.zc1_get_current(self.h, _p(out)))
         return out
 
+    def add_laser(self, start, a0, omega0, *, fwhm=0.0, rise=0.0, flat=0.0, fall=0.0, polarization=0.0):
+        """emf_add_laser (em1d/emf.c:191-260): a plane-wave pulse ending at
+        `start`; `fwhm`, when set, overrides rise/flat/fall"""
+        L = _zc.Laser(type=0, start=float(start), fwhm=float(fwhm), rise=float(rise), flat=float(flat),
+                      fall=float(fall), a0=float(a0), omega0=float(omega0), polarization=float(polarization))
+        _zc._ck(self.lib.zc1_add_laser(self.h, C.byref(L)))
+
     def step(self, n=1):
         _zc._ck(self.lib.zc1_step(self.h, int(n)))
+
+    def launches(self):
+        """kernels launched by the steps so far"""
+        v = C.c_longlong()
+        _zc._ck(self.lib.zc1_get_launches(self.h, C.byref(v)))
+        return v.value
+
+    KINDS = ("push", "compact", "inject", "sort", "current", "emf")
+
+    def set_profile(self, on=True):
+        _zc._ck(self.lib.zc1_set_profile(self.h, int(bool(on))))
+
+    def profile(self):
+        """{kind: (device ms, launches)} since set_profile(True)"""
+        ms = np.zeros(len(self.KINDS))
+        n = np.zeros(len(self.KINDS), dtype=np.int64)
+        _zc._ck(self.lib.zc1_get_profile(self.h, _p(ms), _p(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KINDS)}
+
+    def last_ms(self):
+        """device time of the last step() call, CUDA events on the simulation's stream"""
+        v = C.c_float()
+        _zc._ck(self.lib.zc1_last_step_ms(self.h, C.byref(v)))
+        return v.value
 
     def energy(self):
         """(field energy per component [6], kinetic energy per species)"""
