@@ -701,7 +701,8 @@ def run_em1d(args):
         sim.step(1)
     n_end = sim.count(0)
     sim.close()
-    # pass 2: per-kernel device times (events around every launch)
+    # pass 2: per-kernel device times (event-record nodes around every
+    # kernel of the step graphs)
     sim = _em1d_sim()
     sim.set_profile(True)
     sim.step(steps)
@@ -746,7 +747,8 @@ def run_em1d(args):
                    "particles_end": int(n_end), "particles_end_timed_pass": int(n_timed),
                    "particles_max": int(max(counts + [n_end])), "window_moves": info["n_move"],
                    "l2": "working set L2-resident (under 6 MB); no flush"},
-        "how": "value = particles pushed summed over the steps / device time of one zc1_step call of the whole run",
+        "how": "value = particles pushed summed over the steps / device time of one zc1_step call of the whole run "
+               "(blocks of 16 steps replayed as CUDA graphs)",
         "e2e": {"value": pushed / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": (E.nbytes + B.nbytes) / steps,
                 "how": "wall clock of create + laser + zc1_step(all) + E/B read; the deck's plasma is injected "
@@ -757,7 +759,8 @@ def run_em1d(args):
         "roofline": {"bound": "hbm", "kernel": "k1_push", "dominant_kernel_kind": dom, "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                      "peak_source": peak_kind,
-                     "note": "40 B per particle; a push moves at most 5 MB, so launch latency, not HBM, bounds it"},
+                     "note": "40 B per particle read and written; a push moves at most 6 MB, L2-resident, so "
+                             "latency (launch, last-CTA bookkeeping), not HBM, bounds it"},
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:

@@ -232,7 +232,8 @@ typedef struct zc1_species_desc {
 ZC_API zc_status zc1_create(const zc1_desc *desc, zc1_sim **sim);
 ZC_API void zc1_destroy(zc1_sim *sim);
 /* particles as loaded by the caller (e.g. the reference's spec_new); a
- * moving window injects cold particles (ufl) into column nx-1 by the profile */
+ * moving window injects cold particles (ufl) into column nx-1 by the profile.
+ * Species are added before the first zc1_step. */
 ZC_API zc_status zc1_add_species(zc1_sim *sim, const zc1_species_desc *desc, const zc1_part *parts, int np,
                                  int *species);
 ZC_API zc_status zc1_set_smooth(zc1_sim *sim, int type, int level);  /* 0 none, 1 binomial, 2 compensated */
@@ -252,12 +253,14 @@ ZC_API zc_status zc1_step(zc1_sim *sim, int nsteps);
 ZC_API zc_status zc1_last_step_ms(zc1_sim *sim, float *ms);
 /* kernels the steps of this simulation have launched so far */
 ZC_API zc_status zc1_get_launches(zc1_sim *sim, long long *launches);
-/* per-kernel device time: with profiling on, every launch of a step is
- * bracketed by CUDA events (which costs time of its own; leave it off for
- * timing runs).  zc1_set_profile resets the sums; zc1_get_profile returns
- * milliseconds and launches per kind since then (a "compact" or "sort" entry
- * covers its three kernels). */
-enum { ZC1_K_PUSH = 0, ZC1_K_COMPACT, ZC1_K_INJECT, ZC1_K_SORT, ZC1_K_CURRENT, ZC1_K_EMF, ZC1_NKIND };
+/* per-kernel device time: with profiling on, every kernel of a step is
+ * bracketed by CUDA events (event-record nodes in the step graphs, which are
+ * then replayed one at a time; this costs time of its own, so leave it off
+ * for timing runs).  zc1_set_profile resets the
+ * sums; zc1_get_profile returns milliseconds and launches per kind since then:
+ * the push (with boundaries, compaction and injection), the cell sort (three
+ * kernels) and the fields kernel (current filter and field advance). */
+enum { ZC1_K_PUSH = 0, ZC1_K_SORT, ZC1_K_FIELDS, ZC1_NKIND };
 ZC_API zc_status zc1_set_profile(zc1_sim *sim, int on);
 ZC_API zc_status zc1_get_profile(zc1_sim *sim, double ms[ZC1_NKIND], long long launches[ZC1_NKIND]);
 /* field energy per component (emf_get_energy, em1d/emf.c:590-612) and each

@@ -110,7 +110,7 @@ class CudaSim1D:
         _zc._ck(self.lib.zc1_get_launches(self.h, C.byref(v)))
         return v.value
 
-    KINDS = ("push", "compact", "inject", "sort", "current", "emf")
+    KINDS = ("push", "sort", "fields")
 
     def set_profile(self, on=True):
         _zc._ck(self.lib.zc1_set_profile(self.h, int(bool(on))))
