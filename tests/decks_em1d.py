@@ -32,3 +32,31 @@ DECKS_1D = {
         smooth=dict(type="compensated", level=2),
         steps=400),
 }
+
+
+# grids wider than the fields kernel keeps in shared memory (its global-memory
+# variant): no committed fixtures, the tests run the C restatement of the
+# em1d step (pinned to the reference by the decks above) beside the GPU
+WIDE_1D = {
+    "wide_periodic": dict(
+        nx=6000, box=300.0, dt=0.045,
+        species=[dict(name="right", m_q=-1.0, ppc=4, ufl=[0.2, 0, 0], uth=[0.001, 0.001, 0.001]),
+                 dict(name="left", m_q=-1.0, ppc=4, ufl=[-0.1, 0.05, 0.03], uth=[0.001, 0.001, 0.001])],
+        smooth=dict(type="compensated", level=1),
+        steps=60),
+    "wide_open": dict(
+        nx=6000, box=120.0, dt=0.019,
+        species=[dict(name="e", m_q=-1.0, ppc=4, uth=[0.02, 0.02, 0.02],
+                      density=dict(type="slab", start=40.0, end=80.0))],
+        laser=dict(start=38.0, fwhm=4.0, a0=1.0, omega0=10.0, polarization=math.pi / 4),
+        open_fields=True, open_particles=True,
+        smooth=dict(type="binomial", level=2),
+        steps=200),
+    "wide_window": dict(
+        nx=6000, box=120.0, dt=0.019,
+        species=[dict(name="e", m_q=-1.0, ppc=4, density=dict(type="step", start=110.0))],
+        laser=dict(start=108.0, fwhm=3.0, a0=2.0, omega0=10.0, polarization=math.pi / 2),
+        moving_window=True,
+        smooth=dict(type="compensated", level=2),
+        steps=200),
+}

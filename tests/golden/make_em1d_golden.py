@@ -28,9 +28,11 @@ from oracle import pyoracle, pyoracle_em1d  # noqa: E402
 NEAR = 10
 
 
-def run(name):
-    d = DECKS_1D[name]
-    s = pyoracle_em1d.RefSim1D(d)
+def run(name, decks=DECKS_1D, backend="ref"):
+    """the fixture arrays of deck `name` of `decks`, on the reference
+    (backend "ref") or on the C restatement (backend "oracle")"""
+    d = decks[name]
+    s = pyoracle_em1d.RefSim1D(d, backend=backend)
     ns = s.nspec
     out = {"q": np.array([s.q(k) for k in range(ns)], dtype=np.float32)}
     for k in range(ns):

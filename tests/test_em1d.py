@@ -15,7 +15,7 @@ import os
 import numpy as np
 import pytest
 
-from decks_em1d import DECKS_1D
+from decks_em1d import DECKS_1D, WIDE_1D
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLD = os.path.join(ROOT, "tests", "golden", "em1d")
@@ -56,7 +56,7 @@ def test_fixtures_match_live_reference():
 import sys
 sys.path[:0] = [{root!r}, {tests!r}]
 import numpy as np
-from decks_em1d import DECKS_1D
+from decks_em1d import DECKS_1D, WIDE_1D
 from oracle.pyoracle_em1d import RefSim1D
 g = np.load({path!r})
 s = RefSim1D(DECKS_1D[{name!r}])
@@ -78,7 +78,7 @@ _CHILD_ORACLE = r"""
 import sys
 sys.path[:0] = [{root!r}, {tests!r}]
 import numpy as np
-from decks_em1d import DECKS_1D
+from decks_em1d import DECKS_1D, WIDE_1D
 from oracle.pyoracle_em1d import RefSim1D
 g = np.load({path!r})
 d = DECKS_1D[{name!r}]
@@ -124,7 +124,7 @@ _CHILD_SORTED = r"""
 import sys
 sys.path[:0] = [{root!r}, {tests!r}]
 import numpy as np
-from decks_em1d import DECKS_1D
+from decks_em1d import DECKS_1D, WIDE_1D
 from oracle.pyoracle_em1d import RefSim1D
 d = DECKS_1D[{name!r}]
 s = RefSim1D(d, stock_sort=True, backend={backend!r})
@@ -153,10 +153,9 @@ def test_oracle_sort_matches_reference(tmp_path):
         assert a[k].tobytes() == b[k].tobytes(), k
 
 
-def _mirror(name, g):
+def _mirror(d, g):
     from zpic_gb300.em1d_gpu import CudaSim1D
 
-    d = DECKS_1D[name]
     sim = CudaSim1D(d["nx"], d["box"], d["dt"], open_fields=d.get("open_fields", False),
                     open_particles=d.get("open_particles", False), moving_window=d.get("moving_window", False))
     for k, sp in enumerate(d["species"]):
@@ -181,7 +180,7 @@ def test_em1d_laser_matches_reference(name):
     deck before the first step, guard cells included, within 1e-6 of the
     field's largest value (double cos on the device against the host's)"""
     g = np.load(os.path.join(GOLD, name + ".npz"))
-    sim = _mirror(name, g)
+    sim = _mirror(DECKS_1D[name], g)
     for f, ref in (("E", g["E0"]), ("B", g["B0"])):
         got = getattr(sim, f)()
         assert np.abs(ref).max() > 0
@@ -192,9 +191,37 @@ def test_em1d_laser_matches_reference(name):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", NAMES)
 def test_em1d_matches_reference(name):
-    g = np.load(os.path.join(GOLD, name + ".npz"))
-    d = DECKS_1D[name]
-    sim = _mirror(name, g)
+    _check_run(DECKS_1D[name], np.load(os.path.join(GOLD, name + ".npz")))
+
+
+_CHILD_WIDE = r"""
+import sys
+sys.path[:0] = [{root!r}, {tests!r}, {golden!r}]
+import numpy as np
+from decks_em1d import WIDE_1D
+import make_em1d_golden
+np.savez({out!r}, **make_em1d_golden.run({name!r}, WIDE_1D, backend="oracle"))
+print("OK")
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(WIDE_1D))
+def test_em1d_wide_matches_oracle(name, tmp_path):
+    """6000-cell grids, beyond the fields kernel's shared memory (its
+    global-memory variant: periodic, open and moving-window boundaries),
+    against the C restatement run live in a fresh process, same bars"""
+    from oracle import pyoracle
+
+    pyoracle.build()
+    out = str(tmp_path / f"{name}.npz")
+    _run_child(_CHILD_WIDE.format(root=ROOT, tests=os.path.join(ROOT, "tests"),
+                                  golden=os.path.join(ROOT, "tests", "golden"), name=name, out=out))
+    _check_run(WIDE_1D[name], np.load(out))
+
+
+def _check_run(d, g):
+    sim = _mirror(d, g)
     ns = len(d["species"])
     for step in range(d["steps"]):
         sim.step(1)
