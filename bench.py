@@ -683,26 +683,15 @@ def em1d_cpu(steps, fast=True):
 
 def run_em1d(args):
     """The em1d step on the reference's 1-D wakefield deck (em1d/input/lwfa.c),
-    the whole run of 1201 steps.  A first pass with a per-step particle count
-    gives the exact particle-steps (particles pushed per step summed); a
-    profiled pass gives each kernel's device time; the timed pass is one
-    zc1_step call of the whole run (CUDA events on the simulation's stream);
-    e2e is the same run through the public API on the wall clock, from
-    creating the simulation to reading E and B back."""
+    the whole run of 1201 steps.  A profiled pass gives each kernel's device
+    time; the timed pass is one zc1_step call of the whole run (CUDA events on
+    the simulation's stream), its particle-steps the device's count of the
+    particles pushed; e2e is the same run through the public API on the wall
+    clock, from creating the simulation to reading E and B back."""
     W = EM1D
     steps = args.steps if args.steps_given else em1d_steps(W["dt"], W["tmax"])
-    # pass 1: per-step counts (particles pushed at step s = count before it)
-    sim = _em1d_sim()
-    pushed, counts = 0, []
-    for _ in range(steps):
-        n = sim.count(0)
-        pushed += n
-        counts.append(n)
-        sim.step(1)
-    n_end = sim.count(0)
-    sim.close()
-    # pass 2: per-kernel device times (event-record nodes around every
-    # kernel of the step graphs)
+    # profiled pass: per-kernel device times (event-record nodes around
+    # every kernel of the step graphs)
     sim = _em1d_sim()
     sim.set_profile(True)
     sim.step(steps)
@@ -721,7 +710,8 @@ def run_em1d(args):
     clocks = clk.stop()
     launches = sim.launches()
     info = sim.info()
-    n_timed = sim.count(0)
+    n_end = sim.count(0)
+    pushed = sim.pushed(0)
     sim.close()
     # e2e: public API, wall clock, fields back on the host
     t0 = time.perf_counter()
@@ -744,8 +734,7 @@ def run_em1d(args):
         "config": {"workload": "em1d laser wakefield (em1d/input/lwfa.c): 1000 cells, box 20, dt 0.019, "
                                f"{steps} steps (tmax 22.8), moving window, laser a0 2 omega0 10 FWHM 2 start 17 "
                                "pol pi/2, density 1 from x=20, 128 ppc cold, compensated smoothing level 4",
-                   "particles_end": int(n_end), "particles_end_timed_pass": int(n_timed),
-                   "particles_max": int(max(counts + [n_end])), "window_moves": info["n_move"],
+                   "particles_end": int(n_end), "particle_steps": int(pushed), "window_moves": info["n_move"],
                    "l2": "working set L2-resident (under 6 MB); no flush"},
         "how": "value = particles pushed summed over the steps / device time of one zc1_step call of the whole run "
                "(blocks of 16 steps replayed as CUDA graphs)",
@@ -772,6 +761,102 @@ def run_em1d(args):
     return 0
 
 
+def run_em1d_scan(args):
+    """A parameter scan of the em1d wakefield deck (mods/em1d_param_scan: the
+    laser FWHM spread evenly over [1.5, 2.5] across the runs, the rest as
+    em1d/input/lwfa.c, full 1201 steps).  The runs go once one after another
+    (each zc1_step to completion) and once side by side (every run on its
+    own stream, blocks of 16 steps enqueued round-robin, one wait per run at
+    the end).  Both are timed on the wall clock; particle-steps are the
+    device's counts of the particles pushed."""
+    W = EM1D
+    n_runs = args.scan_runs if args.scan_runs_given else 64
+    steps = args.steps if args.steps_given else em1d_steps(W["dt"], W["tmax"])
+    fwhm = [1.5 + k * (1.0 / max(n_runs - 1, 1)) for k in range(n_runs)]
+
+    def make(k, ctas=0):
+        from zpic_gb300.em1d_gpu import PART_DTYPE, CudaSim1D
+
+        sim = CudaSim1D(W["nx"], W["box"], W["dt"], moving_window=True, push_ctas=ctas)
+        q = float(np.float32(np.copysign(1.0, W["m_q"]) / W["ppc"]))
+        sim.add_species(W["m_q"], q, W["ppc"], np.zeros(0, dtype=PART_DTYPE), density=W["density"])
+        L = W["laser"]
+        sim.add_laser(L["start"], L["a0"], L["omega0"], fwhm=fwhm[k], polarization=L["polarization"])
+        sim.set_smooth(*W["smooth"])
+        return sim
+
+    # warm-up: both launch modes once on a short run
+    for _ in range(max(args.warmup, 3)):
+        w = [make(k) for k in range(2)]
+        for s in w:
+            s.step(32, wait=False)
+        for s in w:
+            s.synchronize()
+            s.close()
+    # one after another
+    sims = [make(k) for k in range(n_runs)]
+    t0 = time.perf_counter()
+    for s in sims:
+        s.step(steps)
+    t_seq = time.perf_counter() - t0
+    ps_seq = sum(s.pushed(0) for s in sims)
+    for s in sims:
+        s.close()
+    # side by side, for a few caps of the push's CTAs per run
+    sweep = {}
+    best = None
+    for ctas in (0, 128, 64, 32):
+        sims = [make(k, ctas) for k in range(n_runs)]
+        clk = ClockSampler(0)
+        clk.start()
+        t0 = time.perf_counter()
+        done = 0
+        while done < steps:
+            blk = min(16, steps - done)
+            for s in sims:
+                s.step(blk, wait=False)
+            done += blk
+        for s in sims:
+            s.synchronize()
+        t_par = time.perf_counter() - t0
+        clocks = clk.stop()
+        ps_par = sum(s.pushed(0) for s in sims)
+        launches = sum(s.launches() for s in sims)
+        moves = [s.info()["n_move"] for s in sims]
+        for s in sims:
+            s.close()
+        sweep[str(ctas)] = ps_par / t_par
+        if best is None or ps_par / t_par > best[0]:
+            best = (ps_par / t_par, ctas, t_par, ps_par, clocks, launches, moves)
+    _, best_ctas, t_par, ps_par, clocks, launches, moves = best
+    line = {
+        "metric": METRIC, "value": ps_par / t_par, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t_par / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (the reference deck's cold plasma, injected by the moving window)",
+        "config": {"workload": f"em1d parameter scan: {n_runs} runs of the em1d wakefield deck (em1d/input/lwfa.c, "
+                               f"{steps} steps each), laser FWHM 1.5..2.5 across the runs "
+                               "(mods/em1d_param_scan/input/lwfa.c)",
+                   "runs": n_runs, "particle_steps": int(ps_par), "window_moves": moves[0],
+                   "push_ctas_per_run": best_ctas,
+                   "l2": "working set L2-resident; no flush"},
+        "how": "value = particle-steps of all runs / wall clock of the side-by-side pass (one stream per run, "
+               "16-step graph blocks enqueued round-robin)",
+        "sequential": {"value": ps_seq / t_seq, "seconds": t_seq,
+                       "how": "the same runs one after another, each zc1_step(all) to completion"},
+        "speedup_over_sequential": (ps_par / t_par) / (ps_seq / t_seq),
+        "push_ctas_sweep": sweep,
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        v, kind, t, n = em1d_cpu(steps)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+                                "sample": f"one run of the deck ({steps} steps, {n} particle-steps, {t:.2f} s)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
@@ -789,13 +874,14 @@ def main():
     ap.add_argument("--sort-every", type=int, default=0)
     ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
     ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint", "lwfa", "wakefield_adjoint",
-                                                              "em1d"])
+                                                              "em1d", "em1d_scan"])
     ap.add_argument("--deterministic", action="store_true", help="fixed-point (bit-reproducible) deposition")
     ap.add_argument("--fd-study", action="store_true", help="wakefield adjoint: finite differences at shrinking steps")
     ap.add_argument("--scan-runs", type=int, default=256)
     ap.add_argument("--scan-group", type=int, default=0, help="runs per batch graph (0: all)")
     args = ap.parse_args()
     args.steps_given = any(a.startswith("--steps") for a in sys.argv[1:])
+    args.scan_runs_given = any(a.startswith("--scan-runs") for a in sys.argv[1:])
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "scan":
@@ -808,6 +894,8 @@ def main():
         return run_wakefield_adjoint(args)
     if args.workload == "em1d":
         return run_em1d(args)
+    if args.workload == "em1d_scan":
+        return run_em1d_scan(args)
 
     from zpic_gb300.replicas import Replicas
 

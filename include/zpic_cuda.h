@@ -217,6 +217,9 @@ typedef struct zc1_desc {
     int open_particles;  /* particles leaving [0, nx) are removed (PART_BC_OPEN) */
     int moving_window;   /* sim_set_moving_window: fields and current without boundary */
     int sort_every;      /* cell sort interval of the particle buffers (0: 16) */
+    int push_ctas;       /* most CTAs of the push and sort kernels (0: one particle per
+                            thread up to a full wave; simulations that run side by side
+                            do better with fewer, each thread then pushing several) */
 } zc1_desc;
 typedef struct zc1_part {  /* em1d/particles.h:29-35 */
     int ix;
@@ -247,10 +250,21 @@ ZC_API zc_status zc1_get_current(zc1_sim *sim, float *J_buf);
  * moving-window boundaries, where the copies are zero for a pulse inside the
  * box. */
 ZC_API zc_status zc1_add_laser(zc1_sim *sim, const zc_laser *laser);
-/* sim_iter x nsteps (em1d/simulation.c:45-56) */
+/* sim_iter x nsteps (em1d/simulation.c:45-56); waits for the steps and
+ * reports their errors */
 ZC_API zc_status zc1_step(zc1_sim *sim, int nsteps);
-/* device time of the last zc1_step call (CUDA events on the simulation's stream) */
+/* the same steps, only enqueued on the simulation's stream: independent
+ * simulations (a parameter scan) then run side by side on one GPU.  The
+ * host still waits when a particle buffer may have to grow.  Errors of the
+ * steps surface at zc1_synchronize. */
+ZC_API zc_status zc1_step_async(zc1_sim *sim, int nsteps);
+/* waits for the enqueued steps; returns their first error */
+ZC_API zc_status zc1_synchronize(zc1_sim *sim);
+/* device time from the first step enqueued after the previous wait to the
+ * last wait (CUDA events on the simulation's stream) */
 ZC_API zc_status zc1_last_step_ms(zc1_sim *sim, float *ms);
+/* particles pushed so far by a species, summed over its steps (particle-steps) */
+ZC_API zc_status zc1_species_pushed(zc1_sim *sim, int species, long long *pushed);
 /* kernels the steps of this simulation have launched so far */
 ZC_API zc_status zc1_get_launches(zc1_sim *sim, long long *launches);
 /* per-kernel device time: with profiling on, every kernel of a step is
@@ -269,7 +283,6 @@ ZC_API zc_status zc1_energy(zc1_sim *sim, double emf_energy[6], double *kin_ener
 ZC_API zc_status zc1_species_count(zc1_sim *sim, int species, int *np);
 ZC_API zc_status zc1_get_particles(zc1_sim *sim, int species, zc1_part *out, int cap, int *np);
 ZC_API zc_status zc1_get_info(zc1_sim *sim, int *iter, int *n_move);
-ZC_API zc_status zc1_synchronize(zc1_sim *sim);
 ZC_API zc_status zc_set_current(zc_sim *sim, const float *J_buf);
 /* field energy per component (emf_get_energy, em2d/emf.c:729-750) and the
  * time-centred kinetic energy of each species after its last advance

@@ -220,6 +220,32 @@ def test_em1d_wide_matches_oracle(name, tmp_path):
     _check_run(WIDE_1D[name], np.load(out))
 
 
+@pytest.mark.gpu
+def test_em1d_async_side_by_side():
+    """Two simulations stepped side by side (zc1_step_async on their own
+    streams, interleaved) keep the fixtures' per-step bars; the device's
+    pushed count equals the sum of the per-step counts."""
+    runs = []
+    for name in ("lwfa", "open_slab"):
+        g = np.load(os.path.join(GOLD, name + ".npz"))
+        runs.append((DECKS_1D[name], g, _mirror(DECKS_1D[name], g)))
+    steps = min(d["steps"] for d, _, _ in runs)
+    pushed_ref = [0, 0]
+    for step in range(steps):
+        for r, (d, g, sim) in enumerate(runs):
+            pushed_ref[r] += int(g["np"][step - 1][0]) if step else int(len(g["p0_0"]))
+            sim.step(1, wait=False)
+        for d, g, sim in runs:
+            sim.synchronize()
+            emf, _ = sim.energy()
+            ref = g["emf_energy"][step]
+            assert np.all(np.abs(emf - ref) <= 1e-5 * max(np.abs(ref).max(), 1e-30) + 1e-12), step
+            assert sim.count(0) == g["np"][step][0], step
+    for r, (d, g, sim) in enumerate(runs):
+        assert sim.pushed(0) == pushed_ref[r]
+        sim.close()
+
+
 def _check_run(d, g):
     sim = _mirror(d, g)
     ns = len(d["species"])

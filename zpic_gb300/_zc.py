@@ -43,7 +43,7 @@ EXPORTS = [
     "zc_host_alloc", "zc_host_free", "zc1_create", "zc1_destroy", "zc1_add_species", "zc1_set_smooth",
     "zc1_set_fields", "zc1_get_fields", "zc1_get_current", "zc1_step", "zc1_energy", "zc1_species_count",
     "zc1_get_particles", "zc1_get_info", "zc1_synchronize", "zc1_add_laser", "zc1_last_step_ms",
-    "zc1_get_launches", "zc1_set_profile", "zc1_get_profile",
+    "zc1_get_launches", "zc1_set_profile", "zc1_get_profile", "zc1_step_async", "zc1_species_pushed",
 ]
 NPHASE = 13
 
@@ -183,6 +183,8 @@ def load(path: str = LIB_PATH):
         "zc1_add_laser": [P, P],
         "zc1_last_step_ms": [P, C.POINTER(C.c_float)],
         "zc1_get_launches": [P, C.POINTER(C.c_longlong)],
+        "zc1_step_async": [P, I],
+        "zc1_species_pushed": [P, I, C.POINTER(C.c_longlong)],
         "zc1_set_profile": [P, I],
         "zc1_get_profile": [P, P, P],
     }

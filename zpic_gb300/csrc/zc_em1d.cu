@@ -69,6 +69,7 @@ struct SpecState1 {
   unsigned done;    // CTAs finished in the running launch (0 between launches)
   double ekin_acc;  // kinetic-energy sum of the running advance
   double ekin;      // the sum of the last completed advance
+  long long pushed;  // particles pushed so far (particle-steps)
 };
 
 struct Push1 {
@@ -361,6 +362,7 @@ __global__ void __launch_bounds__(256, 4) k1_push(Parts b0, Parts b1, SpecState1
     st->ekin_acc = 0.0;
     st->iter = iter0 + 1;
     st->n_move = nmove0 + shift;
+    st->pushed += n;
     __threadfence();
     st->done = 0u;
   }
@@ -721,6 +723,7 @@ struct zc1_sim {
   float box, dx, dt;
   int device;
   int field_bc, current_periodic, part_open, mw, sort_every;
+  int push_ctas = 0;         // cap of the push's CTAs (0: one wave)
   int iter = 0, n_move = 0;  // mirrors of the field's device counters
   Smooth1 smooth{};
   cudaStream_t st = nullptr;
@@ -731,6 +734,7 @@ struct zc1_sim {
   size_t fields_smem = 0;  // dynamic shared memory of the fields kernel (0: global variant)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
+  int timing = 0;          // steps enqueued since ev0, not yet waited for
   long long launches = 0;  // kernels launched by the steps so far
   // the captured block of sort_every steps (the last one sorts), and the
   // same block with an event pair around every kernel for profiling
@@ -784,11 +788,16 @@ struct Guard1 {
 };
 
 constexpr int kPushThreads = 256;
-constexpr int kSortBlocks = 152 * 4;
+constexpr int kMaxCtas = 152 * 4;  // the push CTAs resident together (4 per SM)
 
-// CTAs of the push: one particle per thread, up to the 4 CTAs per SM that
-// stay resident together (one wave)
-int push_blocks(int cap) { return std::max(1, std::min(152 * 4, (cap + kPushThreads - 1) / kPushThreads)); }
+// CTAs of the push: one particle per thread, up to one wave, or up to the
+// simulation's own cap (simulations that share the GPU leave each other room)
+int push_blocks(const zc1_sim *s, int cap) {
+  const int most = s->push_ctas > 0 ? std::min(s->push_ctas, kMaxCtas) : kMaxCtas;
+  return std::max(1, std::min(most, (cap + kPushThreads - 1) / kPushThreads));
+}
+
+int sort_blocks(const zc1_sim *s) { return s->push_ctas > 0 ? std::min(s->push_ctas, kMaxCtas) : kMaxCtas; }
 
 zc_status alloc_parts(Parts &p, int cap) {
   CK1(cudaMalloc(&p.ix, sizeof(int) * (size_t)std::max(cap, 1)));
@@ -935,9 +944,9 @@ void prof_collect(zc1_sim *s) {
 int enqueue_sort(zc1_sim *s, Species1 &p) {
   const int pf = prof_begin(s, ZC1_K_SORT);
   cudaMemsetAsync(s->d_cnt, 0, sizeof(int) * s->nx, s->st);
-  k1_cell_count<<<kSortBlocks, 256, 0, s->st>>>(p.buf[0], p.buf[1], p.d_st, s->d_cnt);
+  k1_cell_count<<<sort_blocks(s), 256, 0, s->st>>>(p.buf[0], p.buf[1], p.d_st, s->d_cnt);
   k1_cell_scan<<<1, 1024, 0, s->st>>>(s->d_cnt, s->nx, p.d_st);
-  k1_cell_scatter<<<kSortBlocks, 256, 0, s->st>>>(p.buf[0], p.buf[1], p.d_st, s->d_cnt);
+  k1_cell_scatter<<<sort_blocks(s), 256, 0, s->st>>>(p.buf[0], p.buf[1], p.d_st, s->d_cnt);
   prof_end(s, pf);
   return 3;
 }
@@ -962,7 +971,7 @@ int enqueue_step(zc1_sim *s, bool sort) {
     C.cap = p.cap;
     C.jstride = 3 * (s->nx + GC0 + GC1);
     const int pf = prof_begin(s, ZC1_K_PUSH);
-    k1_push<<<push_blocks(p.cap), kPushThreads, 0, s->st>>>(p.buf[0], p.buf[1], p.d_st, s->E, s->B, s->Jdep, C,
+    k1_push<<<push_blocks(s, p.cap), kPushThreads, 0, s->st>>>(p.buf[0], p.buf[1], p.d_st, s->E, s->B, s->Jdep, C,
                                                             p.inj, s->d_err);
     prof_end(s, pf);
     k += 1;
@@ -1077,6 +1086,7 @@ zc_status zc1_create(const zc1_desc *d, zc1_sim **out) {
   s->current_periodic = s->mw ? 0 : 1;
   s->part_open = d->open_particles ? 1 : 0;
   s->sort_every = d->sort_every > 0 ? d->sort_every : 16;
+  s->push_ctas = d->push_ctas > 0 ? d->push_ctas : 0;
   Guard1 g(s->device);
   const size_t gbytes = sizeof(float) * 3 * (s->nx + GC0 + GC1);
   cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
@@ -1098,12 +1108,16 @@ zc_status zc1_create(const zc1_desc *d, zc1_sim **out) {
   if (e == cudaSuccess) e = cudaMemset(s->mur, 0, sizeof(float) * 12);
   if (e == cudaSuccess) e = cudaMemset(s->d_fs, 0, sizeof(FieldState1));
   if (e == cudaSuccess) e = cudaMemset(s->d_err, 0, sizeof(int));
-  // the fields kernel keeps its four grids in shared memory when they fit
+  // the fields kernel keeps its four grids in shared memory when they fit.
+  // Its dynamic shared-memory ceiling is a property of the kernel for the
+  // whole process, so it is raised to the device's maximum (a ceiling, not an
+  // allocation) rather than to this grid's size, which could lower it below
+  // what another simulation launches with.
   int optin = 0;
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device);
   const size_t smem = 4 * gbytes;
   if (e == cudaSuccess && smem <= (size_t)optin) {
-    e = cudaFuncSetAttribute(k1_fields<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k1_fields<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e == cudaSuccess) s->fields_smem = smem;
   }
   if (e != cudaSuccess) {
@@ -1159,7 +1173,13 @@ zc_status zc1_add_species(zc1_sim *s, const zc1_species_desc *d, const zc1_part 
   p.inj.end = d->end;
   p.inj.dx = s->dx;
   for (int c = 0; c < 3; ++c) p.inj.ufl[c] = d->ufl[c];
-  p.cap = std::max(np + np / 4 + 1024, 1024);
+  // a window that injects fills up to about nx * ppc particles: room for
+  // that from the start keeps the host from reading the count back (a wait
+  // on the stream) while the window fills
+  long long want = std::max(np + np / 4 + 1024, 1024);
+  if (s->mw && d->density != 1) want = std::max(want, (long long)(1.25 * s->nx * d->ppc) + 1024);
+  if (want > (1LL << 30)) return fail1(ZC_EOVERFLOW, "1-D particle buffer above 2^30 particles");
+  p.cap = (int)want;
   for (int b = 0; b < 2; ++b) TRY1(alloc_parts(p.buf[b], p.cap));
   CK1(cudaMalloc(&p.d_st, sizeof(SpecState1)));
   // reference records (AoS) -> SoA
@@ -1272,10 +1292,13 @@ zc_status zc1_get_current(zc1_sim *s, float *J) {
   return ZC_OK;
 }
 
-zc_status zc1_step(zc1_sim *s, int nsteps) {
+zc_status zc1_step_async(zc1_sim *s, int nsteps) {
   if (!s || nsteps < 0) return fail1(ZC_EINVAL, "invalid argument");
   Guard1 g(s->device);
-  CK1(cudaEventRecord(s->ev0, s->st));
+  if (!s->timing) {
+    CK1(cudaEventRecord(s->ev0, s->st));
+    s->timing = 1;
+  }
   int k = 0;
   while (k < nsteps) {
     const bool aligned = !s->sp.empty() && s->sort_every > 0 && s->sp[0].iter % s->sort_every == 0;
@@ -1291,11 +1314,12 @@ zc_status zc1_step(zc1_sim *s, int nsteps) {
       prof_collect(s);
     }
   }
-  CK1(cudaEventRecord(s->ev1, s->st));
-  CK1(cudaEventSynchronize(s->ev1));
-  cudaEventElapsedTime(&s->last_ms, s->ev0, s->ev1);
-  prof_collect(s);
-  return check_err(s);
+  return ZC_OK;
+}
+
+zc_status zc1_step(zc1_sim *s, int nsteps) {
+  TRY1(zc1_step_async(s, nsteps));
+  return zc1_synchronize(s);
 }
 
 zc_status zc1_set_profile(zc1_sim *s, int on) {
@@ -1393,7 +1417,23 @@ zc_status zc1_get_info(zc1_sim *s, int *iter, int *n_move) {
 zc_status zc1_synchronize(zc1_sim *s) {
   if (!s) return fail1(ZC_EINVAL, "null simulation handle");
   Guard1 g(s->device);
+  if (s->timing) {
+    CK1(cudaEventRecord(s->ev1, s->st));
+    CK1(cudaEventSynchronize(s->ev1));
+    cudaEventElapsedTime(&s->last_ms, s->ev0, s->ev1);
+    s->timing = 0;
+  }
   CK1(cudaStreamSynchronize(s->st));
+  prof_collect(s);
+  return check_err(s);
+}
+
+zc_status zc1_species_pushed(zc1_sim *s, int k, long long *pushed) {
+  if (!s || !pushed || k < 0 || k >= (int)s->sp.size()) return fail1(ZC_EINVAL, "invalid argument");
+  Guard1 g(s->device);
+  SpecState1 h;
+  TRY1(read_state(s, s->sp[k], h));
+  *pushed = h.pushed;
   return ZC_OK;
 }
 

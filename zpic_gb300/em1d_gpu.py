@@ -27,7 +27,7 @@ SMOOTH = {"none": 0, "binomial": 1, "compensated": 2}
 class Desc1(C.Structure):
     _fields_ = [("nx", C.c_int), ("box", C.c_float), ("dt", C.c_float), ("device", C.c_int),
                 ("open_fields", C.c_int), ("open_particles", C.c_int), ("moving_window", C.c_int),
-                ("sort_every", C.c_int)]
+                ("sort_every", C.c_int), ("push_ctas", C.c_int)]
 
 
 class SpeciesDesc1(C.Structure):
@@ -41,11 +41,11 @@ def _p(a):
 
 class CudaSim1D:
     def __init__(self, nx, box, dt, *, device=0, open_fields=False, open_particles=False, moving_window=False,
-                 sort_every=0):
+                 sort_every=0, push_ctas=0):
         self.lib = _zc.load()
         self.nx = int(nx)
         d = Desc1(self.nx, float(box), float(dt), int(device), int(bool(open_fields)), int(bool(open_particles)),
-                  int(bool(moving_window)), int(sort_every))
+                  int(bool(moving_window)), int(sort_every), int(push_ctas))
         h = C.c_void_p()
         _zc._ck(self.lib.zc1_create(C.byref(d), C.byref(h)))
         self.h = h
@@ -101,8 +101,22 @@ class CudaSim1D:
                       fall=float(fall), a0=float(a0), omega0=float(omega0), polarization=float(polarization))
         _zc._ck(self.lib.zc1_add_laser(self.h, C.byref(L)))
 
-    def step(self, n=1):
-        _zc._ck(self.lib.zc1_step(self.h, int(n)))
+    def step(self, n=1, wait=True):
+        """n steps; with wait=False they are only enqueued (simulations then
+        overlap on the GPU) until synchronize()"""
+        if wait:
+            _zc._ck(self.lib.zc1_step(self.h, int(n)))
+        else:
+            _zc._ck(self.lib.zc1_step_async(self.h, int(n)))
+
+    def synchronize(self):
+        _zc._ck(self.lib.zc1_synchronize(self.h))
+
+    def pushed(self, k):
+        """particles species k has pushed so far (particle-steps)"""
+        v = C.c_longlong()
+        _zc._ck(self.lib.zc1_species_pushed(self.h, int(k), C.byref(v)))
+        return v.value
 
     def launches(self):
         """kernels launched by the steps so far"""
