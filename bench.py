@@ -327,8 +327,8 @@ def run_lwfa(args):
     start 17, focus 20, axis 25.6, polarisation along y (polarization 0);
     cold electrons of density 1 from x = 20, 4 x 2 ppc; binomial smoothing
     along x, level 4.  The particles are loaded as spec_new does; the column
-    the window uncovers is injected from the host, as
-    spec_move_window does."""
+    the window uncovers is drawn on the device as spec_move_window draws it
+    for a cold species (--host-injection: from the host provider)."""
     from zpic_gb300 import em2d
     from zpic_gb300._zc import PART_DTYPE, CudaSim
 
@@ -352,7 +352,11 @@ def run_lwfa(args):
     sim.add_laser(type="gaussian", start=17.0, fwhm=2.0, a0=2.0, omega0=10.0, W0=4.0, focus=20.0, axis=25.6,
                   polarization=0.0)
     sim.set_moving_window()
-    sim.set_injector(lambda species, n_move: col)
+    if args.host_injection:
+        sim.set_injector(lambda species, n_move: col)
+    else:
+        sim.set_device_injector(0, "step", start=20.0)
+        sim.set_graphs(True)  # blocks keyed by their window moves and injected lattice
     sim.set_smooth("binomial", 4, "none", 0)
     n0 = sim.count(0)
     clk = ClockSampler(0)
@@ -373,8 +377,11 @@ def run_lwfa(args):
                                "Gaussian laser a0 2 omega0 10 W0 4 FWHM 2 start 17 focus 20 pol y, density 1 "
                                "from x=20, 4x2 ppc cold, binomial x smoothing level 4",
                    "particles_start": int(n0), "particles_end": int(n1), "window_moves": info["n_move"],
+                   "injection": "host provider" if args.host_injection else "device",
+                   "graphs": not args.host_injection, "graph_captures": info["captures"],
                    "push_build": "exact" if args.exact else "fast"},
-        "how": "value = mean particle count x steps / device time of zc_step(3000) (host injection included)",
+        "how": "value = mean particle count x steps / device time of zc_step(3000) (injection included: "
+               + ("host provider" if args.host_injection else "drawn on the device") + ")",
         "wake": {"on_axis_Ex_max_abs": float(np.abs(Ex).max()), "on_axis_Ex_rms": float(np.sqrt(np.mean(Ex ** 2)))},
         "clocks": clocks,
     }
@@ -879,6 +886,8 @@ def main():
     ap.add_argument("--fd-study", action="store_true", help="wakefield adjoint: finite differences at shrinking steps")
     ap.add_argument("--scan-runs", type=int, default=256)
     ap.add_argument("--scan-group", type=int, default=0, help="runs per batch graph (0: all)")
+    ap.add_argument("--host-injection", action="store_true",
+                    help="lwfa: the window's new column from the host provider instead of the device")
     args = ap.parse_args()
     args.steps_given = any(a.startswith("--steps") for a in sys.argv[1:])
     args.scan_runs_given = any(a.startswith("--scan-runs") for a in sys.argv[1:])

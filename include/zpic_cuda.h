@@ -151,6 +151,20 @@ ZC_API zc_status zc_species_inject(zc_sim *sim, int species, const zc_part *part
 ZC_API zc_status zc_species_get_particles(zc_sim *sim, int species, zc_part *out, int cap, int *np);
 ZC_API zc_status zc_species_count(zc_sim *sim, int species, int *np);
 ZC_API zc_status zc_set_injector(zc_sim *sim, zc_inject_fn fn, void *user);
+/* Window injection drawn on the device for a cold species (uth = 0), instead
+ * of the provider: after each window move, the species' ppc lattice in every
+ * row of column nx-1 that passes the density test, with momenta ufl
+ * (spec_move_window + spec_inject_particles + spec_set_x/spec_set_u,
+ * em2d/particles.c:159-354, 476-492, 619-640).  Profiles: 0 uniform,
+ * 1 empty, 2 step (start), 3 slab (start, end).  The reference's generator
+ * is not advanced (a cold species draws nothing from it that matters, but a
+ * later thermal draw would see a different sequence). */
+typedef struct {
+    int type;
+    float start, end;
+    float ufl[3];
+} zc_column_profile;
+ZC_API zc_status zc_set_device_injection(zc_sim *sim, int species, const zc_column_profile *prof);
 
 /* --- configuration ------------------------------------------------------- */
 /* replaces sim_set_smooth (em2d/simulation.c:134-147) */

@@ -147,6 +147,59 @@ def test_moving_window_matches_oracle(name):
     assert g.info()["n_move"] == cpu.n_move()
 
 
+@pytest.mark.parametrize("name", ["lwfa_window", "window_smooth_xy"])
+def test_moving_window_device_injection(name):
+    """The window's new column drawn on the device (zc_set_device_injection,
+    cold step profile) against the oracle's spec_move_window: the same
+    particle counts every step, fields within 1e-5, the particles of the
+    injected column identical."""
+    cpu, g = mirror(name)
+    sp = DECKS[name]["species"][0]
+    assert not any(sp.get("uth", [0, 0, 0]))
+    dens = sp["density"]
+    g.set_device_injector(0, dens["type"], start=dens.get("start", 0.0), end=dens.get("end", 0.0),
+                          ufl=sp.get("ufl", (0.0, 0.0, 0.0)))
+    for step in range(40):
+        cpu.iter()
+        g.step(1)
+        assert g.count(0) == cpu.np_(0), step
+        for f in ("E", "B"):
+            err = field_err(getattr(g, f)(), getattr(cpu, f)())
+            assert err <= 1e-5, f"{f} relative error {err:.2e} at step {step}"
+    assert g.info()["n_move"] == cpu.n_move()
+    # the last column: particles that entered with the latest moves
+    nx = cpu.nx[0]
+    a, b = canon(cpu.particles(0)), canon(g.particles(0))
+    ca, cb = a[a["ix"] == nx - 1], b[b["ix"] == nx - 1]
+    assert ca.size == cb.size and ca.size > 0
+    assert np.allclose(np.sort(ca["x"]), np.sort(cb["x"]), atol=1e-5)
+    assert np.array_equal(np.bincount(ca["iy"], minlength=cpu.nx[1]), np.bincount(cb["iy"], minlength=cpu.nx[1]))
+
+
+@pytest.mark.parametrize("name", ["lwfa_window", "window_smooth_xy"])
+def test_moving_window_graph_replay(name):
+    """Moving window with device injection under graph replay (blocks keyed
+    by their window moves and injected lattice): particle counts and fields
+    against the oracle after every call, calls of 4 steps so that blocks
+    start both aligned and mid-way, and graphs actually captured."""
+    cpu, g = mirror(name)
+    sp = DECKS[name]["species"][0]
+    dens = sp["density"]
+    g.set_device_injector(0, dens["type"], start=dens.get("start", 0.0), end=dens.get("end", 0.0),
+                          ufl=sp.get("ufl", (0.0, 0.0, 0.0)))
+    g.set_graphs(True)
+    for call in range(16):
+        n = 4 if call % 3 else 20
+        cpu.iter(n)
+        g.step(n)
+        assert g.count(0) == cpu.np_(0), call
+        for f in ("E", "B"):
+            err = field_err(getattr(g, f)(), getattr(cpu, f)())
+            assert err <= 1e-5, f"{f} relative error {err:.2e} after call {call}"
+    assert g.info()["n_move"] == cpu.n_move()
+    assert g.info()["captures"] > 0
+
+
 @pytest.mark.parametrize("name", ["lwfa_window", "plane_slab"])
 def test_laser_launch(name):
     """The GPU laser kernel against the oracle's emf_add_laser."""

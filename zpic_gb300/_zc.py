@@ -44,6 +44,7 @@ EXPORTS = [
     "zc1_set_fields", "zc1_get_fields", "zc1_get_current", "zc1_step", "zc1_energy", "zc1_species_count",
     "zc1_get_particles", "zc1_get_info", "zc1_synchronize", "zc1_add_laser", "zc1_last_step_ms",
     "zc1_get_launches", "zc1_set_profile", "zc1_get_profile", "zc1_step_async", "zc1_species_pushed",
+    "zc_set_device_injection",
 ]
 NPHASE = 13
 
@@ -83,6 +84,10 @@ class Laser(C.Structure):
                 ("flat", C.c_float), ("fall", C.c_float), ("a0", C.c_float), ("omega0", C.c_float),
                 ("polarization", C.c_float), ("W0", C.c_float), ("focus", C.c_float),
                 ("axis", C.c_float)]
+
+
+class ColumnProfile(C.Structure):
+    _fields_ = [("type", C.c_int), ("start", C.c_float), ("end", C.c_float), ("ufl", C.c_float * 3)]
 
 
 class Info(C.Structure):
@@ -184,6 +189,7 @@ def load(path: str = LIB_PATH):
         "zc1_last_step_ms": [P, C.POINTER(C.c_float)],
         "zc1_get_launches": [P, C.POINTER(C.c_longlong)],
         "zc1_step_async": [P, I],
+        "zc_set_device_injection": [P, I, P],
         "zc1_species_pushed": [P, I, C.POINTER(C.c_longlong)],
         "zc1_set_profile": [P, I],
         "zc1_get_profile": [P, P, P],
@@ -312,6 +318,13 @@ class CudaSim:
 
         self._inj = (INJECT_FN(cb), keep)
         _ck(self.lib.zc_set_injector(self.h, self._inj[0], None))
+
+    def set_device_injector(self, species, density="uniform", start=0.0, end=0.0, ufl=(0.0, 0.0, 0.0)):
+        """window injection drawn on the device for a cold species: density
+        "uniform", "empty", "step" (start) or "slab" (start, end)"""
+        types = {"uniform": 0, "empty": 1, "step": 2, "slab": 3}
+        prof = ColumnProfile(types[density], float(start), float(end), (C.c_float * 3)(*ufl))
+        _ck(self.lib.zc_set_device_injection(self.h, int(species), C.byref(prof)))
 
     # ---- configuration ----
     def set_smooth(self, xtype="none", xlevel=0, ytype="none", ylevel=0):

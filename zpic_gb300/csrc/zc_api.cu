@@ -123,6 +123,9 @@ struct SpeciesState {
   bool pending = false;
   // energy
   double *d_ekin_tile = nullptr, *d_ekin_extra = nullptr, *d_ekin = nullptr;
+  // window injection drawn on the device (zc_set_device_injection)
+  int dinj = 0;
+  zc_column_profile dprof{};
 };
 
 // host state that a step changes (buffer parities and counters)
@@ -200,6 +203,10 @@ struct zc_sim {
   // prefix of a block for the remainder of a call
   int use_graph = 0;
   StepGraph blk, tail;
+  // moving-window blocks (every species injecting on the device), one per
+  // signature of the block's host decisions (window moves, injected lattice)
+  std::vector<StepGraph> mw_blk;
+  std::vector<std::vector<long long>> mw_sig;
   int n_relayout = 0, n_capture = 0;
   cudaEvent_t ev_blk[2] = {nullptr, nullptr};
   // per-step energy history on the device: row = 6 field components, then
@@ -486,6 +493,9 @@ zc_status set_current_scale(zc_sim *s, const SpeciesState &p, PushConst &C) {
   return ZC_OK;
 }
 
+zc_status inject_column_device(zc_sim *s, SpeciesState &p);
+int column_lattice(const zc_sim *s, const SpeciesState &p, int n_move, ColumnInject &C, unsigned long long &mask);
+
 zc_status spec_advance_impl(zc_sim *s, int k) {
   SpeciesState &p = s->sp[k];
   cudaStream_t st = s->st;
@@ -566,7 +576,10 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
                          s->deterministic, st));
   }
   p.iter += 1;
-  if (shift) {
+  if (shift && p.dinj) {
+    p.n_move += 1;
+    TRY(inject_column_device(s, p));
+  } else if (shift) {
     p.n_move += 1;
     if (!s->inj) return fail(ZC_ESTATE, "moving window needs an injection provider (zc_set_injector)");
     const zc_part *parts = nullptr;
@@ -603,6 +616,63 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
       CK(cudaFreeAsync(d_tile_cnt, st));
     }
   }
+  return ZC_OK;
+}
+
+// the column a window move uncovers, drawn on the device for a cold species
+// (spec_move_window + spec_inject_particles, em2d/particles.c:476-492,
+// 619-640): the ppc lattice of every row of column nx-1 that passes the
+// uniform / step / slab test, momenta ufl (a cold species' thermal part is
+// zero and so is its per-cell mean).  The lattice offsets and the density
+// test use the reference's float and double arithmetic.
+// the lattice positions of column nx-1 that pass the density test at window
+// offset n_move, in spec_set_x's order (bit q of mask: lattice point q);
+// returns their count
+int column_lattice(const zc_sim *s, const SpeciesState &p, int n_move, ColumnInject &C, unsigned long long &mask) {
+  const zc_column_profile &D = p.dprof;
+  C = ColumnInject{};
+  mask = 0;
+  if (D.type == 1) return 0;  // empty
+  C.ix = s->G.nx - 1;
+  C.ny = s->G.ny;
+  const float dpcx = 1.0f / p.ppc[0], dpcy = 1.0f / p.ppc[1];
+  const float start = D.start / s->dx[0] - n_move;
+  const float end = D.end / s->dx[0] - n_move;
+  int cnt = 0;
+  for (int jj = 0; jj < p.ppc[1]; ++jj)
+    for (int ii = 0; ii < p.ppc[0]; ++ii) {
+      const float x = (float)(dpcx * (ii + 0.5));
+      const float y = (float)(dpcy * (jj + 0.5));
+      bool take = true;
+      if (D.type == 2) take = C.ix + x > start;
+      if (D.type == 3) take = C.ix + x > start && C.ix + x < end;
+      if (take) {
+        mask |= 1ULL << (jj * p.ppc[0] + ii);
+        C.px[cnt] = x;
+        C.py[cnt] = y;
+        ++cnt;
+      }
+    }
+  C.cnt = cnt;
+  C.ux = D.ufl[0];
+  C.uy = D.ufl[1];
+  C.uz = D.ufl[2];
+  return cnt;
+}
+
+zc_status inject_column_device(zc_sim *s, SpeciesState &p) {
+  ColumnInject C;
+  unsigned long long mask = 0;
+  const int cnt = column_lattice(s, p, p.n_move, C, mask);
+  if (cnt == 0) return ZC_OK;
+  const int n = C.ny * cnt;
+  // sized by zc_set_device_injection for a whole column (no sync here: the
+  // step may be under graph capture)
+  if (n > s->inj_list_cap) return fail(ZC_ESTATE, "device injection list too small");
+  Phase ph(s, ZC_PHASE_WINDOW, 2);
+  CK(launch_inject_column(s->inj_list, C, s->st));
+  CK(launch_append_list(s->inj_list, n, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur), layout(s),
+                        s->d_err, s->st));
   return ZC_OK;
 }
 
@@ -714,6 +784,9 @@ void drop_graph(StepGraph &g) {
 void invalidate_graph(zc_sim *s) {
   drop_graph(s->blk);
   drop_graph(s->tail);
+  for (auto &g : s->mw_blk) drop_graph(g);
+  s->mw_blk.clear();
+  s->mw_sig.clear();
 }
 
 // steps per captured block: the buffer parities (particle buffers, outboxes,
@@ -813,16 +886,61 @@ void account_steps(zc_sim *s, const StepGraph &g) {
     p.cur = g.after.cur[k];
     p.spill_cur = g.after.spill_cur[k];
     p.ob_in = g.after.ob_in[k];
+    p.n_move += g.after.sp_n_move[k] - g.before.sp_n_move[k];
   }
+  s->n_move += g.after.n_move - g.before.n_move;
   s->eb_cur = g.after.eb_cur;
   s->j_cur = g.after.j_cur;
   for (int k = 0; k < ZC_NPHASE; ++k) s->prof_launch[k] += g.after.launch[k] - g.before.launch[k];
 }
 
 // Captured blocks replace eager steps when graphs are on and nothing in the
-// step needs the host: no moving window (its injection calls back into the
-// host) and no per-phase event timing.
-bool graph_possible(const zc_sim *s) { return s->use_graph && !s->mw && !s->profiling && !s->sp.empty(); }
+// step needs the host: no per-phase event timing, and under a moving window
+// every species injecting on the device (a provider calls back into the
+// host).
+bool graph_possible(const zc_sim *s) {
+  if (!s->use_graph || s->profiling || s->sp.empty()) return false;
+  if (s->mw)
+    for (const auto &p : s->sp)
+      if (!p.dinj) return false;
+  return true;
+}
+
+// the host decisions of the next n steps of a moving-window run, replayed
+// from the counters with the step's own float tests: per species and step
+// whether the window moves (spec_move_window, particles.c:621) and then the
+// lattice the injection takes, per step whether the fields move
+// (emf_move_window, emf.c:650).  A captured block is valid wherever its
+// signature repeats.
+std::vector<long long> block_signature(const zc_sim *s, int n) {
+  std::vector<long long> sig;
+  std::vector<int> it(s->sp.size()), nm(s->sp.size());
+  for (size_t k = 0; k < s->sp.size(); ++k) {
+    it[k] = s->sp[k].iter;
+    nm[k] = s->sp[k].n_move;
+  }
+  int iter = s->iter, nmove = s->n_move;
+  for (int step = 0; step < n; ++step) {
+    for (size_t k = 0; k < s->sp.size(); ++k) {
+      const int i1 = it[k] + 1;
+      const int shift = ((i1 * s->dt) > (s->dx[0] * (nm[k] + 1))) ? 1 : 0;
+      it[k] = i1;
+      sig.push_back(shift);
+      if (shift) {
+        nm[k] += 1;
+        ColumnInject C;
+        unsigned long long mask = 0;
+        column_lattice(s, s->sp[k], nm[k], C, mask);
+        sig.push_back((long long)mask);
+      }
+    }
+    iter += 1;
+    const int fshift = ((iter * s->dt) > s->dx[0] * (nmove + 1)) ? 1 : 0;
+    nmove += fshift;
+    sig.push_back(fshift);
+  }
+  return sig;
+}
 
 // Runs *nsteps by graph replay where it can: eager steps up to a block
 // boundary, whole blocks, then the rest as a prefix of a block (its graph is
@@ -860,6 +978,63 @@ zc_status step_graph(zc_sim *s, int *nsteps) {
     CK(cudaGraphLaunch(s->tail.exec, s->st));
     account_steps(s, s->tail);
     *nsteps = 0;
+  }
+  return ZC_OK;
+}
+
+// step_graph for a moving window with device injection: blocks are keyed by
+// their signature (window moves, injected lattice) as well as the buffer
+// parities; a few dozen signatures recur along a run.  The rest of a call
+// that is shorter than a block runs eagerly.
+zc_status step_graph_mw(zc_sim *s, int *nsteps) {
+  const int P = block_period(s);
+  while (*nsteps > 0 && s->iter % P != 0) {
+    TRY(iter_impl(s));
+    --*nsteps;
+  }
+  constexpr size_t kMaxBlocks = 64;
+  int launched = 0;
+  while (*nsteps >= P) {
+    const std::vector<long long> sig = block_signature(s, P);
+    const Counters now = save_counters(s);
+    StepGraph *g = nullptr;
+    for (size_t i = 0; i < s->mw_blk.size(); ++i)
+      if (s->mw_blk[i].valid && s->mw_blk[i].nsteps == P && s->mw_sig[i] == sig &&
+          same_parities(s->mw_blk[i].before, now)) {
+        g = &s->mw_blk[i];
+        break;
+      }
+    if (!g) {
+      if (s->mw_blk.size() >= kMaxBlocks) {
+        drop_graph(s->mw_blk.front());
+        s->mw_blk.erase(s->mw_blk.begin());
+        s->mw_sig.erase(s->mw_sig.begin());
+      }
+      s->mw_blk.emplace_back();
+      s->mw_sig.push_back(sig);
+      const zc_status st = capture_steps(s, P, s->mw_blk.back());
+      if (st != ZC_OK) {
+        s->mw_blk.pop_back();
+        s->mw_sig.pop_back();
+        return st;
+      }
+      g = &s->mw_blk.back();
+    }
+    CK(cudaGraphLaunch(g->exec, s->st));
+    account_steps(s, *g);
+    *nsteps -= P;
+    const int b = launched & 1;
+    CK(cudaMemcpyAsync(s->h_pinned + 2 + b, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaEventRecord(s->ev_blk[b], s->st));
+    if (launched > 0) {
+      CK(cudaEventSynchronize(s->ev_blk[1 - b]));
+      if (s->h_pinned[3 - b]) {
+        CK(cudaStreamSynchronize(s->st));
+        s->h_pinned[2] = s->h_pinned[3] = 0;
+        TRY(check_errors(s, true));
+      }
+    }
+    ++launched;
   }
   return ZC_OK;
 }
@@ -1278,6 +1453,27 @@ zc_status zc_species_get_particles(zc_sim *s, int k, zc_part *out, int cap, int 
   return ZC_OK;
 }
 
+zc_status zc_set_device_injection(zc_sim *s, int k, const zc_column_profile *prof) {
+  if (!s || !prof) return fail(ZC_EINVAL, "null argument");
+  if (k < 0 || k >= (int)s->sp.size()) return fail(ZC_EINVAL, "invalid species");
+  if (prof->type < 0 || prof->type > 3) return fail(ZC_EINVAL, "device injection takes uniform, empty, step or slab");
+  SpeciesState &p = s->sp[k];
+  if (p.ppc[0] <= 0 || p.ppc[1] <= 0 || p.ppc[0] * p.ppc[1] > 64)
+    return fail(ZC_EINVAL, "device injection takes up to 64 particles per cell");
+  DeviceGuard g(s->device);
+  const long long need = (long long)s->G.ny * p.ppc[0] * p.ppc[1];
+  if (need > s->inj_list_cap) {
+    CK(cudaStreamSynchronize(s->st));
+    free_particles(s->inj_list);
+    TRY(alloc_particles(s->inj_list, need));
+    s->inj_list_cap = need;
+  }
+  p.dprof = *prof;
+  p.dinj = 1;
+  invalidate_graph(s);
+  return ZC_OK;
+}
+
 zc_status zc_set_injector(zc_sim *s, zc_inject_fn fn, void *user) {
   if (!s) return fail(ZC_EINVAL, "null simulation handle");
   s->inj = fn;
@@ -1385,7 +1581,7 @@ zc_status zc_step(zc_sim *s, int nsteps) {
   if (nsteps < 0) return fail(ZC_EINVAL, "nsteps must be >= 0");
   DeviceGuard g(s->device);
   CK(cudaEventRecord(s->ev0, s->st));
-  if (graph_possible(s)) TRY(step_graph(s, &nsteps));
+  if (graph_possible(s)) TRY(s->mw ? step_graph_mw(s, &nsteps) : step_graph(s, &nsteps));
   for (int n = 0; n < nsteps; ++n) {
     TRY(iter_impl(s));
     // spill lists are drained into the tiles at least every 16 steps

@@ -152,6 +152,15 @@ cudaError_t launch_tile_order(const Particles &src, const unsigned *key, const i
                               const Particles &dst, int ntiles, int smax, const LayoutConst &L, cudaStream_t st);
 cudaError_t launch_append_list(const Particles &list, int n, const Particles &buf, const TileSet &T,
                                const Spill &S, const LayoutConst &L, int *err, cudaStream_t st);
+// a column of cold particles injected after a window move: per row of the
+// column, the ppc lattice positions that pass the density test, in the order
+// of spec_set_x (em2d/particles.c:159-211, 335-349)
+struct ColumnInject {
+  int ix, ny, cnt;  // column, rows, particles per cell
+  float ux, uy, uz;
+  float px[64], py[64];
+};
+cudaError_t launch_inject_column(const Particles &list, const ColumnInject &C, cudaStream_t st);
 cudaError_t launch_gather_aos(const Particles &buf, const int *off, const int *np, const long long *dst_off,
                               int *aos, int ntiles, cudaStream_t st);
 cudaError_t launch_list_to_aos(const Particles &list, const int *n_ptr, int n_cap, int *aos, long long d0,

@@ -573,6 +573,21 @@ cudaError_t launch_settle(const Particles &buf, const TileSet &T, const Outbox &
   return cudaGetLastError();
 }
 
+__global__ void k_inject_column(Particles list, ColumnInject C) {
+  const int n = C.ny * C.cnt;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int j = t / C.cnt, q = t - j * C.cnt;
+    store_particle(list, t, C.ix, j, C.px[q], C.py[q], C.ux, C.uy, C.uz);
+  }
+}
+
+cudaError_t launch_inject_column(const Particles &list, const ColumnInject &C, cudaStream_t st) {
+  const int n = C.ny * C.cnt;
+  if (n <= 0) return cudaSuccess;
+  k_inject_column<<<(n + 255) / 256, 256, 0, st>>>(list, C);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, int *cnt, const LayoutConst &L,
                                  int *err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
