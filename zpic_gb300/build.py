@@ -84,6 +84,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
           "-fvisibility=hidden", os.path.join(CSRC, "em2d", "em2d_host.c"), os.path.join(CSRC, "em2d", "zdf_io.c"),
           "-o", em2d + ".tmp", "-L", LIBDIR, "-lzpic_cuda", "-Wl,-rpath,$ORIGIN", "-lm"])
     os.replace(em2d + ".tmp", em2d)
+    # the em1d drop-in C API over the 1-D step (zc1_*)
+    em1d = os.path.join(LIBDIR, "libzpic_em1d.so")
+    _run([os.environ.get("CC", "gcc"), "-O2", "-std=c99", "-D_DEFAULT_SOURCE", "-fPIC", "-shared", "-pthread",
+          "-fvisibility=hidden", os.path.join(CSRC, "em1d", "em1d_host.c"), os.path.join(CSRC, "em2d", "zdf_io.c"),
+          "-o", em1d + ".tmp", "-L", LIBDIR, "-lzpic_cuda", "-Wl,-rpath,$ORIGIN", "-lm"])
+    os.replace(em1d + ".tmp", em1d)
     return lib
 
 
