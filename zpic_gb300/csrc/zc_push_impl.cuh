@@ -537,28 +537,29 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     }
     errbits |= (valid && bad) ? ERR_ESCAPE : 0;
     const bool split = valid && ((di != 0) || (dj != 0));
+    const bool single = valid && !split;
     // the whole motion inside the cell: one segment (particles.c:781-797);
-    // crossing motions are queued below and contribute nothing here
+    // crossing motions are queued below and contribute nothing here: every
+    // contribution is proportional to dx, dy or qvz, so zeroing those three
+    // zeroes all eight
     Seg a;
     a.x0 = x;
     a.y0 = y;
-    a.dx = mx;
-    a.dy = my;
+    a.dx = single ? mx : 0.f;
+    a.dy = single ? my : 0.f;
     a.x1 = x + mx;
     a.y1 = y + my;
-    a.qvz = qvz * 0.5f;
+    a.qvz = single ? qvz * 0.5f : 0.f;
     a.ix = li;
     a.iy = lj;
     SegCurrent cur = segment_current(a, Cl.qnx, Cl.qny);
-    const bool single = valid && !split;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) cur.v[q] = single ? cur.v[q] : 0.f;
     const float sx0 = x, sy0 = y, smx = mx, smy = my, sqvz = qvz;
     const int spk = li | (lj << 8) | ((di + 1) << 16) | ((dj + 1) << 18);
     x = x1;
     y = y1;
     const bool keep = apply_boundary(ix, iy, di, dj, Cl);
-    const int dest = ix / TX + (iy / TY) * Cl.ntx;
+    // (the cell is inside the grid when the particle is kept; dest is unused otherwise)
+    const int dest = (int)((unsigned)ix / TX) + (int)((unsigned)iy / TY) * Cl.ntx;
     const int code = (valid && keep) ? ((dest == t) ? 1 : 2) : 0;  // 1 stays, 2 leaves
 
     // segmented warp reduction of the single-segment currents over runs of
