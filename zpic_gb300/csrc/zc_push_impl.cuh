@@ -562,6 +562,33 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     const int dest = (int)((unsigned)ix / TX) + (int)((unsigned)iy / TY) * Cl.ntx;
     const int code = (valid && keep) ? ((dest == t) ? 1 : 2) : 0;  // 1 stays, 2 leaves
 
+    // output slots: one shared-memory atomic per warp and kind; lanes keep
+    // their order inside the warp's run.  Stored before the current sums, so
+    // that the particle's registers are free while they run.
+    const unsigned mstay = __ballot_sync(0xffffffffu, code == 1);
+    const unsigned mleave = __ballot_sync(0xffffffffu, code == 2);
+    int sb = 0, lb = 0;
+    if (lane == 0) {
+      if (mstay) sb = atomicAdd(&s_stay, __popc(mstay));
+      if (mleave) lb = atomicAdd(&s_leave, __popc(mleave));
+    }
+    sb = __shfl_sync(0xffffffffu, sb, 0);
+    lb = __shfl_sync(0xffffffffu, lb, 0);
+    const unsigned below = (1u << lane) - 1;
+    if (code == 1) {
+      const int s = sb + __popc(mstay & below);
+      if (s < cap) store_particle(pout, base + s, ix, iy, x, y, ux, uy, uz);
+      else spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
+    } else if (code == 2) {
+      const int s = lb + __popc(mleave & below);
+      if (s < O.cap) {
+        store_particle(O.p, obase + s, ix, iy, x, y, ux, uy, uz);
+        O.dst[obase + s] = dest;
+      } else {
+        spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
+      }
+    }
+
     // segmented warp reduction of the single-segment currents over runs of
     // lanes that start in the same cell (the runs are contiguous because
     // the tile is sorted by cell; unsorted input only makes runs shorter);
@@ -645,31 +672,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       }
     }
 
-    // output slots: one shared-memory atomic per warp and kind; lanes keep
-    // their order inside the warp's run
-    const unsigned mstay = __ballot_sync(0xffffffffu, code == 1);
-    const unsigned mleave = __ballot_sync(0xffffffffu, code == 2);
-    int sb = 0, lb = 0;
-    if (lane == 0) {
-      if (mstay) sb = atomicAdd(&s_stay, __popc(mstay));
-      if (mleave) lb = atomicAdd(&s_leave, __popc(mleave));
-    }
-    sb = __shfl_sync(0xffffffffu, sb, 0);
-    lb = __shfl_sync(0xffffffffu, lb, 0);
-    const unsigned below = (1u << lane) - 1;
-    if (code == 1) {
-      const int s = sb + __popc(mstay & below);
-      if (s < cap) store_particle(pout, base + s, ix, iy, x, y, ux, uy, uz);
-      else spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
-    } else if (code == 2) {
-      const int s = lb + __popc(mleave & below);
-      if (s < O.cap) {
-        store_particle(O.p, obase + s, ix, iy, x, y, ux, uy, uz);
-        O.dst[obase + s] = dest;
-      } else {
-        spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
-      }
-    }
   };
 
   // incoming particles: warp w scans the outboxes of neighbours w, w + NW,
