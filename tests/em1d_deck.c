@@ -10,7 +10,8 @@
  * Decks: "lwfa" (moving window, laser, cold step plasma injected by the
  * window), "twostream" (two periodic drifting streams), "absorbing" (open
  * fields and particles set by writing the struct fields after sim_new, a
- * laser entering a warm slab).  Reports are written after loading and after
+ * laser entering a warm slab), "density" (a ramp and a custom profile,
+ * compared at loading only).  Reports are written after loading and after
  * the last step, into the working directory.
  */
 #include <math.h>
@@ -86,6 +87,35 @@ static void setup_absorbing(t_simulation *sim)
     sim_set_smooth(sim, &smooth);
 }
 
+static float custom_profile(float x, void *data)
+{
+    (void)data;
+    return 1.0f + 0.5f * sinf(x / 2.0f) * sinf(x / 2.0f);
+}
+
+/* loading only: a linear ramp and a custom profile (periodic, no window) */
+static void setup_density(t_simulation *sim)
+{
+    const int nx = 200;
+    const float box = 10.0f, dt = 0.04f;
+    t_species *sp = (t_species *)malloc(2 * sizeof(t_species));
+    t_density ramp;
+    memset(&ramp, 0, sizeof(ramp));
+    ramp.type = RAMP;
+    ramp.start = 2.0f;
+    ramp.end = 8.0f;
+    ramp.ramp[0] = 0.5f;
+    ramp.ramp[1] = 2.0f;
+    spec_new(&sp[0], "ramp", -1.0f, 16, NULL, NULL, nx, box, dt, &ramp);
+    t_density custom;
+    memset(&custom, 0, sizeof(custom));
+    custom.type = CUSTOM;
+    custom.custom = &custom_profile;
+    const float uth[] = {0.01f, 0.02f, 0.03f};
+    spec_new(&sp[1], "custom", -1.0f, 8, NULL, uth, nx, box, dt, &custom);
+    sim_new(sim, nx, box, dt, 10.0f, 0, sp, 2);
+}
+
 static void reports(t_simulation *sim)
 {
     for (int fc = 0; fc < 3; fc++) {
@@ -116,6 +146,8 @@ int main(int argc, char **argv)
         setup_twostream(&sim);
     else if (!strcmp(argv[1], "absorbing"))
         setup_absorbing(&sim);
+    else if (!strcmp(argv[1], "density"))
+        setup_density(&sim);
     else {
         fprintf(stderr, "unknown deck %s\n", argv[1]);
         return 2;

@@ -21,6 +21,8 @@ REF = "/root/reference/em1d"
 OUT = os.path.join(HERE, "em1d_reports")
 DECK_C = os.path.join(ROOT, "tests", "em1d_deck.c")
 STEPS = {"lwfa": 60, "twostream": 40, "absorbing": 60}
+# decks compared at loading only (profiles the GPU step loads but does not inject)
+LOAD_ONLY = ["density"]
 REF_SRC = ["particles.c", "current.c", "emf.c", "simulation.c", "random.c", "timer.c", "zdf.c"]
 FLAGS = ["-O2", "-std=c99", "-fno-fast-math", "-ffp-contract=off", "-D_DEFAULT_SOURCE", "-w"]
 
@@ -41,7 +43,7 @@ def main():
     with tempfile.TemporaryDirectory() as tmp:
         exe = os.path.join(tmp, "em1d_deck_ref")
         build_reference(exe)
-        for deck, steps in STEPS.items():
+        for deck, steps in list(STEPS.items()) + [(d, 0) for d in LOAD_ONLY]:
             d = os.path.join(OUT, deck)
             shutil.rmtree(d, ignore_errors=True)
             os.makedirs(d)
