@@ -169,9 +169,12 @@ static entry_t *reg_by_species(const t_species *spec, int *idx)
     for (int k = 0; k < MAX_SIMS; k++) {
         entry_t *e = g_reg[k];
         if (!e || !e->sim->species) continue;
-        const ptrdiff_t d = spec - e->sim->species;
-        if (d >= 0 && d < e->sim->n_species) {
-            if (idx) *idx = (int)d;
+        /* an address range test (subtracting pointers into different
+         * arrays is not defined in C) */
+        const uintptr_t a = (uintptr_t)spec, lo = (uintptr_t)e->sim->species;
+        const uintptr_t hi = lo + (uintptr_t)e->sim->n_species * sizeof(t_species);
+        if (a >= lo && a < hi && (a - lo) % sizeof(t_species) == 0) {
+            if (idx) *idx = (int)((a - lo) / sizeof(t_species));
             return e;
         }
     }
