@@ -148,6 +148,15 @@ int main(int argc, char **argv)
         setup_absorbing(&sim);
     else if (!strcmp(argv[1], "density"))
         setup_density(&sim);
+    else if (!strcmp(argv[1], "extfld")) {
+        /* external fields: the 1-D GPU step has none, the drop-in stops */
+        setup_twostream(&sim);
+        t_emf_ext_fld ext;
+        memset(&ext, 0, sizeof(ext));
+        ext.B_type = EMF_FLD_TYPE_UNIFORM;
+        ext.B_0.x = 0.5f;
+        sim_set_ext_fld(&sim, &ext);
+    }
     else {
         fprintf(stderr, "unknown deck %s\n", argv[1]);
         return 2;

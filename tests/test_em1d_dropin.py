@@ -144,6 +144,15 @@ def test_reports_at_load_match_reference(built, tmp_path, deck):
     assert out.splitlines()[0] == open(os.path.join(ref, "stdout.txt")).read().splitlines()[0]
 
 
+def test_external_fields_stop_the_program(built, tmp_path):
+    """The 1-D GPU step has no external fields: the drop-in stops with a
+    message and the reference's exit status for invalid settings."""
+    exe = _build_deck(tmp_path)
+    r = subprocess.run([exe, "extfld", "0"], cwd=str(tmp_path), capture_output=True, text=True, timeout=120)
+    assert r.returncode == 255
+    assert "external fields are not supported" in r.stderr
+
+
 def test_golden_reports_are_the_references(tmp_path):
     """The committed fixtures are what the reference writes (where it exists)."""
     if not os.path.isdir(REF):
