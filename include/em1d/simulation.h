@@ -15,7 +15,12 @@
  * The phase calls current_zero, spec_advance and current_update do nothing;
  * emf_advance runs the whole step.  The reference's own step order
  * (em1d/simulation.c:45-56, mods/em1d_param_scan/main.c) therefore gives the
- * same result, and other orders are not supported. */
+ * same result, and other orders are not supported.
+ *
+ * Like the reference, the library keeps process-global state (the random
+ * generator, the registry of simulations behind the structs): one thread
+ * drives it.  Several simulations may live at once; for scans of many runs
+ * on one GPU, the C-ABI's zc1_step_async is the faster route. */
 #ifndef ZPIC_EM1D_SIMULATION_H
 #define ZPIC_EM1D_SIMULATION_H
 #include <stdint.h>
