@@ -132,3 +132,40 @@ def rel_l2(a, b):
     b = np.asarray(b, dtype=np.float64)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / max(nb, 1e-30))
+
+
+# The benchmark configurations the tests hold to the reference at full size
+# (or, for the 2048^2 thermal plasma, on a 256^2 box of the same density,
+# cell size, time step, ppc and smoothing).
+CONFIG_DECKS = {
+    # Weibel instability: 128^2 cells, box 12.8^2, dt 0.07, two electron
+    # species drifting +-0.6 c along z with uth 0.1, 4x4 ppc each
+    # (524,288 particles), periodic, no smoothing, 500 steps
+    # (em2d/input/weibel.c with electron-electron streams and 4x4 ppc)
+    "c1_weibel": dict(
+        nx=[128, 128], box=[12.8, 12.8], dt=0.07,
+        species=[dict(name="e1", m_q=-1.0, ppc=[4, 4], ufl=[0, 0, 0.6], uth=[0.1, 0.1, 0.1]),
+                 dict(name="e2", m_q=-1.0, ppc=[4, 4], ufl=[0, 0, -0.6], uth=[0.1, 0.1, 0.1])],
+        steps=500),
+    # uniform thermal plasma of the 2048^2 throughput workload on a 256^2
+    # box: dx = dy = 0.1, dt 0.05, uth 0.05, 4x4 ppc (1,048,576 particles),
+    # compensated level-1 smoothing on x and y
+    "c2_thermal_256": dict(
+        nx=[256, 256], box=[25.6, 25.6], dt=0.05,
+        species=[dict(name="e", m_q=-1.0, ppc=[4, 4], uth=[0.05, 0.05, 0.05])],
+        smooth=dict(xtype="compensated", xlevel=1, ytype="compensated", ylevel=1),
+        steps=10),
+    # moving-window laser wakefield: 2000 x 256 cells, box 40 x 51.2,
+    # dt 0.014, 3000 steps; Gaussian laser a0 2, omega0 10, W0 4, FWHM 2,
+    # start 17, focus 20, axis 25.6, polarisation along y; cold electrons of
+    # density 1 from x = 20, 4x2 ppc; binomial x smoothing, level 4
+    # (em2d/input/lwfa.c at the larger box)
+    "c5_lwfa": dict(
+        nx=[2000, 256], box=[40.0, 51.2], dt=0.014,
+        species=[dict(name="e", m_q=-1.0, ppc=[4, 2], density=dict(type="step", start=20.0))],
+        laser=dict(type="gaussian", start=17.0, fwhm=2.0, a0=2.0, omega0=10.0, W0=4.0,
+                   focus=20.0, axis=25.6, polarization=0.0),
+        moving_window=True,
+        smooth=dict(xtype="binomial", xlevel=4),
+        steps=3000),
+}

@@ -111,3 +111,48 @@ def field_err_joint(a, b):
     nb = np.linalg.norm(b)
     na = np.linalg.norm(a - b)
     return 0.0 if nb == 0 and na == 0 else na / max(nb, 1e-30)
+
+
+def field_err_components(a, b):
+    """Relative L2 error of each component over the interior."""
+    a = np.asarray(a, dtype=np.float64)[1:-2, 1:-2]
+    b = np.asarray(b, dtype=np.float64)[1:-2, 1:-2]
+    out = []
+    for c in range(3):
+        nb = np.linalg.norm(b[..., c])
+        na = np.linalg.norm(a[..., c] - b[..., c])
+        out.append(0.0 if nb == 0 and na == 0 else na / max(nb, 1e-30))
+    return np.array(out)
+
+
+def reordered_twin(name, deck=None, seed=0):
+    """The oracle on the same deck with every species' particles in a
+    shuffled buffer order: the same physics, only the float32 order of the
+    current sums differs.  How far it drifts from the oracle in unshuffled
+    order is the floor of any implementation that sums in another order."""
+    twin = build_cpu(name, deck=deck)
+    rng = np.random.default_rng(seed)
+    for k in range(twin.n_species):
+        p = twin.particles(k)
+        twin.set_particles(k, p[rng.permutation(p.size)])
+    return twin
+
+
+def check_fields(g, cpu, twin, where, bar=1e-5):
+    """The spec's bar, per field and per component: each of E, B, J within
+    ``bar`` relative L2 of the oracle as a whole vector field, and each
+    component within ``bar`` or, where summation order alone moves it
+    further (currents that cancel between species or within a cell), within
+    twice the oracle's own drift under reordering (``twin``).  Returns the
+    largest per-component error for reporting."""
+    worst = 0.0
+    for f in ("E", "B", "J"):
+        a, b, t = getattr(g, f)(), getattr(cpu, f)(), getattr(twin, f)()
+        joint = field_err_joint(a, b)
+        assert joint <= bar, f"{f} relative error {joint:.2e} (whole field) {where}"
+        err, floor = field_err_components(a, b), field_err_components(t, b)
+        for c in range(3):
+            assert err[c] <= max(bar, 2 * floor[c]), \
+                f"{f}{'xyz'[c]} relative error {err[c]:.2e} (order floor {floor[c]:.2e}) {where}"
+        worst = max(worst, float(err.max()))
+    return worst

@@ -10,16 +10,18 @@ Bars (written per test):
   net current);
 * full steps: per-step field relative L2 error <= 1e-5 over the first 10
   steps (the bar of the specification).  The exact build meets it for every
-  field component separately; the FMA build is held to it for the whole
-  vector field (its per-component error on weak components, e.g. the plasma
-  Ex beside a laser, reaches ~1.3e-5 after 10 steps);
+  field component separately.  The FMA build meets it for every field as a
+  whole, and for every component except where the oracle itself, run with
+  its particles in another buffer order, drifts by about as much: the weak
+  plasma Ex beside the plane laser moves by 9.8e-6 from reordering alone,
+  and the FMA build's 1.3e-5 there is held to twice that floor;
 * energies: relative error <= 1e-6.
 """
 import numpy as np
 import pytest
 
 from decks import DECKS, build_cpu
-from gpu_util import canon, field_err, field_err_joint, mirror
+from gpu_util import canon, check_fields, field_err, field_err_joint, mirror, reordered_twin
 
 pytestmark = pytest.mark.gpu
 
@@ -96,13 +98,17 @@ def test_emf_advance_bit_exact(name):
 @pytest.mark.parametrize("name", sorted(n for n in DECKS if not DECKS[n].get("moving_window")))
 def test_steps_match_oracle(name, fast):
     cpu, g = mirror(name, fast_math=fast)
+    twin = reordered_twin(name)
     for step in range(10):
         cpu.iter()
+        twin.iter()
         g.step(1)
-        for f in ("E", "B", "J"):
-            metric = field_err_joint if fast else field_err
-            err = metric(getattr(g, f)(), getattr(cpu, f)())
-            assert err <= 1e-5, f"{f} relative error {err:.2e} at step {step}"
+        if fast:
+            check_fields(g, cpu, twin, f"at step {step}")
+        else:
+            for f in ("E", "B", "J"):
+                err = field_err(getattr(g, f)(), getattr(cpu, f)())
+                assert err <= 1e-5, f"{f} relative error {err:.2e} at step {step}"
         emf_g, kin_g = g.energy()
         emf_c = cpu.emf_energy()
         assert np.all(np.abs(emf_g - emf_c) <= 1e-5 * np.abs(emf_c).max() + 1e-30)
