@@ -457,11 +457,21 @@ ZC_API zc_status zc_adj_times(zc_adj *adj, float *forward_ms, float *backward_ms
  * those calls bring).  Its scratch is a fixed device array of
  * ZC_STATIC_MAX_ROWS rows; larger grids are rejected with ZC_EINVAL.  The
  * first call on a device looks up that array's address, so make it before
- * any stream capture.  All calls share the array: calls that overlap on the
- * GPU race and must be serialised. */
+ * any stream capture.  The address is kept per device ordinal for the
+ * runtime's primary context: callers on another driver-API context of the
+ * device, or after a cudaDeviceReset in the process, are not supported.
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised. */
 #define ZC_STATIC_MAX_ROWS 8192
 ZC_API zc_status zc_field_energy_static(const float *E, const float *B, size_t plane, int pitch, int nx,
                                         int ny, float dx, float dy, double *energy, void *stream);
+
+/* Test hook, no counterpart in the reference: writes the error word that the
+ * kernels set on a failed check (ZC_EPARTICLE_ESCAPE, ZC_ETIMEOUT or
+ * ZC_EOVERFLOW), between steps, so that the next zc_step reports it exactly
+ * as a failure seen on the device; callers exercise their error paths with
+ * it without making a kernel fail.  Other statuses: ZC_EINVAL. */
+ZC_API zc_status zc_post_device_error(zc_sim *sim, zc_status which);
 
 /* message of the last failing call on this thread */
 ZC_API const char *zc_last_error(void);

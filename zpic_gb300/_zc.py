@@ -44,7 +44,7 @@ EXPORTS = [
     "zc1_set_fields", "zc1_get_fields", "zc1_get_current", "zc1_step", "zc1_energy", "zc1_species_count",
     "zc1_get_particles", "zc1_get_info", "zc1_synchronize", "zc1_add_laser", "zc1_last_step_ms",
     "zc1_get_launches", "zc1_set_profile", "zc1_get_profile", "zc1_step_async", "zc1_species_pushed",
-    "zc_set_device_injection",
+    "zc_set_device_injection", "zc_post_device_error",
 ]
 NPHASE = 13
 
@@ -132,6 +132,7 @@ def load(path: str = LIB_PATH):
         "zc_add_laser": [P, C.POINTER(Laser)],
         "zc_set_ext_fld": [P, I, P, P, I, P, P],
         "zc_step": [P, I],
+        "zc_post_device_error": [P, I],
         "zc_current_zero": [P],
         "zc_spec_advance": [P, I],
         "zc_current_update": [P],

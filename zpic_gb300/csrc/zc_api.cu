@@ -1091,6 +1091,21 @@ const char *zc_status_string(zc_status s) {
   return "unknown";
 }
 
+zc_status zc_post_device_error(zc_sim *s, zc_status which) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  const int bits = which == ZC_EPARTICLE_ESCAPE ? ERR_ESCAPE
+                   : which == ZC_ETIMEOUT       ? ERR_TIMEOUT
+                   : which == ZC_EOVERFLOW      ? ERR_OVERFLOW
+                                                : 0;
+  if (!bits) return fail(ZC_EINVAL, "only the statuses the device reports can be posted");
+  // between steps: nothing of this simulation is in flight afterwards
+  CK(cudaStreamSynchronize(s->st));
+  s->h_pinned[0] = bits;
+  CK(cudaMemcpyAsync(s->d_err, s->h_pinned, sizeof(int), cudaMemcpyHostToDevice, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  return ZC_OK;
+}
+
 zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
   if (!d || !out) return fail(ZC_EINVAL, "null argument");
   *out = nullptr;
