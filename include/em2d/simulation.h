@@ -3,10 +3,16 @@
  *
  * Link input decks against libzpic_em2d.so (which loads libzpic_cuda.so).
  * The time step runs on the GPU; t_species.part, t_emf.E_buf/B_buf and
- * t_current.J_buf are host mirrors in the reference layout.  The reporting
- * and energy calls refresh them; a program that reads or edits them directly
- * between steps calls sim_sync_host() before reading and sim_sync_device()
- * after editing (two additions to the reference API). */
+ * t_current.J_buf are host mirrors in the reference layout.  By default
+ * sim_iter keeps them valid as the reference's own buffers are: edits made
+ * to the particle and field mirrors between steps are uploaded before the
+ * step, and every mirror is refreshed after it (particles in the GPU's tile
+ * order).  With ZPIC_EM2D_MIRRORS=demand in the environment at sim_new, the
+ * per-step copies are skipped: the reports refresh what they write, and a
+ * program that reads or edits the mirrors directly calls sim_sync_host()
+ * before reading and sim_sync_device() after editing (two additions to the
+ * reference API).  The per-phase calls (spec_advance, current_update,
+ * emf_advance) never refresh the mirrors. */
 #ifndef ZPIC_EM2D_SIMULATION_H
 #define ZPIC_EM2D_SIMULATION_H
 #include <stdint.h>
@@ -47,6 +53,12 @@ void sim_set_ext_fld(t_simulation *sim, t_emf_ext_fld *ext_fld);
 /* additions: host mirrors <-> GPU state */
 void sim_sync_host(t_simulation *sim);
 void sim_sync_device(t_simulation *sim);
+/* mirror policy of this simulation: 1 kept valid across every sim_iter (the
+ * default), 0 refreshed on demand only (as ZPIC_EM2D_MIRRORS=demand) */
+void sim_set_mirrors(t_simulation *sim, int every_step);
+/* the libzpic_cuda handle behind a simulation (NULL if sim_new did not
+ * create it), for callers that use both APIs on one run */
+struct zc_sim *sim_gpu_handle(t_simulation *sim);
 /* grid forms of emf_set_ext_fld / emf_init_fld: custom fields given as host
  * grids in the reference layout (every buffer cell), for callers whose
  * callbacks cannot return a float3 by value; types as enum emf_fld_type */

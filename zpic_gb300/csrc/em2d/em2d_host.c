@@ -13,8 +13,10 @@
  *   - parameter checks with the reference's exit(-1) behaviour
  *     (em2d/simulation.c:106-110, 136-146; em2d/emf.c:246-270);
  *   - host mirrors of the device state (t_species.part, t_emf.E_buf/B_buf,
- *     t_current.J_buf), refreshed by sim_sync_host (and the particle mirror
- *     by the particle report);
+ *     t_current.J_buf), kept valid across every sim_iter (edits uploaded
+ *     before the step, all mirrors refreshed after it) unless
+ *     ZPIC_EM2D_MIRRORS=demand, in which case sim_sync_host and the reports
+ *     refresh them;
  *   - the ZDF report files, gathered from the device and written on a
  *     background thread (zdf_io.c).
  * Everything per time step (push, deposit, current update, field advance,
@@ -127,6 +129,12 @@ typedef struct {
     zc_sim *gpu;
     zc_part *inj;      /* injection buffer, owned here */
     int inj_cap;
+    /* host mirrors kept valid across sim_iter (see mirrors_mode): the state
+     * of every mirror as last synchronised, to find edits made in between */
+    int mirrors;
+    t_part **shadow;
+    int *shadow_np, *shadow_cap;
+    float3 *shadow_E, *shadow_B;
 } entry_t;
 
 #define MAX_SIMS 4096
@@ -557,6 +565,24 @@ EXPORT double emf_time(void) { return g_emf_time; }
 
 EXPORT int report(int n, int ndump) { return (ndump > 0) ? !(n % ndump) : 0; }
 
+/* Mirror policy of a new simulation.  The reference's structs are read and
+ * written directly by its callers (the Cython module's Species.particles,
+ * EMF.Ex ... views, em2d.pyx:306-312,1055-1060; decks that read
+ * species->part in sim_report).  By default every sim_iter therefore uploads
+ * what was edited in the mirrors since the last step (particles, E, B) and
+ * refreshes every mirror after the step, so direct reads and writes behave
+ * as with the reference.  ZPIC_EM2D_MIRRORS=demand turns that off: the
+ * mirrors are then refreshed only by sim_sync_host and the reports, and
+ * edits are uploaded only by sim_sync_device (no per-step copies). */
+static int mirrors_mode(void)
+{
+    const char *v = getenv("ZPIC_EM2D_MIRRORS");
+    return !(v && strcmp(v, "demand") == 0);
+}
+
+static void shadow_save(entry_t *e);
+static void refresh_mirrors(entry_t *e);
+
 EXPORT void sim_new(t_simulation *sim, int nx[], float box[], float dt, float tmax, int ndump,
                     t_species *species, int n_species)
 {
@@ -598,6 +624,8 @@ EXPORT void sim_new(t_simulation *sim, int nx[], float box[], float dt, float tm
                  "sim_new (species upload)");
     }
     zc_check(zc_set_injector(e->gpu, provide_column, e), "sim_new");
+    e->mirrors = mirrors_mode();
+    if (e->mirrors) shadow_save(e);
 }
 
 EXPORT void sim_delete(t_simulation *sim)
@@ -607,6 +635,13 @@ EXPORT void sim_delete(t_simulation *sim)
     if (e) {
         zc_sim_destroy(e->gpu);
         free(e->inj);
+        if (e->shadow)
+            for (int k = 0; k < sim->n_species; k++) free(e->shadow[k]);
+        free(e->shadow);
+        free(e->shadow_np);
+        free(e->shadow_cap);
+        free(e->shadow_E);
+        free(e->shadow_B);
         memset(e, 0, sizeof(*e));
     }
     for (int k = 0; k < sim->n_species; k++) spec_delete(&sim->species[k]);
@@ -639,11 +674,15 @@ static void after_steps(entry_t *e, int nsteps, int species_only, int k_only)
     g_spec_time += ms * 1e-3;
 }
 
+static void push_host_edits(entry_t *e);
+
 EXPORT void sim_iter(t_simulation *sim)
 {
     entry_t *e = need(reg_by_sim(sim), "sim_iter");
+    if (e->mirrors) push_host_edits(e);
     zc_check(zc_step(e->gpu, 1), "sim_iter");
     after_steps(e, 1, 0, 0);
+    if (e->mirrors) refresh_mirrors(e);
 }
 
 EXPORT void spec_advance(t_species *spec, t_emf *emf, t_current *current)
@@ -729,6 +768,7 @@ EXPORT void emf_add_laser(t_emf *const emf, t_emf_laser *laser)
     L.focus = laser->focus;
     L.axis = laser->axis;
     zc_check(zc_add_laser(e->gpu, &L), "emf_add_laser");
+    if (e->mirrors) refresh_mirrors(e);
 }
 
 EXPORT void sim_set_smooth(t_simulation *sim, t_smooth *smooth)
@@ -795,6 +835,7 @@ EXPORT void emf_set_ext_fld(t_emf *const emf, t_emf_ext_fld *ext)
         if (!emf->ext_fld.B_part_buf) emf->ext_fld.B_part_buf = (float3 *)calloc(n, sizeof(float3));
         emf->B_part = emf->ext_fld.B_part_buf + 1 + emf->nrow;
     } else emf->B_part = emf->B;
+    if (e->mirrors) refresh_mirrors(e);
 }
 
 /* grid forms of emf_set_ext_fld / emf_init_fld for callers whose field
@@ -821,6 +862,7 @@ EXPORT void emf_set_ext_fld_grid(t_emf *const emf, int E_type, const float E0[3]
         if (!emf->ext_fld.B_part_buf) emf->ext_fld.B_part_buf = (float3 *)calloc(n, sizeof(float3));
         emf->B_part = emf->ext_fld.B_part_buf + 1 + emf->nrow;
     } else emf->B_part = emf->B;
+    if (e->mirrors) refresh_mirrors(e);
 }
 
 EXPORT void emf_init_fld_grid(t_emf *const emf, const float *E_grid, const float *B_grid)
@@ -828,6 +870,7 @@ EXPORT void emf_init_fld_grid(t_emf *const emf, const float *E_grid, const float
     entry_t *e = need(reg_by_emf(emf), "emf_init_fld_grid");
     if (emf->iter != 0) die("emf_init_fld should only be called at initialization, aborting...");
     zc_check(zc_set_fields(e->gpu, E_grid, B_grid), "emf_init_fld_grid");
+    if (e->mirrors) refresh_mirrors(e);
 }
 
 EXPORT void emf_init_fld(t_emf *const emf, t_emf_init_fld *init)
@@ -850,6 +893,7 @@ EXPORT void emf_init_fld(t_emf *const emf, t_emf_init_fld *init)
             }
     }
     zc_check(zc_set_fields(e->gpu, (const float *)emf->E_buf, (const float *)emf->B_buf), "emf_init_fld");
+    if (e->mirrors) refresh_mirrors(e);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -865,9 +909,9 @@ static void pull_species(entry_t *e, int k)
     sp->np = np;
 }
 
-EXPORT void sim_sync_host(t_simulation *sim)
+static void sync_host(entry_t *e)
 {
-    entry_t *e = need(reg_by_sim(sim), "sim_sync_host");
+    t_simulation *sim = e->sim;
     zc_check(zc_get_fields(e->gpu, (float *)sim->emf.E_buf, (float *)sim->emf.B_buf), "sim_sync_host");
     if (sim->emf.ext_fld.E_part_buf || sim->emf.ext_fld.B_part_buf)
         zc_check(zc_get_particle_fields(e->gpu, (float *)sim->emf.ext_fld.E_part_buf,
@@ -884,6 +928,38 @@ EXPORT void sim_sync_host(t_simulation *sim)
     free(kin);
 }
 
+EXPORT void sim_sync_host(t_simulation *sim)
+{
+    entry_t *e = need(reg_by_sim(sim), "sim_sync_host");
+    sync_host(e);
+    if (e->mirrors) shadow_save(e);
+}
+
+EXPORT zc_sim *sim_gpu_handle(t_simulation *sim)
+{
+    entry_t *e = reg_by_sim(sim);
+    return e ? e->gpu : NULL;
+}
+
+EXPORT void sim_set_mirrors(t_simulation *sim, int every_step)
+{
+    entry_t *e = need(reg_by_sim(sim), "sim_set_mirrors");
+    e->mirrors = every_step ? 1 : 0;
+    if (e->mirrors) {
+        refresh_mirrors(e);
+        return;
+    }
+    if (e->shadow)  /* the remembered copies are not needed on demand */
+        for (int k = 0; k < sim->n_species; k++) {
+            free(e->shadow[k]);
+            e->shadow[k] = NULL;
+            e->shadow_np[k] = e->shadow_cap[k] = 0;
+        }
+    free(e->shadow_E);
+    free(e->shadow_B);
+    e->shadow_E = e->shadow_B = NULL;
+}
+
 EXPORT void sim_sync_device(t_simulation *sim)
 {
     entry_t *e = need(reg_by_sim(sim), "sim_sync_device");
@@ -892,6 +968,64 @@ EXPORT void sim_sync_device(t_simulation *sim)
     for (int k = 0; k < sim->n_species; k++)
         zc_check(zc_species_set_particles(e->gpu, k, (const zc_part *)sim->species[k].part, sim->species[k].np),
                  "sim_sync_device");
+    if (e->mirrors) shadow_save(e);
+}
+
+static void *xrealloc(void *p, size_t n)
+{
+    void *q = realloc(p, n ? n : 1);
+    if (!q) die("(*error*) out of memory (host mirrors)");
+    return q;
+}
+
+/* remembers every mirror as it is now (after a synchronisation) */
+static void shadow_save(entry_t *e)
+{
+    t_simulation *sim = e->sim;
+    const int ns = sim->n_species;
+    if (!e->shadow) {
+        e->shadow = (t_part **)calloc((size_t)(ns > 0 ? ns : 1), sizeof(t_part *));
+        e->shadow_np = (int *)calloc((size_t)(ns > 0 ? ns : 1), sizeof(int));
+        e->shadow_cap = (int *)calloc((size_t)(ns > 0 ? ns : 1), sizeof(int));
+        if (!e->shadow || !e->shadow_np || !e->shadow_cap) die("(*error*) out of memory (host mirrors)");
+    }
+    for (int k = 0; k < ns; k++) {
+        const t_species *sp = &sim->species[k];
+        if (sp->np > e->shadow_cap[k]) {
+            e->shadow[k] = (t_part *)xrealloc(e->shadow[k], (size_t)sp->np * sizeof(t_part));
+            e->shadow_cap[k] = sp->np;
+        }
+        if (sp->np > 0) memcpy(e->shadow[k], sp->part, (size_t)sp->np * sizeof(t_part));
+        e->shadow_np[k] = sp->np;
+    }
+    const size_t n = (size_t)sim->emf.nrow * (sim->emf.nx[1] + 3) * sizeof(float3);
+    if (!e->shadow_E) e->shadow_E = (float3 *)xrealloc(NULL, n);
+    if (!e->shadow_B) e->shadow_B = (float3 *)xrealloc(NULL, n);
+    memcpy(e->shadow_E, sim->emf.E_buf, n);
+    memcpy(e->shadow_B, sim->emf.B_buf, n);
+}
+
+/* uploads what the caller changed in the mirrors since they were last
+ * synchronised: a species whose count or records differ, and E, B */
+static void push_host_edits(entry_t *e)
+{
+    t_simulation *sim = e->sim;
+    for (int k = 0; k < sim->n_species; k++) {
+        const t_species *sp = &sim->species[k];
+        if (sp->np != e->shadow_np[k] ||
+            (sp->np > 0 && memcmp(sp->part, e->shadow[k], (size_t)sp->np * sizeof(t_part)) != 0))
+            zc_check(zc_species_set_particles(e->gpu, k, (const zc_part *)sp->part, sp->np), "sim_iter");
+    }
+    const size_t n = (size_t)sim->emf.nrow * (sim->emf.nx[1] + 3) * sizeof(float3);
+    if (memcmp(sim->emf.E_buf, e->shadow_E, n) != 0 || memcmp(sim->emf.B_buf, e->shadow_B, n) != 0)
+        zc_check(zc_set_fields(e->gpu, (const float *)sim->emf.E_buf, (const float *)sim->emf.B_buf), "sim_iter");
+}
+
+/* every mirror refreshed from the device */
+static void refresh_mirrors(entry_t *e)
+{
+    sync_host(e);
+    shadow_save(e);
 }
 
 /* ------------------------------------------------------------------------- */

@@ -124,6 +124,8 @@ def _load():
         "sim_set_smooth": (None, [C.POINTER(t_simulation), C.POINTER(t_smooth)]),
         "sim_add_laser": (None, [C.POINTER(t_simulation), C.POINTER(t_emf_laser)]),
         "sim_sync_host": (None, [C.POINTER(t_simulation)]),
+        "sim_set_mirrors": (None, [C.POINTER(t_simulation), C.c_int]),
+        "sim_gpu_handle": (P, [C.POINTER(t_simulation)]),
         "sim_sync_device": (None, [C.POINTER(t_simulation)]),
         "sim_set_gpu_options": (None, [C.c_int, C.c_int, C.c_int, C.c_int]),
         "emf_get_energy": (None, [C.POINTER(t_emf), P]),
@@ -670,6 +672,9 @@ class Simulation:
         self.report = report
         lib.sim_new(self._s, _ptr(self._nx), _ptr(self._box), float(dt), 0.0, 0, self._spec if n else None, n)
         self._alive = True
+        # this class refreshes the mirrors when a view is taken and uploads
+        # edits before a step itself, so the library's per-step copies are off
+        lib.sim_set_mirrors(self._s, 0)
         self.n = 0
         self.t = 0.0
         self.emf = EMF(self)
