@@ -42,16 +42,23 @@ def test_static_energy_matches_zc_energy_on_two_calls():
     from zpic_gb300._zc import CudaSim
 
     out = torch.zeros(6, dtype=torch.float64, device="cuda:0")  # caller-owned output
+    # torch zero-fills `out` on its own stream; the library writes it on the
+    # simulation's stream, so the fill must be finished first
+    torch.cuda.synchronize()
     # the second grid is smaller: rows left in the shared scratch by the first
     # call must not leak into the second result
-    for nx, ny, seed in ((96, 64, 1), (40, 24, 2)):
+    for call, (nx, ny, seed) in enumerate(((96, 64, 1), (40, 24, 2))):
         g = CudaSim([nx, ny], [nx * 0.1, ny * 0.1], 0.05)
         E, B = _fields(nx, ny, seed)
         g.set_fields(E=E, B=B)
         ref, _ = g.energy()
+        g.synchronize()
+        free_before = torch.cuda.mem_get_info(0)[0]
         st = _call_static(g, nx, ny, out)
         assert st == 0, g.lib.zc_last_error().decode()
         g.synchronize()
+        if call:  # after the first call's one-time set-up: no device memory taken
+            assert torch.cuda.mem_get_info(0)[0] == free_before
         got = out.cpu().numpy()
         np.testing.assert_allclose(got, ref, rtol=1e-6)
         g.close()

@@ -28,6 +28,8 @@ namespace {
 static __device__ __align__(256) double g_energy_rows[ZC_STATIC_MAX_ROWS * 6];
 
 // device address of g_energy_rows for each device ordinal, looked up once
+// in the runtime's primary context of that device (a cudaDeviceReset in
+// the host process makes the cached address stale)
 constexpr int kMaxDevices = 64;
 double *g_rows_addr[kMaxDevices] = {};
 std::mutex g_rows_mutex;
@@ -104,6 +106,9 @@ extern "C" ZC_API zc_status zc_field_energy_static(const float *E, const float *
     rows = g_rows_addr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
+  // clear an error left by earlier, unrelated work, so that only this call's
+  // launch errors are reported below
+  (void)cudaGetLastError();
   k_energy_rows<<<ny, 256, 0, st>>>(E, B, plane, pitch, nx, rows);
   k_energy_rows_sum<<<1, 32, 0, st>>>(rows, ny, energy, dx, dy);
   cudaError_t e = cudaGetLastError();
