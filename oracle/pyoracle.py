@@ -21,6 +21,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# root of the reference source tree (its em2d/, em1d/, python/ folders); the
+# checker builds and the fixture generators read it there, nothing else does
+REFERENCE_ROOT = os.environ.get("ZPIC_REFERENCE", "/root/reference")
 
 PART_DTYPE = np.dtype([("ix", "<i4"), ("iy", "<i4"), ("x", "<f4"), ("y", "<f4"),
                        ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4")])
@@ -56,7 +59,8 @@ class _Laser(C.Structure):
 def build(quiet: bool = True) -> None:
     """Compile the checker libraries with ``make`` (oracle always, _ref when
     the reference sources exist)."""
-    out = subprocess.run(["make", "-C", HERE, "-j4", "all"], capture_output=True, text=True)
+    out = subprocess.run(["make", "-C", HERE, "-j4", "all", f"ZPIC_REFERENCE={REFERENCE_ROOT}"],
+                         capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

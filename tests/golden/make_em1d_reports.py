@@ -17,7 +17,7 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference/em1d"
+REF = os.path.join(os.environ.get("ZPIC_REFERENCE", "/root/reference"), "em1d")
 OUT = os.path.join(HERE, "em1d_reports")
 DECK_C = os.path.join(ROOT, "tests", "em1d_deck.c")
 STEPS = {"lwfa": 60, "twostream": 40, "absorbing": 60}

@@ -28,7 +28,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLD = os.path.join(ROOT, "tests", "golden", "em1d_reports")
 INC = os.path.join(ROOT, "include", "em1d")
 LIBDIR = os.path.join(ROOT, "zpic_gb300", "lib")
-REF = "/root/reference/em1d"
+REF = os.path.join(os.environ.get("ZPIC_REFERENCE", "/root/reference"), "em1d")
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 from make_em1d_reports import LOAD_ONLY, STEPS  # noqa: E402
 

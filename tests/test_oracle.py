@@ -76,7 +76,7 @@ print("OK")
 """
 
 
-@pytest.mark.skipif(not pyoracle.ref_available() and not os.path.isdir("/root/reference/em2d"),
+@pytest.mark.skipif(not pyoracle.ref_available() and not os.path.isdir(os.path.join(pyoracle.REFERENCE_ROOT, "em2d")),
                     reason="reference sources not present on this machine")
 @pytest.mark.parametrize("name", sorted(DECKS))
 def test_oracle_matches_reference_phase_by_phase(name):
