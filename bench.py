@@ -147,15 +147,13 @@ def peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per launch of the push kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "push_tiles_thermal2048.md")
+    """DRAM bytes (read + write) per launch of the push kernel, from one ncu
+    capture recorded in profiles/push_traffic.json (None when absent)."""
     try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
+        with open(os.path.join(ROOT, "profiles", "push_traffic.json")) as f:
+            return float(json.load(f)["dram_bytes_per_launch"])
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 # ---------------------------------------------------------------------------
@@ -742,7 +740,7 @@ def run_em1d(args):
     # roofline of the dominant kernel
     dom = max(prof, key=lambda k: prof[k][0])
     hbm, peak_kind = peaks()
-    push_ms, push_n = prof["push"]
+    push_ms, push_n = push_prof
     push_bytes = EM1D_PART_BYTES * pushed / max(push_n, 1)
     achieved = push_bytes / (push_ms * 1e-3 / max(push_n, 1)) / 1e9
     line = {
@@ -887,6 +885,7 @@ def main():
     ap.add_argument("--tile", default="32x16")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-exact-line", action="store_true", help="skip the exact push build's figure")
     ap.add_argument("--exact", action="store_true",
                     help="bit-exact push build (every float32 op rounded as the reference C)")
     ap.add_argument("--sort-every", type=int, default=0)
@@ -940,9 +939,10 @@ def main():
     sm = W["smooth"]
     sim.set_smooth(sm[0], sm[1], sm[2], sm[3])
 
-    # ---- device-resident timed region ----
+    # ---- device-resident timed region: CUDA events around the whole run
+    # (zc_step) and around every push launch (the roofline's kernel) ----
     sim.step(args.warmup)
-    sim.set_profiling(True)
+    sim.set_profiling("push")
     sim.reset_profile()
     clk = ClockSampler(local)
     barrier()
@@ -953,9 +953,17 @@ def main():
     clocks = clk.stop()
     barrier()
     ms = allmax(ms)
+    timed_prof = sim.profile()  # launch counts of every phase; device time of the push
+    push_prof = timed_prof["push"]
+    value = N * args.steps * world / (ms / 1e3)
+    # the per-phase breakdown: more steps with every phase bracketed by
+    # events (untimed; the events add a little to each step)
+    sim.set_profiling(True)
+    sim.reset_profile()
+    nph = max(16, min(args.steps, 64))
+    sim.step(nph)
     prof = sim.profile()
     sim.set_profiling(False)
-    value = N * args.steps * world / (ms / 1e3)
 
     # ---- end to end through the C-ABI with host buffers ----
     import torch
@@ -988,7 +996,7 @@ def main():
     d2h = (6 + 1) * 8
 
     # ---- roofline of the dominant kernel (push + deposit) ----
-    push_ms, push_n = prof["push"]
+    push_ms, push_n = push_prof
     push_avg = push_ms / max(push_n, 1)
     cells = nx * ny
     push_bytes = N * PART_BYTES + cells * PUSH_CELL_BYTES
@@ -996,7 +1004,7 @@ def main():
     achieved = push_bytes / (push_avg / 1e3) / 1e9
     traffic = ncu_traffic()
     step_bytes = N * PART_BYTES + cells * (STEP_CELL_BYTES + 4 * SMOOTH_PASS_BYTES)
-    launches = sum(n for _, n in prof.values())
+    launches = sum(n for _, n in timed_prof.values())
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -1021,8 +1029,30 @@ def main():
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": push_bytes,
                      "avg_launch_ms": push_avg,
                      "step_achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9},
-        "phases_ms_per_step": {k: round(v[0] / args.steps, 5) for k, v in prof.items() if v[1] or v[0]},
+        "phases_ms_per_step": {k: round(v[0] / nph, 5) for k, v in prof.items() if v[1] or v[0]},
+        "phases_how": f"{nph} more steps after the timed ones, every phase bracketed by CUDA events",
     }
+    # ---- the exact push build on the same workload and timed region,
+    # beside the fast build's headline ----
+    sim.close()
+    if not args.exact and not args.deterministic and not args.no_exact_line:
+        ex = CudaSim(W["nx"], W["box"], W["dt"], device=local, tile=tile, fast_math=False,
+                     sort_every=args.sort_every)
+        ex.add_species(W["m_q"], float(q), W["ppc"], parts)
+        ex.set_smooth(sm[0], sm[1], sm[2], sm[3])
+        ex.step(args.warmup)
+        barrier()
+        ex.synchronize()
+        ex.step(args.steps)
+        ms_x = allmax(ex.last_ms())
+        ex.close()
+        line["exact_build"] = {"value": N * args.steps * world / (ms_x / 1e3), "unit": UNIT,
+                               "ms_per_step": ms_x / args.steps,
+                               "parity": "every field component within 1e-5 of the oracle (IEEE float32 "
+                                         "operations as the reference)"}
+        line["config"]["parity"] = ("fast push build: every field within 1e-5 relative L2 of the oracle over "
+                                    "10 steps, and every component on a 256x256 box of this workload "
+                                    "(tests/test_gpu_configs.py)")
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, kind, n = cpu_run(512, 512, 3, 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
@@ -1030,7 +1060,6 @@ def main():
                                           f"steps, single-threaded C, host {platform.machine()}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    sim.close()
     rep.close()
     return 0
 

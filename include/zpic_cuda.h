@@ -318,11 +318,13 @@ ZC_API zc_status zc_synchronize(zc_sim *sim);
 ZC_API zc_status zc_last_step_ms(zc_sim *sim, float *ms);
 
 /* --- per-phase device timing ------------------------------------------- */
-/* With profiling on, every phase of the step is bracketed by CUDA events on
- * the handle's stream; zc_get_profile returns, per phase, the summed device
- * milliseconds and the number of kernel launches since the last reset.  The
- * reference's own counters are wall-clock totals of spec_advance and
- * emf_advance (em2d/particles.c:26-59, em2d/emf.c:27-37). */
+/* With profiling on (zc_set_profiling 1), every phase of the step is
+ * bracketed by CUDA events on the handle's stream; with 2, only the push
+ * (ZC_PHASE_PUSH), so that the rest of the step runs as without profiling.
+ * zc_get_profile returns, per phase, the summed device milliseconds and the
+ * number of kernel launches since the last reset.  The reference's own
+ * counters are wall-clock totals of spec_advance and emf_advance
+ * (em2d/particles.c:26-59, em2d/emf.c:27-37). */
 enum {
     ZC_PHASE_PUSH = 0,      /* fused push + deposit, one CTA per tile */
     ZC_PHASE_SPILL,         /* push of particles outside the tiles */
@@ -339,7 +341,7 @@ enum {
     ZC_PHASE_HISTORY,       /* per-step energy history */
     ZC_NPHASE
 };
-ZC_API zc_status zc_set_profiling(zc_sim *sim, int enable);
+ZC_API zc_status zc_set_profiling(zc_sim *sim, int mode);  /* 0 off, 1 every phase, 2 the push only */
 ZC_API zc_status zc_get_profile(zc_sim *sim, double ms[ZC_NPHASE], long long launches[ZC_NPHASE]);
 ZC_API zc_status zc_reset_profile(zc_sim *sim);
 ZC_API const char *zc_phase_name(int phase);

@@ -445,7 +445,10 @@ class CudaSim:
                 "ntiles": (i.ntiles[0], i.ntiles[1]), "relayouts": i.relayouts, "captures": i.captures}
 
     def set_profiling(self, on=True):
-        _ck(self.lib.zc_set_profiling(self.h, int(bool(on))))
+        """Per-phase device timing: True (or 1) every phase, "push" (2) the
+        push only (the rest of the step runs untimed), False off."""
+        mode = 2 if on == "push" else int(bool(on))
+        _ck(self.lib.zc_set_profiling(self.h, mode))
 
     def reset_profile(self):
         _ck(self.lib.zc_reset_profile(self.h))

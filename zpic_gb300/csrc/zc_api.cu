@@ -103,7 +103,8 @@ struct SpeciesState {
   int ppc[2] = {1, 1};
   int iter = 0, n_move = 0;
   // tile layout
-  int *d_off = nullptr, *d_cap = nullptr, *d_np = nullptr;
+  int *d_off = nullptr, *d_cap = nullptr, *d_np = nullptr;  // np: slots in use (particles and holes)
+  int *d_vcnt = nullptr;  // particles (not holes) per tile, filled on demand
   std::vector<int> h_off, h_cap;
   long long alloc = 0;   // particles per buffer
   Particles buf[2] = {};
@@ -121,6 +122,10 @@ struct SpeciesState {
   long long ob_alloc = 0;
   int ob_in = 0;
   bool pending = false;
+  // tiles in plain cell order (sorted or laid out since the last push): the
+  // next push reads full chunks in that order and leaves them in the
+  // lane-run layout (tile_slot)
+  bool fresh = true;
   // energy
   double *d_ekin_tile = nullptr, *d_ekin_extra = nullptr, *d_ekin = nullptr;
   // window injection drawn on the device (zc_set_device_injection)
@@ -132,7 +137,7 @@ struct SpeciesState {
 struct Counters {
   int iter = 0, n_move = 0;
   std::vector<int> sp_iter, sp_n_move, cur, spill_cur, ob_in;
-  std::vector<bool> pending;
+  std::vector<bool> pending, fresh;
   int eb_cur = 0, j_cur = 0;
   long long launch[ZC_NPHASE] = {};
 };
@@ -239,7 +244,7 @@ struct Phase {
   cudaEvent_t b = nullptr;
   Phase(zc_sim *s_, int ph_, int nlaunch) : s(s_), ph(ph_) {
     s->prof_launch[ph] += nlaunch;
-    if (!s->profiling) return;
+    if (!s->profiling || (s->profiling == 2 && ph != ZC_PHASE_PUSH)) return;
     b = next_event();
     cudaEventRecord(b, s->st);
   }
@@ -325,7 +330,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   int *d_cnt = nullptr, *d_fill = nullptr, *d_np_old = nullptr, *d_off_old = nullptr;
   TRY(dalloc(&d_cnt, nt));
   TRY(dalloc(&d_fill, nt));
-  CK(cudaMemcpyAsync(d_cnt, p.d_np, sizeof(int) * nt, cudaMemcpyDeviceToDevice, st));
+  CK(launch_count_valid(p.buf[p.cur], p.d_off, p.d_np, d_cnt, nt, st));  // holes do not count
   TRY(dalloc(&d_np_old, nt));
   TRY(dalloc(&d_off_old, nt));
   CK(cudaMemcpyAsync(d_np_old, p.d_np, sizeof(int) * nt, cudaMemcpyDeviceToDevice, st));
@@ -407,6 +412,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   p.d_key = nkey;
   p.h_off = off;
   p.h_cap = cap;
+  p.fresh = true;
   dfree(d_cnt);
   dfree(d_fill);
   dfree(d_np_old);
@@ -519,6 +525,7 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   C.nty = s->nty;
   C.shift = shift;
   C.mw = s->mw;
+  C.fresh = 0;
   TRY(set_current_scale(s, p, C));
   const int in = p.spill_cur, out = 1 - p.spill_cur;
   {
@@ -548,9 +555,12 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
     Phase ph(s, ZC_PHASE_SORT, 1);
     CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles, st));
     p.cur = 1 - p.cur;
+    p.fresh = true;
     a.pin = p.buf[p.cur];
     a.pout = p.buf[1 - p.cur];
   }
+  a.C.fresh = p.fresh ? 1 : 0;
+  p.fresh = false;
   {
     Phase ph(s, ZC_PHASE_PUSH, 1);
     CK(launch_push_tiles(a, st));
@@ -804,6 +814,7 @@ Counters save_counters(const zc_sim *s) {
     c.spill_cur.push_back(p.spill_cur);
     c.ob_in.push_back(p.ob_in);
     c.pending.push_back(p.pending);
+    c.fresh.push_back(p.fresh);
   }
   c.eb_cur = s->eb_cur;
   c.j_cur = s->j_cur;
@@ -814,7 +825,7 @@ Counters save_counters(const zc_sim *s) {
 // the buffer parities a captured graph starts from
 bool same_parities(const Counters &a, const Counters &b) {
   return a.cur == b.cur && a.spill_cur == b.spill_cur && a.ob_in == b.ob_in && a.eb_cur == b.eb_cur &&
-         (a.iter % 2) == (b.iter % 2);
+         a.fresh == b.fresh && (a.iter % 2) == (b.iter % 2);
 }
 
 // the graph g holds n steps from the current state (block-aligned)
@@ -849,6 +860,7 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G) {
     p.spill_cur = before.spill_cur[k];
     p.ob_in = before.ob_in[k];
     p.pending = before.pending[k];
+    p.fresh = before.fresh[k];
   }
   s->eb_cur = before.eb_cur;
   s->j_cur = before.j_cur;
@@ -886,6 +898,7 @@ void account_steps(zc_sim *s, const StepGraph &g) {
     p.cur = g.after.cur[k];
     p.spill_cur = g.after.spill_cur[k];
     p.ob_in = g.after.ob_in[k];
+    p.fresh = g.after.fresh[k];
     p.n_move += g.after.sp_n_move[k] - g.before.sp_n_move[k];
   }
   s->n_move += g.after.n_move - g.before.n_move;
@@ -1221,6 +1234,7 @@ zc_status zc_sim_destroy(zc_sim *s) {
     dfree(p.d_off);
     dfree(p.d_cap);
     dfree(p.d_np);
+    dfree(p.d_vcnt);
     for (int b = 0; b < 2; ++b) {
       free_particles(p.ob[b].p);
       dfree(p.ob[b].dst);
@@ -1283,6 +1297,7 @@ zc_status zc_species_create(zc_sim *s, const zc_species_desc *d, const zc_part *
   TRY(dalloc(&p.d_off, nt));
   TRY(dalloc(&p.d_cap, nt));
   TRY(dalloc(&p.d_np, nt));
+  TRY(dalloc(&p.d_vcnt, nt));
   CK(cudaMemsetAsync(p.d_np, 0, sizeof(int) * nt, s->st));
   CK(cudaMemsetAsync(p.d_off, 0, sizeof(int) * nt, s->st));
   CK(cudaMemsetAsync(p.d_cap, 0, sizeof(int) * nt, s->st));
@@ -1374,6 +1389,7 @@ zc_status zc_species_create_device(zc_sim *s, float m_q, const int ppc[2], const
   I.seed_lo = (unsigned)seed;
   I.seed_hi = (unsigned)(seed >> 32);
   CK(launch_init_tiles(p.buf[p.cur], p.d_off, d_colpts, d_colmask, I, L, s->ntiles, s->st));
+  p.fresh = true;
   CK(cudaStreamSynchronize(s->st));
   dfree(d_colpts);
   dfree(d_colmask);
@@ -1423,7 +1439,8 @@ zc_status zc_species_count(zc_sim *s, int k, int *np) {
   TRY(settle(s, p));
   std::vector<int> c(s->ntiles);
   int sc = 0;
-  CK(cudaMemcpyAsync(c.data(), p.d_np, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
+  CK(launch_count_valid(p.buf[p.cur], p.d_off, p.d_np, p.d_vcnt, s->ntiles, s->st));
+  CK(cudaMemcpyAsync(c.data(), p.d_vcnt, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
   CK(cudaMemcpyAsync(&sc, p.d_spill_cnt + p.spill_cur, sizeof(int), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   long long tot = std::min(sc, p.spill_cap);
@@ -1439,7 +1456,8 @@ zc_status zc_species_get_particles(zc_sim *s, int k, zc_part *out, int cap, int 
   TRY(settle(s, p));
   std::vector<int> c(s->ntiles);
   int sc = 0;
-  CK(cudaMemcpyAsync(c.data(), p.d_np, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
+  CK(launch_count_valid(p.buf[p.cur], p.d_off, p.d_np, p.d_vcnt, s->ntiles, s->st));
+  CK(cudaMemcpyAsync(c.data(), p.d_vcnt, sizeof(int) * s->ntiles, cudaMemcpyDeviceToHost, s->st));
   CK(cudaMemcpyAsync(&sc, p.d_spill_cnt + p.spill_cur, sizeof(int), cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   sc = std::min(sc, p.spill_cap);
@@ -1863,12 +1881,13 @@ zc_status zc_synchronize(zc_sim *s) {
   return check_errors(s, true);
 }
 
-zc_status zc_set_profiling(zc_sim *s, int on) {
+zc_status zc_set_profiling(zc_sim *s, int mode) {
   if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (mode < 0 || mode > 2) return fail(ZC_EINVAL, "profiling mode must be 0, 1 or 2");
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
   collect_profile(s);
-  s->profiling = on ? 1 : 0;
+  s->profiling = mode;
   return ZC_OK;
 }
 

@@ -44,27 +44,28 @@ __global__ void k_planes_to_aos(const float *planes, float *aos, Grid G, int nco
 // current guard-cell fold (current_update_gc, em2d/current.c:118-159)
 // ---------------------------------------------------------------------------
 __global__ void k_fold_x(float *J, Grid G) {
-  const int by = blockIdx.x * blockDim.x + threadIdx.x;  // every buffer row
-  if (by >= G.ny + 3) return;
-  for (int c = 0; c < 3; ++c)
-    for (int b = 0; b < 3; ++b) {  // cells -1, 0, 1 receive nx-1, nx, nx+1
-      const size_t lo = gidx(G, c, b, by), hi = gidx(G, c, G.nx + b, by);
-      const float v = J[lo] + J[hi];
-      J[lo] = v;
-      J[hi] = v;
-    }
+  // one thread per (buffer row, component, guard column): cells -1, 0, 1
+  // receive nx-1, nx, nx+1
+  const int n = (G.ny + 3) * 9;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+    const int by = g / 9, c = (g % 9) / 3, b = g % 3;
+    const size_t lo = gidx(G, c, b, by), hi = gidx(G, c, G.nx + b, by);
+    const float v = J[lo] + J[hi];
+    J[lo] = v;
+    J[hi] = v;
+  }
 }
 
 __global__ void k_fold_y(float *J, Grid G) {
-  const int bx = blockIdx.x * blockDim.x + threadIdx.x;  // every buffer column
-  if (bx >= G.nx + 3) return;
-  for (int c = 0; c < 3; ++c)
-    for (int b = 0; b < 3; ++b) {
-      const size_t lo = gidx(G, c, bx, b), hi = gidx(G, c, bx, G.ny + b);
-      const float v = J[lo] + J[hi];
-      J[lo] = v;
-      J[hi] = v;
-    }
+  // one thread per (buffer column, component, guard row)
+  const int gx = G.nx + 3, n = gx * 9;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+    const int bx = g % gx, cb = g / gx, c = cb / 3, b = cb % 3;
+    const size_t lo = gidx(G, c, bx, b), hi = gidx(G, c, bx, G.ny + b);
+    const float v = J[lo] + J[hi];
+    J[lo] = v;
+    J[hi] = v;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -303,17 +304,29 @@ __global__ void __launch_bounds__(256) k_yee(const __grid_constant__ CUtensorMap
 // unless the window moves, y always.  Guards only read interior rows.
 // ---------------------------------------------------------------------------
 __global__ void k_emf_gc(float *EB, Grid G, int mw) {
+  // one thread per guard cell: buffer columns 0, nx+1, nx+2 of every row
+  // (not under a moving window), then buffer rows 0, ny+1, ny+2 of every
+  // column (the corners come up twice and get the same value)
   const int gx = G.nx + 3, gy = G.ny + 3;
-  const int bx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int by = blockIdx.y;
-  if (bx >= gx || by >= gy) return;
-  const bool gxg = (bx == 0 || bx > G.nx), gyg = (by == 0 || by > G.ny);
-  if (!gxg && !gyg) return;
-  int sx = bx, sy = by;
-  if (gxg && !mw) sx = (bx == 0) ? G.nx : bx - G.nx;
-  if (gyg) sy = (by == 0) ? G.ny : by - G.ny;
-  if (sx == bx && sy == by) return;
-  for (int c = 0; c < 6; ++c) EB[gidx(G, c, bx, by)] = EB[gidx(G, c, sx, sy)];
+  const int ncol = mw ? 0 : 3 * gy, n = ncol + 3 * gx;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+    int bx, by;
+    if (g < ncol) {
+      const int b = g % 3;
+      by = g / 3;
+      bx = b ? G.nx + b : 0;
+    } else {
+      const int h = g - ncol, b = h / gx;
+      bx = h % gx;
+      by = b ? G.ny + b : 0;
+    }
+    const bool gxg = (bx == 0 || bx > G.nx), gyg = (by == 0 || by > G.ny);
+    int sx = bx, sy = by;
+    if (gxg && !mw) sx = (bx == 0) ? G.nx : bx - G.nx;
+    if (gyg) sy = (by == 0) ? G.ny : by - G.ny;
+    if (sx == bx && sy == by) continue;
+    for (int c = 0; c < 6; ++c) EB[gidx(G, c, bx, by)] = EB[gidx(G, c, sx, sy)];
+  }
 }
 
 // E_part = E + external, B_part = B + external (emf_update_part_fld,
@@ -457,8 +470,8 @@ cudaError_t launch_planes_to_aos(const float *planes, float *aos, const Grid &G,
 }
 
 cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
-  if (!mw) k_fold_x<<<(G.ny + 3 + 127) / 128, 128, 0, st>>>(J, G);
-  k_fold_y<<<(G.nx + 3 + 127) / 128, 128, 0, st>>>(J, G);
+  if (!mw) k_fold_x<<<((G.ny + 3) * 9 + 255) / 256, 256, 0, st>>>(J, G);
+  k_fold_y<<<((G.nx + 3) * 9 + 255) / 256, 256, 0, st>>>(J, G);
   return cudaGetLastError();
 }
 
@@ -495,7 +508,7 @@ cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float 
 }
 
 cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st) {
-  k_emf_gc<<<grid_rows(G, 256), 256, 0, st>>>(EB, G, mw);
+  k_emf_gc<<<(3 * (G.nx + 3) + 3 * (G.ny + 3) + 255) / 256, 256, 0, st>>>(EB, G, mw);
   return cudaGetLastError();
 }
 

@@ -18,8 +18,20 @@
 // -- the same quantities as t_part (em2d/particles.h:29-37), 24 bytes per
 // particle moved with two vector accesses -- partitioned into rectangular
 // tiles of TX x TY cells.  Tile t owns the contiguous segment
-// [off[t], off[t] + cap[t]) and holds np[t] particles at its start.  Two
-// copies (A, B) alternate every step.
+// [off[t], off[t] + cap[t]); its first np[t] slots are in use.  Two copies
+// (A, B) alternate every step.
+//
+// Slots keep their particle from step to step: the push writes a particle
+// back to the slot it came from, and a particle that leaves the tile leaves
+// a hole there (cell word kHole); particles arriving from other tiles are
+// appended after slot np.  The periodic cell sort compacts the holes away
+// and stores the tile in plain cell order.  The push that follows reads
+// every full chunk of 32 * kLaneRun particles in that order (lane l takes
+// particle l * kLaneRun + k at its k-th step) and writes it back transposed
+// (tile_slot: that particle goes to slot k * 32 + l); every later push
+// reads and writes slot k * 32 + l (coalesced), so lane l keeps meeting
+// the chunk's particles l * kLaneRun ... l * kLaneRun + kLaneRun - 1 one
+// after another, which lie in one or two cells.
 #pragma once
 
 #include <cuda.h>
@@ -40,6 +52,13 @@ struct Particles {       // one particle buffer
   float4 *u;             // ux, uy, uz, packed cell
   float2 *xy;            // x, y
 };
+
+// particles a push lane takes from one chunk, one after another
+constexpr int kLaneRun = 8;
+constexpr int kChunk = 32 * kLaneRun;
+// cell word of an empty slot (no cell has both indices 0xffff: grids have at
+// most 65535 cells per axis)
+constexpr unsigned kHole = 0xffffffffu;
 
 struct PRec {            // one particle in registers
   int ix, iy;
@@ -78,7 +97,24 @@ __device__ __forceinline__ void store_particle(const Particles &p, long long k, 
 __device__ __forceinline__ void store_particle(const Particles &p, long long k, const PRec &q) {
   store_particle(p, k, q.ix, q.iy, q.x, q.y, q.ux, q.uy, q.uz);
 }
+
+__device__ __forceinline__ bool is_hole_word(float w) { return (unsigned)__float_as_int(w) == kHole; }
+__device__ __forceinline__ bool is_hole(const Particles &p, long long k) { return is_hole_word(p.u[k].w); }
+__device__ __forceinline__ void store_hole(const Particles &p, long long k) {
+  p.u[k] = make_float4(0.f, 0.f, 0.f, __int_as_float((int)kHole));
+}
 #endif
+
+// Slot of the i-th particle (in cell order) of a tile of n particles in the
+// lane-run layout: full chunks of kChunk particles transposed (particle
+// l * kLaneRun + k of a chunk at slot k * 32 + l), the last, partial chunk
+// in order.
+__host__ __device__ __forceinline__ int tile_slot(int i, int n) {
+  const int c0 = i & ~(kChunk - 1);
+  if (c0 + kChunk > n) return i;
+  const int r = i - c0;
+  return c0 + (r % kLaneRun) * 32 + r / kLaneRun;
+}
 
 struct Grid {            // geometry of the padded SoA grids
   int nx, ny;            // interior cells

@@ -13,6 +13,9 @@ struct PushConst {
   int nx, ny, ntx, nty;
   int shift;                              // moving-window shift applied this step (0/1)
   int mw;                                 // absorbing boundaries along x
+  int fresh;                              // tiles in plain cell order (sorted or laid out since the
+                                          // last push): full chunks are read in that order and
+                                          // written back in the lane-run layout
   // tile current as integers (see jsplit): a contribution v counts as
   // rint(v js) = h 2^2L + m 2^L + l; js_invl = 2^-L, js_twol = 2^L,
   // js_inv2l = 2^-2L, js_two2l = 2^2L, js_lo = 1 / js; deterministic global
@@ -133,9 +136,13 @@ ZC_SPILL_LAUNCHER(launch_push_spill_fast_det);
 // fixed-point current planes <-> float planes (n values)
 cudaError_t launch_fixed_to_float(const unsigned long long *src, float *dst, size_t n, cudaStream_t st);
 cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, size_t n, cudaStream_t st);
-// stable counting sort of every tile by cell (src -> dst, same layout)
-cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, const int *np,
+// counting sort of every tile by cell (src -> dst, same offsets): holes
+// dropped, np set to the particle count, plain cell order
+cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
                             const LayoutConst &L, int ntiles, cudaStream_t st);
+// particles (slots that are not holes) of every tile into cnt
+cudaError_t launch_count_valid(const Particles &buf, const int *off, const int *np, int *cnt, int ntiles,
+                               cudaStream_t st);
 // moves the particles pending in an outbox into their tiles (appended)
 cudaError_t launch_settle(const Particles &buf, const TileSet &T, const Outbox &O, const Spill &S, int *err,
                           int ntx, int nty, int mw, cudaStream_t st);

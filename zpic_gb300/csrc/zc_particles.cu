@@ -8,8 +8,8 @@
 //                 wait in the outboxes of its (up to 8) neighbours (the push
 //                 does this itself; this kernel settles the outboxes before
 //                 the particles are read back, counted or re-laid out).
-//   k_cellsort    one CTA per tile: counting sort of the tile by cell, so
-//                 that the lanes of a push warp share cells.
+//   k_cellsort    one CTA per tile: counting sort of the tile by cell (holes
+//                 dropped), so that the push lanes meet runs of one cell.
 //   re-layout     upload, moving-window injection and capacity changes.
 #include <algorithm>
 
@@ -115,17 +115,41 @@ __global__ void k_count_list(Particles list, const int *n_ptr, int n_cap, int *c
   }
 }
 
-// tile particles keep their tile and their order: copy to the new offsets
-__global__ void k_copy_tiles(Particles src, const int *off_old, const int *np_old, Particles dst,
-                             const int *off_new, unsigned *key, int *fill) {
+// tile particles keep their tile and their order: copy to the new offsets,
+// holes dropped (one CTA of 256 threads per tile)
+__global__ void __launch_bounds__(256) k_copy_tiles(Particles src, const int *off_old, const int *np_old,
+                                                    Particles dst, const int *off_new, unsigned *key, int *fill) {
+  __shared__ int swarp[8];
   const int t = blockIdx.x;
   const int n = np_old[t];
   const long long a = off_old[t], b = off_new[t];
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    store_particle(dst, b + k, load_particle(src, a + k));
-    if (key) key[b + k] = (unsigned)k;
+  int placed = 0;
+  for (int k0 = 0; k0 < n; k0 += 256) {
+    const int k = k0 + threadIdx.x;
+    const bool f = k < n && !is_hole(src, a + k);
+    int tot;
+    const int pre = block_exclusive_scan<256>(f ? 1 : 0, tot, swarp);
+    if (f) {
+      const int q = placed + pre;
+      store_particle(dst, b + q, load_particle(src, a + k));
+      if (key) key[b + q] = (unsigned)q;
+    }
+    placed += tot;
   }
-  if (threadIdx.x == 0) fill[t] = n;
+  if (threadIdx.x == 0) fill[t] = placed;
+}
+
+// particles (not holes) in every tile's slots
+__global__ void __launch_bounds__(256) k_count_valid(Particles buf, const int *off, const int *np, int *cnt) {
+  __shared__ int swarp[8];
+  const int t = blockIdx.x;
+  const int n = np[t];
+  const long long a = off[t];
+  int c = 0;
+  for (int k = threadIdx.x; k < n; k += 256) c += is_hole(buf, a + k) ? 0 : 1;
+  int tot;
+  block_exclusive_scan<256>(c, tot, swarp);
+  if (threadIdx.x == 0) cnt[t] = tot;
 }
 
 // list particles are appended to their tile; `key0 + k` remembers the order
@@ -149,12 +173,12 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 
 // Counting sort of every tile by local cell (one CTA of 1024 threads per
 // tile, src -> dst at the same offsets): a shared-memory histogram, a scan,
-// then every particle takes the next slot of its cell.  The order inside a
-// cell follows the atomics' timing.  The reference sorts its whole buffer by
-// cell every n_sort steps for cache reuse (spec_sort,
-// em2d/particles.c:942-1007); here the per-tile sort keeps the lanes of a
-// push warp on shared cells.
-__global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst, const int *off, const int *np,
+// then every particle takes the next slot of its cell; holes are dropped
+// and np becomes the particle count.  The order inside a cell follows the
+// atomics' timing.  The reference sorts its whole buffer by cell every
+// n_sort steps for cache reuse (spec_sort, em2d/particles.c:942-1007); here
+// the per-tile sort gives the push lanes runs of particles in one cell.
+__global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst, const int *off, int *np,
                                                    LayoutConst L) {
   constexpr int MAXC = 1024;
   __shared__ int cursor[MAXC];
@@ -166,26 +190,34 @@ __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst,
   const long long b = off[t];
   for (int c = threadIdx.x; c < ncell; c += 1024) cursor[c] = 0;
   __syncthreads();
-  auto cell_of = [&](long long g) {
-    int ix, iy;
-    load_cell(src, g, ix, iy);
-    const int c = (ix - cx0) + (iy - cy0) * L.TX;
+  auto cell_of_word = [&](float w) {  // -1 for a hole
+    const unsigned u = (unsigned)__float_as_int(w);
+    if (u == kHole) return -1;
+    const int c = ((int)(u & 0xffffu) - cx0) + ((int)(u >> 16) - cy0) * L.TX;
     return min(max(c, 0), ncell - 1);
   };
-  for (int k = threadIdx.x; k < n; k += 1024) atomicAdd(&cursor[cell_of(b + k)], 1);
+  for (int k = threadIdx.x; k < n; k += 1024) {
+    const int c = cell_of_word(src.u[b + k].w);
+    if (c >= 0) atomicAdd(&cursor[c], 1);
+  }
   __syncthreads();
+  int nvalid;
   {
     const int v = (threadIdx.x < ncell) ? cursor[threadIdx.x] : 0;
-    int tot;
-    const int pre = block_exclusive_scan<1024>(v, tot, swarp);
+    const int pre = block_exclusive_scan<1024>(v, nvalid, swarp);
     if (threadIdx.x < ncell) cursor[threadIdx.x] = pre;
   }
   __syncthreads();
   for (int k = threadIdx.x; k < n; k += 1024) {
-    const long long s = b + k;
-    const int slot = atomicAdd(&cursor[cell_of(s)], 1);
-    store_particle(dst, b + slot, load_particle(src, s));
+    const float4 u = src.u[b + k];
+    const int c = cell_of_word(u.w);
+    if (c < 0) continue;
+    const float2 xy = src.xy[b + k];
+    const int slot = atomicAdd(&cursor[c], 1);
+    dst.u[b + slot] = u;
+    dst.xy[b + slot] = xy;
   }
+  if (threadIdx.x == 0) np[t] = nvalid;
 }
 
 // Orders every tile deterministically after a re-layout: by cell, and
@@ -264,23 +296,33 @@ __global__ void k_clamp_counts(int *np, const int *cap, int ntiles) {
     np[t] = min(np[t], cap[t]);
 }
 
-// tiles + spill -> AoS records in tile order (download)
-__global__ void k_gather_aos(Particles buf, const int *off, const int *np, const long long *dst_off,
-                             int *aos, int ntiles) {
+// tiles + spill -> AoS records in tile order (download), holes dropped;
+// dst_off from the tiles' particle counts (one CTA of 256 threads per tile)
+__global__ void __launch_bounds__(256) k_gather_aos(Particles buf, const int *off, const int *np,
+                                                    const long long *dst_off, int *aos, int ntiles) {
+  __shared__ int swarp[8];
   const int t = blockIdx.x;
   if (t >= ntiles) return;
   const int n = np[t];
   const long long a = off[t], d = dst_off[t];
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    int *r = aos + 7LL * (d + k);
-    const PRec q = load_particle(buf, a + k);
-    r[0] = q.ix;
-    r[1] = q.iy;
-    r[2] = __float_as_int(q.x);
-    r[3] = __float_as_int(q.y);
-    r[4] = __float_as_int(q.ux);
-    r[5] = __float_as_int(q.uy);
-    r[6] = __float_as_int(q.uz);
+  int placed = 0;
+  for (int k0 = 0; k0 < n; k0 += 256) {
+    const int k = k0 + threadIdx.x;
+    const bool f = k < n && !is_hole(buf, a + k);
+    int tot;
+    const int pre = block_exclusive_scan<256>(f ? 1 : 0, tot, swarp);
+    if (f) {
+      int *r = aos + 7LL * (d + placed + pre);
+      const PRec q = load_particle(buf, a + k);
+      r[0] = q.ix;
+      r[1] = q.iy;
+      r[2] = __float_as_int(q.x);
+      r[3] = __float_as_int(q.y);
+      r[4] = __float_as_int(q.ux);
+      r[5] = __float_as_int(q.uy);
+      r[6] = __float_as_int(q.uz);
+    }
+    placed += tot;
   }
 }
 
@@ -308,6 +350,7 @@ __global__ void k_charge_tiles(Particles buf, const int *off, const int *np, flo
   const int n = np[t];
   const long long a = off[t];
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    if (is_hole(buf, a + k)) continue;
     const PRec r = load_particle(buf, a + k);
     const int c = r.ix + nrow * r.iy;
     const float w1 = r.x, w2 = r.y;
@@ -471,7 +514,8 @@ __global__ void k_pha_tiles(Particles buf, const int *off, const int *np, int nt
   if (t >= ntiles) return;
   const int n = np[t];
   const long long a = off[t];
-  for (int k = threadIdx.x; k < n; k += blockDim.x) pha_add(pha, load_particle(buf, a + k), P);
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    if (!is_hole(buf, a + k)) pha_add(pha, load_particle(buf, a + k), P);
 }
 
 __global__ void k_pha_list(Particles list, const int *n_ptr, int n_cap, float *pha, PhaConst P) {
@@ -561,9 +605,15 @@ cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, siz
   return cudaGetLastError();
 }
 
-cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, const int *np,
+cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
                             const LayoutConst &L, int ntiles, cudaStream_t st) {
   k_cellsort<<<ntiles, 1024, 0, st>>>(src, dst, off, np, L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count_valid(const Particles &buf, const int *off, const int *np, int *cnt, int ntiles,
+                               cudaStream_t st) {
+  k_count_valid<<<ntiles, 256, 0, st>>>(buf, off, np, cnt);
   return cudaGetLastError();
 }
 

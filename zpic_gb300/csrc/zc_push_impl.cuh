@@ -398,18 +398,33 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 
 // ---------------------------------------------------------------------------
 // K1: push + deposit, one CTA per tile.  The input of tile t is its own
-// particles plus the particles that the previous step posted for it in the
+// slots plus the particles that the previous step posted for it in the
 // outboxes of its (up to 8) neighbouring tiles (`Oin`); leavers of this step
-// go to this tile's slot of `O`.  Stayers are compacted into the tile's
-// segment of `pout`: every warp reserves its slots with one shared-memory
-// atomic, so the lanes of a warp keep their (cell-sorted) order while the
-// order of the warps' runs follows their timing.  The particles bound for
-// the tile are first listed from the neighbours' outboxes (one warp per
-// neighbour) and pushed in full warps after the own particles.  The main
-// loop has no block-wide barrier.
+// go to this tile's slot of `O`.
+//
+// Own particles keep their slots: each is written back to the slot it was
+// read from (a particle that leaves writes a hole there), so the cell order
+// the sort gave the tile survives until the next sort except for the few
+// particles that change cell.  The particles bound for the tile are listed
+// from the neighbours' outboxes (one warp per neighbour), pushed in full
+// warps after the own ones and appended after slot np.  The main loop has
+// no block-wide barrier.
+//
+// Warp w takes the chunks w, w + NW, ... of kChunk slots, 32 slots at a
+// time.  In the float builds lane l meets the chunk's particles l kLaneRun
+// ... l kLaneRun + kLaneRun - 1 of the sorted order one after another, and
+// sums their single-segment currents in registers while they stay in one
+// cell; a lane adds its sums to J when its cell changes.  The deterministic
+// builds read every chunk in cell order across the lanes and pre-reduce
+// with segmented warp sums of fixed-point parts.
 // ---------------------------------------------------------------------------
+// resident CTAs per SM the float builds are compiled for (64 registers a
+// thread at 8)
+#ifndef ZC_PUSH_MIN_CTAS
+#define ZC_PUSH_MIN_CTAS 8
+#endif
 template <int TX, int TY, int NT, bool DET>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
+__global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
                                                    Particles pin,
                                                    Particles pout, TileSet T, Outbox Oin, Outbox O, Spill S,
                                                    double *ekin_tile, int *err, PushConst C, FixedJ fj) {
@@ -431,8 +446,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   constexpr int QCAP = QFLUSH - 1 + 32;
   __shared__ float qf[NW][5][QCAP];  // x0, y0, dx, dy, qvz
   __shared__ int qi[NW][QCAP];       // local cell and shifts, packed
-  // prefetched particles, one chunk per warp: each lane reads its slot into
-  // registers before it copies the next chunk's particle into the slot
+  // prefetched particles, 32 slots per warp: each lane reads its slot into
+  // registers before it copies the next slot's particle into it
   __shared__ __align__(16) float4 pf_u[NW][32];
   __shared__ __align__(16) float2 pf_xy[NW][32];
   __shared__ int nb[8], s_nnb;        // distinct neighbour tiles
@@ -441,12 +456,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   constexpr int INCAP = 64;
   __shared__ int s_in[INCAP];
   __shared__ int s_nin;
-  __shared__ int s_stay, s_leave;     // output counters (warp-aggregated atomics)
+  __shared__ int s_app, s_leave;      // appended arrivals, leavers (warp-aggregated atomics)
 
   const int t = blockIdx.x;
   const int tx = t % C.ntx, ty = t / C.ntx;
   const int cx0 = tx * TX, cy0 = ty * TY;  // first cell of the tile = buffer coords of its halo
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1;
   int errbits = 0;
   int qcount = 0;  // warp-uniform
 
@@ -471,7 +487,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       }
     s_nnb = c;
     s_nin = 0;
-    s_stay = 0;
+    s_app = 0;
     s_leave = 0;
     s_ekin[0] = 0;
     s_ekin[1] = 0;
@@ -502,6 +518,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
   const int nnb = s_nnb;
   float ks = 0.f, kc = 0.f;
   long long khi = 0, klo = 0;  // DET: fixed-point kinetic energy of this thread's particles
+  // float builds: this lane's running single-segment current and its local
+  // cell (-1: none)
+  SegCurrent acc;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc.v[q] = 0.f;
+  int acc_key = -1;
 
   // deposits queued motion e of this warp (all segments, direct atomics)
   auto deposit_queued = [&](int e) {
@@ -512,9 +534,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     add_current(dep, a.ix, a.iy, segment_current(a, Cl.qnx, Cl.qny));
   };
 
-  // one particle per lane: push, deposit, boundary, compaction; the 32 lanes
-  // of a warp call it together (warp-level collectives only)
-  auto process = [&](bool valid, int ix, int iy, float x, float y, float ux, float uy, float uz) {
+  // one particle per lane: push, deposit, boundary, output; the 32 lanes of
+  // a warp call it together (warp-level collectives only).  `oslot` is the
+  // lane's own slot (>= 0: the output goes back there, a particle or a
+  // hole) or negative (no own slot); `incoming` marks arriving particles,
+  // which are appended after slot np if they stay.
+  auto process = [&](bool valid, int oslot, bool incoming, int ix, int iy, float x, float y, float ux, float uy,
+                     float uz) {
     // every lane runs the same instructions; invalid lanes carry a zero
     // particle and are masked out by `valid` where it matters
     int li = ix - cx0, lj = iy - cy0;
@@ -562,38 +588,45 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
     const int dest = (int)((unsigned)ix / TX) + (int)((unsigned)iy / TY) * Cl.ntx;
     const int code = (valid && keep) ? ((dest == t) ? 1 : 2) : 0;  // 1 stays, 2 leaves
 
-    // output slots: one shared-memory atomic per warp and kind; lanes keep
-    // their order inside the warp's run.  Stored before the current sums, so
-    // that the particle's registers are free while they run.
-    const unsigned mstay = __ballot_sync(0xffffffffu, code == 1);
-    const unsigned mleave = __ballot_sync(0xffffffffu, code == 2);
-    int sb = 0, lb = 0;
-    if (lane == 0) {
-      if (mstay) sb = atomicAdd(&s_stay, __popc(mstay));
-      if (mleave) lb = atomicAdd(&s_leave, __popc(mleave));
+    // output, before the current sums so that the particle's registers are
+    // free while they run: an own slot takes the particle back, or a hole
+    if (oslot >= 0) {
+      if (code == 1) store_particle(pout, base + oslot, ix, iy, x, y, ux, uy, uz);
+      else store_hole(pout, base + oslot);
     }
-    sb = __shfl_sync(0xffffffffu, sb, 0);
-    lb = __shfl_sync(0xffffffffu, lb, 0);
-    const unsigned below = (1u << lane) - 1;
-    if (code == 1) {
-      const int s = sb + __popc(mstay & below);
-      if (s < cap) store_particle(pout, base + s, ix, iy, x, y, ux, uy, uz);
-      else spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
-    } else if (code == 2) {
-      const int s = lb + __popc(mleave & below);
-      if (s < O.cap) {
-        store_particle(O.p, obase + s, ix, iy, x, y, ux, uy, uz);
-        O.dst[obase + s] = dest;
-      } else {
-        spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
+    // leavers to the outbox, arrivals that stay appended after slot np: one
+    // shared-memory atomic per warp and kind
+    const unsigned mleave = __ballot_sync(0xffffffffu, code == 2);
+    const unsigned mapp = incoming ? __ballot_sync(0xffffffffu, code == 1) : 0u;
+    if (mleave | mapp) {
+      int lb = 0, ab = 0;
+      if (lane == 0) {
+        if (mleave) lb = atomicAdd(&s_leave, __popc(mleave));
+        if (mapp) ab = atomicAdd(&s_app, __popc(mapp));
+      }
+      lb = __shfl_sync(0xffffffffu, lb, 0);
+      ab = __shfl_sync(0xffffffffu, ab, 0);
+      if (code == 2) {
+        const int s = lb + __popc(mleave & below);
+        if (s < O.cap) {
+          store_particle(O.p, obase + s, ix, iy, x, y, ux, uy, uz);
+          O.dst[obase + s] = dest;
+        } else {
+          spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
+        }
+      } else if (incoming && code == 1) {
+        const int s = n_own + ab + __popc(mapp & below);
+        if (s < cap) store_particle(pout, base + s, ix, iy, x, y, ux, uy, uz);
+        else spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
       }
     }
 
-    // segmented warp reduction of the single-segment currents over runs of
-    // lanes that start in the same cell (the runs are contiguous because
-    // the tile is sorted by cell; unsorted input only makes runs shorter);
-    // as many halving steps as the longest run needs
-    {
+    if constexpr (DET) {
+      // segmented warp reduction of the single-segment currents over runs
+      // of lanes that start in the same cell (the lanes read the chunk in
+      // cell order), as many halving steps as the longest run needs; each
+      // lane's contributions rounded to fixed point first, then summed as
+      // integers: the same total whatever lanes hold which particles
       const int key = valid ? (li + lj * TX) : -1 - lane;
       const int knext = __shfl_down_sync(0xffffffffu, key, 1);
       const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
@@ -601,51 +634,48 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       const int run_last = __ffs(lastmask & (0xffffffffu << lane)) - 1;
       const unsigned maxlen = __reduce_max_sync(0xffffffffu, (unsigned)(run_last - lane + 1));
       const bool head = valid && (lane == 0 || kprev != key);
-      if constexpr (DET) {
-        // each lane's contributions rounded to fixed point, then summed as
-        // integers: the same total whatever lanes hold which particles
-        int ih[8], im[8], il[8];
+      int ih[8], im[8], il[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) jsplit(cur.v[q], Cl, ih[q], im[q], il[q]);
+      for (int q = 0; q < 8; ++q) jsplit(cur.v[q], Cl, ih[q], im[q], il[q]);
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          if ((unsigned)off >= maxlen) break;
-          const bool take = lane + off <= run_last;
+      for (int off = 1; off < 32; off <<= 1) {
+        if ((unsigned)off >= maxlen) break;
+        const bool take = lane + off <= run_last;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int oh = __shfl_down_sync(0xffffffffu, ih[q], off);
-            const int om = __shfl_down_sync(0xffffffffu, im[q], off);
-            const int ol = __shfl_down_sync(0xffffffffu, il[q], off);
-            if (take) {
-              ih[q] += oh;
-              im[q] += om;
-              il[q] += ol;
-            }
+        for (int q = 0; q < 8; ++q) {
+          const int oh = __shfl_down_sync(0xffffffffu, ih[q], off);
+          const int om = __shfl_down_sync(0xffffffffu, im[q], off);
+          const int ol = __shfl_down_sync(0xffffffffu, il[q], off);
+          if (take) {
+            ih[q] += oh;
+            im[q] += om;
+            il[q] += ol;
           }
         }
-        if (head) {
-          dep.addi(0, li, lj, ih[0], im[0], il[0]);
-          dep.addi(0, li, lj + 1, ih[1], im[1], il[1]);
-          dep.addi(1, li, lj, ih[2], im[2], il[2]);
-          dep.addi(1, li + 1, lj, ih[3], im[3], il[3]);
-          dep.addi(2, li, lj, ih[4], im[4], il[4]);
-          dep.addi(2, li + 1, lj, ih[5], im[5], il[5]);
-          dep.addi(2, li, lj + 1, ih[6], im[6], il[6]);
-          dep.addi(2, li + 1, lj + 1, ih[7], im[7], il[7]);
-        }
-      } else {
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          if ((unsigned)off >= maxlen) break;
-          const bool take = lane + off <= run_last;
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const float o = __shfl_down_sync(0xffffffffu, cur.v[q], off);
-            if (take) cur.v[q] += o;
-          }
-        }
-        if (head) add_current(dep, li, lj, cur);
       }
+      if (head) {
+        dep.addi(0, li, lj, ih[0], im[0], il[0]);
+        dep.addi(0, li, lj + 1, ih[1], im[1], il[1]);
+        dep.addi(1, li, lj, ih[2], im[2], il[2]);
+        dep.addi(1, li + 1, lj, ih[3], im[3], il[3]);
+        dep.addi(2, li, lj, ih[4], im[4], il[4]);
+        dep.addi(2, li + 1, lj, ih[5], im[5], il[5]);
+        dep.addi(2, li, lj + 1, ih[6], im[6], il[6]);
+        dep.addi(2, li + 1, lj + 1, ih[7], im[7], il[7]);
+      }
+    } else {
+      // the lane's running sum: added to J when the lane's cell changes
+      // (the sum is over this lane's particles of one cell, in order)
+      const int key = li + lj * TX;
+      const bool change = valid && key != acc_key;
+      const bool flush = change && acc_key >= 0;
+      if (__any_sync(0xffffffffu, flush)) {
+        if (flush) add_current(dep, acc_key % TX, acc_key / TX, acc);
+      }
+      const float carry = change ? 0.0f : 1.0f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc.v[q] = __fmaf_rn(acc.v[q], carry, cur.v[q]);  // acc + cur, or cur
+      acc_key = change ? key : acc_key;
     }
 
     // queue the cell-crossing motions; deposit them once QFLUSH are waiting
@@ -653,7 +683,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       const unsigned sm = __ballot_sync(0xffffffffu, split);
       if (sm) {
         if (split) {
-          const int e = qcount + __popc(sm & ((1u << lane) - 1));
+          const int e = qcount + __popc(sm & below);
           qf[warp][0][e] = sx0;
           qf[warp][1][e] = sy0;
           qf[warp][2][e] = smx;
@@ -671,7 +701,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
         }
       }
     }
-
   };
 
   // incoming particles: warp w scans the outboxes of neighbours w, w + NW,
@@ -688,60 +717,93 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
       if (!bm) continue;
       int slot = 0;
       if (lane == 0) slot = atomicAdd(&s_nin, __popc(bm));
-      slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(bm & ((1u << lane) - 1));
+      slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(bm & below);
       if (bound && slot < INCAP) s_in[slot] = (e << 4) | m;
       const bool over = bound && slot >= INCAP;
       if (__any_sync(0xffffffffu, over)) {
         PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (over) r = load_particle(Oin.p, ob + e);
-        process(over, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
+        process(over, -2, true, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
       }
     }
   }
   __syncthreads();
 
-  // own particles: warp w takes chunks w, w + NW, ... of 32; the next
-  // chunk is copied into shared memory while this one is pushed
+  // own slots: warp w takes chunks w, w + NW, ... of kChunk slots, 32 at a
+  // time (a unit); its next unit is copied into shared memory while it is
+  // pushed.  In a full chunk lane l of the float builds takes the chunk's
+  // particle l kLaneRun + k of the cell order at step k; the deterministic
+  // builds take particle 32 k + l (cell order across the lanes).  That
+  // particle sits at its tile_slot, or, just after a sort (C.fresh), at its
+  // plain cell-order position; it goes back to its tile_slot.  A partial
+  // chunk is read and written in place.
   {
-    if (warp * 32 + lane < n_own) {
-      cp_async16(&pf_u[warp][lane], &pin.u[base + warp * 32 + lane]);
-      cp_async8(&pf_xy[warp][lane], &pin.xy[base + warp * 32 + lane]);
+    // read and write slots of this lane in unit u; false: no slot
+    const auto slots = [&](int u, int &rs, int &ws) -> bool {
+      const int c0 = (warp + NW * (u / kLaneRun)) * kChunk;
+      const int k = u % kLaneRun;
+      const int i = c0 + k * 32 + lane;
+      if (c0 + kChunk > n_own) {
+        rs = ws = i;
+        return i < n_own;
+      }
+      if constexpr (DET) {
+        const int j = k * 32 + lane;
+        ws = c0 + (j % kLaneRun) * 32 + j / kLaneRun;
+        rs = Cl.fresh ? c0 + j : ws;
+      } else {
+        ws = i;
+        rs = Cl.fresh ? c0 + lane * kLaneRun + k : ws;
+      }
+      return true;
+    };
+    const auto ubase = [&](int u) { return (warp + NW * (u / kLaneRun)) * kChunk + (u % kLaneRun) * 32; };
+    {
+      int rs, ws;
+      if (ubase(0) < n_own && slots(0, rs, ws)) {
+        cp_async16(&pf_u[warp][lane], &pin.u[base + rs]);
+        cp_async8(&pf_xy[warp][lane], &pin.xy[base + rs]);
+      }
     }
     cp_async_commit();
-    for (int k0 = warp * 32; k0 < n_own; k0 += NT) {
-      cp_async_wait<0>();  // this chunk's copies (each lane its own slot) are in
-      const int k = k0 + lane;
-      const bool valid = k < n_own;
+    for (int u = 0; ubase(u) < n_own; ++u) {
+      cp_async_wait<0>();  // this unit's copies (each lane its own slot) are in
+      int rs, ws;
+      const bool inr = slots(u, rs, ws);
       PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if (valid) {
-        const float4 u = pf_u[warp][lane];
+      bool valid = false;
+      if (inr) {
+        const float4 uu = pf_u[warp][lane];
         const float2 xy = pf_xy[warp][lane];
-        const unsigned c = (unsigned)__float_as_int(u.w);
-        r.ix = (int)(c & 0xffffu);
-        r.iy = (int)(c >> 16);
-        r.x = xy.x;
-        r.y = xy.y;
-        r.ux = u.x;
-        r.uy = u.y;
-        r.uz = u.z;
+        const unsigned c = (unsigned)__float_as_int(uu.w);
+        valid = c != kHole;
+        if (valid) {
+          r.ix = (int)(c & 0xffffu);
+          r.iy = (int)(c >> 16);
+          r.x = xy.x;
+          r.y = xy.y;
+          r.ux = uu.x;
+          r.uy = uu.y;
+          r.uz = uu.z;
+        }
       }
-      const int kn = k0 + NT + lane;
-      if (kn < n_own) {
-        cp_async16(&pf_u[warp][lane], &pin.u[base + kn]);
-        cp_async8(&pf_xy[warp][lane], &pin.xy[base + kn]);
+      {
+        int rn, wn;
+        if (ubase(u + 1) < n_own && slots(u + 1, rn, wn)) {
+          cp_async16(&pf_u[warp][lane], &pin.u[base + rn]);
+          cp_async8(&pf_xy[warp][lane], &pin.xy[base + rn]);
+        }
       }
       cp_async_commit();
-      process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
+      process(valid, inr ? ws : -2, false, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
     }
     cp_async_wait<0>();
   }
 
-  // the listed incoming particles, in chunks of 32 that continue the own
-  // chunks' round robin over the warps
+  // the listed incoming particles, in units of 32 spread over the warps
   {
     const int nin = min(s_nin, INCAP);
-    const int own_chunks = (n_own + 31) / 32;
-    for (int i = (warp + NW - own_chunks % NW) % NW; i * 32 < nin; i += NW) {
+    for (int i = warp; i * 32 < nin; i += NW) {
       const int k = i * 32 + lane;
       const bool valid = k < nin;
       PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -749,15 +811,17 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_push_tiles(const __grid_const
         const int v = s_in[k];
         r = load_particle(Oin.p, (long long)nb[v & 15] * Oin.cap + (v >> 4));
       }
-      process(valid, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
+      process(valid, -2, true, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
     }
   }
 
   if (lane < qcount) deposit_queued(lane);  // what is left in the queue
+  if constexpr (!DET)
+    if (acc_key >= 0) add_current(dep, acc_key % TX, acc_key / TX, acc);  // the lanes' last sums
 
   __syncthreads();
   if (threadIdx.x == 0) {
-    T.np[t] = min(s_stay, cap);
+    T.np[t] = n_own + min(s_app, cap - n_own);
     O.cnt[t] = min(s_leave, O.cap);
   }
   if constexpr (DET) {
@@ -806,6 +870,7 @@ __global__ void __launch_bounds__(NT) k_push_spill(const float *EB, float *J, Fi
                                                    int *err, PushConst C) {
   __shared__ double sred[NT / 32];
   const int n = min(*sin_cnt, sin_cap);
+  if (n == 0) return;  // the usual case: nothing spilled (uniform across the grid)
   const GlobalFields fld{EB, G.pitch, G.plane};
   const auto dep = [&] {
     if constexpr (DET)
