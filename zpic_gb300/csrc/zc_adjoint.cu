@@ -31,9 +31,12 @@
 // trajectory crosses a cell edge or the half-cell of the staggered gather).
 //
 // Checkpoints: the state (particles, E, B) is kept every K steps of the
-// forward run; the reverse sweep recomputes each segment of K steps from its
-// checkpoint, keeping the pre-step states of that segment, and then walks
-// it backwards.
+// forward run, which also keeps the pre-step states of its last two
+// segments (of its last one when two would take more than 8 GiB); the
+// reverse sweep walks those back directly, and recomputes every earlier
+// segment of K steps from its checkpoint, keeping its pre-step states, before
+// walking it backwards.  A kept step writes its particles straight into the
+// next step's slot, so keeping costs only the copies of E and B.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -967,12 +970,15 @@ struct Engine : EngineBase {
   R *E = nullptr, *B = nullptr, *J = nullptr, *tmp = nullptr;
   std::vector<std::pair<R, R>> passes;  // current filter passes along x
   std::vector<char> shifts;             // window moves of the last forward run, per step
-  // checkpoints (state + E + B) every K steps, and one segment of pre-step states
+  // checkpoints (state + E + B) every K steps, and the pre-step states of
+  // kseg segments (slot k: step k of the kept stretch)
   std::vector<DevState<R>> ck_s;
   std::vector<R *> ck_f;  // 6 planes each
   int nck = 0;            // checkpoints of the last forward run (slots are reused)
   std::vector<DevState<R>> seg_s;
   std::vector<R *> seg_f;
+  int kseg = 1;           // segments the forward run keeps (the last ones)
+  int keep0 = 0;          // first step kept by the last forward run
   int steps_done = 0;
   bool have_state = false;
   // reverse
@@ -1058,9 +1064,14 @@ struct Engine : EngineBase {
     TRY_(alloc(&d_cross, np));
     TRY_(alloc(&d_ncross, 1));
     TRY_(alloc(&d_scr, 16));
-    seg_s.resize(K);
-    seg_f.resize(K);
-    for (int k = 0; k < K; ++k) {
+    // the forward run keeps the pre-step states of its last two segments
+    // when they take at most 8 GiB (the reverse sweep then recomputes one
+    // segment fewer), else of the last one
+    const double slot_bytes = (double)state_span() + 6.0 * sizeof(R) * (double)pl;
+    kseg = (2.0 * K * slot_bytes <= 8.0 * (1 << 30)) ? 2 : 1;
+    seg_s.resize((size_t)kseg * K);
+    seg_f.resize((size_t)kseg * K);
+    for (int k = 0; k < kseg * K; ++k) {
       TRY_(alloc_state(seg_s[k]));
       TRY_(alloc(&seg_f[k], 6 * pl));
     }
@@ -1142,14 +1153,14 @@ struct Engine : EngineBase {
     return ZC_OK;
   }
 
-  zc_status copy_state(DevState<R> &dst, const DevState<R> &src) {
+  zc_status copy_state(const DevState<R> &dst, const DevState<R> &src) {
     ACK(cudaMemcpyAsync(dst.ix, src.ix, state_span(), cudaMemcpyDeviceToDevice, st));
     return ZC_OK;
   }
 
-  // keeps the pre-step state of step n of a segment in slot k
-  zc_status keep_pre_step(int k) {
-    TRY_(copy_state(seg_s[k], cur));
+  // keeps the pre-step fields of a step in slot k (the particles of a kept
+  // step are written there by the step before it)
+  zc_status keep_pre_fields(int k) {
     ACK(cudaMemcpyAsync(seg_f[k], E, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
     ACK(cudaMemcpyAsync(seg_f[k] + 3 * pl, B, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
     return ZC_OK;
@@ -1172,9 +1183,16 @@ struct Engine : EngineBase {
 
   // one step of the forward engine: cur -> nxt, E, B advanced
   zc_status step(int n, double *ekin) {
+    TRY_(step_into(n, cur, nxt, ekin));
+    std::swap(cur, nxt);
+    return ZC_OK;
+  }
+
+  // one step of the forward engine: particles src -> dst, E, B advanced
+  zc_status step_into(int n, const DevState<R> &src, const DevState<R> &dst, double *ekin) {
     const Params<R> P = params(n, shifts[n]);
     ACK(cudaMemsetAsync(J, 0, sizeof(R) * 3 * pl, st));
-    k_adj_push<R><<<grid_for(np, 256), 256, 0, st>>>(cur.view(np), nxt.view(np), w, birth, planes(E), planes(B),
+    k_adj_push<R><<<grid_for(np, 256), 256, 0, st>>>(src.view(np), dst.view(np), w, birth, planes(E), planes(B),
                                                       planes(J), ekin, P);
     ACK(cudaGetLastError());
     // current filter passes along x (current_smooth, em2d/current.c:427-459)
@@ -1200,11 +1218,10 @@ struct Engine : EngineBase {
       k_adj_yee_b<R><<<grid_for(pl), 256, 0, st>>>(E, B, nx, ny, hx, hy);
     }
     ACK(cudaGetLastError());
-    std::swap(cur, nxt);
     return ZC_OK;
   }
 
-  zc_status save_checkpoint() {
+  zc_status save_checkpoint(const DevState<R> &from) {
     if (nck == (int)ck_s.size()) {
       DevState<R> s;
       R *f = nullptr;
@@ -1213,15 +1230,15 @@ struct Engine : EngineBase {
       ck_s.push_back(s);
       ck_f.push_back(f);
     }
-    TRY_(copy_state(ck_s[nck], cur));
+    TRY_(copy_state(ck_s[nck], from));
     ACK(cudaMemcpyAsync(ck_f[nck], E, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
     ACK(cudaMemcpyAsync(ck_f[nck] + 3 * pl, B, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
     ++nck;
     return ZC_OK;
   }
 
-  zc_status restore_checkpoint(int k) {
-    TRY_(copy_state(cur, ck_s[k]));
+  zc_status restore_checkpoint(int k, const DevState<R> &to) {
+    TRY_(copy_state(to, ck_s[k]));
     ACK(cudaMemcpyAsync(E, ck_f[k], sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
     ACK(cudaMemcpyAsync(B, ck_f[k] + 3 * pl, sizeof(R) * 3 * pl, cudaMemcpyDeviceToDevice, st));
     return ZC_OK;
@@ -1252,13 +1269,23 @@ struct Engine : EngineBase {
     ACK(cudaEventRecord(e0, st));
     nck = 0;
     ACK(cudaMemsetAsync(d_scr + 1, 0, sizeof(double), st));
-    // the last segment's pre-step states are kept on the way: the reverse
-    // sweep starts with them and need not recompute that segment
+    // the last kseg segments' pre-step states are kept on the way (each
+    // kept step writes its particles straight into the next slot): the
+    // reverse sweep starts with them and need not recompute those segments
     const int last0 = ((nsteps - 1) / K) * K;
+    keep0 = std::max(0, last0 - (kseg - 1) * K);
     for (int n = 0; n < nsteps; ++n) {
-      if (n % K == 0) TRY_(save_checkpoint());
-      if (n >= last0) TRY_(keep_pre_step(n - last0));
-      TRY_(step(n, n == nsteps - 1 ? d_scr + 1 : nullptr));
+      double *ek = n == nsteps - 1 ? d_scr + 1 : nullptr;
+      if (n < keep0) {
+        if (n % K == 0) TRY_(save_checkpoint(cur));
+        TRY_(step(n, ek));
+        continue;
+      }
+      const int k = n - keep0;
+      if (k == 0) TRY_(copy_state(seg_s[0], cur));
+      if (n % K == 0) TRY_(save_checkpoint(seg_s[k]));
+      TRY_(keep_pre_fields(k));
+      TRY_(step_into(n, seg_s[k], n + 1 < nsteps ? seg_s[k + 1] : cur, ek));
     }
     steps_done = nsteps;
     ACK(cudaEventRecord(e1, st));
@@ -1314,18 +1341,21 @@ struct Engine : EngineBase {
     ACK(cudaMemsetAsync(dwv, 0, sizeof(R) * np, st));
     for (int sgi = nck - 1; sgi >= 0; --sgi) {
       const int n0 = sgi * K, n1 = std::min(steps_done, n0 + K);
-      // recompute the segment from its checkpoint, keeping pre-step states
-      // (the last one was kept by the forward run)
-      if (sgi != nck - 1) {
-        TRY_(restore_checkpoint(sgi));
+      // slots of this segment: kept by the forward run, or recomputed from
+      // its checkpoint into the first K slots (each step writing its
+      // particles straight into the next slot)
+      const bool kept = n0 >= keep0;
+      const int s0 = kept ? n0 - keep0 : 0;
+      if (!kept) {
+        TRY_(restore_checkpoint(sgi, seg_s[0]));
         for (int n = n0; n < n1; ++n) {
-          TRY_(keep_pre_step(n - n0));
-          if (n + 1 < n1) TRY_(step(n, nullptr));
+          TRY_(keep_pre_fields(n - n0));
+          if (n + 1 < n1) TRY_(step_into(n, seg_s[n - n0], seg_s[n - n0 + 1], nullptr));
         }
       }
       // walk the segment backwards
       for (int n = n1 - 1; n >= n0; --n) {
-        const int k = n - n0;
+        const int k = s0 + n - n0;
         TRY_(field_reverse(n));
         const Params<R> P = params(n, shifts[n]);
         ACK(cudaMemsetAsync(d_ncross, 0, sizeof(int), st));
@@ -1349,7 +1379,7 @@ struct Engine : EngineBase {
     TRY_(download(dEh, lamE, 3 * pl));
     TRY_(download(dBh, lamB, 3 * pl));
     // the engine's state goes back to the start of the run
-    TRY_(restore_checkpoint(0));
+    TRY_(restore_checkpoint(0, cur));
     ACK(cudaStreamSynchronize(st));
     cudaEventElapsedTime(&bwd_ms, e0, e1);
     steps_done = 0;
