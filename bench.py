@@ -466,6 +466,11 @@ def run_adjoint(args):
     for eps in (1e-4, 1e-5, 1e-6):
         fa = np.array([(Lf(amps + eps * e) - Lf(amps - eps * e)) / (2 * eps) for e in np.eye(len(amps))])
         fds[eps] = (fa, (Lf(amps, eps) - Lf(amps, -eps)) / (2 * eps))
+    # the float64 objective's own run-to-run noise (its deposit sums in the
+    # order the atomics land): the same inputs three times; a central
+    # difference at step eps carries up to noise / eps of it
+    reps = [Lf(amps) for _ in range(3)]
+    noise = float(max(reps) - min(reps))
     eps = 1e-6
     fd, fdd = fds[eps]
     rel_a = float(np.linalg.norm(ga - fd) / np.linalg.norm(fd))
@@ -474,7 +479,10 @@ def run_adjoint(args):
     rel_d64 = float(abs(gd64 - fdd) / abs(fdd))
     fd_steps = {f"{e:g}": {"amplitudes_rel_err_adjoint64": float(np.linalg.norm(ga64 - v[0]) / np.linalg.norm(v[0])),
                            "drift_rel_err_adjoint64": float(abs(gd64 - v[1]) / abs(v[1])),
-                           "fd_drift": v[1]} for e, v in fds.items()}
+                           "fd_drift": v[1],
+                           "drift_fd_noise_rel": noise / e / abs(v[1]),
+                           "amplitudes_fd_noise_rel": noise / e / float(np.linalg.norm(v[0]))}
+                for e, v in fds.items()}
     sim.close()
     sim64.close()
     grad_ms = fwd_ms + bwd_ms
@@ -496,7 +504,8 @@ def run_adjoint(args):
                                                "forward_ms": f64_ms[0], "backward_ms": f64_ms[1],
                                                "gradient_over_forward": (f64_ms[0] + f64_ms[1]) / f64_ms[0]},
                            "float32_adjoint": {"amplitudes_rel_err_vs_fd64": rel_a, "drift_rel_err_vs_fd64": rel_d},
-                           "eps": eps, "fd_by_step": fd_steps, "fd_amplitudes": fd.tolist(), "adjoint64_amplitudes": ga64.tolist(),
+                           "eps": eps, "fd_by_step": fd_steps, "objective64_noise": noise,
+                           "objective64": reps[0], "fd_amplitudes": fd.tolist(), "adjoint64_amplitudes": ga64.tolist(),
                            "adjoint32_amplitudes": ga.tolist(), "fd_drift": fdd, "adjoint64_drift": gd64,
                            "adjoint32_drift": gd},
         "clocks": clocks,

@@ -122,10 +122,6 @@ struct SpeciesState {
   long long ob_alloc = 0;
   int ob_in = 0;
   bool pending = false;
-  // tiles in plain cell order (sorted or laid out since the last push): the
-  // next push reads full chunks in that order and leaves them in the
-  // lane-run layout (tile_slot)
-  bool fresh = true;
   // energy
   double *d_ekin_tile = nullptr, *d_ekin_extra = nullptr, *d_ekin = nullptr;
   // window injection drawn on the device (zc_set_device_injection)
@@ -137,7 +133,7 @@ struct SpeciesState {
 struct Counters {
   int iter = 0, n_move = 0;
   std::vector<int> sp_iter, sp_n_move, cur, spill_cur, ob_in;
-  std::vector<bool> pending, fresh;
+  std::vector<bool> pending;
   int eb_cur = 0, j_cur = 0;
   long long launch[ZC_NPHASE] = {};
 };
@@ -412,7 +408,6 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   p.d_key = nkey;
   p.h_off = off;
   p.h_cap = cap;
-  p.fresh = true;
   dfree(d_cnt);
   dfree(d_fill);
   dfree(d_np_old);
@@ -525,7 +520,6 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   C.nty = s->nty;
   C.shift = shift;
   C.mw = s->mw;
-  C.fresh = 0;
   TRY(set_current_scale(s, p, C));
   const int in = p.spill_cur, out = 1 - p.spill_cur;
   {
@@ -555,12 +549,9 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
     Phase ph(s, ZC_PHASE_SORT, 1);
     CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles, st));
     p.cur = 1 - p.cur;
-    p.fresh = true;
     a.pin = p.buf[p.cur];
     a.pout = p.buf[1 - p.cur];
   }
-  a.C.fresh = p.fresh ? 1 : 0;
-  p.fresh = false;
   {
     Phase ph(s, ZC_PHASE_PUSH, 1);
     CK(launch_push_tiles(a, st));
@@ -814,7 +805,6 @@ Counters save_counters(const zc_sim *s) {
     c.spill_cur.push_back(p.spill_cur);
     c.ob_in.push_back(p.ob_in);
     c.pending.push_back(p.pending);
-    c.fresh.push_back(p.fresh);
   }
   c.eb_cur = s->eb_cur;
   c.j_cur = s->j_cur;
@@ -825,7 +815,7 @@ Counters save_counters(const zc_sim *s) {
 // the buffer parities a captured graph starts from
 bool same_parities(const Counters &a, const Counters &b) {
   return a.cur == b.cur && a.spill_cur == b.spill_cur && a.ob_in == b.ob_in && a.eb_cur == b.eb_cur &&
-         a.fresh == b.fresh && (a.iter % 2) == (b.iter % 2);
+         (a.iter % 2) == (b.iter % 2);
 }
 
 // the graph g holds n steps from the current state (block-aligned)
@@ -860,7 +850,6 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G) {
     p.spill_cur = before.spill_cur[k];
     p.ob_in = before.ob_in[k];
     p.pending = before.pending[k];
-    p.fresh = before.fresh[k];
   }
   s->eb_cur = before.eb_cur;
   s->j_cur = before.j_cur;
@@ -898,7 +887,6 @@ void account_steps(zc_sim *s, const StepGraph &g) {
     p.cur = g.after.cur[k];
     p.spill_cur = g.after.spill_cur[k];
     p.ob_in = g.after.ob_in[k];
-    p.fresh = g.after.fresh[k];
     p.n_move += g.after.sp_n_move[k] - g.before.sp_n_move[k];
   }
   s->n_move += g.after.n_move - g.before.n_move;
@@ -1389,7 +1377,6 @@ zc_status zc_species_create_device(zc_sim *s, float m_q, const int ppc[2], const
   I.seed_lo = (unsigned)seed;
   I.seed_hi = (unsigned)(seed >> 32);
   CK(launch_init_tiles(p.buf[p.cur], p.d_off, d_colpts, d_colmask, I, L, s->ntiles, s->st));
-  p.fresh = true;
   CK(cudaStreamSynchronize(s->st));
   dfree(d_colpts);
   dfree(d_colmask);

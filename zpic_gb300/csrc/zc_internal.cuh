@@ -25,13 +25,12 @@
 // back to the slot it came from, and a particle that leaves the tile leaves
 // a hole there (cell word kHole); particles arriving from other tiles are
 // appended after slot np.  The periodic cell sort compacts the holes away
-// and stores the tile in plain cell order.  The push that follows reads
-// every full chunk of 32 * kLaneRun particles in that order (lane l takes
-// particle l * kLaneRun + k at its k-th step) and writes it back transposed
-// (tile_slot: that particle goes to slot k * 32 + l); every later push
-// reads and writes slot k * 32 + l (coalesced), so lane l keeps meeting
-// the chunk's particles l * kLaneRun ... l * kLaneRun + kLaneRun - 1 one
-// after another, which lie in one or two cells.
+// and stores the tile in cell order, every full chunk of 32 * kLaneRun
+// particles transposed (tile_slot: particle l * kLaneRun + k of the chunk
+// at slot k * 32 + l).  A push warp reads and writes slot k * 32 + l at its
+// k-th step (coalesced), so lane l meets the chunk's particles
+// l * kLaneRun ... l * kLaneRun + kLaneRun - 1 one after another, which lie
+// in one or two cells.
 #pragma once
 
 #include <cuda.h>
@@ -54,7 +53,10 @@ struct Particles {       // one particle buffer
 };
 
 // particles a push lane takes from one chunk, one after another
-constexpr int kLaneRun = 8;
+#ifndef ZC_LANE_RUN
+#define ZC_LANE_RUN 8
+#endif
+constexpr int kLaneRun = ZC_LANE_RUN;
 constexpr int kChunk = 32 * kLaneRun;
 // cell word of an empty slot (no cell has both indices 0xffff: grids have at
 // most 65535 cells per axis)

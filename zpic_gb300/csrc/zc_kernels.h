@@ -13,9 +13,6 @@ struct PushConst {
   int nx, ny, ntx, nty;
   int shift;                              // moving-window shift applied this step (0/1)
   int mw;                                 // absorbing boundaries along x
-  int fresh;                              // tiles in plain cell order (sorted or laid out since the
-                                          // last push): full chunks are read in that order and
-                                          // written back in the lane-run layout
   // tile current as integers (see jsplit): a contribution v counts as
   // rint(v js) = h 2^2L + m 2^L + l; js_invl = 2^-L, js_twol = 2^L,
   // js_inv2l = 2^-2L, js_two2l = 2^2L, js_lo = 1 / js; deterministic global
@@ -137,7 +134,7 @@ ZC_SPILL_LAUNCHER(launch_push_spill_fast_det);
 cudaError_t launch_fixed_to_float(const unsigned long long *src, float *dst, size_t n, cudaStream_t st);
 cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, size_t n, cudaStream_t st);
 // counting sort of every tile by cell (src -> dst, same offsets): holes
-// dropped, np set to the particle count, plain cell order
+// dropped, np set to the particle count, cell order through tile_slot
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
                             const LayoutConst &L, int ntiles, cudaStream_t st);
 // particles (slots that are not holes) of every tile into cnt

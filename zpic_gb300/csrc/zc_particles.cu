@@ -173,9 +173,9 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 
 // Counting sort of every tile by local cell (one CTA of 1024 threads per
 // tile, src -> dst at the same offsets): a shared-memory histogram, a scan,
-// then every particle takes the next slot of its cell; holes are dropped
-// and np becomes the particle count.  The order inside a cell follows the
-// atomics' timing.  The reference sorts its whole buffer by cell every
+// then every particle takes the next position of its cell, stored at its
+// tile_slot (the lane-run layout); holes are dropped and np becomes the
+// particle count.  The order inside a cell follows the atomics' timing.  The reference sorts its whole buffer by cell every
 // n_sort steps for cache reuse (spec_sort, em2d/particles.c:942-1007); here
 // the per-tile sort gives the push lanes runs of particles in one cell.
 __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst, const int *off, int *np,
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst,
     const int c = cell_of_word(u.w);
     if (c < 0) continue;
     const float2 xy = src.xy[b + k];
-    const int slot = atomicAdd(&cursor[c], 1);
+    const int slot = tile_slot(atomicAdd(&cursor[c], 1), nvalid);
     dst.u[b + slot] = u;
     dst.xy[b + slot] = xy;
   }
@@ -265,7 +265,7 @@ __global__ void k_tile_order(Particles src, const unsigned *key, const int *off,
   }
   for (int p = threadIdx.x; p < n; p += blockDim.x) {
     const int from = sorted ? (int)(sk[p] & 0xfffffu) : p;
-    const long long s = b + from, d = b + p;
+    const long long s = b + from, d = b + (sorted ? tile_slot(p, n) : p);
     store_particle(dst, d, load_particle(src, s));
   }
 }
@@ -433,6 +433,7 @@ __global__ void __launch_bounds__(256) k_init_tiles(Particles buf, const int *of
   }
   __syncthreads();
   const int row = spre[wx];  // particles in one row of cells of the tile
+  const int ntile = row * wy;
   const long long base = off[t];
   for (int cell = threadIdx.x; cell < L.TX * L.TY; cell += blockDim.x) {
     const int li = cell % L.TX, lj = cell / L.TX;
@@ -440,8 +441,9 @@ __global__ void __launch_bounds__(256) k_init_tiles(Particles buf, const int *of
     const int i = cx0 + li, j = cy0 + lj;
     const int nc = colpts[i] * I.ppcy;
     if (nc == 0) continue;
-    // cell order inside the tile: local index li + lj * TX
-    const long long o = base + (long long)lj * row + spre[li];
+    // cell order inside the tile: local index li + lj * TX; position p of
+    // that order is stored at slot tile_slot(p, ntile)
+    const int o = lj * row + spre[li];
     const unsigned mask = colmask[i];
     float mx = 0.f, my = 0.f, mz = 0.f;
     int m = 0;
@@ -457,7 +459,8 @@ __global__ void __launch_bounds__(256) k_init_tiles(Particles buf, const int *of
         mx += ux;
         my += uy;
         mz += uz;
-        store_particle(buf, o + m, i, j, I.hx * (a + 0.5f), I.hy * (b + 0.5f), ux, uy, uz);
+        store_particle(buf, base + tile_slot(o + m, ntile), i, j, I.hx * (a + 0.5f), I.hy * (b + 0.5f), ux, uy,
+                       uz);
         ++m;
       }
     // remove the cell's mean momentum, add the fluid drift (particles.c:102-146)
@@ -466,8 +469,9 @@ __global__ void __launch_bounds__(256) k_init_tiles(Particles buf, const int *of
     my *= inv;
     mz *= inv;
     for (int k = 0; k < m; ++k) {
-      PRec r = load_particle(buf, o + k);
-      store_particle(buf, o + k, r.ix, r.iy, r.x, r.y, r.ux - mx + I.ufl[0], r.uy - my + I.ufl[1],
+      const long long q = base + tile_slot(o + k, ntile);
+      PRec r = load_particle(buf, q);
+      store_particle(buf, q, r.ix, r.iy, r.x, r.y, r.ux - mx + I.ufl[0], r.uy - my + I.ufl[1],
                      r.uz - mz + I.ufl[2]);
     }
   }

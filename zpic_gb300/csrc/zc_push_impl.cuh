@@ -731,31 +731,26 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
 
   // own slots: warp w takes chunks w, w + NW, ... of kChunk slots, 32 at a
   // time (a unit); its next unit is copied into shared memory while it is
-  // pushed.  In a full chunk lane l of the float builds takes the chunk's
-  // particle l kLaneRun + k of the cell order at step k; the deterministic
-  // builds take particle 32 k + l (cell order across the lanes).  That
-  // particle sits at its tile_slot, or, just after a sort (C.fresh), at its
-  // plain cell-order position; it goes back to its tile_slot.  A partial
-  // chunk is read and written in place.
+  // pushed.  In a full chunk lane l of the float builds takes slot 32 k + l
+  // at step k, which holds the chunk's particle l kLaneRun + k in cell
+  // order; the deterministic builds take the particle 32 k + l of the cell
+  // order, at its tile_slot.  Every particle goes back to the slot it came
+  // from.
   {
     // read and write slots of this lane in unit u; false: no slot
     const auto slots = [&](int u, int &rs, int &ws) -> bool {
       const int c0 = (warp + NW * (u / kLaneRun)) * kChunk;
       const int k = u % kLaneRun;
       const int i = c0 + k * 32 + lane;
-      if (c0 + kChunk > n_own) {
-        rs = ws = i;
-        return i < n_own;
-      }
       if constexpr (DET) {
-        const int j = k * 32 + lane;
-        ws = c0 + (j % kLaneRun) * 32 + j / kLaneRun;
-        rs = Cl.fresh ? c0 + j : ws;
-      } else {
-        ws = i;
-        rs = Cl.fresh ? c0 + lane * kLaneRun + k : ws;
+        if (c0 + kChunk <= n_own) {
+          const int j = k * 32 + lane;
+          rs = ws = c0 + (j % kLaneRun) * 32 + j / kLaneRun;
+          return true;
+        }
       }
-      return true;
+      rs = ws = i;
+      return i < n_own;
     };
     const auto ubase = [&](int u) { return (warp + NW * (u / kLaneRun)) * kChunk + (u % kLaneRun) * 32; };
     {
