@@ -216,6 +216,180 @@ __global__ void __launch_bounds__(32 * kSmoothWarps) k_smooth(const float *Jin, 
 }
 
 // ---------------------------------------------------------------------------
+// The same filter for up to 4 passes per axis, four columns per lane: a
+// warp owns 128 consecutive buffer columns (the first and last lane hold
+// halo columns only), so it writes 120 of them, moves its rows with 16-byte
+// copies where a lane's four columns are stored side by side (periodic
+// images and columns outside a moving window's buffer are copied one by
+// one) and filters four columns per instruction.  Every cell sees the
+// same float operations in the same order as k_smooth (and as one kernel
+// per pass, em2d/current.c:316-413).
+// ---------------------------------------------------------------------------
+constexpr int kS4Rows = 32;  // interior rows per warp
+constexpr int kS4Ring = 8;   // rows in flight per warp
+constexpr int kS4Warps = 8;  // warps per CTA
+constexpr int kS4W = 120;    // columns a warp writes
+
+__device__ __forceinline__ float4 f3pt4(float sa, float sb, const float4 &l, const float4 &m, const float4 &u,
+                                        const bool (&on)[4]) {
+  float4 r;
+  r.x = on[0] ? f3pt(sa, sb, l.x, m.x, u.x) : m.x;
+  r.y = on[1] ? f3pt(sa, sb, l.y, m.y, u.y) : m.y;
+  r.z = on[2] ? f3pt(sa, sb, l.z, m.z, u.z) : m.z;
+  r.w = on[3] ? f3pt(sa, sb, l.w, m.w, u.w) : m.w;
+  return r;
+}
+
+template <int NX, int NY>
+__global__ void __launch_bounds__(32 * kS4Warps) k_smooth4(const float *Jin, float *Jout, Grid G, SmoothPasses PX,
+                                                           SmoothPasses PY, int mw) {
+  __shared__ __align__(16) float4 ring[kS4Warps][kS4Ring][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gx = G.nx + 3;
+  const int nstrip = (gx + kS4W - 1) / kS4W;
+  const int nblk = (G.ny + kS4Rows - 1) / kS4Rows;
+  const int wid = blockIdx.x * kS4Warps + w;
+  if (wid >= nstrip * nblk) return;  // whole warps leave together
+  const int c = blockIdx.y;
+  const int strip = wid % nstrip, blk = wid / nstrip;
+  const int b0 = strip * kS4W - 4 + 4 * lane;  // this lane's first buffer column
+  // per column: source column (periodic image), presence, x and y filtering
+  int src[4];
+  bool have[4], xf[4], yf[4];
+  bool direct = true;  // four present columns stored side by side: one 16-byte copy
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int b = b0 + e, q = 4 * lane + e;
+    src[e] = b;
+    have[e] = true;
+    if (mw) have[e] = b >= 0 && b < gx;
+    else if (b < 1 || b > G.nx) src[e] = ((b - 1) % G.nx + G.nx) % G.nx + 1;
+    xf[e] = (q >= 1 && q <= 126) && (!mw || (b >= 1 && b <= G.nx));
+    yf[e] = b >= 1 && b <= G.nx;
+    direct = direct && have[e] && src[e] == b;
+  }
+  const bool writer = lane >= 1 && lane <= 30;
+  const float *pin = Jin + c * G.plane;
+  float *out = Jout + c * G.plane;
+  const int j0 = blk * kS4Rows;
+  const int nrows = min(kS4Rows, G.ny - j0);
+  const int R = nrows + 2 * NY;  // rows walked
+  float4 *slot = &ring[w][0][lane];
+  int jw = (j0 - NY) % G.ny;  // interior row of walk row 0
+  if (jw < 0) jw += G.ny;
+  auto copy_row = [&](float4 *dst, int jrow) {  // buffer row jrow + 1
+    const float *r = pin + (size_t)(jrow + 1) * G.pitch;
+    if (direct) {
+      cp_async16(dst, r + b0);
+    } else {
+      float *d = reinterpret_cast<float *>(dst);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) cp_async4_zfill(d + e, have[e] ? r + src[e] : Jin, have[e]);
+    }
+  };
+  int jl = jw;  // interior row of the next row to copy
+#pragma unroll 1
+  for (int d = 0; d < kS4Ring; ++d) {
+    if (d < R) copy_row(slot + d * 32, jl);
+    cp_async_commit();
+    jl = (jl + 1 == G.ny) ? 0 : jl + 1;
+  }
+  float4 glo, ghi;  // guard rows -1 and ny as stored
+  {
+    float lo[4], hi[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      lo[e] = have[e] ? pin[src[e]] : 0.f;
+      hi[e] = have[e] ? pin[(size_t)(G.ny + 1) * G.pitch + src[e]] : 0.f;
+    }
+    glo = make_float4(lo[0], lo[1], lo[2], lo[3]);
+    ghi = make_float4(hi[0], hi[1], hi[2], hi[3]);
+  }
+  // writes four columns of one output buffer row (the last strip may end
+  // past the buffer)
+  auto put = [&](int brow, const float4 &v) {
+    float *o = out + (size_t)brow * G.pitch + b0;
+    if (b0 + 3 < gx) {
+      *reinterpret_cast<float4 *>(o) = v;
+    } else {
+      const float a[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (b0 + e < gx) o[e] = a[e];
+    }
+  };
+  if (NY == 0 && blk == 0 && writer) {
+    // without y passes the y guard rows keep their values
+    put(0, glo);
+    put(G.ny + 1, ghi);
+    float t[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) t[e] = have[e] ? pin[(size_t)(G.ny + 2) * G.pitch + src[e]] : 0.f;
+    put(G.ny + 2, make_float4(t[0], t[1], t[2], t[3]));
+  }
+  float4 s0[NY > 0 ? NY : 1], s1[NY > 0 ? NY : 1];  // each stage's last two rows
+  int jprev = (jw == 0) ? G.ny - 1 : jw - 1;       // interior row of walk row rr - 1
+
+  auto step = [&](int rr, auto fill) {
+    constexpr bool FILL = decltype(fill)::value;
+    cp_async_wait<kS4Ring - 1>();  // row rr has arrived
+    const int k = rr & (kS4Ring - 1);
+    float4 v = slot[k * 32];
+    // the slot is free again: copy row rr + kS4Ring into it
+    if (rr + kS4Ring < R) copy_row(slot + k * 32, jl);
+    cp_async_commit();
+    jl = (jl + 1 == G.ny) ? 0 : jl + 1;
+#pragma unroll
+    for (int p = 0; p < NX; ++p) {
+      const float l = __shfl_up_sync(0xffffffffu, v.w, 1);
+      const float u = __shfl_down_sync(0xffffffffu, v.x, 1);
+      const float4 lv = make_float4(l, v.x, v.y, v.z), uv = make_float4(v.y, v.z, v.w, u);
+      v = f3pt4(PX.sa[p], PX.sb[p], lv, v, uv, xf);
+    }
+    // stage p receives walk row rr - p and emits the middle row once it
+    // holds the two rows below
+    bool emit = true;
+#pragma unroll
+    for (int p = 0; p < NY; ++p) {
+      const bool ready = !FILL || rr - p >= p + 2;
+      float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (ready) {
+        float4 lo = s0[p], hi = v;
+        if (p == 0) {
+          // the middle row next to a y guard row reads it as stored
+          lo = (jprev == 0) ? glo : lo;
+          hi = (jprev == G.ny - 1) ? ghi : hi;
+        }
+        e = f3pt4(PY.sa[p], PY.sb[p], lo, s1[p], hi, yf);
+      }
+      s0[p] = s1[p];
+      s1[p] = v;
+      if (FILL && !ready) {
+        emit = false;
+        break;
+      }
+      v = e;
+    }
+    jprev = (jprev + 1 == G.ny) ? 0 : jprev + 1;
+    // the last stage emits walk row rr - NY; rows NY .. R-1-NY are the output
+    if ((!FILL || (emit && rr >= 2 * NY)) && writer) {
+      const int j = j0 + rr - 2 * NY;
+      put(j + 1, v);
+      if (NY > 0) {
+        if (j == G.ny - 1) put(0, v);
+        if (j < 2) put(G.ny + 1 + j, v);
+      }
+    }
+  };
+  const int nfill = min(2 * NY, R);
+#pragma unroll 1
+  for (int rr = 0; rr < nfill; ++rr) step(rr, std::true_type{});
+#pragma unroll 2
+  for (int rr = nfill; rr < R; ++rr) step(rr, std::false_type{});
+  cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 // fused Yee advance: B half step, E full step, B half step
 // (yee_b / yee_e, em2d/emf.c:500-562), one 32 x 16 output tile per CTA.
 // E/B and J tiles with their halo arrive by TMA; B1 and E1 live in shared
@@ -478,6 +652,24 @@ cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
 cudaError_t launch_smooth(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
                           const SmoothPasses &PY, int mw, cudaStream_t st) {
   if (PX.n > kMaxSmoothPasses || PY.n > kMaxSmoothPasses || PX.n > 15) return cudaErrorInvalidValue;
+  if (PX.n <= 4 && PY.n <= 4) {
+    // four columns per lane
+    const long long warps4 = (long long)((G.nx + 3 + kS4W - 1) / kS4W) * ((G.ny + kS4Rows - 1) / kS4Rows);
+    const dim3 grid4((unsigned)((warps4 + kS4Warps - 1) / kS4Warps), 3);
+#define ZC_SMOOTH4(A, B)                                                          \
+    if (PX.n == A && PY.n == B) {                                                 \
+      k_smooth4<A, B><<<grid4, 32 * kS4Warps, 0, st>>>(Jin, Jout, G, PX, PY, mw); \
+      return cudaGetLastError();                                                  \
+    }
+#define ZC_SMOOTH4_ROW(A) ZC_SMOOTH4(A, 0) ZC_SMOOTH4(A, 1) ZC_SMOOTH4(A, 2) ZC_SMOOTH4(A, 3) ZC_SMOOTH4(A, 4)
+    ZC_SMOOTH4_ROW(0)
+    ZC_SMOOTH4_ROW(1)
+    ZC_SMOOTH4_ROW(2)
+    ZC_SMOOTH4_ROW(3)
+    ZC_SMOOTH4_ROW(4)
+#undef ZC_SMOOTH4_ROW
+#undef ZC_SMOOTH4
+  }
   const int W = 32 - 2 * PX.n;
   const long long warps = (long long)((G.nx + 3 + W - 1) / W) * ((G.ny + kSmoothRows - 1) / kSmoothRows);
   const dim3 grid((unsigned)((warps + kSmoothWarps - 1) / kSmoothWarps), 3);
