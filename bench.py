@@ -449,7 +449,7 @@ def run_adjoint(args):
     # float64: the adjoint's own gradient and central differences of the engine
     sim64 = adjoint.AdjointSim(nx, box, dt, n, q, checkpoint_every=K, precision="float64")
     load(sim64, st["w"])
-    sim64.forward(steps)
+    L64, _ = sim64.forward(steps)
     g64 = sim64.backward()
     f64_ms = sim64.times()
     ga64 = adjoint.amplitude_gradient(g64["w"], st["X"], kk)
@@ -504,6 +504,10 @@ def run_adjoint(args):
                                                "forward_ms": f64_ms[0], "backward_ms": f64_ms[1],
                                                "gradient_over_forward": (f64_ms[0] + f64_ms[1]) / f64_ms[0]},
                            "float32_adjoint": {"amplitudes_rel_err_vs_fd64": rel_a, "drift_rel_err_vs_fd64": rel_d},
+                           "float32_vs_float64": {
+                               "objective_rel": float(abs(L - L64) / abs(L64)),
+                               "amplitudes_rel_l2": float(np.linalg.norm(ga - ga64) / np.linalg.norm(ga64)),
+                               "drift_rel": float(abs(gd - gd64) / abs(gd64))},
                            "eps": eps, "fd_by_step": fd_steps, "objective64_noise": noise,
                            "objective64": reps[0], "fd_amplitudes": fd.tolist(), "adjoint64_amplitudes": ga64.tolist(),
                            "adjoint32_amplitudes": ga.tolist(), "fd_drift": fdd, "adjoint64_drift": gd64,
@@ -592,7 +596,7 @@ def run_wakefield_adjoint(args):
     sim.close()
     sim64 = make("float64")
     load(sim64, 1.0, kn)
-    sim64.forward(steps)
+    L64, _ = sim64.forward(steps)
     g64 = sim64.backward()
     f64_ms = sim64.times()
     ga0_64 = float((g64["E"] * W["E"]).sum() + (g64["B"] * W["B"]).sum()) / a0
@@ -634,7 +638,14 @@ def run_wakefield_adjoint(args):
                            "float32_adjoint": {"dL_da0_rel_err_vs_fd64": rel(ga0, fd_a0),
                                                "knots_rel_err_vs_fd64": {str(k): rel(gk[k], v)
                                                                          for k, v in fd_k.items()}},
-                           "fd_da0": fd_a0, "fd_knots": {str(k): v for k, v in fd_k.items()}},
+                           "fd_da0": fd_a0, "fd_knots": {str(k): v for k, v in fd_k.items()},
+                           # how far float32 arithmetic alone moves the run: the objective and the
+                           # whole gradient of the float32 engine against the float64 engine's
+                           "float32_vs_float64": {
+                               "objective_rel": rel(L, L64),
+                               "dL_da0_rel": rel(ga0, ga0_64),
+                               "knots_rel_l2": float(np.linalg.norm(gk - gk64) / np.linalg.norm(gk64)),
+                               "knots_rel": [rel(a, b) for a, b in zip(gk, gk64)]}},
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)

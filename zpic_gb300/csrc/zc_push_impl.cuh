@@ -418,10 +418,10 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
 // builds read every chunk in cell order across the lanes and pre-reduce
 // with segmented warp sums of fixed-point parts.
 // ---------------------------------------------------------------------------
-// resident CTAs per SM the float builds are compiled for (64 registers a
-// thread at 8)
+// resident CTAs per SM the float builds are compiled for: 7 (up to 72
+// registers a thread) measured faster than 8 (64, with spills) and 6
 #ifndef ZC_PUSH_MIN_CTAS
-#define ZC_PUSH_MIN_CTAS 8
+#define ZC_PUSH_MIN_CTAS 7
 #endif
 template <int TX, int TY, int NT, bool DET>
 __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push_tiles(const __grid_constant__ CUtensorMap tm_eb,
