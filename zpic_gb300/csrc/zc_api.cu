@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/zpic_cuda.h"
@@ -825,8 +826,10 @@ bool graph_ready(const zc_sim *s, const StepGraph &g, int n) {
 
 // Captures n steps, starting at a block boundary, as a graph.  Capturing
 // does not run anything: the host state advanced by the capture is put
-// back afterwards.
-zc_status capture_steps(zc_sim *s, int n, StepGraph &G) {
+// back afterwards.  Without `instantiate` the graph is only recorded (a
+// batch copies it into its own graph); ensure_exec instantiates it when the
+// simulation replays it itself.
+zc_status capture_steps(zc_sim *s, int n, StepGraph &G, bool instantiate = true) {
   drop_graph(G);
   if (s->iter % block_period(s) != 0) return fail(ZC_ESTATE, "graph capture off a block boundary");
   const Counters before = save_counters(s);
@@ -860,10 +863,12 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G) {
   }
   if (e != cudaSuccess) return fail(ZC_ECUDA, "stream capture failed: %s", cudaGetErrorString(e));
   cudaGraphExec_t x = nullptr;
-  const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
-  if (ei != cudaSuccess) {
-    cudaGraphDestroy(g);
-    return fail(ZC_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(ei));
+  if (instantiate) {
+    const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+    if (ei != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return fail(ZC_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(ei));
+    }
   }
   G.graph = g;
   G.exec = x;
@@ -873,6 +878,17 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G) {
   G.valid = true;
   G.id = ++g_capture_id;
   s->n_capture += 1;
+  return ZC_OK;
+}
+
+// instantiates a graph that was only recorded
+zc_status ensure_exec(StepGraph &G) {
+  if (G.exec) return ZC_OK;
+  const cudaError_t e = cudaGraphInstantiate(&G.exec, G.graph, 0);
+  if (e != cudaSuccess) {
+    G.exec = nullptr;
+    return fail(ZC_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+  }
   return ZC_OK;
 }
 
@@ -958,6 +974,7 @@ zc_status step_graph(zc_sim *s, int *nsteps) {
   int launched = 0;
   while (*nsteps >= P) {
     if (!graph_ready(s, s->blk, P)) TRY(capture_steps(s, P, s->blk));
+    TRY(ensure_exec(s->blk));
     CK(cudaGraphLaunch(s->blk.exec, s->st));
     account_steps(s, s->blk);
     *nsteps -= P;
@@ -976,6 +993,7 @@ zc_status step_graph(zc_sim *s, int *nsteps) {
   }
   if (*nsteps > 0) {
     if (!graph_ready(s, s->tail, *nsteps)) TRY(capture_steps(s, *nsteps, s->tail));
+    TRY(ensure_exec(s->tail));
     CK(cudaGraphLaunch(s->tail.exec, s->st));
     account_steps(s, s->tail);
     *nsteps = 0;
@@ -1021,6 +1039,7 @@ zc_status step_graph_mw(zc_sim *s, int *nsteps) {
       }
       g = &s->mw_blk.back();
     }
+    TRY(ensure_exec(*g));
     CK(cudaGraphLaunch(g->exec, s->st));
     account_steps(s, *g);
     *nsteps -= P;
@@ -2024,10 +2043,39 @@ void drop_parent(zc_batch::Parent &g) {
 zc_status batch_ready(zc_batch *b, zc_batch::Parent &pg, int n) {
   const bool have = pg.valid && pg.nsteps == n && pg.ids.size() == b->sims.size();
   bool ok = have;
+  // the members to (re)capture, recorded by a few host threads at once
+  // (each member captures on its own stream; nothing runs)
+  std::vector<int> todo;
+  for (size_t k = 0; k < b->sims.size(); ++k) {
+    zc_sim *s = b->sims[k];
+    if (!graph_ready(s, (n == b->period) ? s->blk : s->tail, n)) todo.push_back((int)k);
+  }
+  if (!todo.empty()) {
+    const int nt = (int)std::min<size_t>(todo.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+    std::vector<zc_status> res(nt, ZC_OK);
+    std::vector<std::string> msg(nt);
+    auto work = [&](int w) {
+      if (cudaSetDevice(b->device) != cudaSuccess) {
+        res[w] = ZC_ECUDA;
+        msg[w] = "cudaSetDevice failed in a capture thread";
+        return;
+      }
+      for (size_t i = w; i < todo.size() && res[w] == ZC_OK; i += nt) {
+        zc_sim *s = b->sims[todo[i]];
+        res[w] = capture_steps(s, n, (n == b->period) ? s->blk : s->tail, false);
+        if (res[w] != ZC_OK) msg[w] = g_err;
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nt; ++w) pool.emplace_back(work, w);
+    work(0);
+    for (auto &t : pool) t.join();
+    for (int w = 0; w < nt; ++w)
+      if (res[w] != ZC_OK) return fail(res[w], "%s", msg[w].c_str());
+  }
   for (size_t k = 0; k < b->sims.size(); ++k) {
     zc_sim *s = b->sims[k];
     StepGraph &g = (n == b->period) ? s->blk : s->tail;
-    if (!graph_ready(s, g, n)) TRY(capture_steps(s, n, g));
     if (have && pg.ids[k] != g.id) {
       // a member was captured again (after a re-layout): its copy in the
       // instantiated graph takes the new parameters in place when the
