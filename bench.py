@@ -471,6 +471,8 @@ def run_adjoint(args):
     # difference at step eps carries up to noise / eps of it
     reps = [Lf(amps) for _ in range(3)]
     noise = float(max(reps) - min(reps))
+    # the drift's differences at still smaller steps
+    fd_drift_small = {f"{e:g}": (Lf(amps, e) - Lf(amps, -e)) / (2 * e) for e in (1e-7, 1e-8)}
     eps = 1e-6
     fd, fdd = fds[eps]
     rel_a = float(np.linalg.norm(ga - fd) / np.linalg.norm(fd))
@@ -509,6 +511,8 @@ def run_adjoint(args):
                                "amplitudes_rel_l2": float(np.linalg.norm(ga - ga64) / np.linalg.norm(ga64)),
                                "drift_rel": float(abs(gd - gd64) / abs(gd64))},
                            "eps": eps, "fd_by_step": fd_steps, "objective64_noise": noise,
+                           "fd_drift_small_steps": {k: {"fd": v, "rel_err_adjoint64": float(abs(gd64 - v) / abs(v))}
+                                                    for k, v in fd_drift_small.items()},
                            "objective64": reps[0], "fd_amplitudes": fd.tolist(), "adjoint64_amplitudes": ga64.tolist(),
                            "adjoint32_amplitudes": ga.tolist(), "fd_drift": fdd, "adjoint64_drift": gd64,
                            "adjoint32_drift": gd},

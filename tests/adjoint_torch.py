@@ -175,7 +175,7 @@ def step(state, E, B, w, P):
     ix, iy, x, y, ux, uy, uz = state
     f = gather(E, B, P, ix, iy, x, y)
     ux, uy, uz, mx, my, qvz = boris(ux, uy, uz, f, P)
-    J = torch.zeros((3, P.ny, P.nx), dtype=T)
+    J = torch.zeros((3, P.ny, P.nx), dtype=T, device=E.device)
     J = deposit(J, P, ix, iy, x, y, mx, my, qvz, w)
     x1, y1 = x + mx, y + my
     di = (x1.detach() >= 1).long() - (x1.detach() < 0).long()
