@@ -89,11 +89,12 @@ def load_run(run: ScanRun):
 
 
 def make_sim(run: ScanRun, species, tile=(32, 16), fast_math=True, sort_every=0, history=True, graphs=True,
-             device=0, tile_slack=1.0) -> CudaSim:
-    """The run's simulation.  Tiles get room for twice their initial
+             device=0, tile_slack=2.0) -> CudaSim:
+    """The run's simulation.  Tiles get room for three times their initial
     particles (``tile_slack``): filaments of the two-stream instability
-    gather particles, and a tile that overflows sends particles to the
-    slower spill path until the next re-layout."""
+    gather particles, and between two cell sorts a tile also holds the holes
+    its leavers left beside the particles that arrived; a tile that overflows
+    sends particles to the slower spill path until the next re-layout."""
     sim = CudaSim(run.nx, run.box, run.dt, device=device, tile=tile, fast_math=fast_math, sort_every=sort_every,
                   tile_slack=tile_slack)
     for m_q, q, ppc, parts in species:
@@ -169,6 +170,16 @@ def run_sequential(sims, runs) -> ScanResult:
 def _counters(sims):
     info = [s.info() for s in sims]
     return {"relayouts": sum(i["relayouts"] for i in info), "captures": sum(i["captures"] for i in info)}
+
+
+def scan_sort_every(steps, longest=8):
+    """The longest cell-sort interval up to ``longest`` whose block of
+    2 x interval steps divides the run: the batch then replays whole blocks
+    only, with no shorter tail block to record."""
+    for k in range(longest, 0, -1):
+        if steps % (2 * k) == 0:
+            return k
+    return longest
 
 
 def autotune_tile(runs, candidates=((16, 16), (32, 16), (16, 8)), sample=64, steps=32, fast_math=True,
