@@ -638,6 +638,12 @@ def run_wakefield_adjoint(args):
         fd_k[k] = (Lf(1.0, kn + e) - Lf(1.0, kn - e)) / (2 * eps)
     sim64.close()
     rel = lambda a, b: float(abs(a - b) / max(abs(b), 1e-300))
+    ks = sorted(fd_k)
+
+    def l2(g_):
+        # the checked knots' gradient as one vector against the differences
+        d = np.array([g_[k] - fd_k[k] for k in ks])
+        return float(np.linalg.norm(d) / np.linalg.norm([fd_k[k] for k in ks]))
     nps = sum(int(((W["birth"] <= s_) ).sum()) for s_ in range(0, steps, max(steps // 30, 1))) * max(steps // 30, 1)
     line = {
         "metric": METRIC, "value": nps / ((fwd_ms + bwd_ms) * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": steps,
@@ -657,10 +663,12 @@ def run_wakefield_adjoint(args):
                            "float64_adjoint": {"forward_ms": f64_ms[0], "backward_ms": f64_ms[1],
                                                "dL_da0_rel_err_vs_fd64": rel(ga0_64, fd_a0),
                                                "knots_rel_err_vs_fd64": {str(k): rel(gk64[k], v)
-                                                                         for k, v in fd_k.items()}},
+                                                                         for k, v in fd_k.items()},
+                                               "knots_rel_l2_vs_fd64": l2(gk64)},
                            "float32_adjoint": {"dL_da0_rel_err_vs_fd64": rel(ga0, fd_a0),
                                                "knots_rel_err_vs_fd64": {str(k): rel(gk[k], v)
-                                                                         for k, v in fd_k.items()}},
+                                                                         for k, v in fd_k.items()},
+                                               "knots_rel_l2_vs_fd64": l2(gk)},
                            "fd_da0": fd_a0, "fd_knots": {str(k): v for k, v in fd_k.items()},
                            # how far float32 arithmetic alone moves the run: the objective and the
                            # whole gradient of the float32 engine against the float64 engine's
