@@ -1034,12 +1034,16 @@ def main():
     t0 = time.perf_counter()
     if args_steps_e2e:
         sim.set_fields(E=Eh, B=Bh)
+        t_f = time.perf_counter()
         sim.set_particles(0, pinned)
+        t_p = time.perf_counter()
     hist = []
     for _ in range(args_steps_e2e):
         sim.step(1)
         hist.append(sim.energy())
     t_e2e = time.perf_counter() - t0
+    e2e_parts = ({"fields_upload_s": t_f - t0, "particles_upload_s": t_p - t_f,
+                  "steps_with_readback_s": t0 + t_e2e - t_p} if args_steps_e2e else {})
     barrier()
     t_e2e = allmax(t_e2e)
     e2e = N * args_steps_e2e * world / t_e2e if args_steps_e2e else None
@@ -1073,7 +1077,7 @@ def main():
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "how": "fields and particles uploaded from pinned host buffers through the C-ABI, "
-                       "then per step zc_step(1) + zc_energy read-back"},
+                       "then per step zc_step(1) + zc_energy read-back", **e2e_parts},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_push_tiles", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

@@ -110,7 +110,6 @@ struct SpeciesState {
   long long alloc = 0;   // particles per buffer
   Particles buf[2] = {};
   int cur = 0;
-  unsigned *d_key = nullptr;
   // spill lists (in: processed this step, out: written this step)
   Particles spill[2] = {};
   int *d_spill_cnt = nullptr;  // [2]
@@ -315,7 +314,9 @@ void invalidate_graph(zc_sim *s);
 
 // Builds the tile layout of a species from per-tile counts and moves its
 // particles (tiles of the current layout, its spill list and an optional
-// new list) into it.  Every tile is then ordered deterministically.
+// new list) into it.  Every tile is then sorted by cell (k_cellsort).  The
+// order inside a cell is not fixed; the deterministic mode sums currents
+// and energies in an order-independent way.
 zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   SpeciesState &p = s->sp[k];
   cudaStream_t st = s->st;
@@ -370,43 +371,30 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
     nbuf[0] = p.buf[0];
     nbuf[1] = p.buf[1];
   }
-  unsigned *nkey = p.d_key;
-  if (grow || !nkey) {
-    TRY(dalloc(&nkey, tot));
-  }
   // destination of the scatter: the buffer that does not hold the particles
   const int src_i = p.cur, tmp_i = 1 - p.cur;
   Particles tmp = grow ? nbuf[1] : p.buf[tmp_i];
   CK(cudaMemcpyAsync(p.d_off, off.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(p.d_cap, cap.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
-  CK(launch_copy_tiles(p.buf[src_i], d_off_old, d_np_old, tmp, p.d_off, nkey, d_fill, nt, st));
+  CK(launch_copy_tiles(p.buf[src_i], d_off_old, d_np_old, tmp, p.d_off, d_fill, nt, st));
   CK(launch_scatter_list(p.spill[p.spill_cur], p.d_spill_cnt + p.spill_cur, p.spill_cap, tmp, p.d_off,
-                         p.d_cap, d_fill, nkey, 1u << 30, L, s->d_err, st));
+                         p.d_cap, d_fill, L, s->d_err, st));
   if (list && list_n > 0)
-    CK(launch_scatter_list(*list, d_list_n, list_n, tmp, p.d_off, p.d_cap, d_fill, nkey, 1u << 31, L,
-                           s->d_err, st));
+    CK(launch_scatter_list(*list, d_list_n, list_n, tmp, p.d_off, p.d_cap, d_fill, L, s->d_err, st));
   CK(cudaMemcpyAsync(p.d_np, cnt.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
-  // order every tile into the other buffer
+  // every tile into the other buffer in cell order (the lane-run layout)
   Particles dst = grow ? nbuf[0] : p.buf[src_i];
-  int smax = 0;
-  for (int t = 0; t < nt; ++t) smax = std::max(smax, cnt[t]);
-  const int smem_cap = 16 * 1024;  // keys held in shared memory (8 bytes each); a power of two
-  int sm = 1;
-  while (sm < smax) sm <<= 1;
-  sm = std::min(sm, smem_cap);
-  CK(launch_tile_order(tmp, nkey, p.d_off, p.d_np, dst, nt, std::max(sm, 1), L, st));
+  CK(launch_cellsort(tmp, dst, p.d_off, p.d_np, L, nt, st));
   CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), st));
   CK(cudaStreamSynchronize(st));
   if (grow) {
     free_particles(p.buf[0]);
     free_particles(p.buf[1]);
-    if (p.d_key) dfree(p.d_key);
     p.buf[0] = nbuf[0];
     p.buf[1] = nbuf[1];
     p.alloc = tot;
     p.cur = 0;
   }
-  p.d_key = nkey;
   p.h_off = off;
   p.h_cap = cap;
   dfree(d_cnt);
@@ -1247,7 +1235,6 @@ zc_status zc_sim_destroy(zc_sim *s) {
       dfree(p.ob[b].dst);
       dfree(p.ob[b].cnt);
     }
-    dfree(p.d_key);
     dfree(p.d_spill_cnt);
     dfree(p.d_ekin_tile);
     dfree(p.d_ekin_extra);

@@ -148,12 +148,10 @@ cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, 
 cudaError_t launch_count_list(const Particles &list, const int *n_ptr, int n_cap, int *cnt, const LayoutConst &L,
                               cudaStream_t st);
 cudaError_t launch_copy_tiles(const Particles &src, const int *off_old, const int *np_old, const Particles &dst,
-                              const int *off_new, unsigned *key, int *fill, int ntiles, cudaStream_t st);
+                              const int *off_new, int *fill, int ntiles, cudaStream_t st);
 cudaError_t launch_scatter_list(const Particles &list, const int *n_ptr, int n_cap, const Particles &dst,
-                                const int *off, const int *cap, int *fill, unsigned *key, unsigned key0,
-                                const LayoutConst &L, int *err, cudaStream_t st);
-cudaError_t launch_tile_order(const Particles &src, const unsigned *key, const int *off, const int *np,
-                              const Particles &dst, int ntiles, int smax, const LayoutConst &L, cudaStream_t st);
+                                const int *off, const int *cap, int *fill, const LayoutConst &L, int *err,
+                                cudaStream_t st);
 cudaError_t launch_append_list(const Particles &list, int n, const Particles &buf, const TileSet &T,
                                const Spill &S, const LayoutConst &L, int *err, cudaStream_t st);
 // a column of cold particles injected after a window move: per row of the

@@ -85,6 +85,21 @@ __device__ __forceinline__ int tile_of(int ix, int iy, const LayoutConst &L) {
   return (ix / L.TX) + (iy / L.TY) * L.ntx;
 }
 
+// adds n_lanes to counter[t] for every group of the calling (active) lanes
+// that share t, with one atomic per group; returns the counter's old value
+// plus this lane's rank in its group (lists in cell order put most lanes of
+// a warp on one tile)
+__device__ __forceinline__ int warp_grouped_add(int *counter, int t) {
+  const unsigned am = __activemask();
+  const unsigned same = __match_any_sync(am, t);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(same) - 1;
+  int first = 0;
+  if (lane == leader) first = atomicAdd(&counter[t], __popc(same));
+  first = __shfl_sync(same, first, leader);
+  return first + __popc(same & ((1u << lane) - 1));
+}
+
 // AoS staging records -> SoA list, counting the particles of each tile
 __global__ void k_stage_to_list(const float4 *aos7, int n, Particles list, int *cnt, LayoutConst L,
                                 int *err) {
@@ -100,7 +115,7 @@ __global__ void k_stage_to_list(const float4 *aos7, int n, Particles list, int *
     }
     store_particle(list, k, ix, iy, __int_as_float(r[2]), __int_as_float(r[3]), __int_as_float(r[4]),
                    __int_as_float(r[5]), __int_as_float(r[6]));
-    atomicAdd(&cnt[tile_of(ix, iy, L)], 1);
+    warp_grouped_add(cnt, tile_of(ix, iy, L));
   }
 }
 
@@ -111,14 +126,14 @@ __global__ void k_count_list(Particles list, const int *n_ptr, int n_cap, int *c
   {
     int ix, iy;
     load_cell(list, k, ix, iy);
-    atomicAdd(&cnt[tile_of(ix, iy, L)], 1);
+    warp_grouped_add(cnt, tile_of(ix, iy, L));
   }
 }
 
-// tile particles keep their tile and their order: copy to the new offsets,
-// holes dropped (one CTA of 256 threads per tile)
+// tile particles keep their tile: copy to the new offsets, holes dropped
+// (one CTA of 256 threads per tile)
 __global__ void __launch_bounds__(256) k_copy_tiles(Particles src, const int *off_old, const int *np_old,
-                                                    Particles dst, const int *off_new, unsigned *key, int *fill) {
+                                                    Particles dst, const int *off_new, int *fill) {
   __shared__ int swarp[8];
   const int t = blockIdx.x;
   const int n = np_old[t];
@@ -132,7 +147,6 @@ __global__ void __launch_bounds__(256) k_copy_tiles(Particles src, const int *of
     if (f) {
       const int q = placed + pre;
       store_particle(dst, b + q, load_particle(src, a + k));
-      if (key) key[b + q] = (unsigned)q;
     }
     placed += tot;
   }
@@ -152,19 +166,17 @@ __global__ void __launch_bounds__(256) k_count_valid(Particles buf, const int *o
   if (threadIdx.x == 0) cnt[t] = tot;
 }
 
-// list particles are appended to their tile; `key0 + k` remembers the order
+// list particles are appended to their tile
 __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Particles dst, const int *off,
-                               const int *cap, int *fill, unsigned *key, unsigned key0, LayoutConst L,
-                               int *err) {
+                               const int *cap, int *fill, LayoutConst L, int *err) {
   const int n = min(*n_ptr, n_cap);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const PRec r = load_particle(list, k);
     const int t = tile_of(r.ix, r.iy, L);
-    const int s = atomicAdd(&fill[t], 1);
+    const int s = warp_grouped_add(fill, t);
     if (s < cap[t]) {
       const long long q = (long long)off[t] + s;
       store_particle(dst, q, r);
-      if (key) key[q] = key0 + (unsigned)k;
     } else {
       atomicOr(err, ERR_OVERFLOW);  // capacities are sized from exact counts: cannot happen
     }
@@ -218,56 +230,6 @@ __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst,
     dst.xy[b + slot] = xy;
   }
   if (threadIdx.x == 0) np[t] = nvalid;
-}
-
-// Orders every tile deterministically after a re-layout: by cell, and
-// within a cell by the key (origin order).  One CTA per tile; tiles larger
-// than the shared-memory sort capacity are copied unsorted (the periodic cell
-// sort fixes them).
-__global__ void k_tile_order(Particles src, const unsigned *key, const int *off, const int *np,
-                             Particles dst, int smax, LayoutConst L) {
-  extern __shared__ unsigned long long sk[];  // (cell << 52) | (key << 20) | local index
-  const int t = blockIdx.x;
-  const int n = np[t];
-  const long long b = off[t];
-  const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
-  const bool sorted = (n <= smax) && (n < (1 << 20));
-  if (sorted) {
-    int m = 1;
-    while (m < n) m <<= 1;
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
-      unsigned long long v = ~0ull;
-      if (k < n) {
-        int ix, iy;
-        load_cell(src, b + k, ix, iy);
-        const unsigned cell = (unsigned)((ix - cx0) + (iy - cy0) * L.TX) & 0xfffu;
-        v = ((unsigned long long)cell << 52) | ((unsigned long long)(key[b + k] & 0xffffffffu) << 20) |
-            (unsigned)k;
-      }
-      sk[k] = v;
-    }
-    __syncthreads();
-    for (int size = 2; size <= m; size <<= 1)
-      for (int stride = size >> 1; stride > 0; stride >>= 1) {
-        for (int k = threadIdx.x; k < m; k += blockDim.x) {
-          const int o = k ^ stride;
-          if (o > k) {
-            const bool up = ((k & size) == 0);
-            const unsigned long long a = sk[k], c = sk[o];
-            if ((a > c) == up) {
-              sk[k] = c;
-              sk[o] = a;
-            }
-          }
-        }
-        __syncthreads();
-      }
-  }
-  for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int from = sorted ? (int)(sk[p] & 0xfffffu) : p;
-    const long long s = b + from, d = b + (sorted ? tile_slot(p, n) : p);
-    store_particle(dst, d, load_particle(src, s));
-  }
 }
 
 // appends a list to the tiles in place (moving-window injection); overflow
@@ -657,26 +619,15 @@ cudaError_t launch_count_list(const Particles &list, const int *n_ptr, int n_cap
 }
 
 cudaError_t launch_copy_tiles(const Particles &src, const int *off_old, const int *np_old, const Particles &dst,
-                              const int *off_new, unsigned *key, int *fill, int ntiles, cudaStream_t st) {
-  k_copy_tiles<<<ntiles, 256, 0, st>>>(src, off_old, np_old, dst, off_new, key, fill);
+                              const int *off_new, int *fill, int ntiles, cudaStream_t st) {
+  k_copy_tiles<<<ntiles, 256, 0, st>>>(src, off_old, np_old, dst, off_new, fill);
   return cudaGetLastError();
 }
 
 cudaError_t launch_scatter_list(const Particles &list, const int *n_ptr, int n_cap, const Particles &dst,
-                                const int *off, const int *cap, int *fill, unsigned *key, unsigned key0,
-                                const LayoutConst &L, int *err, cudaStream_t st) {
-  k_scatter_list<<<512, 256, 0, st>>>(list, n_ptr, n_cap, dst, off, cap, fill, key, key0, L, err);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_tile_order(const Particles &src, const unsigned *key, const int *off, const int *np,
-                              const Particles &dst, int ntiles, int smax, const LayoutConst &L, cudaStream_t st) {
-  const size_t sh = (size_t)smax * sizeof(unsigned long long);
-  if (sh > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_tile_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
-    if (e != cudaSuccess) return e;
-  }
-  k_tile_order<<<ntiles, 1024, sh, st>>>(src, key, off, np, dst, smax, L);
+                                const int *off, const int *cap, int *fill, const LayoutConst &L, int *err,
+                                cudaStream_t st) {
+  k_scatter_list<<<512, 256, 0, st>>>(list, n_ptr, n_cap, dst, off, cap, fill, L, err);
   return cudaGetLastError();
 }
 
