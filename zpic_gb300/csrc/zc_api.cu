@@ -8,6 +8,8 @@
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -312,6 +314,64 @@ zc_status settle(zc_sim *s, SpeciesState &p) {
 
 void invalidate_graph(zc_sim *s);
 
+// Tile offsets and capacities from per-tile particle counts: room for the
+// count or for the nominal full-density tile, whichever is larger, plus
+// slack.  New A/B buffers are allocated when the species' do not hold the
+// layout (nbuf then holds them; otherwise nbuf aliases the species').
+struct TilePlan {
+  std::vector<int> off, cap;
+  long long tot = 0;
+  bool grow = false;
+  Particles nbuf[2] = {};
+};
+
+zc_status plan_tiles(zc_sim *s, SpeciesState &p, const std::vector<int> &cnt, TilePlan &pl) {
+  const int nt = s->ntiles;
+  const long long nominal = (long long)p.ppc[0] * p.ppc[1] * s->TX * s->TY;
+  pl.off.assign(nt, 0);
+  pl.cap.assign(nt, 0);
+  pl.tot = 0;
+  int max_cap = 0;
+  for (int t = 0; t < nt; ++t) {
+    long long base = std::max<long long>(cnt[t], nominal);
+    long long c = (long long)std::ceil(base * (1.0 + s->slack)) + 32;
+    c = (c + 31) / 32 * 32;
+    if (c > (1LL << 30)) return fail(ZC_ENOMEM, "tile capacity too large");
+    pl.off[t] = (int)pl.tot;
+    pl.cap[t] = (int)c;
+    pl.tot += c;
+    max_cap = std::max(max_cap, (int)c);
+  }
+  if (pl.tot >= (1LL << 31)) return fail(ZC_ENOMEM, "species too large for 32-bit tile offsets");
+  TRY(ensure_outbox(s, p, max_cap));
+  p.max_cap = max_cap;
+  pl.grow = pl.tot > p.alloc;
+  if (pl.grow) {
+    TRY(alloc_particles(pl.nbuf[0], pl.tot));
+    TRY(alloc_particles(pl.nbuf[1], pl.tot));
+  } else {
+    pl.nbuf[0] = p.buf[0];
+    pl.nbuf[1] = p.buf[1];
+  }
+  CK(cudaMemcpyAsync(p.d_off, pl.off.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, s->st));
+  CK(cudaMemcpyAsync(p.d_cap, pl.cap.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, s->st));
+  return ZC_OK;
+}
+
+// takes the planned layout as the species' (stream synchronised)
+void adopt_tiles(SpeciesState &p, TilePlan &pl) {
+  if (pl.grow) {
+    free_particles(p.buf[0]);
+    free_particles(p.buf[1]);
+    p.buf[0] = pl.nbuf[0];
+    p.buf[1] = pl.nbuf[1];
+    p.alloc = pl.tot;
+    p.cur = 0;
+  }
+  p.h_off = pl.off;
+  p.h_cap = pl.cap;
+}
+
 // Builds the tile layout of a species from per-tile counts and moves its
 // particles (tiles of the current layout, its spill list and an optional
 // new list) into it.  Every tile is then sorted by cell (k_cellsort).  The
@@ -342,40 +402,11 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   CK(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * nt, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
 
-  // capacities: room for the count or for the nominal full-density tile,
-  // whichever is larger, plus slack
-  const long long nominal = (long long)p.ppc[0] * p.ppc[1] * s->TX * s->TY;
-  std::vector<int> off(nt), cap(nt);
-  long long tot = 0;
-  int max_cap = 0;
-  for (int t = 0; t < nt; ++t) {
-    long long base = std::max<long long>(cnt[t], nominal);
-    long long c = (long long)std::ceil(base * (1.0 + s->slack)) + 32;
-    c = (c + 31) / 32 * 32;
-    if (c > (1LL << 30)) return fail(ZC_ENOMEM, "tile capacity too large");
-    off[t] = (int)tot;
-    cap[t] = (int)c;
-    tot += c;
-    max_cap = std::max(max_cap, (int)c);
-  }
-  if (tot >= (1LL << 31)) return fail(ZC_ENOMEM, "species too large for 32-bit tile offsets");
-  TRY(ensure_outbox(s, p, max_cap));
-  p.max_cap = max_cap;
-
-  Particles nbuf[2] = {};
-  const bool grow = tot > p.alloc;
-  if (grow) {
-    TRY(alloc_particles(nbuf[0], tot));
-    TRY(alloc_particles(nbuf[1], tot));
-  } else {
-    nbuf[0] = p.buf[0];
-    nbuf[1] = p.buf[1];
-  }
+  TilePlan pl;
+  TRY(plan_tiles(s, p, cnt, pl));
   // destination of the scatter: the buffer that does not hold the particles
   const int src_i = p.cur, tmp_i = 1 - p.cur;
-  Particles tmp = grow ? nbuf[1] : p.buf[tmp_i];
-  CK(cudaMemcpyAsync(p.d_off, off.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(p.d_cap, cap.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
+  Particles tmp = pl.grow ? pl.nbuf[1] : p.buf[tmp_i];
   CK(launch_copy_tiles(p.buf[src_i], d_off_old, d_np_old, tmp, p.d_off, d_fill, nt, st));
   CK(launch_scatter_list(p.spill[p.spill_cur], p.d_spill_cnt + p.spill_cur, p.spill_cap, tmp, p.d_off,
                          p.d_cap, d_fill, L, s->d_err, st));
@@ -383,20 +414,11 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
     CK(launch_scatter_list(*list, d_list_n, list_n, tmp, p.d_off, p.d_cap, d_fill, L, s->d_err, st));
   CK(cudaMemcpyAsync(p.d_np, cnt.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
   // every tile into the other buffer in cell order (the lane-run layout)
-  Particles dst = grow ? nbuf[0] : p.buf[src_i];
+  Particles dst = pl.grow ? pl.nbuf[0] : p.buf[src_i];
   CK(launch_cellsort(tmp, dst, p.d_off, p.d_np, L, nt, st));
   CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), st));
   CK(cudaStreamSynchronize(st));
-  if (grow) {
-    free_particles(p.buf[0]);
-    free_particles(p.buf[1]);
-    p.buf[0] = nbuf[0];
-    p.buf[1] = nbuf[1];
-    p.alloc = tot;
-    p.cur = 0;
-  }
-  p.h_off = off;
-  p.h_cap = cap;
+  adopt_tiles(p, pl);
   dfree(d_cnt);
   dfree(d_fill);
   dfree(d_np_old);
@@ -405,20 +427,80 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   return ZC_OK;
 }
 
-// host AoS -> device SoA list (temporary), returns the list
-zc_status upload_list(zc_sim *s, const zc_part *parts, int n, Particles &list) {
-  TRY(alloc_particles(list, std::max(n, 1)));
-  if (n <= 0) return ZC_OK;
-  void *d_aos = nullptr;
-  CK(cudaMalloc(&d_aos, sizeof(zc_part) * (size_t)n));
-  CK(cudaMemcpyAsync(d_aos, parts, sizeof(zc_part) * (size_t)n, cudaMemcpyHostToDevice, s->st));
+// Loads a list into a species whose tiles and spill list are empty, straight
+// into the sorted layout: the per-cell counts of the list (counted while it
+// was staged) give the tile counts, the layout, and every cell's first
+// position; one scatter then puts every particle where k_cellsort would.
+zc_status load_sorted(zc_sim *s, int k, const Particles &list, int n, int *d_cell) {
+  SpeciesState &p = s->sp[k];
+  cudaStream_t st = s->st;
+  invalidate_graph(s);
+  s->n_relayout += 1;
+  const LayoutConst L = layout(s);
+  const int nt = s->ntiles;
   int *d_cnt = nullptr;
-  TRY(dalloc(&d_cnt, s->ntiles));
-  CK(cudaMemsetAsync(d_cnt, 0, sizeof(int) * s->ntiles, s->st));
-  CK(launch_stage_to_list(d_aos, n, list, d_cnt, layout(s), s->d_err, s->st));
-  CK(cudaStreamSynchronize(s->st));
-  cudaFree(d_aos);
+  TRY(dalloc(&d_cnt, nt));
+  CK(launch_cell_starts(d_cell, d_cnt, L, nt, st));
+  std::vector<int> cnt(nt);
+  CK(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * nt, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  TilePlan pl;
+  zc_status r = plan_tiles(s, p, cnt, pl);
+  if (r != ZC_OK) {
+    dfree(d_cnt);
+    return r;
+  }
+  Particles dst = pl.grow ? pl.nbuf[0] : p.buf[p.cur];
+  CK(launch_scatter_sorted(list, n, dst, p.d_off, d_cnt, d_cell, L, st));
+  CK(cudaMemcpyAsync(p.d_np, d_cnt, sizeof(int) * nt, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), st));
+  CK(cudaStreamSynchronize(st));
+  adopt_tiles(p, pl);
   dfree(d_cnt);
+  return ZC_OK;
+}
+
+// The device address of a host buffer that the staging kernel may read in
+// place: the whole buffer page-locked and mapped (cudaHostAlloc'd or
+// registered memory; over the host link the kernel reads it as fast as a
+// copy would move it) and 4-byte aligned.  Null for any other buffer, which
+// is copied to the device first.
+const void *mapped_records(const void *h, size_t bytes) {
+  if (!h || bytes == 0 || ((uintptr_t)h & 3)) return nullptr;
+  cudaPointerAttributes a0{}, a1{};
+  const char *last = (const char *)h + bytes - 1;
+  if (cudaPointerGetAttributes(&a0, h) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  if ((const char *)a1.devicePointer - (const char *)a0.devicePointer != (ptrdiff_t)(bytes - 1)) return nullptr;
+  return a0.devicePointer;
+}
+
+// host AoS -> device SoA list (temporary).  With d_cell, also the particles
+// of every cell (nx * ny counters, allocated here, the caller frees them).
+zc_status upload_list(zc_sim *s, const zc_part *parts, int n, Particles &list, int **d_cell = nullptr) {
+  TRY(alloc_particles(list, std::max(n, 1)));
+  int *cell = nullptr;
+  if (d_cell) {
+    TRY(dalloc(&cell, (size_t)s->nx * s->ny));
+    CK(cudaMemsetAsync(cell, 0, sizeof(int) * (size_t)s->nx * s->ny, s->st));
+    *d_cell = cell;
+  }
+  if (n <= 0) return ZC_OK;
+  const size_t bytes = sizeof(zc_part) * (size_t)n;
+  const void *src = mapped_records(parts, bytes);
+  void *d_aos = nullptr;
+  if (!src) {
+    CK(cudaMalloc(&d_aos, bytes));
+    CK(cudaMemcpyAsync(d_aos, parts, bytes, cudaMemcpyHostToDevice, s->st));
+    src = d_aos;
+  }
+  CK(launch_stage_to_list(src, n, list, cell, layout(s), s->d_err, s->st));
+  CK(cudaStreamSynchronize(s->st));
+  if (d_aos) cudaFree(d_aos);
   return ZC_OK;
 }
 
@@ -1401,8 +1483,10 @@ zc_status zc_species_set_particles(zc_sim *s, int k, const zc_part *parts, int n
     if (p.ob[b].cnt) CK(cudaMemsetAsync(p.ob[b].cnt, 0, sizeof(int) * s->ntiles, s->st));
   p.pending = false;
   Particles list{};
-  TRY(upload_list(s, parts, np, list));
-  zc_status r = relayout(s, k, &list, np);
+  int *d_cell = nullptr;
+  zc_status r = upload_list(s, parts, np, list, &d_cell);
+  if (r == ZC_OK) r = load_sorted(s, k, list, np, d_cell);
+  dfree(d_cell);
   free_particles(list);
   if (r != ZC_OK) return r;
   return check_errors(s, false);

@@ -143,8 +143,15 @@ cudaError_t launch_count_valid(const Particles &buf, const int *off, const int *
 // moves the particles pending in an outbox into their tiles (appended)
 cudaError_t launch_settle(const Particles &buf, const TileSet &T, const Outbox &O, const Spill &S, int *err,
                           int ntx, int nty, int mw, cudaStream_t st);
-cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, int *cnt, const LayoutConst &L,
-                                 int *err, cudaStream_t st);
+// AoS records (device memory or mapped host memory) -> SoA list; cell_cnt
+// (nx * ny counters, or null) receives the particles of every cell
+cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, int *cell_cnt,
+                                 const LayoutConst &L, int *err, cudaStream_t st);
+// per tile: cell counts -> first positions of the cells (in place), tile counts
+cudaError_t launch_cell_starts(int *cell, int *cnt, const LayoutConst &L, int ntiles, cudaStream_t st);
+// list -> tiles in the sorted (lane-run) layout, from the cell starts
+cudaError_t launch_scatter_sorted(const Particles &list, int n, const Particles &dst, const int *off,
+                                  const int *cnt, int *cell_pos, const LayoutConst &L, cudaStream_t st);
 cudaError_t launch_count_list(const Particles &list, const int *n_ptr, int n_cap, int *cnt, const LayoutConst &L,
                               cudaStream_t st);
 cudaError_t launch_copy_tiles(const Particles &src, const int *off_old, const int *np_old, const Particles &dst,

@@ -100,22 +100,64 @@ __device__ __forceinline__ int warp_grouped_add(int *counter, int t) {
   return first + __popc(same & ((1u << lane) - 1));
 }
 
-// AoS staging records -> SoA list, counting the particles of each tile
-__global__ void k_stage_to_list(const float4 *aos7, int n, Particles list, int *cnt, LayoutConst L,
-                                int *err) {
-  // records are 7 words; read them as words
-  const int *w = reinterpret_cast<const int *>(aos7);
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int *r = w + 7LL * k;
-    int ix = r[0], iy = r[1];
-    if (ix < 0 || ix >= L.nx || iy < 0 || iy >= L.ny) {
-      atomicOr(err, ERR_ESCAPE);
-      ix = min(max(ix, 0), L.nx - 1);
-      iy = min(max(iy, 0), L.ny - 1);
+// AoS records (7 words: ix, iy, x, y, ux, uy, uz) -> SoA list.  A CTA of
+// 256 threads reads its 256 records as 1792 consecutive words into shared
+// memory (coalesced whether the records sit in device memory or in mapped
+// host memory, read straight over the host link), then every thread takes
+// one record (stride 7 words: no bank conflicts).  cell_cnt (nx * ny
+// counters), when given, receives the particles of every cell.
+__global__ void __launch_bounds__(256) k_stage_to_list(const int *w, int n, Particles list, int *cell_cnt,
+                                                       LayoutConst L, int *err) {
+  __shared__ int sw[256 * 7];
+  for (long long b0 = (long long)blockIdx.x * 256; b0 < n; b0 += (long long)gridDim.x * 256) {
+    const int m = (int)min(256LL, n - b0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < m * 7; j += 256) sw[j] = w[b0 * 7 + j];
+    __syncthreads();
+    if (threadIdx.x < m) {
+      const int *r = sw + threadIdx.x * 7;
+      int ix = r[0], iy = r[1];
+      if (ix < 0 || ix >= L.nx || iy < 0 || iy >= L.ny) {
+        atomicOr(err, ERR_ESCAPE);
+        ix = min(max(ix, 0), L.nx - 1);
+        iy = min(max(iy, 0), L.ny - 1);
+      }
+      store_particle(list, b0 + threadIdx.x, ix, iy, __int_as_float(r[2]), __int_as_float(r[3]),
+                     __int_as_float(r[4]), __int_as_float(r[5]), __int_as_float(r[6]));
+      if (cell_cnt) warp_grouped_add(cell_cnt, ix + iy * L.nx);
     }
-    store_particle(list, k, ix, iy, __int_as_float(r[2]), __int_as_float(r[3]), __int_as_float(r[4]),
-                   __int_as_float(r[5]), __int_as_float(r[6]));
-    warp_grouped_add(cnt, tile_of(ix, iy, L));
+  }
+}
+
+// Per tile (one CTA of 1024 threads, one thread per cell of the tile): the
+// exclusive scan of its cell counts in the tile's cell order (local x
+// fastest, as k_cellsort orders), written back in place as every cell's first
+// position, and the tile's count into cnt.
+__global__ void __launch_bounds__(1024) k_cell_starts(int *cell, int *cnt, LayoutConst L) {
+  __shared__ int swarp[32];
+  const int t = blockIdx.x;
+  const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
+  const int lx = threadIdx.x % L.TX, ly = threadIdx.x / L.TX;
+  const int ix = cx0 + lx, iy = cy0 + ly;
+  const bool in = threadIdx.x < L.TX * L.TY && ix < L.nx && iy < L.ny;
+  const long long g = (long long)iy * L.nx + ix;
+  const int v = in ? cell[g] : 0;
+  int tot;
+  const int pre = block_exclusive_scan<1024>(v, tot, swarp);
+  if (in) cell[g] = pre;
+  if (threadIdx.x == 0) cnt[t] = tot;
+}
+
+// list particles straight into the sorted tile layout: the particle takes the
+// next position of its cell (cell starts from k_cell_starts) and is stored
+// at that position's tile_slot, as k_cellsort places it
+__global__ void k_scatter_sorted(Particles list, int n, Particles dst, const int *off, const int *cnt,
+                                 int *cell_pos, LayoutConst L) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const PRec r = load_particle(list, k);
+    const int t = tile_of(r.ix, r.iy, L);
+    const int pos = warp_grouped_add(cell_pos, r.ix + r.iy * L.nx);
+    store_particle(dst, (long long)off[t] + tile_slot(pos, cnt[t]), r);
   }
 }
 
@@ -604,11 +646,24 @@ cudaError_t launch_inject_column(const Particles &list, const ColumnInject &C, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, int *cnt, const LayoutConst &L,
-                                 int *err, cudaStream_t st) {
+cudaError_t launch_stage_to_list(const void *aos, int n, const Particles &list, int *cell_cnt,
+                                 const LayoutConst &L, int *err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  const int nb = (int)std::min<long long>((n + 255) / 256, 4096);
-  k_stage_to_list<<<nb, 256, 0, st>>>(reinterpret_cast<const float4 *>(aos), n, list, cnt, L, err);
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+  k_stage_to_list<<<nb, 256, 0, st>>>(reinterpret_cast<const int *>(aos), n, list, cell_cnt, L, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cell_starts(int *cell, int *cnt, const LayoutConst &L, int ntiles, cudaStream_t st) {
+  k_cell_starts<<<ntiles, 1024, 0, st>>>(cell, cnt, L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_sorted(const Particles &list, int n, const Particles &dst, const int *off,
+                                  const int *cnt, int *cell_pos, const LayoutConst &L, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+  k_scatter_sorted<<<nb, 256, 0, st>>>(list, n, dst, off, cnt, cell_pos, L);
   return cudaGetLastError();
 }
 
