@@ -225,9 +225,18 @@ __global__ void __launch_bounds__(32 * kSmoothWarps) k_smooth(const float *Jin, 
 // same float operations in the same order as k_smooth (and as one kernel
 // per pass, em2d/current.c:316-413).
 // ---------------------------------------------------------------------------
-constexpr int kS4Rows = 32;  // interior rows per warp
-constexpr int kS4Ring = 8;   // rows in flight per warp
-constexpr int kS4Warps = 8;  // warps per CTA
+#ifndef ZC_S4_ROWS
+#define ZC_S4_ROWS 32
+#endif
+#ifndef ZC_S4_RING
+#define ZC_S4_RING 8
+#endif
+#ifndef ZC_S4_WARPS
+#define ZC_S4_WARPS 8
+#endif
+constexpr int kS4Rows = ZC_S4_ROWS;    // interior rows per warp
+constexpr int kS4Ring = ZC_S4_RING;    // rows in flight per warp (a power of two)
+constexpr int kS4Warps = ZC_S4_WARPS;  // warps per CTA
 constexpr int kS4W = 120;    // columns a warp writes
 
 __device__ __forceinline__ float4 f3pt4(float sa, float sb, const float4 &l, const float4 &m, const float4 &u,
