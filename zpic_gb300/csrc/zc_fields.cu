@@ -239,18 +239,35 @@ constexpr int kS4Ring = ZC_S4_RING;    // rows in flight per warp (a power of tw
 constexpr int kS4Warps = ZC_S4_WARPS;  // warps per CTA
 constexpr int kS4W = 120;    // columns a warp writes
 
+#ifndef ZC_S4_MINB
+#define ZC_S4_MINB 3
+#endif
+
+// one [sa, sb, sa] tap on two columns at once: packed float32 pairs, each
+// half rounded as the scalar products and sums of f3pt are
+__device__ __forceinline__ float2 f3pt2(float sa, float sb, float2 l, float2 m, float2 u) {
+  const float2 a = make_float2(sa, sa), b = make_float2(sb, sb);
+  return __fadd2_rn(__fadd2_rn(__fmul2_rn(a, l), __fmul2_rn(b, m)), __fmul2_rn(a, u));
+}
+
+// four columns; with SEL the columns whose `on` is false keep m
+template <bool SEL>
 __device__ __forceinline__ float4 f3pt4(float sa, float sb, const float4 &l, const float4 &m, const float4 &u,
                                         const bool (&on)[4]) {
-  float4 r;
-  r.x = on[0] ? f3pt(sa, sb, l.x, m.x, u.x) : m.x;
-  r.y = on[1] ? f3pt(sa, sb, l.y, m.y, u.y) : m.y;
-  r.z = on[2] ? f3pt(sa, sb, l.z, m.z, u.z) : m.z;
-  r.w = on[3] ? f3pt(sa, sb, l.w, m.w, u.w) : m.w;
+  const float2 a = f3pt2(sa, sb, make_float2(l.x, l.y), make_float2(m.x, m.y), make_float2(u.x, u.y));
+  const float2 b = f3pt2(sa, sb, make_float2(l.z, l.w), make_float2(m.z, m.w), make_float2(u.z, u.w));
+  float4 r = make_float4(a.x, a.y, b.x, b.y);
+  if (SEL) {
+    r.x = on[0] ? r.x : m.x;
+    r.y = on[1] ? r.y : m.y;
+    r.z = on[2] ? r.z : m.z;
+    r.w = on[3] ? r.w : m.w;
+  }
   return r;
 }
 
 template <int NX, int NY>
-__global__ void __launch_bounds__(32 * kS4Warps) k_smooth4(const float *Jin, float *Jout, Grid G, SmoothPasses PX,
+__global__ void __launch_bounds__(32 * kS4Warps, ZC_S4_MINB) k_smooth4(const float *Jin, float *Jout, Grid G, SmoothPasses PX,
                                                            SmoothPasses PY, int mw) {
   __shared__ __align__(16) float4 ring[kS4Warps][kS4Ring][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -277,6 +294,19 @@ __global__ void __launch_bounds__(32 * kS4Warps) k_smooth4(const float *Jin, flo
     yf[e] = b >= 1 && b <= G.nx;
     direct = direct && have[e] && src[e] == b;
   }
+  // Warp-uniform: whether any column must keep its value in an x or a y
+  // pass.  The warp's outer columns (q = 0 and 127) do not count for x:
+  // filtered with a wrong neighbour, their error moves one column inward per
+  // pass and reaches at most column 3 after 4 passes, and columns 0..3 and
+  // 124..127 are never written.
+  bool xkeep = false, ykeep = false;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int q = 4 * lane + e;
+    xkeep = xkeep || (!xf[e] && q >= 1 && q <= 126);
+    ykeep = ykeep || !yf[e];
+  }
+  const bool xsel = __any_sync(0xffffffffu, xkeep), ysel = __any_sync(0xffffffffu, ykeep);
   const bool writer = lane >= 1 && lane <= 30;
   const float *pin = Jin + c * G.plane;
   float *out = Jout + c * G.plane;
@@ -353,7 +383,7 @@ __global__ void __launch_bounds__(32 * kS4Warps) k_smooth4(const float *Jin, flo
       const float l = __shfl_up_sync(0xffffffffu, v.w, 1);
       const float u = __shfl_down_sync(0xffffffffu, v.x, 1);
       const float4 lv = make_float4(l, v.x, v.y, v.z), uv = make_float4(v.y, v.z, v.w, u);
-      v = f3pt4(PX.sa[p], PX.sb[p], lv, v, uv, xf);
+      v = xsel ? f3pt4<true>(PX.sa[p], PX.sb[p], lv, v, uv, xf) : f3pt4<false>(PX.sa[p], PX.sb[p], lv, v, uv, xf);
     }
     // stage p receives walk row rr - p and emits the middle row once it
     // holds the two rows below
@@ -369,7 +399,8 @@ __global__ void __launch_bounds__(32 * kS4Warps) k_smooth4(const float *Jin, flo
           lo = (jprev == 0) ? glo : lo;
           hi = (jprev == G.ny - 1) ? ghi : hi;
         }
-        e = f3pt4(PY.sa[p], PY.sb[p], lo, s1[p], hi, yf);
+        e = ysel ? f3pt4<true>(PY.sa[p], PY.sb[p], lo, s1[p], hi, yf)
+                 : f3pt4<false>(PY.sa[p], PY.sb[p], lo, s1[p], hi, yf);
       }
       s0[p] = s1[p];
       s1[p] = v;
