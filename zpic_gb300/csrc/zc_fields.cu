@@ -243,20 +243,15 @@ constexpr int kS4W = 120;    // columns a warp writes
 #define ZC_S4_MINB 3
 #endif
 
-// one [sa, sb, sa] tap on two columns at once: packed float32 pairs, each
-// half rounded as the scalar products and sums of f3pt are
-__device__ __forceinline__ float2 f3pt2(float sa, float sb, float2 l, float2 m, float2 u) {
-  const float2 a = make_float2(sa, sa), b = make_float2(sb, sb);
-  return __fadd2_rn(__fadd2_rn(__fmul2_rn(a, l), __fmul2_rn(b, m)), __fmul2_rn(a, u));
-}
-
 // four columns; with SEL the columns whose `on` is false keep m
+// (scalar float32 operations: packed pair products and sums were measured
+// to round differently from the scalar ones once a product and a sum follow
+// each other, so the bit-exact filter keeps the scalar form)
 template <bool SEL>
 __device__ __forceinline__ float4 f3pt4(float sa, float sb, const float4 &l, const float4 &m, const float4 &u,
                                         const bool (&on)[4]) {
-  const float2 a = f3pt2(sa, sb, make_float2(l.x, l.y), make_float2(m.x, m.y), make_float2(u.x, u.y));
-  const float2 b = f3pt2(sa, sb, make_float2(l.z, l.w), make_float2(m.z, m.w), make_float2(u.z, u.w));
-  float4 r = make_float4(a.x, a.y, b.x, b.y);
+  float4 r = make_float4(f3pt(sa, sb, l.x, m.x, u.x), f3pt(sa, sb, l.y, m.y, u.y), f3pt(sa, sb, l.z, m.z, u.z),
+                         f3pt(sa, sb, l.w, m.w, u.w));
   if (SEL) {
     r.x = on[0] ? r.x : m.x;
     r.y = on[1] ? r.y : m.y;
