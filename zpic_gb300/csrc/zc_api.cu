@@ -678,14 +678,10 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
       CK(cudaMallocAsync(&d_aos, sizeof(zc_part) * (size_t)n, st));
       CK(cudaMemcpyAsync(d_aos, s->h_inj, sizeof(zc_part) * (size_t)n, cudaMemcpyHostToDevice, st));
       CK(cudaEventRecord(s->inj_done, st));
-      int *d_tile_cnt = nullptr;  // per-tile counts of the staging kernel (not needed here)
-      CK(cudaMallocAsync((void **)&d_tile_cnt, sizeof(int) * s->ntiles, st));
-      CK(cudaMemsetAsync(d_tile_cnt, 0, sizeof(int) * s->ntiles, st));
-      CK(launch_stage_to_list(d_aos, n, s->inj_list, d_tile_cnt, layout(s), s->d_err, st));
+      CK(launch_stage_to_list(d_aos, n, s->inj_list, nullptr, layout(s), s->d_err, st));  // no cell counts
       CK(launch_append_list(s->inj_list, n, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur),
                             layout(s), s->d_err, st));
       CK(cudaFreeAsync(d_aos, st));
-      CK(cudaFreeAsync(d_tile_cnt, st));
     }
   }
   return ZC_OK;
