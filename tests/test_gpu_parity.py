@@ -310,28 +310,3 @@ def test_fast_push_close_to_exact():
     for f in ("ux", "uy", "uz"):
         assert np.allclose(np.sort(a[f]), np.sort(b[f]), rtol=1e-5, atol=1e-7)
     assert field_err(gf.J(), ge.J()) <= 1e-5
-
-
-@pytest.mark.parametrize("name", ["weibel_smooth", "lwfa_window"])
-def test_sort_histogram_survives_host_calls(name):
-    """The push before a cell sort leaves per-cell counts for it; host calls
-    between steps that move particles into the tiles (count, download,
-    charge) make the sort count again.  Deterministic runs with and without
-    such calls, and with graphs, end on the same bits."""
-    n = len(DECKS[name]["species"])
-    runs = []
-    for calls, graphs in ((False, False), (True, False), (True, True)):
-        cpu, g = mirror(name, deterministic=True, sort_every=3)
-        g.set_graphs(graphs)
-        for step in range(14):
-            g.step(1)
-            if calls and step % 4 == 1:
-                g.count(0)
-                g.particles(n - 1)
-        runs.append((g.E(), g.B(), g.J(), [canon(g.particles(k)) for k in range(n)]))
-        g.close()
-    for r in runs[1:]:
-        for f in range(3):
-            assert np.array_equal(runs[0][f], r[f])
-        for a, b in zip(runs[0][3], r[3]):
-            assert a.tobytes() == b.tobytes()

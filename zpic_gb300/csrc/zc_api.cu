@@ -124,11 +124,6 @@ struct SpeciesState {
   long long ob_alloc = 0;
   int ob_in = 0;
   bool pending = false;
-  // per-cell counts of every tile (TX * TY a tile) written by the last push
-  // when the next step sorts; hist_ok: they describe the tiles as they are
-  // (anything else that changes the tiles clears it)
-  int *d_hist = nullptr;
-  bool hist_ok = false;
   // energy
   double *d_ekin_tile = nullptr, *d_ekin_extra = nullptr, *d_ekin = nullptr;
   // window injection drawn on the device (zc_set_device_injection)
@@ -140,7 +135,7 @@ struct SpeciesState {
 struct Counters {
   int iter = 0, n_move = 0;
   std::vector<int> sp_iter, sp_n_move, cur, spill_cur, ob_in;
-  std::vector<bool> pending, hist_ok;
+  std::vector<bool> pending;
   int eb_cur = 0, j_cur = 0;
   long long launch[ZC_NPHASE] = {};
 };
@@ -309,7 +304,6 @@ zc_status ensure_outbox(zc_sim *s, SpeciesState &p, int max_cap) {
 // moves the particles still waiting in the outboxes into their tiles
 zc_status settle(zc_sim *s, SpeciesState &p) {
   if (!p.pending) return ZC_OK;
-  p.hist_ok = false;  // the tiles take the pending particles
   Phase ph(s, ZC_PHASE_MIGRATE, 1);
   CK(launch_settle(p.buf[p.cur], tiles(p, s->ntiles), p.ob[p.ob_in], spill_of(p, p.spill_cur), s->d_err, s->ntx,
                    s->nty, s->mw, s->st));
@@ -376,7 +370,6 @@ void adopt_tiles(SpeciesState &p, TilePlan &pl) {
   }
   p.h_off = pl.off;
   p.h_cap = pl.cap;
-  p.hist_ok = false;
 }
 
 // Builds the tile layout of a species from per-tile counts and moves its
@@ -422,8 +415,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   CK(cudaMemcpyAsync(p.d_np, cnt.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
   // every tile into the other buffer in cell order (the lane-run layout)
   Particles dst = pl.grow ? pl.nbuf[0] : p.buf[src_i];
-  CK(launch_cellsort(tmp, dst, p.d_off, p.d_np, nullptr, p.d_cap, s->d_err, L, nt, st));
-  p.hist_ok = false;
+  CK(launch_cellsort(tmp, dst, p.d_off, p.d_np, L, nt, st));
   CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), st));
   CK(cudaStreamSynchronize(st));
   adopt_tiles(p, pl);
@@ -534,7 +526,6 @@ zc_status check_errors(zc_sim *s, bool relayout_spill) {
   }
   if (e & ERR_OVERFLOW) return fail(ZC_EOVERFLOW, "particle spill buffer exhausted: particles were lost");
   if (e & ERR_TIMEOUT) return fail(ZC_ETIMEOUT, "a TMA barrier wait timed out");
-  if (e & ERR_SORT) return fail(ZC_ESTATE, "a cell sort met other counts than its histogram: particles misplaced");
   if (e & ERR_ESCAPE) return fail(ZC_EPARTICLE_ESCAPE, "a particle moved more than one cell or left its tile");
   return ZC_OK;
 }
@@ -627,20 +618,15 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   if (s->sort_every > 0 && p.iter % s->sort_every == 0) {
     // keep the tiles sorted by cell (the push warps then share cells)
     Phase ph(s, ZC_PHASE_SORT, 1);
-    CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, p.hist_ok ? p.d_hist : nullptr, p.d_cap,
-                       s->d_err, layout(s), s->ntiles, st));
+    CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles, st));
     p.cur = 1 - p.cur;
     a.pin = p.buf[p.cur];
     a.pout = p.buf[1 - p.cur];
   }
-  // the push before a sort counts its tiles' particles per cell for it
-  const bool want_hist = s->sort_every > 0 && (p.iter + 1) % s->sort_every == 0;
-  if (want_hist) a.T.hist = p.d_hist;
   {
     Phase ph(s, ZC_PHASE_PUSH, 1);
     CK(launch_push_tiles(a, st));
   }
-  p.hist_ok = want_hist;
   const float *EBpart = s->EBp ? s->EBp : s->EB[s->eb_cur];
   {
     Phase ph(s, ZC_PHASE_SPILL, 1);
@@ -662,7 +648,6 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
                          s->deterministic, st));
   }
   p.iter += 1;
-  if (shift) p.hist_ok = false;  // the injected column joins the tiles
   if (shift && p.dinj) {
     p.n_move += 1;
     TRY(inject_column_device(s, p));
@@ -887,7 +872,6 @@ Counters save_counters(const zc_sim *s) {
     c.spill_cur.push_back(p.spill_cur);
     c.ob_in.push_back(p.ob_in);
     c.pending.push_back(p.pending);
-    c.hist_ok.push_back(p.hist_ok);
   }
   c.eb_cur = s->eb_cur;
   c.j_cur = s->j_cur;
@@ -898,7 +882,7 @@ Counters save_counters(const zc_sim *s) {
 // the buffer parities a captured graph starts from
 bool same_parities(const Counters &a, const Counters &b) {
   return a.cur == b.cur && a.spill_cur == b.spill_cur && a.ob_in == b.ob_in && a.eb_cur == b.eb_cur &&
-         a.hist_ok == b.hist_ok && (a.iter % 2) == (b.iter % 2);
+         (a.iter % 2) == (b.iter % 2);
 }
 
 // the graph g holds n steps from the current state (block-aligned)
@@ -935,7 +919,6 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G, bool instantiate = true)
     p.spill_cur = before.spill_cur[k];
     p.ob_in = before.ob_in[k];
     p.pending = before.pending[k];
-    p.hist_ok = before.hist_ok[k];
   }
   s->eb_cur = before.eb_cur;
   s->j_cur = before.j_cur;
@@ -983,7 +966,6 @@ void account_steps(zc_sim *s, const StepGraph &g) {
     SpeciesState &p = s->sp[k];
     p.iter += n;
     p.pending = g.after.pending[k];
-    p.hist_ok = g.after.hist_ok[k];
     p.cur = g.after.cur[k];
     p.spill_cur = g.after.spill_cur[k];
     p.ob_in = g.after.ob_in[k];
@@ -1326,7 +1308,6 @@ zc_status zc_sim_destroy(zc_sim *s) {
     dfree(p.d_cap);
     dfree(p.d_np);
     dfree(p.d_vcnt);
-    dfree(p.d_hist);
     for (int b = 0; b < 2; ++b) {
       free_particles(p.ob[b].p);
       dfree(p.ob[b].dst);
@@ -1389,7 +1370,6 @@ zc_status zc_species_create(zc_sim *s, const zc_species_desc *d, const zc_part *
   TRY(dalloc(&p.d_cap, nt));
   TRY(dalloc(&p.d_np, nt));
   TRY(dalloc(&p.d_vcnt, nt));
-  TRY(dalloc(&p.d_hist, (size_t)nt * s->TX * s->TY));
   CK(cudaMemsetAsync(p.d_np, 0, sizeof(int) * nt, s->st));
   CK(cudaMemsetAsync(p.d_off, 0, sizeof(int) * nt, s->st));
   CK(cudaMemsetAsync(p.d_cap, 0, sizeof(int) * nt, s->st));
@@ -1480,7 +1460,6 @@ zc_status zc_species_create_device(zc_sim *s, float m_q, const int ppc[2], const
   }
   I.seed_lo = (unsigned)seed;
   I.seed_hi = (unsigned)(seed >> 32);
-  p.hist_ok = false;
   CK(launch_init_tiles(p.buf[p.cur], p.d_off, d_colpts, d_colmask, I, L, s->ntiles, s->st));
   CK(cudaStreamSynchronize(s->st));
   dfree(d_colpts);
@@ -1518,7 +1497,6 @@ zc_status zc_species_inject(zc_sim *s, int k, const zc_part *parts, int np) {
   TRY(settle(s, p));
   Particles list{};
   TRY(upload_list(s, parts, np, list));
-  p.hist_ok = false;
   CK(launch_append_list(list, np, p.buf[p.cur], tiles(p, s->ntiles), spill_of(p, p.spill_cur), layout(s), s->d_err,
                         s->st));
   CK(cudaStreamSynchronize(s->st));

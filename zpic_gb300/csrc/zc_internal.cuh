@@ -45,7 +45,6 @@ enum : int {
   ERR_ESCAPE = 2,        // particle outside its cell/tile (moved > 1 cell)
   ERR_OVERFLOW = 4,      // spill buffer full: particles lost
   ERR_SPILLED = 8,       // particles went to the spill buffer (host re-layout due)
-  ERR_SORT = 16,         // a cell sort met other counts than the histogram it was given
 };
 
 struct Particles {       // one particle buffer

@@ -26,9 +26,6 @@ struct TileSet {
   const int *off, *cap;
   int *np;
   int ntiles;
-  // when set, the push leaves every tile's particles per cell (TX * TY
-  // counters a tile) for the cell sort that follows it
-  int *hist = nullptr;
 };
 
 struct Outbox {                           // particles leaving a tile, per tile `cap` slots
@@ -137,12 +134,9 @@ ZC_SPILL_LAUNCHER(launch_push_spill_fast_det);
 cudaError_t launch_fixed_to_float(const unsigned long long *src, float *dst, size_t n, cudaStream_t st);
 cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, size_t n, cudaStream_t st);
 // counting sort of every tile by cell (src -> dst, same offsets): holes
-// dropped, np set to the particle count, cell order through tile_slot.
-// hist: the per-cell counts of every tile (TX * TY a tile) left by the push
-// that wrote src, or null (the sort counts them itself)
+// dropped, np set to the particle count, cell order through tile_slot
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
-                            const int *hist, const int *cap, int *err, const LayoutConst &L, int ntiles,
-                            cudaStream_t st);
+                            const LayoutConst &L, int ntiles, cudaStream_t st);
 // particles (slots that are not holes) of every tile into cnt
 cudaError_t launch_count_valid(const Particles &buf, const int *off, const int *np, int *cnt, int ntiles,
                                cudaStream_t st);

@@ -229,70 +229,48 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 // tile, src -> dst at the same offsets): a shared-memory histogram, a scan,
 // then every particle takes the next position of its cell, stored at its
 // tile_slot (the lane-run layout); holes are dropped and np becomes the
-// particle count.  The order inside a cell follows the atomics' timing.
-// With `hist` (the counts the push that wrote src left) the counting pass,
-// a read of every particle's cell word, is skipped; a histogram that does
-// not match the tile is reported (ERR_SORT) and no write leaves the tile.
-// The reference sorts its whole buffer by cell every n_sort steps for cache
-// reuse (spec_sort, em2d/particles.c:942-1007); here the per-tile sort gives
-// the push lanes runs of particles in one cell.
+// particle count.  The order inside a cell follows the atomics' timing.  The reference sorts its whole buffer by cell every
+// n_sort steps for cache reuse (spec_sort, em2d/particles.c:942-1007); here
+// the per-tile sort gives the push lanes runs of particles in one cell.
 __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst, const int *off, int *np,
-                                                   const int *hist, const int *cap, int *err, LayoutConst L) {
+                                                   LayoutConst L) {
   constexpr int MAXC = 1024;
-  __shared__ int cursor[MAXC], start[MAXC];
+  __shared__ int cursor[MAXC];
   __shared__ int swarp[32];
   const int t = blockIdx.x;
   const int ncell = L.TX * L.TY;
   const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
   const int n = np[t];
   const long long b = off[t];
+  for (int c = threadIdx.x; c < ncell; c += 1024) cursor[c] = 0;
+  __syncthreads();
   auto cell_of_word = [&](float w) {  // -1 for a hole
     const unsigned u = (unsigned)__float_as_int(w);
     if (u == kHole) return -1;
     const int c = ((int)(u & 0xffffu) - cx0) + ((int)(u >> 16) - cy0) * L.TX;
     return min(max(c, 0), ncell - 1);
   };
-  if (hist) {
-    // counts left by the push that wrote these tiles: no counting pass
-    for (int c = threadIdx.x; c < ncell; c += 1024) cursor[c] = hist[(long long)t * ncell + c];
-  } else {
-    for (int c = threadIdx.x; c < ncell; c += 1024) cursor[c] = 0;
-    __syncthreads();
-    for (int k = threadIdx.x; k < n; k += 1024) {
-      const int c = cell_of_word(src.u[b + k].w);
-      if (c >= 0) atomicAdd(&cursor[c], 1);
-    }
+  for (int k = threadIdx.x; k < n; k += 1024) {
+    const int c = cell_of_word(src.u[b + k].w);
+    if (c >= 0) atomicAdd(&cursor[c], 1);
   }
   __syncthreads();
   int nvalid;
   {
     const int v = (threadIdx.x < ncell) ? cursor[threadIdx.x] : 0;
     const int pre = block_exclusive_scan<1024>(v, nvalid, swarp);
-    if (threadIdx.x < ncell) cursor[threadIdx.x] = start[threadIdx.x] = pre;
+    if (threadIdx.x < ncell) cursor[threadIdx.x] = pre;
   }
   __syncthreads();
-  const int room = cap[t];
-  bool lost = false;
   for (int k = threadIdx.x; k < n; k += 1024) {
     const float4 u = src.u[b + k];
     const int c = cell_of_word(u.w);
     if (c < 0) continue;
     const float2 xy = src.xy[b + k];
     const int slot = tile_slot(atomicAdd(&cursor[c], 1), nvalid);
-    if (slot < room) {  // (always, unless a histogram was out of date)
-      dst.u[b + slot] = u;
-      dst.xy[b + slot] = xy;
-    } else {
-      lost = true;
-    }
+    dst.u[b + slot] = u;
+    dst.xy[b + slot] = xy;
   }
-  __syncthreads();
-  if (hist) {
-    // every cell must have met exactly its count
-    const int c = threadIdx.x;
-    if (c < ncell && cursor[c] != (c + 1 < ncell ? start[c + 1] : nvalid)) lost = true;
-  }
-  if (lost) atomicOr(err, ERR_SORT);
   if (threadIdx.x == 0) np[t] = nvalid;
 }
 
@@ -636,9 +614,8 @@ cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, siz
 }
 
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
-                            const int *hist, const int *cap, int *err, const LayoutConst &L, int ntiles,
-                            cudaStream_t st) {
-  k_cellsort<<<ntiles, 1024, 0, st>>>(src, dst, off, np, hist, cap, err, L);
+                            const LayoutConst &L, int ntiles, cudaStream_t st) {
+  k_cellsort<<<ntiles, 1024, 0, st>>>(src, dst, off, np, L);
   return cudaGetLastError();
 }
 

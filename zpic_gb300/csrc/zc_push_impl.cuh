@@ -484,9 +484,6 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
   __shared__ int s_in[INCAP];
   __shared__ int s_nin;
   __shared__ int s_app, s_leave;      // appended arrivals, leavers (warp-aggregated atomics)
-  // the tile's particles per cell after this push (when T.hist is set: the
-  // cell sort of the next step takes these counts instead of counting)
-  __shared__ int s_hist[TX * TY];
 
   const int t = blockIdx.x;
   const int tx = t % C.ntx, ty = t / C.ntx;
@@ -529,9 +526,6 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
   }
   if constexpr (DET)
     for (int k = threadIdx.x; k < 3 * LAY::N; k += NT) sJi[k] = 0;
-  const bool want_hist = T.hist != nullptr;
-  if (want_hist)
-    for (int k = threadIdx.x; k < TX * TY; k += NT) s_hist[k] = 0;
   const bool loaded = mbar_wait_bounded(&bar, 0);
   if (!loaded) errbits |= ERR_TIMEOUT;
   __syncthreads();
@@ -626,7 +620,6 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
     if (oslot >= 0) {
       if (code == 1) store_particle(pout, base + oslot, ix, iy, x, y, ux, uy, uz);
       else store_hole(pout, base + oslot);
-      if (want_hist && code == 1) atomicAdd(&s_hist[(ix - cx0) + (iy - cy0) * TX], 1);
     }
     // leavers to the outbox, arrivals that stay appended after slot np: one
     // shared-memory atomic per warp and kind
@@ -650,12 +643,8 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
         }
       } else if (incoming && code == 1) {
         const int s = n_own + ab + __popc(mapp & below);
-        if (s < cap) {
-          store_particle(pout, base + s, ix, iy, x, y, ux, uy, uz);
-          if (want_hist) atomicAdd(&s_hist[(ix - cx0) + (iy - cy0) * TX], 1);
-        } else {
-          spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
-        }
+        if (s < cap) store_particle(pout, base + s, ix, iy, x, y, ux, uy, uz);
+        else spill_particle(S, &errbits, ix, iy, x, y, ux, uy, uz);
       }
     }
 
@@ -857,8 +846,6 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
     T.np[t] = n_own + min(s_app, cap - n_own);
     O.cnt[t] = min(s_leave, O.cap);
   }
-  if (want_hist)
-    for (int k = threadIdx.x; k < TX * TY; k += NT) T.hist[(long long)t * (TX * TY) + k] = s_hist[k];
   if constexpr (DET) {
     // integer sums: exact in any order
 #pragma unroll
