@@ -232,9 +232,14 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 // particle count.  The order inside a cell follows the atomics' timing.  The reference sorts its whole buffer by cell every
 // n_sort steps for cache reuse (spec_sort, em2d/particles.c:942-1007); here
 // the per-tile sort gives the push lanes runs of particles in one cell.
-__global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst, const int *off, int *np,
-                                                   LayoutConst L) {
-  constexpr int MAXC = 1024;
+#ifndef ZC_SORT_ILP
+#define ZC_SORT_ILP 3
+#endif
+__global__ void __launch_bounds__(1024, 2) k_cellsort(Particles src, Particles dst, const int *off, int *np,
+                                                      LayoutConst L) {
+  // each thread keeps ILP particles' loads in flight at once: with one load
+  // at a time the sort waits on memory latency (it ran at half the HBM rate)
+  constexpr int MAXC = 1024, ILP = ZC_SORT_ILP;
   __shared__ int cursor[MAXC];
   __shared__ int swarp[32];
   const int t = blockIdx.x;
@@ -250,9 +255,19 @@ __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst,
     const int c = ((int)(u & 0xffffu) - cx0) + ((int)(u >> 16) - cy0) * L.TX;
     return min(max(c, 0), ncell - 1);
   };
-  for (int k = threadIdx.x; k < n; k += 1024) {
-    const int c = cell_of_word(src.u[b + k].w);
-    if (c >= 0) atomicAdd(&cursor[c], 1);
+  const float hole = __int_as_float((int)kHole);
+  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * 1024) {
+    float w[ILP];
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int k = k0 + q * 1024;
+      w[q] = (k < n) ? __ldg(&src.u[b + k].w) : hole;
+    }
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int c = cell_of_word(w[q]);
+      if (c >= 0) atomicAdd(&cursor[c], 1);
+    }
   }
   __syncthreads();
   int nvalid;
@@ -262,14 +277,27 @@ __global__ void __launch_bounds__(1024) k_cellsort(Particles src, Particles dst,
     if (threadIdx.x < ncell) cursor[threadIdx.x] = pre;
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < n; k += 1024) {
-    const float4 u = src.u[b + k];
-    const int c = cell_of_word(u.w);
-    if (c < 0) continue;
-    const float2 xy = src.xy[b + k];
-    const int slot = tile_slot(atomicAdd(&cursor[c], 1), nvalid);
-    dst.u[b + slot] = u;
-    dst.xy[b + slot] = xy;
+  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * 1024) {
+    float4 u[ILP];
+    float2 xy[ILP];
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int k = k0 + q * 1024;
+      if (k < n) {
+        u[q] = __ldg(&src.u[b + k]);
+        xy[q] = __ldg(&src.xy[b + k]);
+      } else {
+        u[q].w = hole;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int c = cell_of_word(u[q].w);
+      if (c < 0) continue;
+      const int slot = tile_slot(atomicAdd(&cursor[c], 1), nvalid);
+      dst.u[b + slot] = u[q];
+      dst.xy[b + slot] = xy[q];
+    }
   }
   if (threadIdx.x == 0) np[t] = nvalid;
 }
