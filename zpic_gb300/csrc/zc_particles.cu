@@ -233,21 +233,24 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 // n_sort steps for cache reuse (spec_sort, em2d/particles.c:942-1007); here
 // the per-tile sort gives the push lanes runs of particles in one cell.
 #ifndef ZC_SORT_ILP
-#define ZC_SORT_ILP 3
+#define ZC_SORT_ILP 2
 #endif
-__global__ void __launch_bounds__(1024, 2) k_cellsort(Particles src, Particles dst, const int *off, int *np,
-                                                      LayoutConst L) {
-  // each thread keeps ILP particles' loads in flight at once: with one load
-  // at a time the sort waits on memory latency (it ran at half the HBM rate)
-  constexpr int MAXC = 1024, ILP = ZC_SORT_ILP;
+#ifndef ZC_SORT_NT
+#define ZC_SORT_NT 1024
+#endif
+template <int NT>
+__global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Particles dst, const int *off, int *np,
+                                                             LayoutConst L) {
+  // each thread keeps ILP particles' loads in flight at once
+  constexpr int MAXC = 1024, ILP = ZC_SORT_ILP, CPT = MAXC / NT;  // cells per thread in the scan
   __shared__ int cursor[MAXC];
-  __shared__ int swarp[32];
+  __shared__ int swarp[NT / 32];
   const int t = blockIdx.x;
   const int ncell = L.TX * L.TY;
   const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
   const int n = np[t];
   const long long b = off[t];
-  for (int c = threadIdx.x; c < ncell; c += 1024) cursor[c] = 0;
+  for (int c = threadIdx.x; c < MAXC; c += NT) cursor[c] = 0;
   __syncthreads();
   auto cell_of_word = [&](float w) {  // -1 for a hole
     const unsigned u = (unsigned)__float_as_int(w);
@@ -256,11 +259,11 @@ __global__ void __launch_bounds__(1024, 2) k_cellsort(Particles src, Particles d
     return min(max(c, 0), ncell - 1);
   };
   const float hole = __int_as_float((int)kHole);
-  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * 1024) {
+  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * NT) {
     float w[ILP];
 #pragma unroll
     for (int q = 0; q < ILP; ++q) {
-      const int k = k0 + q * 1024;
+      const int k = k0 + q * NT;
       w[q] = (k < n) ? __ldg(&src.u[b + k].w) : hole;
     }
 #pragma unroll
@@ -272,17 +275,27 @@ __global__ void __launch_bounds__(1024, 2) k_cellsort(Particles src, Particles d
   __syncthreads();
   int nvalid;
   {
-    const int v = (threadIdx.x < ncell) ? cursor[threadIdx.x] : 0;
-    const int pre = block_exclusive_scan<1024>(v, nvalid, swarp);
-    if (threadIdx.x < ncell) cursor[threadIdx.x] = pre;
+    // thread i scans cells i CPT .. i CPT + CPT - 1 (cells past ncell hold 0)
+    int v[CPT], sum = 0;
+#pragma unroll
+    for (int e = 0; e < CPT; ++e) {
+      v[e] = cursor[threadIdx.x * CPT + e];
+      sum += v[e];
+    }
+    int pre = block_exclusive_scan<NT>(sum, nvalid, swarp);
+#pragma unroll
+    for (int e = 0; e < CPT; ++e) {
+      cursor[threadIdx.x * CPT + e] = pre;
+      pre += v[e];
+    }
   }
   __syncthreads();
-  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * 1024) {
+  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * NT) {
     float4 u[ILP];
     float2 xy[ILP];
 #pragma unroll
     for (int q = 0; q < ILP; ++q) {
-      const int k = k0 + q * 1024;
+      const int k = k0 + q * NT;
       if (k < n) {
         u[q] = __ldg(&src.u[b + k]);
         xy[q] = __ldg(&src.xy[b + k]);
@@ -643,7 +656,7 @@ cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, siz
 
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
                             const LayoutConst &L, int ntiles, cudaStream_t st) {
-  k_cellsort<<<ntiles, 1024, 0, st>>>(src, dst, off, np, L);
+  k_cellsort<ZC_SORT_NT><<<ntiles, ZC_SORT_NT, 0, st>>>(src, dst, off, np, L);
   return cudaGetLastError();
 }
 
