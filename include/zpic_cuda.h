@@ -182,6 +182,13 @@ ZC_API zc_status zc_set_ext_fld(zc_sim *sim, int E_type, const float E0[3], cons
 /* --- the step ------------------------------------------------------------ */
 /* sim_iter x nsteps (em2d/simulation.c:45-56) */
 ZC_API zc_status zc_step(zc_sim *sim, int nsteps);
+/* zc_step without the wait at the end: the steps are queued on the
+ * simulation's stream and the call returns (it waits only every 16 queued
+ * steps, to look at the spill list).  Device errors of queued steps are
+ * returned by the next waiting call (zc_synchronize, zc_step, zc_energy,
+ * ...).  With zc_energy_async a run reports every step without idling the
+ * device between steps. */
+ZC_API zc_status zc_step_async(zc_sim *sim, int nsteps);
 /* the phases of sim_iter, for callers that drive them one by one */
 ZC_API zc_status zc_current_zero(zc_sim *sim);                 /* em2d/current.c:98-107 */
 ZC_API zc_status zc_spec_advance(zc_sim *sim, int species);    /* em2d/particles.c:1104-1269 */
@@ -302,6 +309,13 @@ ZC_API zc_status zc_set_current(zc_sim *sim, const float *J_buf);
  * time-centred kinetic energy of each species after its last advance
  * (spec->energy, em2d/particles.c:1231); FP64 reductions on the device */
 ZC_API zc_status zc_energy(zc_sim *sim, double emf_energy[6], double *kin_energy);
+/* zc_energy without the wait: the reductions and the copies into the two
+ * host arrays are queued behind the work already queued, and the arrays
+ * hold the values once zc_synchronize (or any waiting call) returns.  A run
+ * that reports energies every step then never idles the device between
+ * steps.  With page-locked arrays the copies are asynchronous; other host
+ * memory is filled before the call returns. */
+ZC_API zc_status zc_energy_async(zc_sim *sim, double emf_energy[6], double *kin_energy);
 /* charge density of one species on an (nx+1)*(ny+1) grid
  * (spec_deposit_charge, em2d/particles.c:1289-1324) */
 ZC_API zc_status zc_species_charge(zc_sim *sim, int species, float *charge);

@@ -68,3 +68,29 @@ def test_deterministic_matches_oracle(name):
     emf_g, kin_g = g.energy()
     for k in range(cpu.n_species):
         assert abs(kin_g[k] - cpu.energy(k)) <= 1e-5 * abs(cpu.energy(k))
+
+
+def test_queued_steps_and_energies_match_waiting_ones():
+    """zc_step_async + zc_energy_async (one wait at the end) give the bits
+    of zc_step + zc_energy, energies of every step included; 20 queued
+    steps cross the wait every 16 steps."""
+    import torch
+
+    name = "thermal"
+    rows = []
+    for queued in (False, True):
+        cpu, g = mirror(name, deterministic=True)
+        out = torch.zeros((20, 7), dtype=torch.float64, pin_memory=True).numpy()
+        for i in range(20):
+            if queued:
+                g.step_async(1)
+                g.energy_async(out[i])
+            else:
+                g.step(1)
+                emf, kin = g.energy()
+                out[i, :6], out[i, 6] = emf, kin[0]
+        g.synchronize()
+        rows.append((out.copy(), g.E(), g.B()))
+        g.close()
+    for a, b in zip(rows[0], rows[1]):
+        assert np.array_equal(a, b)

@@ -114,3 +114,27 @@ def test_em2d_drop_in_exits_like_the_reference():
     assert "not reached" not in r.stdout
     assert r.returncode == 255, (r.returncode, r.stderr[-2000:])  # exit(-1)
     assert "(*error*) sim_iter" in r.stderr and "moved more than one cell" in r.stderr
+
+
+def test_queued_steps_report_errors_at_the_next_wait():
+    """zc_step_async returns without waiting: a device error of a queued step
+    comes back from the next waiting call, and the run goes on."""
+    from zpic_gb300._zc import ZcError
+
+    cpu, g = mirror("weibel_smooth")
+    try:
+        cpu.iter(2)
+        g.step_async(2)
+        assert g.lib.zc_post_device_error(g.h, ESCAPE) == 0
+        g.step_async(1)  # queued: no status yet
+        cpu.iter(1)
+        with pytest.raises(ZcError) as exc:
+            g.synchronize()
+        assert exc.value.status == ESCAPE
+        cpu.iter(3)
+        g.step_async(3)
+        g.synchronize()
+        for f in ("E", "B", "J"):
+            assert field_err(getattr(g, f)(), getattr(cpu, f)()) <= 1e-5, f
+    finally:
+        g.close()

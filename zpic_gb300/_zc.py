@@ -32,8 +32,8 @@ EXPORTS = [
     "zc_species_inject", "zc_species_get_particles", "zc_species_count", "zc_set_injector",
     "zc_set_smooth", "zc_set_moving_window", "zc_add_laser", "zc_set_ext_fld", "zc_step",
     "zc_current_zero", "zc_spec_advance", "zc_current_update", "zc_emf_advance", "zc_set_fields",
-    "zc_get_fields", "zc_get_particle_fields", "zc_get_current", "zc_set_current", "zc_energy",
-    "zc_species_charge", "zc_get_info", "zc_grid_view_get", "zc_synchronize", "zc_last_step_ms",
+    "zc_get_fields", "zc_get_particle_fields", "zc_get_current", "zc_set_current", "zc_energy", "zc_energy_async",
+    "zc_species_charge", "zc_get_info", "zc_grid_view_get", "zc_synchronize", "zc_last_step_ms", "zc_step_async",
     "zc_last_error", "zc_status_string", "zc_set_profiling", "zc_get_profile", "zc_reset_profile",
     "zc_phase_name", "zc_field_energy_static", "zc_set_graphs", "zc_history_enable", "zc_history_get",
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
@@ -143,10 +143,12 @@ def load(path: str = LIB_PATH):
         "zc_get_current": [P, P],
         "zc_set_current": [P, P],
         "zc_energy": [P, P, P],
+        "zc_energy_async": [P, P, P],
         "zc_species_charge": [P, I, P],
         "zc_get_info": [P, C.POINTER(Info)],
         "zc_grid_view_get": [P, C.POINTER(GridView)],
         "zc_synchronize": [P],
+        "zc_step_async": [P, I],
         "zc_last_step_ms": [P, C.POINTER(C.c_float)],
         "zc_set_profiling": [P, I],
         "zc_get_profile": [P, P, P],
@@ -355,6 +357,11 @@ class CudaSim:
 
     iter = step
 
+    def step_async(self, n=1):
+        """Queues n steps and returns without waiting (errors come back from
+        the next waiting call, e.g. ``synchronize()``)."""
+        _ck(self.lib.zc_step_async(self.h, int(n)))
+
     def current_zero(self):
         _ck(self.lib.zc_current_zero(self.h))
 
@@ -419,6 +426,16 @@ class CudaSim:
         kin = np.zeros(max(self.n_species, 1), dtype=np.float64)
         _ck(self.lib.zc_energy(self.h, _p(emf), _p(kin)))
         return emf, kin[: self.n_species]
+
+    def energy_async(self, out):
+        """Queues the energies into ``out`` (float64, 6 + n_species: the
+        field components, then the kinetic energy of every species) and
+        returns at once; ``out`` holds them after ``synchronize()``.  Use
+        page-locked memory for ``out`` to keep the copies asynchronous."""
+        if out.dtype != np.float64 or out.size < 6 + self.n_species or not out.flags.c_contiguous:
+            raise ValueError("out: contiguous float64 array of 6 + n_species values")
+        kin = out[6:] if self.n_species else None
+        _ck(self.lib.zc_energy_async(self.h, _p(out), _p(kin) if kin is not None else None))
 
     def charge(self, k, out=None):
         rho = np.zeros((self.nx[1] + 1, self.nx[0] + 1), dtype=np.float32) if out is None else out

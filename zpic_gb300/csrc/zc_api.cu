@@ -195,6 +195,7 @@ struct zc_sim {
   int sort_every = 8;             // steps between per-tile cell sorts
   float slack = 0.5f;
   int accumulated_err = 0;
+  int queued_steps = 0;           // steps zc_step_async queued since the last wait
   // per-phase profiling: event pairs recorded during a call, summed on sync
   int profiling = 0;
   std::vector<cudaEvent_t> ev_pool;
@@ -1263,7 +1264,7 @@ zc_status zc_sim_create(const zc_sim_desc *d, zc_sim **out) {
     st = fail(ZC_ENOMEM, "cudaMallocHost failed");
     goto bad;
   }
-  s->energy_blocks = 2 * 152;
+  s->energy_blocks = 8 * 152;  // 64 warps a multiprocessor: enough field reads in flight
   TRYC(dalloc(&s->d_part, 6 * s->energy_blocks));
   TRYC(dalloc(&s->d_emf, 6));
   TRYC(dalloc(&s->stage, (size_t)(s->nx + 3) * (s->ny + 3) * 3));
@@ -1705,6 +1706,24 @@ zc_status zc_step(zc_sim *s, int nsteps) {
   return check_errors(s, true);
 }
 
+zc_status zc_step_async(zc_sim *s, int nsteps) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (nsteps < 0) return fail(ZC_EINVAL, "nsteps must be >= 0");
+  DeviceGuard g(s->device);
+  for (int n = 0; n < nsteps; ++n) {
+    TRY(iter_impl(s));
+    // every 16 queued steps: wait, and drain a spill list that has filled
+    if (++s->queued_steps >= 16) {
+      CK(cudaMemcpyAsync(s->h_pinned, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+      CK(cudaStreamSynchronize(s->st));
+      s->queued_steps = 0;
+      collect_profile(s);
+      if (s->h_pinned[0]) TRY(check_errors(s, true));
+    }
+  }
+  return ZC_OK;
+}
+
 zc_status zc_current_zero(zc_sim *s) {
   if (!s) return fail(ZC_EINVAL, "null simulation handle");
   DeviceGuard g(s->device);
@@ -1850,9 +1869,8 @@ zc_status zc_set_current(zc_sim *s, const float *J) {
   return ZC_OK;
 }
 
-zc_status zc_energy(zc_sim *s, double emf[6], double *kin) {
-  if (!s) return fail(ZC_EINVAL, "null simulation handle");
-  DeviceGuard g(s->device);
+// queues the field-energy reduction and the copies of the energies to the host
+zc_status queue_energy(zc_sim *s, double *emf, double *kin) {
   if (emf) {
     CK(launch_emf_energy(s->EB[s->eb_cur], s->G, s->d_part, s->energy_blocks, s->d_emf, s->dx[0], s->dx[1], s->st));
     CK(cudaMemcpyAsync(emf, s->d_emf, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
@@ -1860,8 +1878,21 @@ zc_status zc_energy(zc_sim *s, double emf[6], double *kin) {
   if (kin)
     for (size_t k = 0; k < s->sp.size(); ++k)
       CK(cudaMemcpyAsync(kin + k, s->sp[k].d_ekin, sizeof(double), cudaMemcpyDeviceToHost, s->st));
+  return ZC_OK;
+}
+
+zc_status zc_energy(zc_sim *s, double emf[6], double *kin) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  TRY(queue_energy(s, emf, kin));
   CK(cudaStreamSynchronize(s->st));
   return ZC_OK;
+}
+
+zc_status zc_energy_async(zc_sim *s, double emf[6], double *kin) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  DeviceGuard g(s->device);
+  return queue_energy(s, emf, kin);
 }
 
 zc_status zc_species_charge(zc_sim *s, int k, float *charge) {
@@ -1950,6 +1981,7 @@ zc_status zc_synchronize(zc_sim *s) {
   if (!s) return fail(ZC_EINVAL, "null simulation handle");
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
+  s->queued_steps = 0;
   collect_profile(s);
   return check_errors(s, true);
 }

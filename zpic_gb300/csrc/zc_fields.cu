@@ -597,12 +597,23 @@ __global__ void __launch_bounds__(256) k_emf_energy_partial(const float *EB, Gri
   }
 }
 
+// the sum over the blocks of component c of the partials, by warp c (lanes
+// take every 32nd block, then a shuffle tree): valid in lane 0
+__device__ __forceinline__ double partial_sum(const double *partial, int nblocks, int c) {
+  const int lane = threadIdx.x & 31;
+  double s = 0;
+  for (int b = lane; b < nblocks; b += 32) s += partial[b * 6 + c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  return s;
+}
+
+// six warps, one per component
 __global__ void k_emf_energy_final(const double *partial, int nblocks, double *out, float dx, float dy) {
-  if (threadIdx.x < 6) {
-    double s = 0;
-    for (int b = 0; b < nblocks; ++b) s += partial[b * 6 + threadIdx.x];
-    out[threadIdx.x] = s * (0.5 * dx * dy);
-  }
+  const int c = threadIdx.x >> 5;
+  if (c >= 6) return;
+  const double s = partial_sum(partial, nblocks, c);
+  if ((threadIdx.x & 31) == 0) out[c] = s * (0.5 * dx * dy);
 }
 
 // ---------------------------------------------------------------------------
@@ -753,7 +764,7 @@ cudaError_t launch_window_shift(const float *EBin, float *EBout, const Grid &G, 
 cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, int nblocks, double *out, float dx,
                               float dy, cudaStream_t st) {
   k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);
-  k_emf_energy_final<<<1, 32, 0, st>>>(partial, nblocks, out, dx, dy);
+  k_emf_energy_final<<<1, 6 * 32, 0, st>>>(partial, nblocks, out, dx, dy);
   return cudaGetLastError();
 }
 
@@ -766,13 +777,12 @@ __global__ void k_energy_history_row(const double *partial, int nblocks, float d
   __syncthreads();
   if (n >= cap) return;
   double *row = hist + (size_t)n * cols;
-  const int t = threadIdx.x;
-  if (t < 6) {
-    double s = 0;
-    for (int b = 0; b < nblocks; ++b) s += partial[b * 6 + t];
-    row[t] = s * (0.5 * dx * dy);
-  } else if (t - 6 < nsp) {
-    row[t] = *ekin[t - 6];
+  const int t = threadIdx.x, c = t >> 5;
+  if (c < 6) {  // warps 0..5: the field components
+    const double s = partial_sum(partial, nblocks, c);
+    if ((t & 31) == 0) row[c] = s * (0.5 * dx * dy);
+  } else if (t - 6 * 32 < nsp) {  // then one thread per species
+    row[6 + t - 6 * 32] = *ekin[t - 6 * 32];
   }
   __syncthreads();
   if (t == 0) *hist_n = n + 1;
@@ -781,9 +791,9 @@ __global__ void k_energy_history_row(const double *partial, int nblocks, float d
 cudaError_t launch_energy_history(const float *EB, const Grid &G, double *partial, int nblocks, double *hist,
                                   int *hist_n, int cap, int cols, double *const *ekin, int nsp, float dx, float dy,
                                   cudaStream_t st) {
-  if (nsp + 6 > 64) return cudaErrorInvalidValue;
+  if (nsp > 64) return cudaErrorInvalidValue;
   k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);
-  k_energy_history_row<<<1, 64, 0, st>>>(partial, nblocks, dx, dy, ekin, nsp, hist, hist_n, cap, cols);
+  k_energy_history_row<<<1, 6 * 32 + 64, 0, st>>>(partial, nblocks, dx, dy, ekin, nsp, hist, hist_n, cap, cols);
   return cudaGetLastError();
 }
 
