@@ -1869,8 +1869,22 @@ zc_status zc_set_current(zc_sim *s, const float *J) {
   return ZC_OK;
 }
 
-// queues the field-energy reduction and the copies of the energies to the host
+// queues the field-energy reduction and the copies of the energies to the
+// host: written by the reduction kernel itself into page-locked host arrays
+// (no copy operations), else through device words and copies
 zc_status queue_energy(zc_sim *s, double *emf, double *kin) {
+  const int nsp = (int)s->sp.size();
+  void *emf_d = emf ? const_cast<void *>(mapped_records(emf, 6 * sizeof(double))) : nullptr;
+  void *kin_d = (kin && nsp) ? const_cast<void *>(mapped_records(kin, nsp * sizeof(double))) : nullptr;
+  const bool direct = (!emf || (emf_d && ((uintptr_t)emf_d & 7) == 0)) &&
+                      (!kin || !nsp || (kin_d && ((uintptr_t)kin_d & 7) == 0)) && nsp <= kEkinRefs && (emf || kin);
+  if (direct) {
+    EkinRefs K{};
+    for (int k = 0; k < nsp; ++k) K.p[k] = s->sp[k].d_ekin;
+    CK(launch_energy_direct(s->EB[s->eb_cur], s->G, s->d_part, s->energy_blocks, s->dx[0], s->dx[1], K,
+                            kin ? nsp : 0, (double *)emf_d, (double *)kin_d, s->st));
+    return ZC_OK;
+  }
   if (emf) {
     CK(launch_emf_energy(s->EB[s->eb_cur], s->G, s->d_part, s->energy_blocks, s->d_emf, s->dx[0], s->dx[1], s->st));
     CK(cudaMemcpyAsync(emf, s->d_emf, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st));

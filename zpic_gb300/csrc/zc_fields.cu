@@ -768,6 +768,21 @@ cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, i
   return cudaGetLastError();
 }
 
+// the field energy from the partials and the kinetic energy of every
+// species, written straight to the caller's (page-locked, mapped) host arrays
+__global__ void k_energy_direct(const double *partial, int nblocks, float dx, float dy, EkinRefs K, int nsp,
+                                double *emf, double *kin) {
+  const int t = threadIdx.x, c = t >> 5;
+  if (c < 6) {
+    if (emf) {  // (the same for every lane of the warp)
+      const double s = partial_sum(partial, nblocks, c);
+      if ((t & 31) == 0) emf[c] = s * (0.5 * dx * dy);
+    }
+  } else if (t - 6 * 32 < nsp && kin) {
+    kin[t - 6 * 32] = *K.p[t - 6 * 32];
+  }
+}
+
 // one history row: the field energy from the partials (the sum of
 // k_emf_energy_final) and the kinetic energy of every species; the row index
 // is a device counter, so a captured step appends where it runs
@@ -786,6 +801,14 @@ __global__ void k_energy_history_row(const double *partial, int nblocks, float d
   }
   __syncthreads();
   if (t == 0) *hist_n = n + 1;
+}
+
+cudaError_t launch_energy_direct(const float *EB, const Grid &G, double *partial, int nblocks, float dx, float dy,
+                                 const EkinRefs &K, int nsp, double *emf, double *kin, cudaStream_t st) {
+  if (nsp > kEkinRefs) return cudaErrorInvalidValue;
+  if (emf) k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);
+  k_energy_direct<<<1, 6 * 32 + kEkinRefs, 0, st>>>(partial, nblocks, dx, dy, K, nsp, emf, kin);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_energy_history(const float *EB, const Grid &G, double *partial, int nblocks, double *hist,

@@ -225,6 +225,16 @@ cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st);
 cudaError_t launch_ext_add(const float *EB, float *EBp, const float *extE, const float *extB, int Etype, int Btype,
                            float3 E0, float3 B0, const Grid &G, cudaStream_t st);
 cudaError_t launch_window_shift(const float *EBin, float *EBout, const Grid &G, cudaStream_t st);
+// the kinetic-energy words of up to kEkinRefs species, by value
+constexpr int kEkinRefs = 32;
+struct EkinRefs {
+  const double *p[kEkinRefs];
+};
+// field energy (emf, 6 values) and the species' kinetic energies (kin) written
+// by the device into the given arrays (device or mapped host memory); either
+// may be null
+cudaError_t launch_energy_direct(const float *EB, const Grid &G, double *partial, int nblocks, float dx, float dy,
+                                 const EkinRefs &K, int nsp, double *emf, double *kin, cudaStream_t st);
 cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, int nblocks, double *out, float dx,
                               float dy, cudaStream_t st);
 // appends one row (6 field-energy components, then each species' kinetic
