@@ -574,7 +574,6 @@ __global__ void k_window_shift(const float *EBin, float *EBout, Grid G) {
 // threads and blocks, partials summed in a fixed order
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_emf_energy_partial(const float *EB, Grid G, double *partial) {
-  __shared__ double sred[8];
   float s[6] = {0, 0, 0, 0, 0, 0}, cc[6] = {0, 0, 0, 0, 0, 0};
   // interior rows over the blocks, interior columns over the threads: no
   // index division, coalesced rows
@@ -591,9 +590,31 @@ __global__ void __launch_bounds__(256) k_emf_energy_partial(const float *EB, Gri
       }
     }
   }
+  // the 32 lanes' sums (s - cc each) as float pairs added with the exact
+  // two-sum (hi + lo carries about 48 bits), then one double per warp: the
+  // float pipes do the tree, FP64 (a slow pipe on this part) only the last
+  // eight additions of a block
+  __shared__ double swarp[6][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
   for (int c = 0; c < 6; ++c) {
-    const double v = block_sum_double<256>((double)s[c] - (double)cc[c], sred);
-    if (threadIdx.x == 0) partial[blockIdx.x * 6 + c] = v;
+    float hi = s[c], lo = -cc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+      const float t = hi + oh, bb = t - hi;
+      const float e = (hi - (t - bb)) + (oh - bb);
+      hi = t;
+      lo = lo + ol + e;
+    }
+    if (lane == 0) swarp[c][warp] = (double)hi + (double)lo;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) v += swarp[threadIdx.x][w];
+    partial[blockIdx.x * 6 + threadIdx.x] = v;
   }
 }
 
