@@ -593,12 +593,12 @@ __global__ void k_charge_fold(float *rho, int nx, int ny, int mw) {
 }
 
 // sum of the per-tile kinetic-energy partials in a fixed order
-__global__ void __launch_bounds__(1024) k_sum_energy(const double *tiles, int ntiles, const double *extra, double *out,
-                                                     float scale_q_mq, float dx, float dy, int det) {
-  __shared__ double sred[32];
+__global__ void k_sum_energy(const double *tiles, int ntiles, const double *extra, double *out, float scale_q_mq,
+                             float dx, float dy, int det) {
+  __shared__ double sred[8];
   double s = 0;
-  for (int t = threadIdx.x; t < ntiles; t += 1024) s += tiles[t];
-  s = block_sum_double<1024>(s, sred);
+  for (int t = threadIdx.x; t < ntiles; t += 256) s += tiles[t];
+  s = block_sum_double<256>(s, sred);
   if (threadIdx.x == 0) {
     if (det) {
       const long long *w = reinterpret_cast<const long long *>(extra);
@@ -758,7 +758,7 @@ cudaError_t launch_charge(const Particles &buf, const int *off, const int *np, i
 
 cudaError_t launch_sum_energy(const double *tiles, int ntiles, const double *extra, double *out, float q_mq,
                               float dx, float dy, int det, cudaStream_t st) {
-  k_sum_energy<<<1, 1024, 0, st>>>(tiles, ntiles, extra, out, q_mq, dx, dy, det);
+  k_sum_energy<<<1, 256, 0, st>>>(tiles, ntiles, extra, out, q_mq, dx, dy, det);
   return cudaGetLastError();
 }
 
