@@ -94,3 +94,28 @@ def test_queued_steps_and_energies_match_waiting_ones():
         g.close()
     for a, b in zip(rows[0], rows[1]):
         assert np.array_equal(a, b)
+
+
+def test_graphs_with_timed_push_keep_bits_and_time_every_push():
+    """Push-only profiling under graph replay: the blocks carry event-record
+    nodes around every push.  The run keeps the bits of an eager untimed run,
+    and every push of the call is timed (eager steps before the first block
+    boundary and after the last, nodes in between)."""
+    name = "weibel_smooth"
+    n = len(DECKS[name]["species"])
+    states = []
+    for graphs, prof in ((False, False), (True, "push")):
+        cpu, g = mirror(name, deterministic=True, sort_every=2)
+        g.set_graphs(graphs)
+        g.step(3)
+        g.set_profiling(prof)
+        g.reset_profile()
+        g.step(21)  # 1 eager, 4 blocks of 4, 4 eager
+        p = g.profile()
+        if prof:
+            ms, launches = p["push"]
+            assert launches == 21 * n
+            assert ms > 0
+        states.append(_state(g, n))
+        g.close()
+    _same(states[0], states[1])

@@ -148,6 +148,10 @@ struct StepGraph {
   bool valid = false;
   unsigned long long id = 0;  // unique per capture (batch graphs hold copies)
   Counters before, after;
+  // captured with the push launches bracketed by event-record nodes (push-only
+  // profiling): their pairs, read after every replay
+  bool timed = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> push_ev;
 };
 
 std::atomic<unsigned long long> g_capture_id{0};
@@ -198,6 +202,8 @@ struct zc_sim {
   int queued_steps = 0;           // steps zc_step_async queued since the last wait
   // per-phase profiling: event pairs recorded during a call, summed on sync
   int profiling = 0;
+  // while a timed graph is captured: where the push's event pairs go
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> *cap_ev = nullptr;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
   size_t ev_used = 0;
@@ -241,14 +247,34 @@ struct Phase {
   zc_sim *s;
   int ph;
   cudaEvent_t b = nullptr;
+  bool node = false;  // recorded as a node of the graph being captured
   Phase(zc_sim *s_, int ph_, int nlaunch) : s(s_), ph(ph_) {
     s->prof_launch[ph] += nlaunch;
+    if (s->cap_ev && ph == ZC_PHASE_PUSH) {
+      if (cudaEventCreate(&b) != cudaSuccess) {
+        b = nullptr;
+        return;
+      }
+      node = true;
+      cudaEventRecordWithFlags(b, s->st, cudaEventRecordExternal);
+      return;
+    }
     if (!s->profiling || (s->profiling == 2 && ph != ZC_PHASE_PUSH)) return;
     b = next_event();
     cudaEventRecord(b, s->st);
   }
   ~Phase() {
     if (!b) return;
+    if (node) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaEventDestroy(b);
+        return;
+      }
+      cudaEventRecordWithFlags(e, s->st, cudaEventRecordExternal);
+      s->cap_ev->push_back({b, e});
+      return;
+    }
     cudaEvent_t e = next_event();
     cudaEventRecord(e, s->st);
     s->ev_pending.push_back({ph, {b, e}});
@@ -845,6 +871,12 @@ zc_status iter_impl(zc_sim *s) {
 void drop_graph(StepGraph &g) {
   if (g.exec) cudaGraphExecDestroy(g.exec);
   if (g.graph) cudaGraphDestroy(g.graph);
+  for (auto &pe : g.push_ev) {
+    cudaEventDestroy(pe.first);
+    cudaEventDestroy(pe.second);
+  }
+  g.push_ev.clear();
+  g.timed = false;
   g.exec = nullptr;
   g.graph = nullptr;
   g.valid = false;
@@ -888,7 +920,8 @@ bool same_parities(const Counters &a, const Counters &b) {
 
 // the graph g holds n steps from the current state (block-aligned)
 bool graph_ready(const zc_sim *s, const StepGraph &g, int n) {
-  return g.valid && g.nsteps == n && s->iter % block_period(s) == 0 && same_parities(g.before, save_counters(s));
+  return g.valid && g.nsteps == n && g.timed == (s->profiling == 2) && s->iter % block_period(s) == 0 &&
+         same_parities(g.before, save_counters(s));
 }
 
 // Captures n steps, starting at a block boundary, as a graph.  Capturing
@@ -901,13 +934,24 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G, bool instantiate = true)
   if (s->iter % block_period(s) != 0) return fail(ZC_ESTATE, "graph capture off a block boundary");
   const Counters before = save_counters(s);
   const int prof = s->profiling;
+  // push-only profiling: the graph brackets every push with event-record nodes
+  const bool timed = prof == 2;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evs;
   s->profiling = 0;
+  if (timed) s->cap_ev = &evs;
   CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
   zc_status st = ZC_OK;
   for (int k = 0; k < n && st == ZC_OK; ++k) st = iter_impl(s);
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(s->st, &g);
+  s->cap_ev = nullptr;
   s->profiling = prof;
+  auto drop_events = [&] {
+    for (auto &pe : evs) {
+      cudaEventDestroy(pe.first);
+      cudaEventDestroy(pe.second);
+    }
+  };
   const Counters after = save_counters(s);
   // put the host state back (nothing ran yet)
   s->iter = before.iter;
@@ -926,20 +970,27 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G, bool instantiate = true)
   for (int k = 0; k < ZC_NPHASE; ++k) s->prof_launch[k] = before.launch[k];
   if (st != ZC_OK) {
     if (g) cudaGraphDestroy(g);
+    drop_events();
     return st;
   }
-  if (e != cudaSuccess) return fail(ZC_ECUDA, "stream capture failed: %s", cudaGetErrorString(e));
+  if (e != cudaSuccess) {
+    drop_events();
+    return fail(ZC_ECUDA, "stream capture failed: %s", cudaGetErrorString(e));
+  }
   cudaGraphExec_t x = nullptr;
   if (instantiate) {
     const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
     if (ei != cudaSuccess) {
       cudaGraphDestroy(g);
+      drop_events();
       return fail(ZC_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(ei));
     }
   }
   G.graph = g;
   G.exec = x;
   G.nsteps = n;
+  G.timed = timed;
+  G.push_ev = std::move(evs);
   G.before = before;
   G.after = after;
   G.valid = true;
@@ -983,11 +1034,25 @@ void account_steps(zc_sim *s, const StepGraph &g) {
 // every species injecting on the device (a provider calls back into the
 // host).
 bool graph_possible(const zc_sim *s) {
-  if (!s->use_graph || s->profiling || s->sp.empty()) return false;
+  if (!s->use_graph || s->sp.empty()) return false;
+  // every phase timed: eager; the push timed: replayed graphs time it with
+  // their event-record nodes (not under a moving window)
+  if (s->profiling == 1 || (s->profiling == 2 && s->mw)) return false;
   if (s->mw)
     for (const auto &p : s->sp)
       if (!p.dinj) return false;
   return true;
+}
+
+// a replayed timed graph: waits for it, then adds its push times
+zc_status collect_graph_times(zc_sim *s, const StepGraph &g) {
+  if (!g.timed || g.push_ev.empty()) return ZC_OK;
+  CK(cudaEventSynchronize(g.push_ev.back().second));
+  for (const auto &pe : g.push_ev) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, pe.first, pe.second) == cudaSuccess) s->prof_ms[ZC_PHASE_PUSH] += ms;
+  }
+  return ZC_OK;
 }
 
 // the host decisions of the next n steps of a moving-window run, replayed
@@ -1044,6 +1109,7 @@ zc_status step_graph(zc_sim *s, int *nsteps) {
     TRY(ensure_exec(s->blk));
     CK(cudaGraphLaunch(s->blk.exec, s->st));
     account_steps(s, s->blk);
+    TRY(collect_graph_times(s, s->blk));
     *nsteps -= P;
     const int b = launched & 1;
     CK(cudaMemcpyAsync(s->h_pinned + 2 + b, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
@@ -1058,7 +1124,9 @@ zc_status step_graph(zc_sim *s, int *nsteps) {
     }
     ++launched;
   }
-  if (*nsteps > 0) {
+  // the rest of the call: a captured prefix of a block (the caller runs it
+  // eagerly when the push is timed: capturing there would stall the device)
+  if (*nsteps > 0 && s->profiling != 2) {
     if (!graph_ready(s, s->tail, *nsteps)) TRY(capture_steps(s, *nsteps, s->tail));
     TRY(ensure_exec(s->tail));
     CK(cudaGraphLaunch(s->tail.exec, s->st));
