@@ -110,11 +110,11 @@ def test_graphs_with_timed_push_keep_bits_and_time_every_push():
         g.step(3)
         g.set_profiling(prof)
         g.reset_profile()
-        g.step(21)  # 1 eager, 4 blocks of 4, 4 eager
+        g.step(22)  # 1 eager step, 5 blocks of 4 steps, 1 eager step
         p = g.profile()
         if prof:
             ms, launches = p["push"]
-            assert launches == 21 * n
+            assert launches == 22 * n
             assert ms > 0
         states.append(_state(g, n))
         g.close()
