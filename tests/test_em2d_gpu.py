@@ -1,7 +1,9 @@
 """The em2d Python API (zpic_gb300.em2d, the reference's Cython class
 interface) on the GPU against the CPU oracle: every deck, 10 steps, per-step
-field relative L2 error <= 1e-5, same particle counts, energies within 1e-5.
-Each deck runs in a fresh process (both generators are process-global)."""
+field relative L2 error <= 1e-5 (each field as a whole; each component
+within 1e-5 or within twice the oracle's own drift when its particles are
+summed in another order), same particle counts, energies within 1e-5.  Each
+deck runs in a fresh process (both generators are process-global)."""
 import os
 import subprocess
 import sys
@@ -18,7 +20,7 @@ import sys
 sys.path[:0] = [{root!r}, {tests!r}]
 import numpy as np
 from decks import DECKS, _resolve, build_cpu
-from gpu_util import field_err
+from gpu_util import field_err_components, field_err_joint, reordered_twin
 from zpic_gb300 import em2d
 
 name = {name!r}
@@ -49,6 +51,7 @@ if "smooth" in d:
     sim.set_smooth(em2d.Smooth(**d["smooth"]))
 
 cpu = build_cpu(name)
+twin = reordered_twin(name)
 for k in range(len(species)):
     a = np.sort(species[k].particles.copy(), order=["iy", "ix", "y", "x"])
     b = np.sort(cpu.particles(k), order=["iy", "ix", "y", "x"])
@@ -57,6 +60,7 @@ steps = 40 if d.get("moving_window") else 10
 for n in range(steps):
     sim.iter()
     cpu.iter()
+    twin.iter()
     for k in range(len(species)):
         assert species[k].particles.size == cpu.np_(k), (n, k)
         assert abs(species[k].energy - cpu.energy(k)) <= 1e-5 * abs(cpu.energy(k)) + 1e-12
@@ -64,9 +68,12 @@ for n in range(steps):
     B = np.stack([sim.emf.Bx, sim.emf.By, sim.emf.Bz], -1)
     Ec, Bc = cpu.E()[1:-2, 1:-2], cpu.B()[1:-2, 1:-2]
     pad = lambda a: np.pad(a, ((1, 2), (1, 2), (0, 0)))
-    for g, c, f in ((E, Ec, "E"), (B, Bc, "B")):
-        err = field_err(pad(g), pad(c))
-        assert err <= (1e-5 if n < 10 else 1e-4), (f, n, err)
+    bar = 1e-5 if n < 10 else 1e-4
+    for g, c, t, f in ((E, Ec, twin.E(), "E"), (B, Bc, twin.B(), "B")):
+        assert field_err_joint(pad(g), pad(c)) <= bar, (f, n, field_err_joint(pad(g), pad(c)))
+        err, floor = field_err_components(pad(g), pad(c)), field_err_components(t, cpu.E() if f == "E" else cpu.B())
+        for comp in range(3):
+            assert err[comp] <= max(bar, 2 * floor[comp]), (f, comp, n, err[comp], floor[comp])
     en = sim.emf.energy
     assert np.allclose(en, cpu.emf_energy(), rtol=1e-4, atol=1e-12), n
 assert sim.n_move == cpu.n_move()
