@@ -51,7 +51,9 @@ if "smooth" in d:
     sim.set_smooth(em2d.Smooth(**d["smooth"]))
 
 cpu = build_cpu(name)
-twin = reordered_twin(name)
+# the reordered twin shares the oracle's process-wide generator, which a
+# moving window draws from every step: only the other decks get one
+twin = None if d.get("moving_window") else reordered_twin(name)
 for k in range(len(species)):
     a = np.sort(species[k].particles.copy(), order=["iy", "ix", "y", "x"])
     b = np.sort(cpu.particles(k), order=["iy", "ix", "y", "x"])
@@ -60,7 +62,8 @@ steps = 40 if d.get("moving_window") else 10
 for n in range(steps):
     sim.iter()
     cpu.iter()
-    twin.iter()
+    if twin is not None:
+        twin.iter()
     for k in range(len(species)):
         assert species[k].particles.size == cpu.np_(k), (n, k)
         assert abs(species[k].energy - cpu.energy(k)) <= 1e-5 * abs(cpu.energy(k)) + 1e-12
@@ -69,9 +72,11 @@ for n in range(steps):
     Ec, Bc = cpu.E()[1:-2, 1:-2], cpu.B()[1:-2, 1:-2]
     pad = lambda a: np.pad(a, ((1, 2), (1, 2), (0, 0)))
     bar = 1e-5 if n < 10 else 1e-4
-    for g, c, t, f in ((E, Ec, twin.E(), "E"), (B, Bc, twin.B(), "B")):
+    for g, c, f in ((E, Ec, "E"), (B, Bc, "B")):
+        full = cpu.E() if f == "E" else cpu.B()
         assert field_err_joint(pad(g), pad(c)) <= bar, (f, n, field_err_joint(pad(g), pad(c)))
-        err, floor = field_err_components(pad(g), pad(c)), field_err_components(t, cpu.E() if f == "E" else cpu.B())
+        err = field_err_components(pad(g), pad(c))
+        floor = field_err_components(getattr(twin, f)(), full) if twin is not None else np.zeros(3)
         for comp in range(3):
             assert err[comp] <= max(bar, 2 * floor[comp]), (f, comp, n, err[comp], floor[comp])
     en = sim.emf.energy
