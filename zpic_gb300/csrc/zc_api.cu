@@ -149,9 +149,11 @@ struct StepGraph {
   unsigned long long id = 0;  // unique per capture (batch graphs hold copies)
   Counters before, after;
   // captured with the push launches bracketed by event-record nodes (push-only
-  // profiling): their pairs, read after every replay
+  // profiling): the events recorded at capture, and the node pairs, which
+  // every replay points at fresh events of the simulation's pool
   bool timed = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> push_ev;
+  std::vector<std::pair<cudaGraphNode_t, cudaGraphNode_t>> push_nodes;
 };
 
 std::atomic<unsigned long long> g_capture_id{0};
@@ -241,6 +243,8 @@ struct DeviceGuard {
   }
 };
 
+cudaEvent_t pool_event(zc_sim *s);
+
 // Brackets a phase with events when profiling is on; counts its launches
 // always.
 struct Phase {
@@ -279,15 +283,18 @@ struct Phase {
     cudaEventRecord(e, s->st);
     s->ev_pending.push_back({ph, {b, e}});
   }
-  cudaEvent_t next_event() {
-    if (s->ev_used == s->ev_pool.size()) {
-      cudaEvent_t e;
-      cudaEventCreate(&e);
-      s->ev_pool.push_back(e);
-    }
-    return s->ev_pool[s->ev_used++];
-  }
+  cudaEvent_t next_event() { return pool_event(s); }
 };
+
+// the next event of the simulation's pool (reused after collect_profile)
+cudaEvent_t pool_event(zc_sim *s) {
+  if (s->ev_used == s->ev_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    s->ev_pool.push_back(e);
+  }
+  return s->ev_pool[s->ev_used++];
+}
 
 // sums the recorded phase times (stream must be synchronised)
 void collect_profile(zc_sim *s) {
@@ -876,6 +883,7 @@ void drop_graph(StepGraph &g) {
     cudaEventDestroy(pe.second);
   }
   g.push_ev.clear();
+  g.push_nodes.clear();
   g.timed = false;
   g.exec = nullptr;
   g.graph = nullptr;
@@ -990,6 +998,32 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G, bool instantiate = true)
   G.exec = x;
   G.nsteps = n;
   G.timed = timed;
+  if (timed) {
+    // the event-record nodes the capture made, in push order
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CK(cudaGraphGetNodes(g, nodes.data(), &nn));
+    std::vector<std::pair<cudaEvent_t, cudaGraphNode_t>> rec;
+    for (cudaGraphNode_t node : nodes) {
+      cudaGraphNodeType ty;
+      CK(cudaGraphNodeGetType(node, &ty));
+      if (ty != cudaGraphNodeTypeEventRecord) continue;
+      cudaEvent_t ev = nullptr;
+      CK(cudaGraphEventRecordNodeGetEvent(node, &ev));
+      rec.push_back({ev, node});
+    }
+    auto node_of = [&](cudaEvent_t ev) -> cudaGraphNode_t {
+      for (const auto &r : rec)
+        if (r.first == ev) return r.second;
+      return nullptr;
+    };
+    for (const auto &pe : evs) {
+      const cudaGraphNode_t nb = node_of(pe.first), ne = node_of(pe.second);
+      if (!nb || !ne) return fail(ZC_ECUDA, "timed graph: an event-record node is missing");
+      G.push_nodes.push_back({nb, ne});
+    }
+  }
   G.push_ev = std::move(evs);
   G.before = before;
   G.after = after;
@@ -1044,14 +1078,19 @@ bool graph_possible(const zc_sim *s) {
   return true;
 }
 
-// a replayed timed graph: waits for it, then adds its push times
-zc_status collect_graph_times(zc_sim *s, const StepGraph &g) {
-  if (!g.timed || g.push_ev.empty()) return ZC_OK;
-  CK(cudaEventSynchronize(g.push_ev.back().second));
-  for (const auto &pe : g.push_ev) {
-    float ms = 0;
-    if (cudaEventElapsedTime(&ms, pe.first, pe.second) == cudaSuccess) s->prof_ms[ZC_PHASE_PUSH] += ms;
-  }
+// launches a captured graph; a timed one first points its push event-record
+// nodes at fresh events of the pool (the change holds for this launch on,
+// earlier launches keep theirs), read with the eager phases' events
+zc_status launch_graph(zc_sim *s, StepGraph &g) {
+  TRY(ensure_exec(g));
+  if (g.timed)
+    for (const auto &pn : g.push_nodes) {
+      cudaEvent_t b = pool_event(s), e = pool_event(s);
+      CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, pn.first, b));
+      CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, pn.second, e));
+      s->ev_pending.push_back({ZC_PHASE_PUSH, {b, e}});
+    }
+  CK(cudaGraphLaunch(g.exec, s->st));
   return ZC_OK;
 }
 
@@ -1106,10 +1145,8 @@ zc_status step_graph(zc_sim *s, int *nsteps) {
   int launched = 0;
   while (*nsteps >= P) {
     if (!graph_ready(s, s->blk, P)) TRY(capture_steps(s, P, s->blk));
-    TRY(ensure_exec(s->blk));
-    CK(cudaGraphLaunch(s->blk.exec, s->st));
+    TRY(launch_graph(s, s->blk));
     account_steps(s, s->blk);
-    TRY(collect_graph_times(s, s->blk));
     *nsteps -= P;
     const int b = launched & 1;
     CK(cudaMemcpyAsync(s->h_pinned + 2 + b, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
@@ -1124,12 +1161,9 @@ zc_status step_graph(zc_sim *s, int *nsteps) {
     }
     ++launched;
   }
-  // the rest of the call: a captured prefix of a block (the caller runs it
-  // eagerly when the push is timed: capturing there would stall the device)
-  if (*nsteps > 0 && s->profiling != 2) {
+  if (*nsteps > 0) {
     if (!graph_ready(s, s->tail, *nsteps)) TRY(capture_steps(s, *nsteps, s->tail));
-    TRY(ensure_exec(s->tail));
-    CK(cudaGraphLaunch(s->tail.exec, s->st));
+    TRY(launch_graph(s, s->tail));
     account_steps(s, s->tail);
     *nsteps = 0;
   }
