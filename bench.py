@@ -1039,9 +1039,13 @@ def main():
 
     def end_to_end(queued):
         """Uploads fields and particles from the pinned host buffers, then
-        runs the steps with every step's energies copied to the host: queued
-        (zc_step_async + zc_energy_async, one wait at the end) or waiting
-        (zc_step + zc_energy, a wait per step)."""
+        runs the steps with every step's energies reaching host memory:
+        queued (the steps queued with zc_step_async, 16-step blocks replayed
+        as graphs, every step writing its energy row straight into the
+        pinned rows: zc_history_stream; one wait at the end) or waiting
+        (zc_step(1) + zc_energy, a wait per step)."""
+        if queued:
+            sim.history_stream(ehist[:args_steps_e2e])
         barrier()
         sim.synchronize()
         t0 = time.perf_counter()
@@ -1049,16 +1053,18 @@ def main():
         t_f = time.perf_counter()
         sim.set_particles(0, pinned)
         t_p = time.perf_counter()
-        for i in range(args_steps_e2e):
-            if queued:
-                sim.step_async(1)
-                sim.energy_async(ehist[i])
-            else:
+        if queued:
+            sim.step_async(args_steps_e2e)
+        else:
+            for i in range(args_steps_e2e):
                 sim.step(1)
                 emf, kin = sim.energy()
                 ehist[i, :6], ehist[i, 6] = emf, kin[0]
         sim.synchronize()
         t = time.perf_counter() - t0
+        if queued:
+            assert len(sim.history()) == args_steps_e2e, "an energy row for every step"
+            sim.history_stream(None)
         parts = {"fields_upload_s": t_f - t0, "particles_upload_s": t_p - t_f, "steps_with_readback_s": t0 + t - t_p}
         barrier()
         return allmax(t), parts
@@ -1105,9 +1111,10 @@ def main():
                    "l2": "inputs larger than L2 (1.88 GB of particles read and written per step)"},
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "how": "fields and particles uploaded from pinned host buffers through the C-ABI, then per "
-                       "step zc_step_async(1) + zc_energy_async into a pinned host row (every step's "
-                       "energies copied to the host), one wait at the end", **e2e_parts,
+                "how": "fields and particles uploaded from pinned host buffers through the C-ABI, then "
+                       "zc_step_async over the steps (graph replay of 16-step blocks) with every step writing "
+                       "its energy row into pinned host memory (zc_history_stream), one wait at the end",
+                **e2e_parts,
                 "waiting_each_step": {"value": e2e_wait, "how": "the same with zc_step(1) + zc_energy, "
                                       "a host wait per step", **e2e_wait_parts}},
         "gpu_launches": launches,

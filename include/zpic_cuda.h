@@ -184,7 +184,8 @@ ZC_API zc_status zc_set_ext_fld(zc_sim *sim, int E_type, const float E0[3], cons
 ZC_API zc_status zc_step(zc_sim *sim, int nsteps);
 /* zc_step without the wait at the end: the steps are queued on the
  * simulation's stream and the call returns (it waits only every 16 queued
- * steps, to look at the spill list).  Device errors of queued steps are
+ * steps, to look at the spill list; with graph replay on, whole blocks are
+ * queued as graphs and the wait trails one block behind).  Device errors of queued steps are
  * returned by the next waiting call (zc_synchronize, zc_step, zc_energy,
  * ...).  With zc_energy_async a run reports every step without idling the
  * device between steps. */
@@ -378,6 +379,13 @@ ZC_API zc_status zc_set_graphs(zc_sim *sim, int enable);
  * call (em2d/simulation.c:183-205) become a device array read once at the
  * end.  Species must be created first.  max_steps = 0 turns it off. */
 ZC_API zc_status zc_history_enable(zc_sim *sim, int max_steps);
+/* the same rows written by the device straight into the caller's
+ * page-locked host memory (`rows`, max_steps * (6 + n_species) doubles,
+ * cudaHostAlloc'd): every step's energies reach the host as the step ends,
+ * with no copy call, also inside replayed graphs.  The rows hold their values
+ * once zc_synchronize (or any waiting call) returns; zc_history_get reads the
+ * count.  rows = NULL with max_steps = 0 turns it off. */
+ZC_API zc_status zc_history_stream(zc_sim *sim, double *rows, int max_steps);
 /* copies up to `cap_rows` rows into `out` (row-major); *nrows receives the
  * rows recorded, *ncols the row length.  out == NULL only queries. */
 ZC_API zc_status zc_history_get(zc_sim *sim, double *out, int cap_rows, int *nrows, int *ncols);

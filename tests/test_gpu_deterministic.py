@@ -119,3 +119,37 @@ def test_graphs_with_timed_push_keep_bits_and_time_every_push():
         states.append(_state(g, n))
         g.close()
     _same(states[0], states[1])
+
+
+def test_history_streamed_to_host_rows_matches_device_history():
+    """zc_history_stream: every step writes its energy row into page-locked
+    host rows, also inside replayed graphs and queued steps; the rows equal
+    the device-side history's and zc_energy's bits.  Pageable rows are
+    refused."""
+    import torch
+    from zpic_gb300._zc import ZcError
+
+    name, steps = "weibel_smooth", 21
+    n = len(DECKS[name]["species"])
+    out = []
+    for stream in (False, True):
+        cpu, g = mirror(name, deterministic=True, sort_every=2)
+        g.set_graphs(True)
+        if stream:
+            rows = torch.zeros((steps, 6 + n), dtype=torch.float64, pin_memory=True).numpy()
+            with pytest.raises(ZcError):
+                g.history_stream(np.zeros((steps, 6 + n)))
+            g.history_stream(rows)
+            g.step_async(steps)
+            g.synchronize()
+            assert len(g.history()) == steps
+            hist = rows.copy()
+        else:
+            g.history_enable(steps)
+            g.step(steps)
+            hist = g.history()
+        emf, kin = g.energy()
+        assert np.array_equal(hist[-1], np.concatenate([emf, kin]))
+        out.append(hist)
+        g.close()
+    assert np.array_equal(out[0], out[1])

@@ -33,7 +33,7 @@ EXPORTS = [
     "zc_set_smooth", "zc_set_moving_window", "zc_add_laser", "zc_set_ext_fld", "zc_step",
     "zc_current_zero", "zc_spec_advance", "zc_current_update", "zc_emf_advance", "zc_set_fields",
     "zc_get_fields", "zc_get_particle_fields", "zc_get_current", "zc_set_current", "zc_energy", "zc_energy_async",
-    "zc_species_charge", "zc_get_info", "zc_grid_view_get", "zc_synchronize", "zc_last_step_ms", "zc_step_async",
+    "zc_species_charge", "zc_get_info", "zc_grid_view_get", "zc_synchronize", "zc_last_step_ms", "zc_step_async", "zc_history_stream",
     "zc_last_error", "zc_status_string", "zc_set_profiling", "zc_get_profile", "zc_reset_profile",
     "zc_phase_name", "zc_field_energy_static", "zc_set_graphs", "zc_history_enable", "zc_history_get",
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
@@ -149,6 +149,7 @@ def load(path: str = LIB_PATH):
         "zc_grid_view_get": [P, C.POINTER(GridView)],
         "zc_synchronize": [P],
         "zc_step_async": [P, I],
+        "zc_history_stream": [P, P, I],
         "zc_last_step_ms": [P, C.POINTER(C.c_float)],
         "zc_set_profiling": [P, I],
         "zc_get_profile": [P, P, P],
@@ -490,6 +491,20 @@ class CudaSim:
         """Records the field and kinetic energies after every step on the
         device (up to ``max_steps`` rows)."""
         _ck(self.lib.zc_history_enable(self.h, int(max_steps)))
+
+    def history_stream(self, rows):
+        """Every step writes its energy row (6 field components, then the
+        kinetic energy of every species) into ``rows``: page-locked float64
+        host memory of shape (max_steps, 6 + n_species), e.g. from
+        ``torch.empty(..., pin_memory=True)``.  ``None`` turns it off."""
+        if rows is None:
+            _ck(self.lib.zc_history_stream(self.h, None, 0))
+            return
+        if rows.dtype != np.float64 or rows.ndim != 2 or rows.shape[1] != 6 + self.n_species \
+                or not rows.flags.c_contiguous:
+            raise ValueError("rows: contiguous float64 (max_steps, 6 + n_species)")
+        self._stream_rows = rows  # kept alive while the device writes into it
+        _ck(self.lib.zc_history_stream(self.h, _p(rows), rows.shape[0]))
 
     def history_reset(self):
         _ck(self.lib.zc_history_reset(self.h))

@@ -224,6 +224,7 @@ struct zc_sim {
   // per-step energy history on the device: row = 6 field components, then
   // the kinetic energy of every species
   double *d_hist = nullptr;
+  bool hist_host = false;         // d_hist is the device address of the caller's host rows
   int *d_hist_n = nullptr;
   int hist_cap = 0, hist_cols = 0, hist_blocks = 0;
   double **d_ekin_ptrs = nullptr;
@@ -1443,6 +1444,8 @@ zc_status zc_sim_destroy(zc_sim *s) {
   for (auto e : s->ev_blk)
     if (e) cudaEventDestroy(e);
   invalidate_graph(s);
+  if (s->hist_host) s->d_hist = nullptr;  // the caller's rows
+  s->hist_host = false;
   dfree(s->d_hist);
   dfree(s->d_hist_n);
   dfree(s->d_hist_part);
@@ -1812,6 +1815,7 @@ zc_status zc_step_async(zc_sim *s, int nsteps) {
   if (!s) return fail(ZC_EINVAL, "null simulation handle");
   if (nsteps < 0) return fail(ZC_EINVAL, "nsteps must be >= 0");
   DeviceGuard g(s->device);
+  if (graph_possible(s)) TRY(s->mw ? step_graph_mw(s, &nsteps) : step_graph(s, &nsteps));
   for (int n = 0; n < nsteps; ++n) {
     TRY(iter_impl(s));
     // every 16 queued steps: wait, and drain a spill list that has filled
@@ -2157,13 +2161,25 @@ zc_status zc_set_graphs(zc_sim *s, int on) {
   return ZC_OK;
 }
 
-zc_status zc_history_enable(zc_sim *s, int max_steps) {
+zc_status history_setup(zc_sim *s, double *rows, int max_steps);
+
+zc_status zc_history_enable(zc_sim *s, int max_steps) { return history_setup(s, nullptr, max_steps); }
+
+zc_status zc_history_stream(zc_sim *s, double *rows, int max_steps) {
+  if (!s) return fail(ZC_EINVAL, "null simulation handle");
+  if (max_steps > 0 && !rows) return fail(ZC_EINVAL, "null row buffer");
+  return history_setup(s, rows, max_steps);
+}
+
+zc_status history_setup(zc_sim *s, double *rows, int max_steps) {
   if (!s) return fail(ZC_EINVAL, "null simulation handle");
   if (max_steps < 0) return fail(ZC_EINVAL, "max_steps must be >= 0");
   if (s->sp.size() + 6 > 64) return fail(ZC_EINVAL, "energy history holds at most 58 species");
   DeviceGuard g(s->device);
   CK(cudaStreamSynchronize(s->st));
   invalidate_graph(s);
+  if (s->hist_host) s->d_hist = nullptr;  // the caller's rows
+  s->hist_host = false;
   dfree(s->d_hist);
   dfree(s->d_hist_n);
   dfree(s->d_hist_part);
@@ -2176,7 +2192,16 @@ zc_status zc_history_enable(zc_sim *s, int max_steps) {
   // per-step history stays cheap
   const long long cells = (long long)s->nx * s->ny;
   s->hist_blocks = (int)std::max<long long>(1, std::min<long long>(s->energy_blocks, (cells + 1023) / 1024));
-  TRY(dalloc(&s->d_hist, (size_t)max_steps * cols));
+  if (rows) {
+    // the caller's page-locked rows, written by the device step by step
+    void *d = const_cast<void *>(mapped_records(rows, sizeof(double) * (size_t)max_steps * cols));
+    if (!d || ((uintptr_t)d & 7))
+      return fail(ZC_EINVAL, "history rows must be page-locked host memory (cudaHostAlloc), 8-byte aligned");
+    s->d_hist = static_cast<double *>(d);
+    s->hist_host = true;
+  } else {
+    TRY(dalloc(&s->d_hist, (size_t)max_steps * cols));
+  }
   TRY(dalloc(&s->d_hist_n, 1));
   TRY(dalloc(&s->d_hist_part, 6 * (size_t)s->hist_blocks));
   TRY(dalloc(&s->d_ekin_ptrs, std::max<size_t>(1, s->sp.size())));
@@ -2203,7 +2228,8 @@ zc_status zc_history_get(zc_sim *s, double *out, int cap_rows, int *nrows, int *
   if (ncols) *ncols = s->hist_cols;
   if (!out || n == 0) return ZC_OK;
   if (cap_rows < n) return fail(ZC_EINVAL, "output buffer holds %d rows, %d recorded", cap_rows, n);
-  CK(cudaMemcpyAsync(out, s->d_hist, sizeof(double) * (size_t)n * s->hist_cols, cudaMemcpyDeviceToHost, s->st));
+  CK(cudaMemcpyAsync(out, s->d_hist, sizeof(double) * (size_t)n * s->hist_cols,
+                     s->hist_host ? cudaMemcpyDefault : cudaMemcpyDeviceToHost, s->st));
   CK(cudaStreamSynchronize(s->st));
   return ZC_OK;
 }
