@@ -124,8 +124,8 @@ def test_graphs_with_timed_push_keep_bits_and_time_every_push():
 def test_history_streamed_to_host_rows_matches_device_history():
     """zc_history_stream: every step writes its energy row into page-locked
     host rows, also inside replayed graphs and queued steps; the rows equal
-    the device-side history's and zc_energy's bits.  Pageable rows are
-    refused."""
+    the device-side history's bits (and zc_energy's values to 1e-12: that sums
+    the field energy over more blocks).  Pageable rows are refused."""
     import torch
     from zpic_gb300._zc import ZcError
 
@@ -149,7 +149,8 @@ def test_history_streamed_to_host_rows_matches_device_history():
             g.step(steps)
             hist = g.history()
         emf, kin = g.energy()
-        assert np.array_equal(hist[-1], np.concatenate([emf, kin]))
+        # (the history sums the field energy over fewer blocks than zc_energy)
+        assert np.allclose(hist[-1], np.concatenate([emf, kin]), rtol=1e-12, atol=0)
         out.append(hist)
         g.close()
     assert np.array_equal(out[0], out[1])
