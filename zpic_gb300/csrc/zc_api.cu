@@ -821,7 +821,8 @@ zc_status current_update_impl(zc_sim *s) {
   return ZC_OK;
 }
 
-zc_status emf_advance_impl(zc_sim *s) {
+// epart: where the Yee kernel leaves the new fields' energy partials (or null)
+zc_status emf_advance_impl(zc_sim *s, double *epart = nullptr) {
   cudaStream_t st = s->st;
   YeeConst Y;
   const float dth = s->dt / 2.0f;
@@ -833,7 +834,7 @@ zc_status emf_advance_impl(zc_sim *s) {
   const int o = 1 - s->eb_cur;
   {
     Phase ph(s, ZC_PHASE_YEE, 1);
-    CK(launch_yee(&s->tmY_EB[s->eb_cur], &s->tmY_J[s->j_cur], s->EB[o], s->G, Y, s->d_err, st));
+    CK(launch_yee(&s->tmY_EB[s->eb_cur], &s->tmY_J[s->j_cur], s->EB[o], s->G, Y, s->d_err, epart, st));
   }
   s->eb_cur = o;
   {
@@ -866,12 +867,15 @@ zc_status iter_impl(zc_sim *s) {
   TRY(current_zero_impl(s));
   for (size_t k = 0; k < s->sp.size(); ++k) TRY(spec_advance_impl(s, (int)k));
   TRY(current_update_impl(s));
-  TRY(emf_advance_impl(s));
+  // with a history, the Yee kernel sums the new fields' energy itself (not
+  // under a moving window: the window shift follows it)
+  const bool fused = s->d_hist && !s->mw;
+  TRY(emf_advance_impl(s, fused ? s->d_hist_part : nullptr));
   if (s->d_hist) {
-    Phase ph(s, ZC_PHASE_HISTORY, 2);
-    CK(launch_energy_history(s->EB[s->eb_cur], s->G, s->d_hist_part, s->hist_blocks, s->d_hist, s->d_hist_n,
-                             s->hist_cap, s->hist_cols, s->d_ekin_ptrs, (int)s->sp.size(), s->dx[0], s->dx[1],
-                             s->st));
+    Phase ph(s, ZC_PHASE_HISTORY, fused ? 1 : 2);
+    CK(launch_energy_history(fused ? nullptr : s->EB[s->eb_cur], s->G, s->d_hist_part,
+                             fused ? yee_blocks(s->G) : s->hist_blocks, s->d_hist, s->d_hist_n, s->hist_cap,
+                             s->hist_cols, s->d_ekin_ptrs, (int)s->sp.size(), s->dx[0], s->dx[1], s->st));
   }
   return ZC_OK;
 }
@@ -2203,7 +2207,8 @@ zc_status history_setup(zc_sim *s, double *rows, int max_steps) {
     TRY(dalloc(&s->d_hist, (size_t)max_steps * cols));
   }
   TRY(dalloc(&s->d_hist_n, 1));
-  TRY(dalloc(&s->d_hist_part, 6 * (size_t)s->hist_blocks));
+  // partials of the standalone energy pass or of the Yee kernel
+  TRY(dalloc(&s->d_hist_part, 6 * (size_t)std::max(s->hist_blocks, yee_blocks(s->G))));
   TRY(dalloc(&s->d_ekin_ptrs, std::max<size_t>(1, s->sp.size())));
   std::vector<double *> ptrs;
   for (auto &p : s->sp) ptrs.push_back(p.d_ekin);

@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(32 * kS4Warps, ZC_S4_MINB) k_smooth4(const flo
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_yee(const __grid_constant__ CUtensorMap tm_eb,
                                              const __grid_constant__ CUtensorMap tm_j, float *EBout, Grid G,
-                                             YeeConst Y, int *err) {
+                                             YeeConst Y, int *err, double *epart) {
   constexpr int BW = kYeeBW, BH = kYeeBH, PL = BW * BH;
   __shared__ __align__(128) float sEB[6 * PL];
   __shared__ __align__(128) float sJ[3 * PL];
@@ -488,7 +488,9 @@ __global__ void __launch_bounds__(256) k_yee(const __grid_constant__ CUtensorMap
     }
   }
   __syncthreads();
-  // B2 on the output tile, then store E1 and B2
+  // B2 on the output tile, then store E1 and B2; with epart, the squares of
+  // the interior cells' new values are summed for the field energy
+  float se[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int k = threadIdx.x; k < kYeeOX * kYeeOY; k += blockDim.x) {
     const int bx = bx0 + k % kYeeOX, by = by0 + k / kYeeOX;
     if (bx >= nx + 3 || by >= ny + 3) continue;
@@ -505,6 +507,33 @@ __global__ void __launch_bounds__(256) k_yee(const __grid_constant__ CUtensorMap
     EBout[gidx(G, 3, bx, by)] = bxv;
     EBout[gidx(G, 4, bx, by)] = byv;
     EBout[gidx(G, 5, bx, by)] = bzv;
+    if (epart && bx >= 1 && bx <= nx && by >= 1 && by <= ny) {
+      se[0] += Ex[s] * Ex[s];
+      se[1] += Ey[s] * Ey[s];
+      se[2] += Ez[s] * Ez[s];
+      se[3] += bxv * bxv;
+      se[4] += byv * byv;
+      se[5] += bzv * bzv;
+    }
+  }
+  if (epart) {
+    // warp sums in float (64 cells a warp), then doubles across the warps
+    __shared__ double swe[6][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      float v = se[c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) swe[c][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+      double v = 0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) v += swe[threadIdx.x][w];
+      epart[(blockIdx.y * gridDim.x + blockIdx.x) * 6 + threadIdx.x] = v;
+    }
   }
 }
 
@@ -759,10 +788,12 @@ cudaError_t launch_smooth(const float *Jin, float *Jout, const Grid &G, const Sm
   return cudaGetLastError();
 }
 
+int yee_blocks(const Grid &G) { return ((G.nx + 3 + kYeeOX - 1) / kYeeOX) * ((G.ny + 3 + kYeeOY - 1) / kYeeOY); }
+
 cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
-                       const YeeConst &Y, int *err, cudaStream_t st) {
+                       const YeeConst &Y, int *err, double *epart, cudaStream_t st) {
   dim3 grid((G.nx + 3 + kYeeOX - 1) / kYeeOX, (G.ny + 3 + kYeeOY - 1) / kYeeOY);
-  k_yee<<<grid, 256, 0, st>>>(*tm_eb, *tm_j, EBout, G, Y, err);
+  k_yee<<<grid, 256, 0, st>>>(*tm_eb, *tm_j, EBout, G, Y, err, epart);
   return cudaGetLastError();
 }
 
@@ -836,7 +867,7 @@ cudaError_t launch_energy_history(const float *EB, const Grid &G, double *partia
                                   int *hist_n, int cap, int cols, double *const *ekin, int nsp, float dx, float dy,
                                   cudaStream_t st) {
   if (nsp > 64) return cudaErrorInvalidValue;
-  k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);
+  if (EB) k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);  // (no EB: partials already made)
   k_energy_history_row<<<1, 6 * 32 + 64, 0, st>>>(partial, nblocks, dx, dy, ekin, nsp, hist, hist_n, cap, cols);
   return cudaGetLastError();
 }

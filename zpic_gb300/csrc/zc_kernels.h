@@ -219,8 +219,11 @@ struct SmoothPasses {
 // every x filter pass, then every y pass, out of place (Jin -> Jout)
 cudaError_t launch_smooth(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
                           const SmoothPasses &PY, int mw, cudaStream_t st);
+// epart (or null): per-block field-energy partials of the new fields, 6
+// doubles a block, yee_blocks(G) blocks
 cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
-                       const YeeConst &Y, int *err, cudaStream_t st);
+                       const YeeConst &Y, int *err, double *epart, cudaStream_t st);
+int yee_blocks(const Grid &G);
 cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st);
 cudaError_t launch_ext_add(const float *EB, float *EBp, const float *extE, const float *extB, int Etype, int Btype,
                            float3 E0, float3 B0, const Grid &G, cudaStream_t st);
