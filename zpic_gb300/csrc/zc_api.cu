@@ -228,6 +228,7 @@ struct zc_sim {
   int *d_hist_n = nullptr;
   int hist_cap = 0, hist_cols = 0, hist_blocks = 0;
   double **d_ekin_ptrs = nullptr;
+  KinSum *d_kin_sums = nullptr;   // with a history: the kinetic sums its row kernel makes
   double *d_hist_part = nullptr;
 };
 
@@ -603,7 +604,8 @@ zc_status set_current_scale(zc_sim *s, const SpeciesState &p, PushConst &C) {
 zc_status inject_column_device(zc_sim *s, SpeciesState &p);
 int column_lattice(const zc_sim *s, const SpeciesState &p, int n_move, ColumnInject &C, unsigned long long &mask);
 
-zc_status spec_advance_impl(zc_sim *s, int k) {
+// kin_later: the step's history row kernel makes the kinetic sum
+zc_status spec_advance_impl(zc_sim *s, int k, bool kin_later = false) {
   SpeciesState &p = s->sp[k];
   cudaStream_t st = s->st;
   // moving window: decided after the push, on the species' own counters
@@ -677,7 +679,7 @@ zc_status spec_advance_impl(zc_sim *s, int k) {
   p.pending = true;
   p.cur = 1 - p.cur;
   p.spill_cur = out;
-  {
+  if (!kin_later) {
     Phase ph(s, ZC_PHASE_KIN_ENERGY, 1);
     CK(launch_sum_energy(p.d_ekin_tile, s->ntiles, p.d_ekin_extra, p.d_ekin, p.q * p.m_q, s->dx[0], s->dx[1],
                          s->deterministic, st));
@@ -865,17 +867,20 @@ zc_status current_zero_impl(zc_sim *s) {
 
 zc_status iter_impl(zc_sim *s) {
   TRY(current_zero_impl(s));
-  for (size_t k = 0; k < s->sp.size(); ++k) TRY(spec_advance_impl(s, (int)k));
+  // with a history, its row kernel makes the kinetic sums, and the Yee
+  // kernel sums the new fields' energy (not under a moving window: the
+  // window shift follows it)
+  const bool hist = s->d_hist != nullptr;
+  for (size_t k = 0; k < s->sp.size(); ++k) TRY(spec_advance_impl(s, (int)k, hist));
   TRY(current_update_impl(s));
-  // with a history, the Yee kernel sums the new fields' energy itself (not
-  // under a moving window: the window shift follows it)
-  const bool fused = s->d_hist && !s->mw;
+  const bool fused = hist && !s->mw;
   TRY(emf_advance_impl(s, fused ? s->d_hist_part : nullptr));
-  if (s->d_hist) {
+  if (hist) {
     Phase ph(s, ZC_PHASE_HISTORY, fused ? 1 : 2);
     CK(launch_energy_history(fused ? nullptr : s->EB[s->eb_cur], s->G, s->d_hist_part,
                              fused ? yee_blocks(s->G) : s->hist_blocks, s->d_hist, s->d_hist_n, s->hist_cap,
-                             s->hist_cols, s->d_ekin_ptrs, (int)s->sp.size(), s->dx[0], s->dx[1], s->st));
+                             s->hist_cols, s->d_ekin_ptrs, s->d_kin_sums, (int)s->sp.size(), s->dx[0], s->dx[1],
+                             s->st));
   }
   return ZC_OK;
 }
@@ -1454,6 +1459,7 @@ zc_status zc_sim_destroy(zc_sim *s) {
   dfree(s->d_hist_n);
   dfree(s->d_hist_part);
   dfree(s->d_ekin_ptrs);
+  dfree(s->d_kin_sums);
   if (s->st) cudaStreamDestroy(s->st);
   delete s;
   return ZC_OK;
@@ -2188,6 +2194,7 @@ zc_status history_setup(zc_sim *s, double *rows, int max_steps) {
   dfree(s->d_hist_n);
   dfree(s->d_hist_part);
   dfree(s->d_ekin_ptrs);
+  dfree(s->d_kin_sums);
   s->hist_cap = 0;
   s->hist_cols = 0;
   if (max_steps == 0) return ZC_OK;
@@ -2210,10 +2217,17 @@ zc_status history_setup(zc_sim *s, double *rows, int max_steps) {
   // partials of the standalone energy pass or of the Yee kernel
   TRY(dalloc(&s->d_hist_part, 6 * (size_t)std::max(s->hist_blocks, yee_blocks(s->G))));
   TRY(dalloc(&s->d_ekin_ptrs, std::max<size_t>(1, s->sp.size())));
+  TRY(dalloc(&s->d_kin_sums, std::max<size_t>(1, s->sp.size())));
   std::vector<double *> ptrs;
-  for (auto &p : s->sp) ptrs.push_back(p.d_ekin);
-  if (!ptrs.empty())
+  std::vector<KinSum> sums;
+  for (auto &p : s->sp) {
+    ptrs.push_back(p.d_ekin);
+    sums.push_back(KinSum{p.d_ekin_tile, p.d_ekin_extra, s->ntiles, s->deterministic, p.q * p.m_q});
+  }
+  if (!ptrs.empty()) {
     CK(cudaMemcpyAsync(s->d_ekin_ptrs, ptrs.data(), sizeof(double *) * ptrs.size(), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->d_kin_sums, sums.data(), sizeof(KinSum) * sums.size(), cudaMemcpyHostToDevice, s->st));
+  }
   CK(cudaMemsetAsync(s->d_hist_n, 0, sizeof(int), s->st));
   CK(cudaStreamSynchronize(s->st));
   s->hist_cap = max_steps;

@@ -68,6 +68,41 @@ __global__ void k_fold_y(float *J, Grid G) {
   }
 }
 
+// Both folds in one launch (periodic x): the x pairs of the rows outside the
+// y guard bands, the y pairs of the columns outside the x guard bands, and
+// every corner quad as the two folds leave it, (J(b,b') + J(nx+b,b')) +
+// (J(b,ny+b') + J(nx+b,ny+b')) in all four cells: the same float additions
+// as k_fold_x followed by k_fold_y.  Needs nx, ny >= 6 (disjoint bands).
+__global__ void k_fold_xy(float *J, Grid G) {
+  const int nx = G.nx, ny = G.ny;
+  const int nA = (ny - 3) * 9, nB = (nx - 3) * 9, n = nA + nB + 27;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+    if (g < nA) {  // row 3 .. ny - 1: x pair b
+      const int by = 3 + g / 9, c = (g % 9) / 3, b = g % 3;
+      const size_t lo = gidx(G, c, b, by), hi = gidx(G, c, nx + b, by);
+      const float v = J[lo] + J[hi];
+      J[lo] = v;
+      J[hi] = v;
+    } else if (g < nA + nB) {  // column 3 .. nx - 1: y pair b
+      const int h = g - nA, bx = 3 + h / 9, c = (h % 9) / 3, b = h % 3;
+      const size_t lo = gidx(G, c, bx, b), hi = gidx(G, c, bx, ny + b);
+      const float v = J[lo] + J[hi];
+      J[lo] = v;
+      J[hi] = v;
+    } else {  // corner quad (b, b')
+      const int h = g - nA - nB, c = h / 9, b = (h % 9) / 3, bp = h % 3;
+      const size_t a00 = gidx(G, c, b, bp), a10 = gidx(G, c, nx + b, bp);
+      const size_t a01 = gidx(G, c, b, ny + bp), a11 = gidx(G, c, nx + b, ny + bp);
+      const float lo = J[a00] + J[a10], hi = J[a01] + J[a11];
+      const float v = lo + hi;
+      J[a00] = v;
+      J[a10] = v;
+      J[a01] = v;
+      J[a11] = v;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // one [sa, sb, sa] filter tap (kernel_x / kernel_y, em2d/current.c:316-413)
 // ---------------------------------------------------------------------------
@@ -740,6 +775,10 @@ cudaError_t launch_planes_to_aos(const float *planes, float *aos, const Grid &G,
 }
 
 cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
+  if (!mw && G.nx >= 6 && G.ny >= 6) {
+    k_fold_xy<<<((G.nx + G.ny - 6) * 9 + 27 + 255) / 256, 256, 0, st>>>(J, G);
+    return cudaGetLastError();
+  }
   if (!mw) k_fold_x<<<((G.ny + 3) * 9 + 255) / 256, 256, 0, st>>>(J, G);
   k_fold_y<<<((G.nx + 3) * 9 + 255) / 256, 256, 0, st>>>(J, G);
   return cudaGetLastError();
@@ -838,16 +877,38 @@ __global__ void k_energy_direct(const double *partial, int nblocks, float dx, fl
 // one history row: the field energy from the partials (the sum of
 // k_emf_energy_final) and the kinetic energy of every species; the row index
 // is a device counter, so a captured step appends where it runs
-__global__ void k_energy_history_row(const double *partial, int nblocks, float dx, float dy,
-                                     double *const *ekin, int nsp, double *hist, int *hist_n, int cap, int cols) {
+__global__ void __launch_bounds__(256) k_energy_history_row(const double *partial, int nblocks, float dx, float dy,
+                                                            double *const *ekin, const KinSum *ks, int nsp,
+                                                            double *hist, int *hist_n, int cap, int cols) {
+  const int t = threadIdx.x, c = t >> 5, lane = t & 31;
+  if (ks && c >= 6) {
+    // warps 6, 7: each species' kinetic energy from its tile partials (as
+    // k_sum_energy would leave it in *ekin), before the row is taken
+    for (int k = c - 6; k < nsp; k += 2) {
+      const KinSum &K = ks[k];
+      double s = 0;
+      for (int i = lane; i < K.ntiles; i += 32) s += K.tiles[i];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        if (K.det) {
+          const long long *w = reinterpret_cast<const long long *>(K.extra);
+          s += efix_join(w[0], w[1]);
+        } else {
+          s += *K.extra;
+        }
+        *ekin[k] = K.q_mq * s * dx * dy;  // spec->energy (particles.c:1231)
+      }
+    }
+  }
+  __syncthreads();
   const int n = *hist_n;
   __syncthreads();
   if (n >= cap) return;
   double *row = hist + (size_t)n * cols;
-  const int t = threadIdx.x, c = t >> 5;
   if (c < 6) {  // warps 0..5: the field components
     const double s = partial_sum(partial, nblocks, c);
-    if ((t & 31) == 0) row[c] = s * (0.5 * dx * dy);
+    if (lane == 0) row[c] = s * (0.5 * dx * dy);
   } else if (t - 6 * 32 < nsp) {  // then one thread per species
     row[6 + t - 6 * 32] = *ekin[t - 6 * 32];
   }
@@ -864,11 +925,11 @@ cudaError_t launch_energy_direct(const float *EB, const Grid &G, double *partial
 }
 
 cudaError_t launch_energy_history(const float *EB, const Grid &G, double *partial, int nblocks, double *hist,
-                                  int *hist_n, int cap, int cols, double *const *ekin, int nsp, float dx, float dy,
-                                  cudaStream_t st) {
+                                  int *hist_n, int cap, int cols, double *const *ekin, const KinSum *ks, int nsp,
+                                  float dx, float dy, cudaStream_t st) {
   if (nsp > 64) return cudaErrorInvalidValue;
   if (EB) k_emf_energy_partial<<<nblocks, 256, 0, st>>>(EB, G, partial);  // (no EB: partials already made)
-  k_energy_history_row<<<1, 6 * 32 + 64, 0, st>>>(partial, nblocks, dx, dy, ekin, nsp, hist, hist_n, cap, cols);
+  k_energy_history_row<<<1, 256, 0, st>>>(partial, nblocks, dx, dy, ekin, ks, nsp, hist, hist_n, cap, cols);
   return cudaGetLastError();
 }
 

@@ -240,11 +240,20 @@ cudaError_t launch_energy_direct(const float *EB, const Grid &G, double *partial
                                  const EkinRefs &K, int nsp, double *emf, double *kin, cudaStream_t st);
 cudaError_t launch_emf_energy(const float *EB, const Grid &G, double *partial, int nblocks, double *out, float dx,
                               float dy, cudaStream_t st);
+// the kinetic-energy sum of one species (what k_sum_energy does)
+struct KinSum {
+  const double *tiles;   // per-tile partials
+  const double *extra;   // spill-list partial (two fixed-point words when det)
+  int ntiles, det;
+  float q_mq;
+};
 // appends one row (6 field-energy components, then each species' kinetic
-// energy) at hist[*hist_n] and increments *hist_n, unless cap rows exist
+// energy) at hist[*hist_n] and increments *hist_n, unless cap rows exist.
+// EB null: the partials are already there (the Yee kernel's).  ks (or null):
+// the kinetic sums are made here first, into *ekin[k]
 cudaError_t launch_energy_history(const float *EB, const Grid &G, double *partial, int nblocks, double *hist,
-                                  int *hist_n, int cap, int cols, double *const *ekin, int nsp, float dx, float dy,
-                                  cudaStream_t st);
+                                  int *hist_n, int cap, int cols, double *const *ekin, const KinSum *ks, int nsp,
+                                  float dx, float dy, cudaStream_t st);
 // dst[k] = *src[k] for k < n (error words of a batch)
 cudaError_t launch_gather_words(int *const *src, int n, int *dst, cudaStream_t st);
 struct LaserConst {
