@@ -685,9 +685,15 @@ __global__ void __launch_bounds__(256) k_emf_energy_partial(const float *EB, Gri
 // the sum over the blocks of component c of the partials, by warp c (lanes
 // take every 32nd block, then a shuffle tree): valid in lane 0
 __device__ __forceinline__ double partial_sum(const double *partial, int nblocks, int c) {
+  // four running sums a lane, so that four loads are in flight
   const int lane = threadIdx.x & 31;
-  double s = 0;
-  for (int b = lane; b < nblocks; b += 32) s += partial[b * 6 + c];
+  double a[4] = {0, 0, 0, 0};
+  for (int b = lane; b < nblocks; b += 128) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (b + 32 * u < nblocks) a[u] += partial[(b + 32 * u) * 6 + c];
+  }
+  double s = (a[0] + a[1]) + (a[2] + a[3]);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   return s;
@@ -880,17 +886,17 @@ __global__ void k_energy_direct(const double *partial, int nblocks, float dx, fl
 __global__ void __launch_bounds__(256) k_energy_history_row(const double *partial, int nblocks, float dx, float dy,
                                                             double *const *ekin, const KinSum *ks, int nsp,
                                                             double *hist, int *hist_n, int cap, int cols) {
+  __shared__ double sred[8];
   const int t = threadIdx.x, c = t >> 5, lane = t & 31;
-  if (ks && c >= 6) {
-    // warps 6, 7: each species' kinetic energy from its tile partials (as
-    // k_sum_energy would leave it in *ekin), before the row is taken
-    for (int k = c - 6; k < nsp; k += 2) {
+  if (ks) {
+    // each species' kinetic energy from its tile partials, by the whole
+    // block (as k_sum_energy would leave it in *ekin), before the row
+    for (int k = 0; k < nsp; ++k) {
       const KinSum &K = ks[k];
       double s = 0;
-      for (int i = lane; i < K.ntiles; i += 32) s += K.tiles[i];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) {
+      for (int i = t; i < K.ntiles; i += 256) s += K.tiles[i];
+      s = block_sum_double<256>(s, sred);
+      if (t == 0) {
         if (K.det) {
           const long long *w = reinterpret_cast<const long long *>(K.extra);
           s += efix_join(w[0], w[1]);
