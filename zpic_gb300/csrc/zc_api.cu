@@ -137,6 +137,7 @@ struct Counters {
   std::vector<int> sp_iter, sp_n_move, cur, spill_cur, ob_in;
   std::vector<bool> pending;
   int eb_cur = 0, j_cur = 0;
+  bool j0_zero = false;
   long long launch[ZC_NPHASE] = {};
 };
 
@@ -175,6 +176,7 @@ struct zc_sim {
   float3 ext_E0{0, 0, 0}, ext_B0{0, 0, 0};
   float *J[2] = {nullptr, nullptr};
   int j_cur = 0;
+  bool j0_zero = false;  // J[0] was cleared by the last Yee launch (no clear needed)
   unsigned long long *Jfix = nullptr;   // deterministic mode: fixed-point J planes
   CUtensorMap tmK_EB[2], tmK_EBp, tmK_J;
   CUtensorMap tmY_EB[2], tmY_J[2];
@@ -833,13 +835,19 @@ zc_status emf_advance_impl(zc_sim *s, double *epart = nullptr) {
   Y.cxe = s->dt / s->dx[0];
   Y.cye = s->dt / s->dx[1];
   Y.dt = s->dt;
+  Y.mw = s->mw;
   const int o = 1 - s->eb_cur;
+  // the Yee kernel writes the guard cells as the guard-cell update leaves
+  // them, and clears the raw deposit buffer once the filter has read it
+  const bool gc = s->nx >= 3 && s->ny >= 3;
+  float *jz = (s->j_cur == 1) ? s->J[0] : nullptr;
   {
     Phase ph(s, ZC_PHASE_YEE, 1);
-    CK(launch_yee(&s->tmY_EB[s->eb_cur], &s->tmY_J[s->j_cur], s->EB[o], s->G, Y, s->d_err, epart, st));
+    CK(launch_yee(&s->tmY_EB[s->eb_cur], &s->tmY_J[s->j_cur], s->EB[o], s->G, Y, s->d_err, epart, jz, gc, st));
   }
+  if (jz) s->j0_zero = true;
   s->eb_cur = o;
-  {
+  if (!gc) {
     Phase ph(s, ZC_PHASE_EMF_GC, 1);
     CK(launch_emf_gc(s->EB[o], s->G, s->mw, st));
   }
@@ -857,16 +865,18 @@ zc_status emf_advance_impl(zc_sim *s, double *epart = nullptr) {
   return ZC_OK;
 }
 
-zc_status current_zero_impl(zc_sim *s) {
+// in a step (in_step) a J[0] the last Yee launch cleared is not cleared again
+zc_status current_zero_impl(zc_sim *s, bool in_step = false) {
   Phase ph(s, ZC_PHASE_ZERO, 0);
-  CK(cudaMemsetAsync(s->J[0], 0, sizeof(float) * 3 * s->G.plane, s->st));
+  if (!(in_step && s->j0_zero)) CK(cudaMemsetAsync(s->J[0], 0, sizeof(float) * 3 * s->G.plane, s->st));
+  s->j0_zero = false;
   if (s->deterministic) CK(cudaMemsetAsync(s->Jfix, 0, sizeof(unsigned long long) * 3 * s->G.plane, s->st));
   s->j_cur = 0;
   return ZC_OK;
 }
 
 zc_status iter_impl(zc_sim *s) {
-  TRY(current_zero_impl(s));
+  TRY(current_zero_impl(s, true));
   // with a history, its row kernel makes the kinetic sums, and the Yee
   // kernel sums the new fields' energy (not under a moving window: the
   // window shift follows it)
@@ -926,6 +936,7 @@ Counters save_counters(const zc_sim *s) {
   }
   c.eb_cur = s->eb_cur;
   c.j_cur = s->j_cur;
+  c.j0_zero = s->j0_zero;
   for (int k = 0; k < ZC_NPHASE; ++k) c.launch[k] = s->prof_launch[k];
   return c;
 }
@@ -933,7 +944,7 @@ Counters save_counters(const zc_sim *s) {
 // the buffer parities a captured graph starts from
 bool same_parities(const Counters &a, const Counters &b) {
   return a.cur == b.cur && a.spill_cur == b.spill_cur && a.ob_in == b.ob_in && a.eb_cur == b.eb_cur &&
-         (a.iter % 2) == (b.iter % 2);
+         a.j0_zero == b.j0_zero && (a.iter % 2) == (b.iter % 2);
 }
 
 // the graph g holds n steps from the current state (block-aligned)
@@ -985,6 +996,7 @@ zc_status capture_steps(zc_sim *s, int n, StepGraph &G, bool instantiate = true)
   }
   s->eb_cur = before.eb_cur;
   s->j_cur = before.j_cur;
+  s->j0_zero = before.j0_zero;
   for (int k = 0; k < ZC_NPHASE; ++k) s->prof_launch[k] = before.launch[k];
   if (st != ZC_OK) {
     if (g) cudaGraphDestroy(g);
@@ -1070,6 +1082,7 @@ void account_steps(zc_sim *s, const StepGraph &g) {
   s->n_move += g.after.n_move - g.before.n_move;
   s->eb_cur = g.after.eb_cur;
   s->j_cur = g.after.j_cur;
+  s->j0_zero = g.after.j0_zero;
   for (int k = 0; k < ZC_NPHASE; ++k) s->prof_launch[k] += g.after.launch[k] - g.before.launch[k];
 }
 
@@ -1978,6 +1991,7 @@ zc_status zc_set_current(zc_sim *s, const float *J) {
   DeviceGuard g(s->device);
   TRY(grid_up(s, J, s->J[0]));
   s->j_cur = 0;
+  s->j0_zero = false;
   if (s->deterministic) {
     CK(launch_float_to_fixed(s->J[0], s->Jfix, 3 * s->G.plane, s->st));
     CK(cudaStreamSynchronize(s->st));

@@ -468,9 +468,21 @@ __global__ void __launch_bounds__(32 * kS4Warps, ZC_S4_MINB) k_smooth4(const flo
 // guard cells evolve as in the reference (they matter with a moving window).
 // Out of place: EB in (TMA) -> EB out.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_yee(const __grid_constant__ CUtensorMap tm_eb,
+// a value stored at (bx, by) and at its periodic guard images (xm, ym; -1: none)
+__device__ __forceinline__ void put_mirrored(float *EB, const Grid &G, int c, int bx, int by, int xm, int ym,
+                                             float v) {
+  EB[gidx(G, c, bx, by)] = v;
+  if (xm >= 0) EB[gidx(G, c, xm, by)] = v;
+  if (ym >= 0) EB[gidx(G, c, bx, ym)] = v;
+  if (xm >= 0 && ym >= 0) EB[gidx(G, c, xm, ym)] = v;
+}
+
+#ifndef ZC_YEE_MINB
+#define ZC_YEE_MINB 6
+#endif
+__global__ void __launch_bounds__(256, ZC_YEE_MINB) k_yee(const __grid_constant__ CUtensorMap tm_eb,
                                              const __grid_constant__ CUtensorMap tm_j, float *EBout, Grid G,
-                                             YeeConst Y, int *err, double *epart) {
+                                             YeeConst Y, int *err, double *epart, float *jzero, int gc) {
   constexpr int BW = kYeeBW, BH = kYeeBH, PL = BW * BH;
   __shared__ __align__(128) float sEB[6 * PL];
   __shared__ __align__(128) float sJ[3 * PL];
@@ -536,12 +548,33 @@ __global__ void __launch_bounds__(256) k_yee(const __grid_constant__ CUtensorMap
       byv += (Y.cxb * (Ez[s + 1] - Ez[s]));
       bzv += (-Y.cxb * (Ey[s + 1] - Ey[s]) + Y.cyb * (Ex[s + BW] - Ex[s]));
     }
-    EBout[gidx(G, 0, bx, by)] = Ex[s];
-    EBout[gidx(G, 1, bx, by)] = Ey[s];
-    EBout[gidx(G, 2, bx, by)] = Ez[s];
-    EBout[gidx(G, 3, bx, by)] = bxv;
-    EBout[gidx(G, 4, bx, by)] = byv;
-    EBout[gidx(G, 5, bx, by)] = bzv;
+    if (jzero) {  // the raw deposit buffer, dead once filtered: cleared for the next step
+      jzero[gidx(G, 0, bx, by)] = 0.f;
+      jzero[gidx(G, 1, bx, by)] = 0.f;
+      jzero[gidx(G, 2, bx, by)] = 0.f;
+    }
+    if (gc) {
+      // guard cells as emf_update_gc leaves them (emf.c:573-637): a guard
+      // cell is not stored here; the cell it copies stores its value there
+      // too (periodic in x unless the window moves, always in y)
+      const bool gxc = !Y.mw && (bx == 0 || bx > nx), gyc = (by == 0 || by > ny);
+      if (gxc || gyc) continue;
+      const int xm = Y.mw ? -1 : (bx == nx ? 0 : (bx <= 2 ? nx + bx : -1));
+      const int ym = by == ny ? 0 : (by <= 2 ? ny + by : -1);
+      put_mirrored(EBout, G, 0, bx, by, xm, ym, Ex[s]);
+      put_mirrored(EBout, G, 1, bx, by, xm, ym, Ey[s]);
+      put_mirrored(EBout, G, 2, bx, by, xm, ym, Ez[s]);
+      put_mirrored(EBout, G, 3, bx, by, xm, ym, bxv);
+      put_mirrored(EBout, G, 4, bx, by, xm, ym, byv);
+      put_mirrored(EBout, G, 5, bx, by, xm, ym, bzv);
+    } else {
+      EBout[gidx(G, 0, bx, by)] = Ex[s];
+      EBout[gidx(G, 1, bx, by)] = Ey[s];
+      EBout[gidx(G, 2, bx, by)] = Ez[s];
+      EBout[gidx(G, 3, bx, by)] = bxv;
+      EBout[gidx(G, 4, bx, by)] = byv;
+      EBout[gidx(G, 5, bx, by)] = bzv;
+    }
     if (epart && bx >= 1 && bx <= nx && by >= 1 && by <= ny) {
       se[0] += Ex[s] * Ex[s];
       se[1] += Ey[s] * Ey[s];
@@ -836,9 +869,10 @@ cudaError_t launch_smooth(const float *Jin, float *Jout, const Grid &G, const Sm
 int yee_blocks(const Grid &G) { return ((G.nx + 3 + kYeeOX - 1) / kYeeOX) * ((G.ny + 3 + kYeeOY - 1) / kYeeOY); }
 
 cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
-                       const YeeConst &Y, int *err, double *epart, cudaStream_t st) {
+                       const YeeConst &Y, int *err, double *epart, float *jzero, bool gc, cudaStream_t st) {
+  if (gc && (G.nx < 3 || G.ny < 3)) return cudaErrorInvalidValue;  // mirrors would overlap
   dim3 grid((G.nx + 3 + kYeeOX - 1) / kYeeOX, (G.ny + 3 + kYeeOY - 1) / kYeeOY);
-  k_yee<<<grid, 256, 0, st>>>(*tm_eb, *tm_j, EBout, G, Y, err, epart);
+  k_yee<<<grid, 256, 0, st>>>(*tm_eb, *tm_j, EBout, G, Y, err, epart, jzero, gc ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -205,6 +205,7 @@ cudaError_t launch_sum_energy(const double *tiles, int ntiles, const double *ext
 struct YeeConst {
   float cxb, cyb;                         // (dt/2)/dx, (dt/2)/dy  (emf.c:507-508)
   float cxe, cye, dt;                     // dt/dx, dt/dy, dt      (emf.c:540-541)
+  int mw;                                 // moving window: x guard cells are not periodic
 };
 
 cudaError_t launch_aos_to_planes(const float *aos, float *planes, const Grid &G, int ncomp, cudaStream_t st);
@@ -220,9 +221,11 @@ struct SmoothPasses {
 cudaError_t launch_smooth(const float *Jin, float *Jout, const Grid &G, const SmoothPasses &PX,
                           const SmoothPasses &PY, int mw, cudaStream_t st);
 // epart (or null): per-block field-energy partials of the new fields, 6
-// doubles a block, yee_blocks(G) blocks
+// doubles a block, yee_blocks(G) blocks.  jzero (or null): a current buffer
+// the kernel clears (3 planes).  gc: the guard cells are written as the
+// guard-cell update leaves them (k_emf_gc then not needed; nx, ny >= 3)
 cudaError_t launch_yee(const CUtensorMap *tm_eb, const CUtensorMap *tm_j, float *EBout, const Grid &G,
-                       const YeeConst &Y, int *err, double *epart, cudaStream_t st);
+                       const YeeConst &Y, int *err, double *epart, float *jzero, bool gc, cudaStream_t st);
 int yee_blocks(const Grid &G);
 cudaError_t launch_emf_gc(float *EB, const Grid &G, int mw, cudaStream_t st);
 cudaError_t launch_ext_add(const float *EB, float *EBp, const float *extE, const float *extB, int Etype, int Btype,
