@@ -264,17 +264,21 @@ def run_scan(args):
     runs = batch.weibel_scan(n_runs=n_runs, steps=steps)
     if not args.sort_every:
         args.sort_every = batch.scan_sort_every(steps)
-    tile, rates = batch.autotune_tile(runs, candidates=((16, 16), (32, 16), (16, 8)), sample=64, steps=32,
+    # the autotuner times half the scan's runs side by side: enough members
+    # in flight that the batch's own concurrency decides
+    tile, rates = batch.autotune_tile(runs, candidates=((16, 16), (32, 16), (16, 8), "by_ppc"),
+                                      sample=max(1, n_runs // 2), steps=3 * 2 * args.sort_every,
                                       sort_every=args.sort_every)
+    tiles = batch.tiles_for(runs, tile)
     nps = sum(r.particles() * r.steps for r in runs)
 
     def fresh(graphs):
         t0 = time.perf_counter()
-        sims = batch.load_sims(runs, tile=tile, sort_every=args.sort_every, graphs=graphs)
+        sims = batch.load_sims(runs, tile=tiles, sort_every=args.sort_every, graphs=graphs)
         return sims, time.perf_counter() - t0
 
     # warm-up: one small batch (graph capture and instantiation paths, clocks)
-    warm = batch.load_sims(runs[:8], tile=tile, sort_every=args.sort_every)
+    warm = batch.load_sims(runs[:8], tile=tiles[:8], sort_every=args.sort_every)
     batch.run_batched(warm, [batch.ScanRun(r.nx, r.ppc, r.uz, r.uth, r.dx, r.dt, r.seed, 32) for r in runs[:8]])
     for s_ in warm:
         s_.close()
@@ -309,7 +313,8 @@ def run_scan(args):
         "config": {"workload": f"batched scan: {n_runs} two-stream runs, grids 64..256 per axis (dx=0.1), "
                                f"ppc 2..8 per axis, uz 0.2..0.8, uth 0.02..0.2, dt=0.9 CFL, {steps} steps, "
                                f"energy history every step",
-                   "particles_total": int(sum(r.particles() for r in runs)), "tile": list(tile),
+                   "particles_total": int(sum(r.particles() for r in runs)),
+                   "tile": tile if isinstance(tile, str) else list(tile),
                    "cell_sort_every": args.sort_every, "tile_slack": 2.0,
                    "batch_groups": res.groups, "fast_math": True},
         "batched": {"rate": res.rate, "device_ms": res.device_ms, "wall_s": t_wall, **res.extra},
@@ -319,7 +324,7 @@ def run_scan(args):
                               "how": "each run alone through zc_step with graph replay, one after another"},
         "speedup_vs_sequential": res.rate / seq.rate,
         "speedup_vs_sequential_graphs": res.rate / seq_g.rate,
-        "autotune_rates": {f"{t[0]}x{t[1]}": v for t, v in rates.items()},
+        "autotune_rates": {(t if isinstance(t, str) else f"{t[0]}x{t[1]}"): v for t, v in rates.items()},
         "e2e": {"value": nps / (t_wall + t_load), "unit": UNIT,
                 "h2d_bytes_per_step": part_bytes / steps, "d2h_bytes_per_step": hist_bytes / steps,
                 "how": "host particle loading and upload of every run, batched stepping, energy histories "

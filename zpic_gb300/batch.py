@@ -182,12 +182,31 @@ def scan_sort_every(steps, longest=8):
     return longest
 
 
-def autotune_tile(runs, candidates=((16, 16), (32, 16), (16, 8)), sample=64, steps=32, fast_math=True,
+def tile_by_ppc(run):
+    """A tile shape that holds some thousands of particles of a species:
+    larger tiles for runs with few particles per cell, so that a tile's fixed
+    work (its field halo, the neighbours' outboxes, the sums at its end) is
+    spread over enough particles."""
+    ppc = run.ppc[0] * run.ppc[1]
+    t = (32, 32) if ppc <= 6 else ((32, 16) if ppc <= 12 else (16, 16))
+    return (min(t[0], run.nx[0]), min(t[1], run.nx[1])) if min(run.nx) >= 32 else (16, 16)
+
+
+def tiles_for(runs, choice):
+    """The per-run tiles of an autotuner choice: one shape for every run, or
+    the policy ``"by_ppc"`` (tile_by_ppc per run)."""
+    if choice == "by_ppc":
+        return [tile_by_ppc(r) for r in runs]
+    return [tuple(choice)] * len(runs)
+
+
+def autotune_tile(runs, candidates=((16, 16), (32, 16), (16, 8), "by_ppc"), sample=64, steps=32, fast_math=True,
                   sort_every=0):
-    """Picks the particle tile of a scan: times a batch of ``sample`` runs
+    """Picks the particle tiles of a scan: times a batch of ``sample`` runs
     (spread evenly over the scan's sizes) for ``steps`` steps with each
-    candidate tile, after one untimed pass of as many steps (graph capture),
-    and returns (best tile, {tile: particle-steps/s})."""
+    candidate (one tile shape for every run, or the per-run policy
+    ``"by_ppc"``), after one untimed pass of as many steps (graph capture),
+    and returns (best candidate, {candidate: particle-steps/s})."""
     order = np.argsort([r.nx[0] * r.nx[1] * r.ppc[0] * r.ppc[1] for r in runs])
     pick = [runs[int(order[int(i)])] for i in np.linspace(0, len(runs) - 1, min(sample, len(runs)))]
     probe = [ScanRun(r.nx, r.ppc, r.uz, r.uth, r.dx, r.dt, r.seed, steps) for r in pick]
@@ -195,8 +214,8 @@ def autotune_tile(runs, candidates=((16, 16), (32, 16), (16, 8)), sample=64, ste
         species = list(ex.map(load_run, probe))
     rates = {}
     for t in candidates:
-        sims = [make_sim(r, sp, tile=t, fast_math=fast_math, sort_every=sort_every, history=True)
-                for r, sp in zip(probe, species)]
+        sims = [make_sim(r, sp, tile=tt, fast_math=fast_math, sort_every=sort_every, history=True)
+                for r, sp, tt in zip(probe, species, tiles_for(probe, t))]
         b = CudaBatch(sims)
         b.step(steps)  # warm-up (graph capture and instantiation)
         b.step(steps)

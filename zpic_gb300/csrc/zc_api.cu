@@ -2366,15 +2366,25 @@ zc_status batch_ready(zc_batch *b, zc_batch::Parent &pg, int n) {
   drop_parent(pg);
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
-  for (zc_sim *s : b->sims) {
-    StepGraph &sg = (n == b->period) ? s->blk : s->tail;
+  // the members' branches are added heaviest first (most particles), so that
+  // the longest chains start first and the block does not end on them
+  std::vector<int> order(b->sims.size());
+  std::vector<long long> weight(b->sims.size(), 0);
+  for (size_t k = 0; k < b->sims.size(); ++k) {
+    order[k] = (int)k;
+    for (const auto &p : b->sims[k]->sp) weight[k] += p.alloc;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return weight[a] > weight[c]; });
+  pg.nodes.assign(b->sims.size(), nullptr);
+  for (int k : order) {
+    StepGraph &sg = (n == b->period) ? b->sims[k]->blk : b->sims[k]->tail;
     cudaGraphNode_t node;
     const cudaError_t e = cudaGraphAddChildGraphNode(&node, g, nullptr, 0, sg.graph);
     if (e != cudaSuccess) {
       cudaGraphDestroy(g);
       return fail(ZC_ECUDA, "cudaGraphAddChildGraphNode failed: %s", cudaGetErrorString(e));
     }
-    pg.nodes.push_back(node);
+    pg.nodes[k] = node;
   }
   cudaGraphExec_t x = nullptr;
   const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
