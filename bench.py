@@ -306,6 +306,15 @@ def run_scan(args):
     seq_g = batch.run_sequential(sims, runs)
     for s_ in sims:
         s_.close()
+    torch.cuda.empty_cache()
+    # the same runs one by one with the plain path's default tile (16 x 16),
+    # which suits a run alone better than the batch's choice
+    seq_d = None
+    if tiles != batch.tiles_for(runs, (16, 16)):
+        sims = batch.load_sims(runs, tile=(16, 16), sort_every=args.sort_every, graphs=True)
+        seq_d = batch.run_sequential(sims, runs)
+        for s_ in sims:
+            s_.close()
     line = {
         "metric": METRIC, "value": res.rate, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 1,
         "ms_per_step": res.device_ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -324,6 +333,10 @@ def run_scan(args):
                               "how": "each run alone through zc_step with graph replay, one after another"},
         "speedup_vs_sequential": res.rate / seq.rate,
         "speedup_vs_sequential_graphs": res.rate / seq_g.rate,
+        **({"sequential_graphs_default_tile": {
+            "rate": seq_d.rate, "device_ms": seq_d.device_ms, "wall_s": seq_d.wall_s,
+            "how": "each run alone through zc_step with graph replay and 16x16 tiles, one after another"},
+            "speedup_vs_sequential_graphs_default_tile": res.rate / seq_d.rate} if seq_d else {}),
         "autotune_rates": {(t if isinstance(t, str) else f"{t[0]}x{t[1]}"): v for t, v in rates.items()},
         "e2e": {"value": nps / (t_wall + t_load), "unit": UNIT,
                 "h2d_bytes_per_step": part_bytes / steps, "d2h_bytes_per_step": hist_bytes / steps,
