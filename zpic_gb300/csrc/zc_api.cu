@@ -669,8 +669,12 @@ zc_status spec_advance_impl(zc_sim *s, int k, bool kin_later = false) {
   const float *EBpart = s->EBp ? s->EBp : s->EB[s->eb_cur];
   {
     Phase ph(s, ZC_PHASE_SPILL, 1);
+    // (normally empty: a grid sized to the run, so that the many small runs
+    // of a batch do not launch a full grid each for nothing)
+    const int spill_blocks = std::max(1, std::min(152, s->ntiles / 4));
     CK(launch_push_spill(EBpart, s->J[0], fixed_j(s), s->G, p.spill[in], p.d_spill_cnt + in, p.spill_cap,
-                         spill_of(p, out), p.d_ekin_extra, s->d_err, C, 152, s->fast, s->deterministic, st));
+                         spill_of(p, out), p.d_ekin_extra, s->d_err, C, spill_blocks, s->fast, s->deterministic,
+                         st));
   }
   if (s->deterministic) {
     // the float J the rest of the step reads: the fixed-point sum so far
