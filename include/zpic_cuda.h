@@ -185,9 +185,9 @@ ZC_API zc_status zc_step(zc_sim *sim, int nsteps);
 /* zc_step without the wait at the end: the steps are queued on the
  * simulation's stream and the call returns (it waits only every 16 queued
  * steps, to look at the spill list; with graph replay on, whole blocks are
- * queued as graphs and the wait trails one block behind).  Device errors of queued steps are
- * returned by the next waiting call (zc_synchronize, zc_step, zc_energy,
- * ...).  With zc_energy_async a run reports every step without idling the
+ * queued as graphs and the wait trails one block behind).  Device errors
+ * of queued steps are returned by the next waiting call (zc_synchronize,
+ * zc_step, zc_energy, ...).  With zc_energy_async a run reports every step without idling the
  * device between steps. */
 ZC_API zc_status zc_step_async(zc_sim *sim, int nsteps);
 /* the phases of sim_iter, for callers that drive them one by one */
@@ -314,8 +314,9 @@ ZC_API zc_status zc_energy(zc_sim *sim, double emf_energy[6], double *kin_energy
  * host arrays are queued behind the work already queued, and the arrays
  * hold the values once zc_synchronize (or any waiting call) returns.  A run
  * that reports energies every step then never idles the device between
- * steps.  With page-locked arrays the copies are asynchronous; other host
- * memory is filled before the call returns. */
+ * steps.  With page-locked arrays the device writes them itself and they
+ * must stay allocated until that wait; other host memory is filled before
+ * the call returns. */
 ZC_API zc_status zc_energy_async(zc_sim *sim, double emf_energy[6], double *kin_energy);
 /* charge density of one species on an (nx+1)*(ny+1) grid
  * (spec_deposit_charge, em2d/particles.c:1289-1324) */
@@ -384,7 +385,8 @@ ZC_API zc_status zc_history_enable(zc_sim *sim, int max_steps);
  * cudaHostAlloc'd): every step's energies reach the host as the step ends,
  * with no copy call, also inside replayed graphs.  The rows hold their values
  * once zc_synchronize (or any waiting call) returns; zc_history_get reads the
- * count.  rows = NULL with max_steps = 0 turns it off. */
+ * count.  The rows must stay allocated while the history streams into them.
+ * rows = NULL with max_steps = 0 turns it off. */
 ZC_API zc_status zc_history_stream(zc_sim *sim, double *rows, int max_steps);
 /* copies up to `cap_rows` rows into `out` (row-major); *nrows receives the
  * rows recorded, *ncols the row length.  out == NULL only queries. */
