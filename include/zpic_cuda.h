@@ -187,8 +187,8 @@ ZC_API zc_status zc_step(zc_sim *sim, int nsteps);
  * steps, to look at the spill list; with graph replay on, whole blocks are
  * queued as graphs and the wait trails one block behind).  Device errors
  * of queued steps are returned by the next waiting call (zc_synchronize,
- * zc_step, zc_energy, ...).  With zc_energy_async a run reports every step without idling the
- * device between steps. */
+ * zc_step, zc_energy, ...).  With zc_energy_async or zc_history_stream a
+ * run reports every step without idling the device between steps. */
 ZC_API zc_status zc_step_async(zc_sim *sim, int nsteps);
 /* the phases of sim_iter, for callers that drive them one by one */
 ZC_API zc_status zc_current_zero(zc_sim *sim);                 /* em2d/current.c:98-107 */
