@@ -213,18 +213,22 @@ def run_reference(args):
     """The reference's CPU em2d on this host, on the bench's own workload.
 
     ``value``: the full 2048^2 deck (67,108,864 particles), one run, as the
-    reference runs it: single-threaded, ``--warmup`` untimed steps then
-    ``--steps`` timed ones.  Beside it, ``host_aggregate``: the host-wide
-    figure of independent single-threaded runs, one per core, each a
-    256^2-cell box of the same density (the reference's fan-out of
-    independent runs for parameter scans)."""
+    reference runs it: single-threaded, up to 2 untimed steps then up to 10
+    timed ones (``--warmup`` / ``--steps`` when smaller: some 3.5 s a step on
+    one core keeps the arm to about a minute; the rate is per step, so the
+    bounded sample measures the same thing).  Beside it,
+    ``host_aggregate``: the host-wide figure of independent single-threaded
+    runs, one per core, each a 256^2-cell box of the same density (the
+    reference's fan-out of independent runs for parameter scans), for the
+    requested steps."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     procs = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
     W = WORKLOAD
     nx, ny = W["nx"]
-    v1, kind, n1 = cpu_run(nx, ny, args.steps, args.warmup)
+    steps1, warm1 = min(args.steps, 10), min(args.warmup, 2)
+    v1, kind, n1 = cpu_run(nx, ny, steps1, warm1)
     vp, kind_p, npr = cpu_run_parallel(256, 256, args.steps, args.warmup, procs)
     line = {
         "impl": "reference", "metric": METRIC, "value": v1, "unit": UNIT, "n_gpus": args.gpus,
@@ -235,8 +239,8 @@ def run_reference(args):
                    "particles_per_gpu": int(n1), "uth": W["uth"], "smoothing": "compensated level 1, x and y"},
         "cpu_baseline": {"value": v1, "unit": UNIT, "cores": 1, "kind": kind,
                          "sample": f"the whole workload ({n1} particles, {nx}x{ny} cells), one single-threaded "
-                                   f"run (the reference is single-threaded), {args.steps} timed steps after "
-                                   f"{args.warmup} warm-up steps; host {platform.machine()}"},
+                                   f"run (the reference is single-threaded), {steps1} timed steps after "
+                                   f"{warm1} warm-up steps; host {platform.machine()}"},
         "host_aggregate": {"value": vp, "unit": UNIT, "cores": procs, "kind": kind_p,
                            "sample": f"{procs} concurrent single-threaded runs, each a 256x256-cell box of the "
                                      f"workload's density ({npr} particles), {args.steps} timed steps after "
