@@ -44,27 +44,28 @@ __global__ void k_planes_to_aos(const float *planes, float *aos, Grid G, int nco
 // current guard-cell fold (current_update_gc, em2d/current.c:118-159)
 // ---------------------------------------------------------------------------
 __global__ void k_fold_x(float *J, Grid G) {
-  // one thread per (buffer row, component, guard column): cells -1, 0, 1
-  // receive nx-1, nx, nx+1
-  const int n = (G.ny + 3) * 9;
+  // one thread per (buffer row, component), in the reference's order: cells
+  // -1, 0, 1 add nx-1, nx, nx+1, then those take the sums (the order matters
+  // when the pairs overlap, nx < 3)
+  const int n = (G.ny + 3) * 3;
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
-    const int by = g / 9, c = (g % 9) / 3, b = g % 3;
-    const size_t lo = gidx(G, c, b, by), hi = gidx(G, c, G.nx + b, by);
-    const float v = J[lo] + J[hi];
-    J[lo] = v;
-    J[hi] = v;
+    const int by = g / 3, c = g % 3;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) J[gidx(G, c, b, by)] += J[gidx(G, c, G.nx + b, by)];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) J[gidx(G, c, G.nx + b, by)] = J[gidx(G, c, b, by)];
   }
 }
 
 __global__ void k_fold_y(float *J, Grid G) {
-  // one thread per (buffer column, component, guard row)
-  const int gx = G.nx + 3, n = gx * 9;
+  // one thread per (buffer column, component), in the reference's order
+  const int gx = G.nx + 3, n = gx * 3;
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
-    const int bx = g % gx, cb = g / gx, c = cb / 3, b = cb % 3;
-    const size_t lo = gidx(G, c, bx, b), hi = gidx(G, c, bx, G.ny + b);
-    const float v = J[lo] + J[hi];
-    J[lo] = v;
-    J[hi] = v;
+    const int bx = g % gx, c = g / gx;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) J[gidx(G, c, bx, b)] += J[gidx(G, c, bx, G.ny + b)];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) J[gidx(G, c, bx, G.ny + b)] = J[gidx(G, c, bx, b)];
   }
 }
 
@@ -818,8 +819,8 @@ cudaError_t launch_fold(float *J, const Grid &G, int mw, cudaStream_t st) {
     k_fold_xy<<<((G.nx + G.ny - 6) * 9 + 27 + 255) / 256, 256, 0, st>>>(J, G);
     return cudaGetLastError();
   }
-  if (!mw) k_fold_x<<<((G.ny + 3) * 9 + 255) / 256, 256, 0, st>>>(J, G);
-  k_fold_y<<<((G.nx + 3) * 9 + 255) / 256, 256, 0, st>>>(J, G);
+  if (!mw) k_fold_x<<<((G.ny + 3) * 3 + 255) / 256, 256, 0, st>>>(J, G);
+  k_fold_y<<<((G.nx + 3) * 3 + 255) / 256, 256, 0, st>>>(J, G);
   return cudaGetLastError();
 }
 
