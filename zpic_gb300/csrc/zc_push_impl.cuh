@@ -780,6 +780,11 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       return i < n_own;
     };
     const auto ubase = [&](int u) { return (warp + NW * (u / kLaneRun)) * kChunk + (u % kLaneRun) * 32; };
+#ifdef ZC_PUSH_LEAN
+    pf_u[warp][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    pf_xy[warp][lane] = make_float2(0.f, 0.f);
+    __syncwarp();
+#endif
     {
       int rs, ws;
       if (ubase(0) < n_own && slots(0, rs, ws)) {
@@ -792,6 +797,24 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       cp_async_wait<0>();  // this unit's copies (each lane its own slot) are in
       int rs, ws;
       const bool inr = slots(u, rs, ws);
+#ifdef ZC_PUSH_LEAN
+      // a lane without a particle carries whatever its prefetch slot holds
+      // (the last unit's particle, a hole's zero momenta, or the zeros the
+      // slots start with): finite values whose results `valid` masks; its
+      // position is set to the cell centre (a hole's is stale)
+      const float4 uu = pf_u[warp][lane];
+      const float2 xy = pf_xy[warp][lane];
+      const unsigned cw = (unsigned)__float_as_int(uu.w);
+      const bool valid = inr && cw != kHole;
+      PRec r;
+      r.ix = (int)(cw & 0xffffu);
+      r.iy = (int)(cw >> 16);
+      r.x = valid ? xy.x : 0.5f;
+      r.y = valid ? xy.y : 0.5f;
+      r.ux = uu.x;
+      r.uy = uu.y;
+      r.uz = uu.z;
+#else
       PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
       bool valid = false;
       if (inr) {
@@ -809,6 +832,7 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
           r.uz = uu.z;
         }
       }
+#endif
       {
         int rn, wn;
         if (ubase(u + 1) < n_own && slots(u + 1, rn, wn)) {
