@@ -168,24 +168,6 @@ __device__ __forceinline__ float lerp2(const F &f, int c, int a, int b, float wa
          (f(c, a, b + 1) * (1.0f - wa) + f(c, a + 1, b + 1) * wa) * wb;
 }
 
-#ifdef ZC_PACKED_GATHER
-// two interpolations at once (packed float32 pairs, fast build only): the
-// same products and sums as lerp2, contracted to fused multiply-adds
-template <class F>
-__device__ __forceinline__ float2 lerp2_pair(const F &f, int c0, int a0, int b0, int c1, int a1, int b1, float2 wa,
-                                             float2 wb) {
-  const float2 one = make_float2(1.0f, 1.0f), mone = make_float2(-1.0f, -1.0f);
-  const float2 va = __ffma2_rn(wa, mone, one), vb = __ffma2_rn(wb, mone, one);
-  const float2 f00 = make_float2(f(c0, a0, b0), f(c1, a1, b1));
-  const float2 f10 = make_float2(f(c0, a0 + 1, b0), f(c1, a1 + 1, b1));
-  const float2 f01 = make_float2(f(c0, a0, b0 + 1), f(c1, a1, b1 + 1));
-  const float2 f11 = make_float2(f(c0, a0 + 1, b0 + 1), f(c1, a1 + 1, b1 + 1));
-  const float2 t0 = __ffma2_rn(f10, wa, __fmul2_rn(f00, va));
-  const float2 t1 = __ffma2_rn(f11, wa, __fmul2_rn(f01, va));
-  return __ffma2_rn(t1, wb, __fmul2_rn(t0, vb));
-}
-#endif
-
 struct Seg {
   float x0, x1, y0, y1, dx, dy, qvz;
   int ix, iy;
@@ -349,21 +331,12 @@ __device__ __forceinline__ float push_particle(const F &fld, int i, int j, float
   const int jh = j + ((y < 0.5f) ? -1 : 0);
   const float w1h = x + ((x < 0.5f) ? 0.5f : -0.5f);
   const float w2h = y + ((y < 0.5f) ? 0.5f : -0.5f);
-#ifdef ZC_PACKED_GATHER
-  // the six interpolations as three packed pairs: Ex and By share their
-  // cells and weights, so do Ey and Bx; Ez and Bz pair different ones
-  const float2 eby = lerp2_pair(fld, 0, ih, j, 4, ih, j, make_float2(w1h, w1h), make_float2(y, y));
-  const float2 ebx = lerp2_pair(fld, 1, i, jh, 3, i, jh, make_float2(x, x), make_float2(w2h, w2h));
-  const float2 ebz = lerp2_pair(fld, 2, i, j, 5, ih, jh, make_float2(x, w1h), make_float2(y, w2h));
-  float ex = eby.x, by = eby.y, ey = ebx.x, bx = ebx.y, ez = ebz.x, bz = ebz.y;
-#else
   float ex = lerp2(fld, 0, ih, j, w1h, y);
   float ey = lerp2(fld, 1, i, jh, x, w2h);
   float ez = lerp2(fld, 2, i, j, x, y);
   float bx = lerp2(fld, 3, i, jh, x, w2h);
   float by = lerp2(fld, 4, ih, j, w1h, y);
   float bz = lerp2(fld, 5, ih, jh, w1h, w2h);
-#endif
 
   const float tem = C.tem;
   ex *= tem;
@@ -780,16 +753,15 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       return i < n_own;
     };
     const auto ubase = [&](int u) { return (warp + NW * (u / kLaneRun)) * kChunk + (u % kLaneRun) * 32; };
-#ifdef ZC_PUSH_LEAN
-    pf_u[warp][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-    pf_xy[warp][lane] = make_float2(0.f, 0.f);
-    __syncwarp();
-#endif
     {
       int rs, ws;
       if (ubase(0) < n_own && slots(0, rs, ws)) {
         cp_async16(&pf_u[warp][lane], &pin.u[base + rs]);
         cp_async8(&pf_xy[warp][lane], &pin.xy[base + rs]);
+      } else {
+        // a lane without a first particle reads these zeros
+        pf_u[warp][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+        pf_xy[warp][lane] = make_float2(0.f, 0.f);
       }
     }
     cp_async_commit();
@@ -797,7 +769,6 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       cp_async_wait<0>();  // this unit's copies (each lane its own slot) are in
       int rs, ws;
       const bool inr = slots(u, rs, ws);
-#ifdef ZC_PUSH_LEAN
       // a lane without a particle carries whatever its prefetch slot holds
       // (the last unit's particle, a hole's zero momenta, or the zeros the
       // slots start with): finite values whose results `valid` masks; its
@@ -814,25 +785,6 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       r.ux = uu.x;
       r.uy = uu.y;
       r.uz = uu.z;
-#else
-      PRec r = {0, 0, 0.f, 0.f, 0.f, 0.f, 0.f};
-      bool valid = false;
-      if (inr) {
-        const float4 uu = pf_u[warp][lane];
-        const float2 xy = pf_xy[warp][lane];
-        const unsigned c = (unsigned)__float_as_int(uu.w);
-        valid = c != kHole;
-        if (valid) {
-          r.ix = (int)(c & 0xffffu);
-          r.iy = (int)(c >> 16);
-          r.x = xy.x;
-          r.y = xy.y;
-          r.ux = uu.x;
-          r.uy = uu.y;
-          r.uz = uu.z;
-        }
-      }
-#endif
       {
         int rn, wn;
         if (ubase(u + 1) < n_own && slots(u + 1, rn, wn)) {
