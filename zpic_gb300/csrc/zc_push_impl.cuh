@@ -389,123 +389,6 @@ __device__ __forceinline__ bool apply_boundary(int &ix, int &iy, int di, int dj,
   return true;
 }
 
-#if defined(ZC_FAST_ALGEBRA) && defined(ZC_PUSH_PAIRS)
-// ---------------------------------------------------------------------------
-// Two particles a lane (fast build): the gather, the Boris push and the
-// single-segment current of particles A and B as packed float32 pairs
-// (each half is the fused or plain float32 operation the scalar fast build
-// contracts to), halving the float instructions.  Per-particle control (cell
-// shifts, boundaries, output) stays scalar.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }  // a - b
-
-template <class F>
-__device__ __forceinline__ float2 lerp2x2(const F &f, int c, int aA, int bA, int aB, int bB, float2 wa, float2 wb) {
-  const float2 va = sub2(f2(1.0f), wa), vb = sub2(f2(1.0f), wb);
-  const float2 f00 = make_float2(f(c, aA, bA), f(c, aB, bB));
-  const float2 f10 = make_float2(f(c, aA + 1, bA), f(c, aB + 1, bB));
-  const float2 f01 = make_float2(f(c, aA, bA + 1), f(c, aB, bB + 1));
-  const float2 f11 = make_float2(f(c, aA + 1, bA + 1), f(c, aB + 1, bB + 1));
-  const float2 t0 = fma2(f10, wa, mul2(f00, va));
-  const float2 t1 = fma2(f11, wa, mul2(f01, va));
-  return fma2(t1, wb, mul2(t0, vb));
-}
-
-// push_particle for particles A (.x) and B (.y) at cells (iA, jA), (iB, jB)
-template <class F>
-__device__ __forceinline__ float2 push_pair(const F &fld, int iA, int jA, int iB, int jB, float2 &x, float2 &y,
-                                            float2 &ux, float2 &uy, float2 &uz, float2 &mx, float2 &my,
-                                            float2 &x1, float2 &y1, int &diA, int &djA, int &diB, int &djB,
-                                            float2 &qvz, bool &badA, bool &badB, const PushConst &C) {
-  const int ihA = iA + ((x.x < 0.5f) ? -1 : 0), ihB = iB + ((x.y < 0.5f) ? -1 : 0);
-  const int jhA = jA + ((y.x < 0.5f) ? -1 : 0), jhB = jB + ((y.y < 0.5f) ? -1 : 0);
-  const float2 w1h = add2(x, make_float2((x.x < 0.5f) ? 0.5f : -0.5f, (x.y < 0.5f) ? 0.5f : -0.5f));
-  const float2 w2h = add2(y, make_float2((y.x < 0.5f) ? 0.5f : -0.5f, (y.y < 0.5f) ? 0.5f : -0.5f));
-  float2 ex = lerp2x2(fld, 0, ihA, jA, ihB, jB, w1h, y);
-  float2 ey = lerp2x2(fld, 1, iA, jhA, iB, jhB, x, w2h);
-  float2 ez = lerp2x2(fld, 2, iA, jA, iB, jB, x, y);
-  float2 bx = lerp2x2(fld, 3, iA, jhA, iB, jhB, x, w2h);
-  float2 by = lerp2x2(fld, 4, ihA, jA, ihB, jB, w1h, y);
-  float2 bz = lerp2x2(fld, 5, ihA, jhA, ihB, jhB, w1h, w2h);
-
-  const float2 tem = f2(C.tem);
-  ex = mul2(ex, tem);
-  ey = mul2(ey, tem);
-  ez = mul2(ez, tem);
-  float2 tx = add2(ux, ex), ty = add2(uy, ey), tz = add2(uz, ez);
-  const float2 u2 = fma2(tz, tz, fma2(ty, ty, mul2(tx, tx)));
-  const float gA = sqrtf(1.0f + u2.x), gB = sqrtf(1.0f + u2.y);
-  const float2 kin = make_float2(u2.x / (gA + 1), u2.y / (gB + 1));
-  const float2 tg = make_float2(C.tem / gA, C.tem / gB);
-  bx = mul2(bx, tg);
-  by = mul2(by, tg);
-  bz = mul2(bz, tg);
-  const float2 b2 = fma2(bz, bz, fma2(by, by, mul2(bx, bx)));
-  const float2 s2 = make_float2(2.0f / (1.0f + b2.x), 2.0f / (1.0f + b2.y));
-  // the cross products as chains of fused pairs, with the negated factors
-  // made once
-  const float2 m1 = f2(-1.0f);
-  const float2 ntx = mul2(tx, m1), nty = mul2(ty, m1), ntz = mul2(tz, m1);
-  const float2 vx = fma2(ntz, by, fma2(ty, bz, tx));
-  const float2 vy = fma2(ntx, bz, fma2(tz, bx, ty));
-  const float2 vz = fma2(nty, bx, fma2(tx, by, tz));
-  bx = mul2(bx, s2);
-  by = mul2(by, s2);
-  bz = mul2(bz, s2);
-  const float2 nvx = mul2(vx, m1), nvy = mul2(vy, m1), nvz = mul2(vz, m1);
-  tx = fma2(nvz, by, fma2(vy, bz, tx));
-  ty = fma2(nvx, bz, fma2(vz, bx, ty));
-  tz = fma2(nvy, bx, fma2(vx, by, tz));
-  ux = add2(tx, ex);
-  uy = add2(ty, ey);
-  uz = add2(tz, ez);
-
-  const float2 un = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
-  const float2 rg = make_float2(1.0f / sqrtf(1.0f + un.x), 1.0f / sqrtf(1.0f + un.y));
-  mx = mul2(mul2(f2(C.dt_dx), rg), ux);
-  my = mul2(mul2(f2(C.dt_dy), rg), uy);
-  badA = !(fabsf(mx.x) < 1.0f && fabsf(my.x) < 1.0f);
-  badB = !(fabsf(mx.y) < 1.0f && fabsf(my.y) < 1.0f);
-  x1 = add2(x, mx);
-  y1 = add2(y, my);
-  diA = (x1.x >= 1.0f) - (x1.x < 0.0f);
-  diB = (x1.y >= 1.0f) - (x1.y < 0.0f);
-  djA = (y1.x >= 1.0f) - (y1.x < 0.0f);
-  djB = (y1.y >= 1.0f) - (y1.y < 0.0f);
-  x1 = sub2(x1, make_float2((float)diA, (float)diB));
-  y1 = sub2(y1, make_float2((float)djA, (float)djB));
-  qvz = mul2(mul2(f2(C.q), uz), rg);
-  return kin;
-}
-
-// the single-segment currents of A and B (the fast build's weights); a
-// motion that leaves the cell has dx = dy = qvz = 0 here (zero current)
-__device__ __forceinline__ void segment_pair(float2 x0, float2 y0, float2 dx, float2 dy, float2 qvz, float qnx,
-                                             float qny, SegCurrent &cA, SegCurrent &cB) {
-  const float2 x1 = add2(x0, dx), y1 = add2(y0, dy);
-  const float2 jx = mul2(f2(qnx), dx), jy = mul2(f2(qny), dy);
-  const float2 ym = mul2(f2(0.5f), add2(y0, y1)), xm = mul2(f2(0.5f), add2(x0, x1));
-  const float2 v1 = mul2(jx, ym), v0 = sub2(jx, v1);
-  const float2 v3 = mul2(jy, xm), v2 = sub2(jy, v3);
-  const float2 c0 = sub2(f2(1.0f), y0), d0 = sub2(f2(1.0f), y1);
-  const float2 p0 = fma2(f2(0.5f), d0, c0), m0 = fma2(f2(-0.5f), c0, d0);
-  const float2 p1 = fma2(f2(0.5f), y1, y0), m1 = fma2(f2(-0.5f), y0, y1);
-  const float2 a0 = sub2(f2(1.0f), x0), b0 = sub2(f2(1.0f), x1);
-  const float2 v4 = mul2(qvz, fma2(b0, m0, mul2(a0, p0)));
-  const float2 v5 = mul2(qvz, fma2(x1, m0, mul2(x0, p0)));
-  const float2 v6 = mul2(qvz, fma2(b0, m1, mul2(a0, p1)));
-  const float2 v7 = mul2(qvz, fma2(x1, m1, mul2(x0, p1)));
-  cA.v[0] = v0.x, cA.v[1] = v1.x, cA.v[2] = v2.x, cA.v[3] = v3.x;
-  cA.v[4] = v4.x, cA.v[5] = v5.x, cA.v[6] = v6.x, cA.v[7] = v7.x;
-  cB.v[0] = v0.y, cB.v[1] = v1.y, cB.v[2] = v2.y, cB.v[3] = v3.y;
-  cB.v[4] = v4.y, cB.v[5] = v5.y, cB.v[6] = v6.y, cB.v[7] = v7.y;
-}
-#endif
-
 __device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
   const float y = v - c;
   const float t = s + y;
@@ -565,14 +448,8 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
   __shared__ int qi[NW][QCAP];       // local cell and shifts, packed
   // prefetched particles, 32 slots per warp: each lane reads its slot into
   // registers before it copies the next slot's particle into it
-#if defined(ZC_FAST_ALGEBRA) && defined(ZC_PUSH_PAIRS)
-  constexpr bool PAIRS = !DET;  // the fast float build takes two particles a lane
-#else
-  constexpr bool PAIRS = false;
-#endif
-  constexpr int NPF = PAIRS ? 2 : 1;
-  __shared__ __align__(16) float4 pf_u[NW][NPF][32];
-  __shared__ __align__(16) float2 pf_xy[NW][NPF][32];
+  __shared__ __align__(16) float4 pf_u[NW][32];
+  __shared__ __align__(16) float2 pf_xy[NW][32];
   __shared__ int nb[8], s_nnb;        // distinct neighbour tiles
   // incoming particles bound for this tile, listed as (outbox slot << 4 |
   // neighbour) so that they are pushed in full warps
@@ -826,101 +703,6 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
     }
   };
 
-#if defined(ZC_FAST_ALGEBRA) && defined(ZC_PUSH_PAIRS)
-  // the own-slot bookkeeping of one particle after the paired physics (the
-  // float build's branch of `process`, for particles with an own slot)
-  auto finish_own = [&](bool valid, int oslot, int li, int lj, int di, int dj, float x1, float y1, float ux,
-                        float uy, float uz, float sx0, float sy0, float smx, float smy, float sqvz, float kin,
-                        bool bad, const SegCurrent &cur) {
-    kahan_add(ks, kc, valid ? kin : 0.f);
-    errbits |= (valid && bad) ? ERR_ESCAPE : 0;
-    const bool split = valid && ((di != 0) || (dj != 0));
-    const int spk = li | (lj << 8) | ((di + 1) << 16) | ((dj + 1) << 18);
-    int ix = cx0 + li, iy = cy0 + lj;
-    const bool keep = apply_boundary(ix, iy, di, dj, Cl);
-    const int dest = (int)((unsigned)ix / TX) + (int)((unsigned)iy / TY) * Cl.ntx;
-    const int code = (valid && keep) ? ((dest == t) ? 1 : 2) : 0;  // 1 stays, 2 leaves
-    if (oslot >= 0) {
-      if (code == 1) store_particle(pout, base + oslot, ix, iy, x1, y1, ux, uy, uz);
-      else store_hole(pout, base + oslot);
-    }
-    const unsigned mleave = __ballot_sync(0xffffffffu, code == 2);
-    if (mleave) {
-      int lb = 0;
-      if (lane == 0) lb = atomicAdd(&s_leave, __popc(mleave));
-      lb = __shfl_sync(0xffffffffu, lb, 0);
-      if (code == 2) {
-        const int s = lb + __popc(mleave & below);
-        if (s < O.cap) {
-          store_particle(O.p, obase + s, ix, iy, x1, y1, ux, uy, uz);
-          O.dst[obase + s] = dest;
-        } else {
-          spill_particle(S, &errbits, ix, iy, x1, y1, ux, uy, uz);
-        }
-      }
-    }
-    {
-      const int key = li + lj * TX;
-      const bool change = valid && key != acc_key;
-      const bool flush = change && acc_key >= 0;
-      if (__any_sync(0xffffffffu, flush)) {
-        if (flush) add_current(dep, acc_key % TX, acc_key / TX, acc);
-      }
-      const float carry = change ? 0.0f : 1.0f;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) acc.v[q] = __fmaf_rn(acc.v[q], carry, cur.v[q]);
-      acc_key = change ? key : acc_key;
-    }
-    {
-      const unsigned sm = __ballot_sync(0xffffffffu, split);
-      if (sm) {
-        if (split) {
-          const int e = qcount + __popc(sm & below);
-          qf[warp][0][e] = sx0;
-          qf[warp][1][e] = sy0;
-          qf[warp][2][e] = smx;
-          qf[warp][3][e] = smy;
-          qf[warp][4][e] = sqvz;
-          qi[warp][e] = spk;
-        }
-        qcount += __popc(sm);
-        __syncwarp();
-        if (qcount >= QFLUSH) {
-          const int nq = min(qcount, 32);
-          qcount -= nq;
-          if (lane < nq) deposit_queued(qcount + lane);
-          __syncwarp();
-        }
-      }
-    }
-  };
-
-  // two own particles a lane, A then B of its lane run: the physics as
-  // packed pairs, the bookkeeping one after the other
-  auto process2 = [&](bool vA, int sA, const PRec &rA, bool vB, int sB, const PRec &rB) {
-    int liA = rA.ix - cx0, ljA = rA.iy - cy0, liB = rB.ix - cx0, ljB = rB.iy - cy0;
-    errbits |= (vA && ((unsigned)liA >= (unsigned)TX || (unsigned)ljA >= (unsigned)TY)) ? ERR_ESCAPE : 0;
-    errbits |= (vB && ((unsigned)liB >= (unsigned)TX || (unsigned)ljB >= (unsigned)TY)) ? ERR_ESCAPE : 0;
-    liA = min(max(liA, 0), TX - 1);
-    ljA = min(max(ljA, 0), TY - 1);
-    liB = min(max(liB, 0), TX - 1);
-    ljB = min(max(ljB, 0), TY - 1);
-    float2 x = make_float2(rA.x, rB.x), y = make_float2(rA.y, rB.y);
-    float2 ux = make_float2(rA.ux, rB.ux), uy = make_float2(rA.uy, rB.uy), uz = make_float2(rA.uz, rB.uz);
-    float2 mx, my, x1, y1, qvz;
-    int diA, djA, diB, djB;
-    bool badA, badB;
-    const float2 kin =
-        push_pair(fld, liA, ljA, liB, ljB, x, y, ux, uy, uz, mx, my, x1, y1, diA, djA, diB, djB, qvz, badA, badB, Cl);
-    const bool sgA = vA && diA == 0 && djA == 0, sgB = vB && diB == 0 && djB == 0;
-    SegCurrent cA, cB;
-    segment_pair(x, y, make_float2(sgA ? mx.x : 0.f, sgB ? mx.y : 0.f), make_float2(sgA ? my.x : 0.f, sgB ? my.y : 0.f),
-                 make_float2(sgA ? qvz.x * 0.5f : 0.f, sgB ? qvz.y * 0.5f : 0.f), Cl.qnx, Cl.qny, cA, cB);
-    finish_own(vA, sA, liA, ljA, diA, djA, x1.x, y1.x, ux.x, uy.x, uz.x, x.x, y.x, mx.x, my.x, qvz.x, kin.x, badA, cA);
-    finish_own(vB, sB, liB, ljB, diB, djB, x1.y, y1.y, ux.y, uy.y, uz.y, x.y, y.y, mx.y, my.y, qvz.y, kin.y, badB, cB);
-  };
-#endif
-
   // incoming particles: warp w scans the outboxes of neighbours w, w + NW,
   // ... for the slots bound for this tile and lists them; a full list
   // leaves the rest to be pushed right here
@@ -971,65 +753,15 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       return i < n_own;
     };
     const auto ubase = [&](int u) { return (warp + NW * (u / kLaneRun)) * kChunk + (u % kLaneRun) * 32; };
-#if defined(ZC_FAST_ALGEBRA) && defined(ZC_PUSH_PAIRS)
-    if constexpr (PAIRS) {
-      // units u and u + 1 (the same chunk: kLaneRun is even) at once
-      const auto fetch = [&](int u, int q) -> bool {
-        int rs, ws;
-        if (ubase(u) < n_own && slots(u, rs, ws)) {
-          cp_async16(&pf_u[warp][q][lane], &pin.u[base + rs]);
-          cp_async8(&pf_xy[warp][q][lane], &pin.xy[base + rs]);
-          return true;
-        }
-        return false;
-      };
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-        if (!fetch(q, q)) {
-          pf_u[warp][q][lane] = make_float4(0.f, 0.f, 0.f, 0.f);  // what a lane without a particle reads
-          pf_xy[warp][q][lane] = make_float2(0.f, 0.f);
-        }
-      cp_async_commit();
-      for (int u = 0; ubase(u) < n_own; u += 2) {
-        cp_async_wait<0>();
-        PRec r[2];
-        bool v[2];
-        int w[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          int rs, ws;
-          const bool inr = slots(u + q, rs, ws);
-          const float4 uu = pf_u[warp][q][lane];
-          const float2 xy = pf_xy[warp][q][lane];
-          const unsigned cw = (unsigned)__float_as_int(uu.w);
-          v[q] = inr && cw != kHole;
-          w[q] = inr ? ws : -2;
-          r[q].ix = (int)(cw & 0xffffu);
-          r[q].iy = (int)(cw >> 16);
-          r[q].x = v[q] ? xy.x : 0.5f;
-          r[q].y = v[q] ? xy.y : 0.5f;
-          r[q].ux = uu.x;
-          r[q].uy = uu.y;
-          r[q].uz = uu.z;
-        }
-#pragma unroll
-        for (int q = 0; q < 2; ++q) fetch(u + 2 + q, q);
-        cp_async_commit();
-        process2(v[0], w[0], r[0], v[1], w[1], r[1]);
-      }
-      cp_async_wait<0>();
-    } else
-#endif
-    {
     {
       int rs, ws;
       if (ubase(0) < n_own && slots(0, rs, ws)) {
-        cp_async16(&pf_u[warp][0][lane], &pin.u[base + rs]);
-        cp_async8(&pf_xy[warp][0][lane], &pin.xy[base + rs]);
+        cp_async16(&pf_u[warp][lane], &pin.u[base + rs]);
+        cp_async8(&pf_xy[warp][lane], &pin.xy[base + rs]);
       } else {
         // a lane without a first particle reads these zeros
-        pf_u[warp][0][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-        pf_xy[warp][0][lane] = make_float2(0.f, 0.f);
+        pf_u[warp][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+        pf_xy[warp][lane] = make_float2(0.f, 0.f);
       }
     }
     cp_async_commit();
@@ -1041,8 +773,8 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       // (the last unit's particle, a hole's zero momenta, or the zeros the
       // slots start with): finite values whose results `valid` masks; its
       // position is set to the cell centre (a hole's is stale)
-      const float4 uu = pf_u[warp][0][lane];
-      const float2 xy = pf_xy[warp][0][lane];
+      const float4 uu = pf_u[warp][lane];
+      const float2 xy = pf_xy[warp][lane];
       const unsigned cw = (unsigned)__float_as_int(uu.w);
       const bool valid = inr && cw != kHole;
       PRec r;
@@ -1056,15 +788,14 @@ __global__ void __launch_bounds__(NT, DET ? 1024 / NT : ZC_PUSH_MIN_CTAS) k_push
       {
         int rn, wn;
         if (ubase(u + 1) < n_own && slots(u + 1, rn, wn)) {
-          cp_async16(&pf_u[warp][0][lane], &pin.u[base + rn]);
-          cp_async8(&pf_xy[warp][0][lane], &pin.xy[base + rn]);
+          cp_async16(&pf_u[warp][lane], &pin.u[base + rn]);
+          cp_async8(&pf_xy[warp][lane], &pin.xy[base + rn]);
         }
       }
       cp_async_commit();
       process(valid, inr ? ws : -2, false, r.ix, r.iy, r.x, r.y, r.ux, r.uy, r.uz);
     }
     cp_async_wait<0>();
-    }
   }
 
   // the listed incoming particles, in units of 32 spread over the warps
