@@ -30,6 +30,26 @@ def test_scan_table():
     assert 0.8e6 < mean_parts < 2.2e6
 
 
+def test_tile_choices():
+    """The autotuner's candidates: one shape for every run, or the per-run
+    policy that gives runs with few particles per cell larger tiles; every
+    tile fits its grid and is a shape the kernels are built for."""
+    from zpic_gb300 import batch
+
+    runs = batch.weibel_scan(n_runs=64)
+    assert batch.tiles_for(runs, (32, 16)) == [(32, 16)] * len(runs)
+    tiles = batch.tiles_for(runs, "by_ppc")
+    supported = {(16, 16), (8, 8), (16, 8), (32, 16), (32, 32), (8, 16), (16, 32)}
+    for r, t in zip(runs, tiles):
+        assert t in supported and t[0] <= r.nx[0] and t[1] <= r.nx[1]
+        ppc = r.ppc[0] * r.ppc[1]
+        assert t == ((32, 32) if ppc <= 6 else (32, 16) if ppc <= 12 else (16, 16))
+    # the sort interval's block (2 sort_every steps) divides the run
+    for steps in (300, 96, 50):
+        se = batch.scan_sort_every(steps)
+        assert 1 <= se <= 8 and steps % (2 * se) == 0
+
+
 _CHILD = r"""
 import sys
 sys.path[:0] = [{root!r}]
