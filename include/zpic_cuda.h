@@ -395,15 +395,24 @@ ZC_API zc_status zc_history_reset(zc_sim *sim);
 
 /* --- batched runs (parameter scans) ---------------------------------------- */
 /* A batch advances many independent simulations together: one CUDA graph
- * holds a block of steps of every member as parallel branches, so small
- * grids that cannot fill the GPU alone share it, and one launch per block
- * replaces hundreds.  Members keep their own handles (data access, energy,
- * history) and must share the block length (same sort_every) and have no
- * moving window.  Replaces the reference's process-level fan-out of a
- * parameter scan (mods/em1d_param_scan/main.c:112-133); each member gives
- * the results it gives alone. */
+ * holds a block of steps of every member of a group as parallel branches,
+ * so small grids that cannot fill the GPU alone share it, and one launch per
+ * block and group replaces hundreds.  Members keep their own handles (data
+ * access, energy, history) and must share the block length (same
+ * sort_every) and have no moving window.  Replaces the reference's
+ * process-level fan-out of a parameter scan
+ * (mods/em1d_param_scan/main.c:112-133); each member gives the results it
+ * gives alone. */
 typedef struct zc_batch zc_batch;
 ZC_API zc_status zc_batch_create(zc_sim *const *sims, int nsims, zc_batch **out);
+/* The members are dealt into groups of about equal particle capacity, each
+ * with its own stream and graphs: a group's first block starts as soon as
+ * its own graph is recorded, and groups do not wait for one another between
+ * blocks.  By default one group per 32 members (1 to 8); ngroups <= 0
+ * restores that, larger counts are capped at the member count.  Results do
+ * not depend on the grouping. */
+ZC_API zc_status zc_batch_set_groups(zc_batch *batch, int ngroups);
+ZC_API zc_status zc_batch_get_groups(zc_batch *batch, int *ngroups);
 /* advances every member by nsteps */
 ZC_API zc_status zc_batch_step(zc_batch *batch, int nsteps);
 /* device time (ms) of the last zc_batch_step, CUDA events */

@@ -87,9 +87,11 @@ def test_history_under_graphs():
     assert np.allclose(h[:, :6].sum(axis=1), e, rtol=1e-5, atol=1e-30)
 
 
-def test_batch_matches_runs_alone():
-    """Three different runs in one batch, one of them started off a block
-    boundary, each checked against its own oracle run."""
+@pytest.mark.parametrize("groups", [None, 2, 3])
+def test_batch_matches_runs_alone(groups):
+    """Three different runs in one batch (one group, or the members dealt
+    into two or three groups on their own streams), one of them started off
+    a block boundary, each checked against its own oracle run."""
     from zpic_gb300._zc import CudaBatch
 
     pairs = [mirror(n, sort_every=2) for n in ("thermal", "weibel_smooth", "custom_ext")]
@@ -98,7 +100,8 @@ def test_batch_matches_runs_alone():
     cpu1.iter(3)
     for cpu, g in pairs:
         g.history_enable(64)
-    b = CudaBatch([g for _, g in pairs])
+    b = CudaBatch([g for _, g in pairs], groups=groups)
+    assert b.groups == (groups or 1)
     b.step(11)
     b.step(5)
     assert b.last_ms() > 0
@@ -140,13 +143,14 @@ def test_scan_batched_equals_sequential():
         s.close()
 
 
-def test_batch_member_relayout_between_steps():
+@pytest.mark.parametrize("groups", [1, 2])
+def test_batch_member_relayout_between_steps(groups):
     """A member re-laid out between batch steps is captured again and its
-    branch of the batch graph updated."""
+    branch of its group's graph updated."""
     from zpic_gb300._zc import CudaBatch
 
     pairs = [mirror(n, sort_every=2) for n in ("thermal", "weibel_smooth")]
-    b = CudaBatch([g for _, g in pairs])
+    b = CudaBatch([g for _, g in pairs], groups=groups)
     b.step(8)
     for cpu, g in pairs:
         cpu.iter(8)
@@ -197,3 +201,31 @@ def test_spill_path_matches_oracle(graphs):
     g.step(8)
     cpu.iter(8)
     _check(cpu, g)
+
+
+def test_batch_groups_with_spilled_member():
+    """Four runs dealt into two groups, one holding more particles in a tile
+    than the tile has room for (its spill list is advanced beside the tiles):
+    each run still gives its oracle run's results, and regrouping between
+    calls changes nothing."""
+    from zpic_gb300._zc import CudaBatch
+
+    pairs = [mirror(n, sort_every=2) for n in ("thermal", "weibel_smooth", "thermal", "custom_ext")]
+    cpu0, g0 = pairs[0]
+    few = _cluster(2500, 5, 5, 3)
+    g0.inject(0, few)
+    cpu0.set_particles(0, np.concatenate([cpu0.particles(0), few]))
+    b = CudaBatch([g for _, g in pairs], groups=2)
+    b.step(8)
+    for cpu, g in pairs:
+        cpu.iter(8)
+        _check(cpu, g)
+    b.set_groups(0)
+    assert b.groups == 1
+    b.set_groups(9)
+    assert b.groups == 4
+    b.step(10)
+    for cpu, g in pairs:
+        cpu.iter(10)
+        _check(cpu, g)
+    b.close()

@@ -37,6 +37,7 @@ EXPORTS = [
     "zc_last_error", "zc_status_string", "zc_set_profiling", "zc_get_profile", "zc_reset_profile",
     "zc_phase_name", "zc_field_energy_static", "zc_set_graphs", "zc_history_enable", "zc_history_get",
     "zc_history_reset", "zc_batch_create", "zc_batch_step", "zc_batch_last_ms", "zc_batch_destroy",
+    "zc_batch_set_groups", "zc_batch_get_groups",
     "zc_adj_create", "zc_adj_destroy", "zc_adj_set_state", "zc_adj_forward", "zc_adj_backward",
     "zc_adj_get_state", "zc_adj_times", "zc_species_phasespace", "zc_species_create_device",
     "zc_adj_set_birth", "zc_adj_set_smooth", "zc_copy_grid_async", "zc_fence_wait", "zc_fence_destroy",
@@ -161,6 +162,8 @@ def load(path: str = LIB_PATH):
         "zc_history_reset": [P],
         "zc_batch_create": [P, I, C.POINTER(P)],
         "zc_batch_step": [P, I],
+        "zc_batch_set_groups": [P, I],
+        "zc_batch_get_groups": [P, C.POINTER(I)],
         "zc_batch_last_ms": [P, C.POINTER(C.c_float)],
         "zc_batch_destroy": [P],
         "zc_adj_create": [C.POINTER(AdjDesc), C.POINTER(P)],
@@ -522,16 +525,28 @@ class CudaSim:
 
 class CudaBatch:
     """Independent simulations advanced together (a ``zc_batch`` handle):
-    one CUDA graph runs a block of steps of every member as parallel
-    branches.  The members stay usable on their own."""
+    one CUDA graph per group of members runs a block of steps of each of
+    them as parallel branches.  ``groups`` sets the group count (None: one
+    per 32 members, 1 to 8).  The members stay usable on their own."""
 
-    def __init__(self, sims):
+    def __init__(self, sims, groups=None):
         self.lib = load()
         self.sims = list(sims)
         arr = (C.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
         h = C.c_void_p()
         _ck(self.lib.zc_batch_create(arr, len(self.sims), C.byref(h)))
         self.h = h
+        if groups is not None:
+            self.set_groups(groups)
+
+    def set_groups(self, n):
+        _ck(self.lib.zc_batch_set_groups(self.h, int(n)))
+
+    @property
+    def groups(self) -> int:
+        v = C.c_int()
+        _ck(self.lib.zc_batch_get_groups(self.h, C.byref(v)))
+        return v.value
 
     def step(self, n=1):
         _ck(self.lib.zc_batch_step(self.h, int(n)))

@@ -2,10 +2,12 @@
 
 The reference scans parameters by running one process per point of the scan
 (mods/em1d_param_scan/main.c:112-133).  Here every run is a ``CudaSim`` with
-its own device state, and a ``CudaBatch`` advances a group of them with one
-CUDA graph per block of steps, whose branches are the runs: small grids that
-cannot fill the GPU alone share it, and one graph launch replaces the
-hundreds of kernel launches of a block.  Each run records its energy history
+its own device state, and a ``CudaBatch`` advances many of them with one
+CUDA graph per group of runs and block of steps, whose branches are the
+runs: small grids that cannot fill the GPU alone share it, and one graph
+launch replaces the hundreds of kernel launches of a block.  The groups run
+on their own streams, so the first group starts while the next one's graph
+is still being recorded.  Each run records its energy history
 (field energy per component and kinetic energy per species, every step) on
 the device.
 
@@ -132,9 +134,10 @@ class ScanResult:
         return self.particle_steps / (self.device_ms * 1e-3)
 
 
-def run_batched(sims, runs, group=None) -> ScanResult:
-    """Advances every run by its step count, ``group`` runs per batch graph
-    (all at once by default)."""
+def run_batched(sims, runs, group=None, stream_groups=None) -> ScanResult:
+    """Advances every run by its step count, ``group`` runs per batch (all
+    at once by default), one after another; each batch deals its members
+    into ``stream_groups`` graph groups (None: the batch's default)."""
     group = group or len(sims)
     steps = runs[0].steps
     if any(r.steps != steps for r in runs):
@@ -142,8 +145,10 @@ def run_batched(sims, runs, group=None) -> ScanResult:
     t0 = time.perf_counter()
     ms = 0.0
     ngroups = 0
+    sg = []
     for g0 in range(0, len(sims), group):
-        b = CudaBatch(sims[g0:g0 + group])
+        b = CudaBatch(sims[g0:g0 + group], groups=stream_groups)
+        sg.append(b.groups)
         b.step(steps)
         ms += b.last_ms()
         b.close()
@@ -151,7 +156,7 @@ def run_batched(sims, runs, group=None) -> ScanResult:
     wall = time.perf_counter() - t0
     hist = [s.history() for s in sims]
     nps = sum(r.particles() * r.steps for r in runs)
-    return ScanResult(hist, ms, wall, nps, ngroups, _counters(sims))
+    return ScanResult(hist, ms, wall, nps, ngroups, {**_counters(sims), "stream_groups": sg})
 
 
 def run_sequential(sims, runs) -> ScanResult:

@@ -2289,9 +2289,9 @@ struct zc_batch {
   std::vector<zc_sim *> sims;
   int device = 0;
   int period = 0;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;  // start and end of a call, its timing
   // one graph per run length (a whole block, a prefix for the remainder):
-  // every member's captured steps as a parallel branch
+  // every member of a group's captured steps as a parallel branch
   struct Parent {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -2299,11 +2299,25 @@ struct zc_batch {
     bool valid = false;
     std::vector<unsigned long long> ids;  // the member captures it copies
     std::vector<cudaGraphNode_t> nodes;   // their child nodes
-  } blk, tail;
-  int **d_errp = nullptr;   // every member's error word
-  int *d_errs = nullptr;    // their copy after a block, [2][n]
-  int *h_errs = nullptr;    // pinned, [2][n]
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_blk[2] = {nullptr, nullptr};
+  };
+  // the members are dealt into groups of about equal particle capacity,
+  // each with its own stream and graphs: a group starts as soon as its own
+  // graph is recorded (the first block of the next group is recorded while
+  // it runs), and the groups do not wait for one another between blocks
+  struct Group {
+    std::vector<int> members;  // member indices, heaviest first
+    int off = 0;               // its first slot in the error-word arrays
+    cudaStream_t st = nullptr;
+    Parent blk, tail;
+    cudaEvent_t ev_blk[2] = {nullptr, nullptr};
+    cudaEvent_t ev_end = nullptr;
+  };
+  std::vector<Group> groups;
+  std::vector<int> group_of;  // member index -> group
+  int **d_errp = nullptr;     // every member's error word, in group order
+  int *d_errs = nullptr;      // their copy after a block, [2][n]
+  int *h_errs = nullptr;      // pinned, [2][n]
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> ev_sim;  // one per member, joins of its stream
   float last_ms = 0;
 };
@@ -2316,17 +2330,70 @@ void drop_parent(zc_batch::Parent &g) {
   g = zc_batch::Parent{};
 }
 
-// makes `pg` run n steps of every member from its current state,
-// recapturing what is stale
-zc_status batch_ready(zc_batch *b, zc_batch::Parent &pg, int n) {
-  const bool have = pg.valid && pg.nsteps == n && pg.ids.size() == b->sims.size();
+void drop_groups(zc_batch *b) {
+  for (auto &G : b->groups) {
+    if (G.st) cudaStreamSynchronize(G.st);
+    drop_parent(G.blk);
+    drop_parent(G.tail);
+    for (auto e : {G.ev_blk[0], G.ev_blk[1], G.ev_end})
+      if (e) cudaEventDestroy(e);
+    if (G.st) cudaStreamDestroy(G.st);
+  }
+  b->groups.clear();
+}
+
+// the group count a batch of n members takes by default: one group up to
+// 32 members, then one more per 32 up to 8
+int default_groups(int n) { return std::max(1, std::min(8, n / 32)); }
+
+// deals the members into `ng` groups: heaviest first (most particle
+// capacity), in snake order, so that the groups carry about the same work
+// and every group's branches start with its longest chains
+zc_status form_groups(zc_batch *b, int ng) {
+  const int n = (int)b->sims.size();
+  ng = std::max(1, std::min(ng, n));
+  drop_groups(b);
+  std::vector<int> order(n);
+  std::vector<long long> weight(n, 0);
+  for (int k = 0; k < n; ++k) {
+    order[k] = k;
+    for (const auto &p : b->sims[k]->sp) weight[k] += p.alloc;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return weight[a] > weight[c]; });
+  b->groups.resize(ng);
+  b->group_of.assign(n, 0);
+  for (int j = 0; j < n; ++j) {
+    const int r = j / ng, q = j % ng;
+    const int g = (r % 2 == 0) ? q : ng - 1 - q;
+    b->groups[g].members.push_back(order[j]);
+    b->group_of[order[j]] = g;
+  }
+  std::vector<int *> ptrs;
+  for (auto &G : b->groups) {
+    G.off = (int)ptrs.size();
+    for (int k : G.members) ptrs.push_back(b->sims[k]->d_err);
+    if (cudaStreamCreateWithFlags(&G.st, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(ZC_ECUDA, "cudaStreamCreate failed");
+    for (auto *e : {&G.ev_blk[0], &G.ev_blk[1], &G.ev_end})
+      if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess)
+        return fail(ZC_ECUDA, "cudaEventCreate failed");
+  }
+  CK(cudaMemcpy(b->d_errp, ptrs.data(), sizeof(int *) * n, cudaMemcpyHostToDevice));
+  return ZC_OK;
+}
+
+// makes `pg` run n steps of every member of group G from its current
+// state, recapturing what is stale
+zc_status batch_ready(zc_batch *b, zc_batch::Group &G, zc_batch::Parent &pg, int n) {
+  const std::vector<int> &mem = G.members;
+  const bool have = pg.valid && pg.nsteps == n && pg.ids.size() == mem.size();
   bool ok = have;
   // the members to (re)capture, recorded by a few host threads at once
   // (each member captures on its own stream; nothing runs)
   std::vector<int> todo;
-  for (size_t k = 0; k < b->sims.size(); ++k) {
+  for (int k : mem) {
     zc_sim *s = b->sims[k];
-    if (!graph_ready(s, (n == b->period) ? s->blk : s->tail, n)) todo.push_back((int)k);
+    if (!graph_ready(s, (n == b->period) ? s->blk : s->tail, n)) todo.push_back(k);
   }
   if (!todo.empty()) {
     const int nt = (int)std::min<size_t>(todo.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
@@ -2351,15 +2418,15 @@ zc_status batch_ready(zc_batch *b, zc_batch::Parent &pg, int n) {
     for (int w = 0; w < nt; ++w)
       if (res[w] != ZC_OK) return fail(res[w], "%s", msg[w].c_str());
   }
-  for (size_t k = 0; k < b->sims.size(); ++k) {
-    zc_sim *s = b->sims[k];
+  for (size_t j = 0; j < mem.size(); ++j) {
+    zc_sim *s = b->sims[mem[j]];
     StepGraph &g = (n == b->period) ? s->blk : s->tail;
-    if (have && pg.ids[k] != g.id) {
+    if (have && pg.ids[j] != g.id) {
       // a member was captured again (after a re-layout): its copy in the
       // instantiated graph takes the new parameters in place when the
       // topology is unchanged, else everything is rebuilt
-      if (cudaGraphExecChildGraphNodeSetParams(pg.exec, pg.nodes[k], g.graph) == cudaSuccess) {
-        pg.ids[k] = g.id;
+      if (cudaGraphExecChildGraphNodeSetParams(pg.exec, pg.nodes[j], g.graph) == cudaSuccess) {
+        pg.ids[j] = g.id;
       } else {
         cudaGetLastError();
         ok = false;
@@ -2370,25 +2437,18 @@ zc_status batch_ready(zc_batch *b, zc_batch::Parent &pg, int n) {
   drop_parent(pg);
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
-  // the members' branches are added heaviest first (most particles), so that
-  // the longest chains start first and the block does not end on them
-  std::vector<int> order(b->sims.size());
-  std::vector<long long> weight(b->sims.size(), 0);
-  for (size_t k = 0; k < b->sims.size(); ++k) {
-    order[k] = (int)k;
-    for (const auto &p : b->sims[k]->sp) weight[k] += p.alloc;
-  }
-  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return weight[a] > weight[c]; });
-  pg.nodes.assign(b->sims.size(), nullptr);
-  for (int k : order) {
-    StepGraph &sg = (n == b->period) ? b->sims[k]->blk : b->sims[k]->tail;
+  // the members' branches are added heaviest first (the group's order), so
+  // that the longest chains start first and the block does not end on them
+  pg.nodes.assign(mem.size(), nullptr);
+  for (size_t j = 0; j < mem.size(); ++j) {
+    StepGraph &sg = (n == b->period) ? b->sims[mem[j]]->blk : b->sims[mem[j]]->tail;
     cudaGraphNode_t node;
     const cudaError_t e = cudaGraphAddChildGraphNode(&node, g, nullptr, 0, sg.graph);
     if (e != cudaSuccess) {
       cudaGraphDestroy(g);
       return fail(ZC_ECUDA, "cudaGraphAddChildGraphNode failed: %s", cudaGetErrorString(e));
     }
-    pg.nodes[k] = node;
+    pg.nodes[j] = node;
   }
   cudaGraphExec_t x = nullptr;
   const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
@@ -2401,7 +2461,7 @@ zc_status batch_ready(zc_batch *b, zc_batch::Parent &pg, int n) {
   pg.nsteps = n;
   pg.valid = true;
   pg.ids.clear();
-  for (zc_sim *s : b->sims) pg.ids.push_back(((n == b->period) ? s->blk : s->tail).id);
+  for (int k : mem) pg.ids.push_back(((n == b->period) ? b->sims[k]->blk : b->sims[k]->tail).id);
   return ZC_OK;
 }
 
@@ -2441,19 +2501,28 @@ zc_status zc_batch_create(zc_sim *const *sims, int nsims, zc_batch **out) {
   if ((st = dalloc(&b->d_errs, 2 * (size_t)nsims)) != ZC_OK) return bad(st);
   if (cudaMallocHost((void **)&b->h_errs, 2 * sizeof(int) * nsims) != cudaSuccess)
     return bad(fail(ZC_ENOMEM, "cudaMallocHost failed"));
-  std::vector<int *> ptrs;
-  for (zc_sim *s : b->sims) ptrs.push_back(s->d_err);
-  if (cudaMemcpy(b->d_errp, ptrs.data(), sizeof(int *) * nsims, cudaMemcpyHostToDevice) != cudaSuccess)
-    return bad(fail(ZC_ECUDA, "upload of member error words failed"));
-  if (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev_blk[0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev_blk[1], cudaEventDisableTiming) != cudaSuccess)
+  std::memset(b->h_errs, 0, 2 * sizeof(int) * nsims);
+  if (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
     return bad(fail(ZC_ECUDA, "cudaEventCreate failed"));
   b->ev_sim.assign(nsims, nullptr);
   for (auto &e : b->ev_sim)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
       return bad(fail(ZC_ECUDA, "cudaEventCreate failed"));
+  if ((st = form_groups(b, default_groups(nsims))) != ZC_OK) return bad(st);
   *out = b;
+  return ZC_OK;
+}
+
+zc_status zc_batch_set_groups(zc_batch *b, int ngroups) {
+  if (!b) return fail(ZC_EINVAL, "null batch handle");
+  DeviceGuard g(b->device);
+  const int n = (int)b->sims.size();
+  return form_groups(b, ngroups > 0 ? std::min(ngroups, n) : default_groups(n));
+}
+
+zc_status zc_batch_get_groups(zc_batch *b, int *ngroups) {
+  if (!b || !ngroups) return fail(ZC_EINVAL, "null argument");
+  *ngroups = (int)b->groups.size();
   return ZC_OK;
 }
 
@@ -2461,12 +2530,11 @@ zc_status zc_batch_destroy(zc_batch *b) {
   if (!b) return ZC_OK;
   DeviceGuard g(b->device);
   if (b->st) cudaStreamSynchronize(b->st);
-  drop_parent(b->blk);
-  drop_parent(b->tail);
+  drop_groups(b);
   dfree(b->d_errp);
   dfree(b->d_errs);
   if (b->h_errs) cudaFreeHost(b->h_errs);
-  for (auto e : {b->ev0, b->ev1, b->ev_blk[0], b->ev_blk[1]})
+  for (auto e : {b->ev0, b->ev1})
     if (e) cudaEventDestroy(e);
   for (auto e : b->ev_sim)
     if (e) cudaEventDestroy(e);
@@ -2508,41 +2576,49 @@ zc_status zc_batch_step(zc_batch *b, int nsteps) {
   if (blocks > 0 || rest > 0) {
     for (int k = 0; k < n; ++k) {
       CK(cudaEventRecord(b->ev_sim[k], b->sims[k]->st));
-      CK(cudaStreamWaitEvent(b->st, b->ev_sim[k], 0));
+      CK(cudaStreamWaitEvent(b->groups[b->group_of[k]].st, b->ev_sim[k], 0));
     }
     for (int i = 0; i < blocks; ++i) {
-      TRY(batch_ready(b, b->blk, P));
-      CK(cudaGraphLaunch(b->blk.exec, b->st));
-      for (zc_sim *s : b->sims) account_steps(s, s->blk);
       const int slot = i & 1;
-      CK(launch_gather_words(b->d_errp, n, b->d_errs + (size_t)slot * n, b->st));
-      CK(cudaMemcpyAsync(b->h_errs + (size_t)slot * n, b->d_errs + (size_t)slot * n, sizeof(int) * n,
-                         cudaMemcpyDeviceToHost, b->st));
-      CK(cudaEventRecord(b->ev_blk[slot], b->st));
+      for (auto &G : b->groups) {
+        const int m = (int)G.members.size();
+        TRY(batch_ready(b, G, G.blk, P));
+        CK(cudaGraphLaunch(G.blk.exec, G.st));
+        for (int k : G.members) account_steps(b->sims[k], b->sims[k]->blk);
+        int *dst = b->d_errs + (size_t)slot * n + G.off;
+        CK(launch_gather_words(b->d_errp + G.off, m, dst, G.st));
+        CK(cudaMemcpyAsync(b->h_errs + (size_t)slot * n + G.off, dst, sizeof(int) * m, cudaMemcpyDeviceToHost,
+                           G.st));
+        CK(cudaEventRecord(G.ev_blk[slot], G.st));
+      }
       if (i > 0) {
         // the previous block's error words, read while this block runs
-        CK(cudaEventSynchronize(b->ev_blk[1 - slot]));
+        for (auto &G : b->groups) CK(cudaEventSynchronize(G.ev_blk[1 - slot]));
         bool any = false;
         for (int k = 0; k < n; ++k) any |= b->h_errs[(size_t)(1 - slot) * n + k] != 0;
         if (any) {
-          CK(cudaStreamSynchronize(b->st));
+          for (auto &G : b->groups) CK(cudaStreamSynchronize(G.st));
           std::memset(b->h_errs, 0, 2 * sizeof(int) * n);
           for (int k = 0; k < n; ++k) {
             zc_sim *s = b->sims[k];
             TRY(check_errors(s, true));  // a spill re-lays a member out
             CK(cudaEventRecord(b->ev_sim[k], s->st));
-            CK(cudaStreamWaitEvent(b->st, b->ev_sim[k], 0));
+            CK(cudaStreamWaitEvent(b->groups[b->group_of[k]].st, b->ev_sim[k], 0));
           }
         }
       }
     }
     if (rest > 0) {
-      TRY(batch_ready(b, b->tail, rest));
-      CK(cudaGraphLaunch(b->tail.exec, b->st));
-      for (zc_sim *s : b->sims) account_steps(s, s->tail);
+      for (auto &G : b->groups) {
+        TRY(batch_ready(b, G, G.tail, rest));
+        CK(cudaGraphLaunch(G.tail.exec, G.st));
+        for (int k : G.members) account_steps(b->sims[k], b->sims[k]->tail);
+      }
     }
-    CK(cudaEventRecord(b->ev_blk[0], b->st));
-    for (zc_sim *s : b->sims) CK(cudaStreamWaitEvent(s->st, b->ev_blk[0], 0));
+    for (auto &G : b->groups) {
+      CK(cudaEventRecord(G.ev_end, G.st));
+      for (int k : G.members) CK(cudaStreamWaitEvent(b->sims[k]->st, G.ev_end, 0));
+    }
   }
   for (int k = 0; k < n; ++k) {
     zc_sim *s = b->sims[k];
