@@ -424,6 +424,59 @@ def run_lwfa(args):
     return 0
 
 
+def run_dropin(args):
+    """The uniform thermal plasma (2048 x 2048, 4 x 4 ppc, uth 0.05,
+    compensated level-1 smoothing along x and y) as a reference input deck:
+    a C program compiled against the em2d drop-in headers and linked to
+    libzpic_em2d (zpic_gb300/csrc/em2d/deck_thermal.c), loading its particles
+    with spec_new and stepping with sim_iter, timed on the host wall clock.
+    Two runs: host mirrors refreshed on demand, and host mirrors kept valid
+    across every sim_iter (the reference's struct semantics)."""
+    import subprocess
+
+    from zpic_gb300 import build
+
+    build.build()
+    root = os.path.dirname(os.path.abspath(__file__))
+    lib = os.path.join(root, "zpic_gb300", "lib")
+    out = os.path.join(root, "zpic_gb300", "_build")
+    os.makedirs(out, exist_ok=True)
+    exe = os.path.join(out, "deck_thermal")
+    subprocess.run(["gcc", "-O2", "-std=c99", "-I", os.path.join(root, "include", "em2d"),
+                    os.path.join(root, "zpic_gb300", "csrc", "em2d", "deck_thermal.c"), "-L", lib, "-lzpic_em2d",
+                    "-Wl,-rpath," + lib, "-lm", "-o", exe], check=True)
+    n = args.nx or 2048
+    tile = tuple(int(v) for v in args.tile.split("x"))
+    steps = args.steps if args.steps_given else 20
+    res = {}
+    for mode, k in (("demand", steps), ("every", max(2, min(steps, 6)))):
+        r = subprocess.run([exe, str(k), mode, str(n), str(tile[0]), str(tile[1]), "0" if args.exact else "1"],
+                           capture_output=True, text=True, timeout=1800)
+        if r.returncode != 0:
+            raise RuntimeError(f"deck_thermal {mode} failed: {r.stderr[-2000:]}")
+        v = dict(line.split() for line in r.stdout.splitlines())
+        res[mode] = {"steps": k, "setup_s": float(v["setup_s"]), "first_step_ms": float(v["first_step_ms"]),
+                     "step_ms": float(v["step_ms"]), "sync_host_ms": float(v["sync_host_ms"]),
+                     "particles": int(v["particles"]),
+                     "kinetic": float(v["kinetic"]), "field": float(v["field"])}
+    d, e = res["demand"], res["every"]
+    mirror_bytes = d["particles"] * 28 + 3 * 3 * 4 * (n + 3) * (n + 3)
+    line = {
+        "metric": METRIC, "value": d["particles"] / (d["step_ms"] * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": steps, "warmup": 1, "ms_per_step": d["step_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (spec_new loading through the drop-in)",
+        "config": {"workload": f"em2d uniform thermal plasma {n}x{n}, 4x4 ppc, uth 0.05, compensated level 1 x "
+                               f"and y, dt 0.05: a C deck through the em2d drop-in (sim_iter)",
+                   "tile": list(tile), "push_build": "exact" if args.exact else "fast"},
+        "how": "value = particles / host wall time of one sim_iter (mirrors on demand), after the first step",
+        "mirrors_on_demand": d,
+        "mirrors_every_step": {**e, "rate": e["particles"] / (e["step_ms"] * 1e-3),
+                               "host_mirror_bytes": mirror_bytes},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 # ---------------------------------------------------------------------------
 # differentiable step: gradient of the final field energy
 # ---------------------------------------------------------------------------
@@ -964,7 +1017,7 @@ def main():
     ap.add_argument("--sort-every", type=int, default=0)
     ap.add_argument("--nx", type=int, default=0, help="square grid override (profiling runs)")
     ap.add_argument("--workload", default="plain", choices=["plain", "scan", "adjoint", "lwfa", "wakefield_adjoint",
-                                                              "em1d", "em1d_scan"])
+                                                              "em1d", "em1d_scan", "dropin"])
     ap.add_argument("--deterministic", action="store_true", help="fixed-point (bit-reproducible) deposition")
     ap.add_argument("--fd-study", action="store_true", help="wakefield adjoint: finite differences at shrinking steps")
     ap.add_argument("--scan-runs", type=int, default=256)
@@ -988,6 +1041,8 @@ def main():
         return run_em1d(args)
     if args.workload == "em1d_scan":
         return run_em1d_scan(args)
+    if args.workload == "dropin":
+        return run_dropin(args)
 
     from zpic_gb300.replicas import Replicas
 
