@@ -229,3 +229,27 @@ def test_batch_groups_with_spilled_member():
         cpu.iter(10)
         _check(cpu, g)
     b.close()
+
+
+@pytest.mark.parametrize("groups", [1, 2])
+def test_batch_member_spills_while_stepping(groups):
+    """A dense cluster streams (ux = 2) from one tile into its neighbour,
+    which has no room for it, while the batch runs: its particles go to the
+    spill list, the batch drains every group's stream and re-lays the member
+    out between blocks, and every run still gives its oracle run's results."""
+    from zpic_gb300._zc import CudaBatch
+
+    pairs = [mirror(n, sort_every=2) for n in ("thermal", "weibel_smooth", "thermal")]
+    cpu0, g0 = pairs[0]
+    jet = _cluster(6000, 14, 8, 4)
+    jet["ux"] += np.float32(2.0)
+    g0.inject(0, jet)
+    cpu0.set_particles(0, np.concatenate([cpu0.particles(0), jet]))
+    r0 = g0.info()["relayouts"]
+    b = CudaBatch([g for _, g in pairs], groups=groups)
+    b.step(16)
+    assert g0.info()["relayouts"] > r0, "the cluster's spill list was drained inside the batch"
+    for cpu, g in pairs:
+        cpu.iter(16)
+        _check(cpu, g)
+    b.close()
