@@ -154,3 +154,25 @@ def test_history_streamed_to_host_rows_matches_device_history():
         out.append(hist)
         g.close()
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("groups", [1, 2, 3])
+def test_batch_gives_the_bits_of_runs_alone(groups):
+    """Three different runs batched (in one, two or three groups on their own
+    streams; 13 steps: three 4-step blocks and a 1-step tail) end with the
+    bits of the same runs stepped alone."""
+    from zpic_gb300._zc import CudaBatch
+
+    names = ("weibel_smooth", "thermal", "custom_ext")
+    alone = []
+    for name in names:
+        _, g = mirror(name, deterministic=True, sort_every=2)
+        g.step(13)
+        alone.append(_state(g, len(DECKS[name]["species"])))
+        g.close()
+    sims = [mirror(name, deterministic=True, sort_every=2)[1] for name in names]
+    b = CudaBatch(sims, groups=groups)
+    b.step(13)
+    for name, g, ref in zip(names, sims, alone):
+        _same(ref, _state(g, len(DECKS[name]["species"])))
+    b.close()

@@ -134,9 +134,11 @@ ZC_SPILL_LAUNCHER(launch_push_spill_fast_det);
 cudaError_t launch_fixed_to_float(const unsigned long long *src, float *dst, size_t n, cudaStream_t st);
 cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, size_t n, cudaStream_t st);
 // counting sort of every tile by cell (src -> dst, same offsets): holes
-// dropped, np set to the particle count, cell order through tile_slot
+// dropped, np set to the particle count, cell order through tile_slot;
+// max_n: the most slots any tile holds (its capacity will do), which sizes
+// the shared-memory staging
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
-                            const LayoutConst &L, int ntiles, cudaStream_t st);
+                            const LayoutConst &L, int ntiles, int max_n, cudaStream_t st);
 // particles (slots that are not holes) of every tile into cnt
 cudaError_t launch_count_valid(const Particles &buf, const int *off, const int *np, int *cnt, int ntiles,
                                cudaStream_t st);

@@ -12,6 +12,7 @@
 //                 dropped), so that the push lanes meet runs of one cell.
 //   re-layout     upload, moving-window injection and capacity changes.
 #include <algorithm>
+#include <atomic>
 
 #include "zc_internal.cuh"
 #include "zc_kernels.h"
@@ -229,53 +230,61 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 // tile, src -> dst at the same offsets): a shared-memory histogram, a scan,
 // then every particle takes the next position of its cell, stored at its
 // tile_slot (the lane-run layout); holes are dropped and np becomes the
-// particle count.  The order inside a cell follows the atomics' timing.  The reference sorts its whole buffer by cell every
-// n_sort steps for cache reuse (spec_sort, em2d/particles.c:942-1007); here
-// the per-tile sort gives the push lanes runs of particles in one cell.
-#ifndef ZC_SORT_ILP
-#define ZC_SORT_ILP 2
-#endif
+// particle count.  The order inside a cell follows the atomics' timing.  The
+// reference sorts its whole buffer by cell every n_sort steps for cache
+// reuse (spec_sort, em2d/particles.c:942-1007); here the per-tile sort gives
+// the push lanes runs of particles in one cell.
+//
+// The tile is staged in shared memory: every thread starts asynchronous
+// copies of its particles' records (16 + 8 bytes each), so that a whole tile
+// is in flight at once; the count reads shared memory.  A tile that fits
+// (n <= S) is then written out in slot order: every particle notes its index
+// at its slot (a 16-bit permutation), and the threads store slot j = thread,
+// thread + NT, ... from the staged records, coalesced (the lane-run layout
+// would otherwise scatter every warp's stores over the tile).  A fuller tile
+// stages its first S particles, reads the rest from global memory and
+// scatters.  Dynamic shared memory: the cell cursors, then S float4, S float2
+// and S 16-bit slots.
 #ifndef ZC_SORT_NT
 #define ZC_SORT_NT 1024
 #endif
 template <int NT>
 __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Particles dst, const int *off, int *np,
-                                                             LayoutConst L) {
-  // each thread keeps ILP particles' loads in flight at once
-  constexpr int MAXC = 1024, ILP = ZC_SORT_ILP, CPT = MAXC / NT;  // cells per thread in the scan
-  __shared__ int cursor[MAXC];
+                                                             LayoutConst L, int S) {
+  constexpr int MAXC = 1024, CPT = MAXC / NT;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  int *cursor = reinterpret_cast<int *>(sm_raw);
+  float4 *su = reinterpret_cast<float4 *>(sm_raw + MAXC * sizeof(int));
+  float2 *sxy = reinterpret_cast<float2 *>(su + S);
+  unsigned short *perm = reinterpret_cast<unsigned short *>(sxy + S);
   __shared__ int swarp[NT / 32];
   const int t = blockIdx.x;
   const int ncell = L.TX * L.TY;
   const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
   const int n = np[t];
+  const int ns = min(n, S);
   const long long b = off[t];
+  for (int k = threadIdx.x; k < ns; k += NT) {
+    cp_async16(&su[k], &src.u[b + k]);
+    cp_async8(&sxy[k], &src.xy[b + k]);
+  }
+  cp_async_commit();
   for (int c = threadIdx.x; c < MAXC; c += NT) cursor[c] = 0;
-  __syncthreads();
   auto cell_of_word = [&](float w) {  // -1 for a hole
     const unsigned u = (unsigned)__float_as_int(w);
     if (u == kHole) return -1;
     const int c = ((int)(u & 0xffffu) - cx0) + ((int)(u >> 16) - cy0) * L.TX;
     return min(max(c, 0), ncell - 1);
   };
-  const float hole = __int_as_float((int)kHole);
-  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * NT) {
-    float w[ILP];
-#pragma unroll
-    for (int q = 0; q < ILP; ++q) {
-      const int k = k0 + q * NT;
-      w[q] = (k < n) ? __ldg(&src.u[b + k].w) : hole;
-    }
-#pragma unroll
-    for (int q = 0; q < ILP; ++q) {
-      const int c = cell_of_word(w[q]);
-      if (c >= 0) atomicAdd(&cursor[c], 1);
-    }
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += NT) {
+    const int c = cell_of_word(k < ns ? su[k].w : __ldg(&src.u[b + k].w));
+    if (c >= 0) atomicAdd(&cursor[c], 1);
   }
   __syncthreads();
   int nvalid;
   {
-    // thread i scans cells i CPT .. i CPT + CPT - 1 (cells past ncell hold 0)
     int v[CPT], sum = 0;
 #pragma unroll
     for (int e = 0; e < CPT; ++e) {
@@ -290,26 +299,33 @@ __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Parti
     }
   }
   __syncthreads();
-  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * NT) {
-    float4 u[ILP];
-    float2 xy[ILP];
-#pragma unroll
-    for (int q = 0; q < ILP; ++q) {
-      const int k = k0 + q * NT;
-      if (k < n) {
-        u[q] = __ldg(&src.u[b + k]);
-        xy[q] = __ldg(&src.xy[b + k]);
-      } else {
-        u[q].w = hole;
-      }
+  if (n <= S) {
+    for (int k = threadIdx.x; k < n; k += NT) {
+      const int c = cell_of_word(su[k].w);
+      if (c >= 0) perm[tile_slot(atomicAdd(&cursor[c], 1), nvalid)] = (unsigned short)k;
     }
-#pragma unroll
-    for (int q = 0; q < ILP; ++q) {
-      const int c = cell_of_word(u[q].w);
+    __syncthreads();
+    for (int j = threadIdx.x; j < nvalid; j += NT) {
+      const int k = perm[j];
+      dst.u[b + j] = su[k];
+      dst.xy[b + j] = sxy[k];
+    }
+  } else {
+    for (int k = threadIdx.x; k < n; k += NT) {
+      float4 u;
+      float2 xy;
+      if (k < ns) {
+        u = su[k];
+        xy = sxy[k];
+      } else {
+        u = __ldg(&src.u[b + k]);
+        xy = __ldg(&src.xy[b + k]);
+      }
+      const int c = cell_of_word(u.w);
       if (c < 0) continue;
       const int slot = tile_slot(atomicAdd(&cursor[c], 1), nvalid);
-      dst.u[b + slot] = u[q];
-      dst.xy[b + slot] = xy[q];
+      dst.u[b + slot] = u;
+      dst.xy[b + slot] = xy;
     }
   }
   if (threadIdx.x == 0) np[t] = nvalid;
@@ -654,9 +670,28 @@ cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, siz
   return cudaGetLastError();
 }
 
+// staging room: the cursors and 26 bytes a particle within 227 KB (and
+// slots that fit 16 bits)
+constexpr int kSortStageMax = 8704;
+constexpr int kSortStageBytes = (int)(sizeof(float4) + sizeof(float2) + sizeof(unsigned short));
+
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
-                            const LayoutConst &L, int ntiles, cudaStream_t st) {
-  k_cellsort<ZC_SORT_NT><<<ntiles, ZC_SORT_NT, 0, st>>>(src, dst, off, np, L);
+                            const LayoutConst &L, int ntiles, int max_n, cudaStream_t st) {
+  // the shared-memory opt-in, once per device
+  static std::atomic<unsigned long long> opted{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(opted.load() & bit)) {
+    e = cudaFuncSetAttribute(k_cellsort<ZC_SORT_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             1024 * (int)sizeof(int) + kSortStageMax * kSortStageBytes);
+    if (e != cudaSuccess) return e;
+    opted.fetch_or(bit);
+  }
+  const int S = std::max(1, std::min(max_n, kSortStageMax));
+  const size_t smem = 1024 * sizeof(int) + (size_t)S * kSortStageBytes;
+  k_cellsort<ZC_SORT_NT><<<ntiles, ZC_SORT_NT, smem, st>>>(src, dst, off, np, L, S);
   return cudaGetLastError();
 }
 
