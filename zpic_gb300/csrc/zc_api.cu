@@ -453,7 +453,7 @@ zc_status relayout(zc_sim *s, int k, const Particles *list, int list_n) {
   CK(cudaMemcpyAsync(p.d_np, cnt.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, st));
   // every tile into the other buffer in cell order (the lane-run layout)
   Particles dst = pl.grow ? pl.nbuf[0] : p.buf[src_i];
-  CK(launch_cellsort(tmp, dst, p.d_off, p.d_np, L, nt, *std::max_element(cnt.begin(), cnt.end()), st));
+  CK(launch_cellsort(tmp, dst, p.d_off, p.d_np, L, nt, *std::max_element(cnt.begin(), cnt.end()), s->d_err, st));
   CK(cudaMemsetAsync(p.d_spill_cnt, 0, 2 * sizeof(int), st));
   CK(cudaStreamSynchronize(st));
   adopt_tiles(p, pl);
@@ -657,7 +657,8 @@ zc_status spec_advance_impl(zc_sim *s, int k, bool kin_later = false) {
   if (s->sort_every > 0 && p.iter % s->sort_every == 0) {
     // keep the tiles sorted by cell (the push warps then share cells)
     Phase ph(s, ZC_PHASE_SORT, 1);
-    CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles, p.max_cap, st));
+    CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles, p.max_cap, s->d_err,
+                       st));
     p.cur = 1 - p.cur;
     a.pin = p.buf[p.cur];
     a.pout = p.buf[1 - p.cur];

@@ -136,9 +136,10 @@ cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, siz
 // counting sort of every tile by cell (src -> dst, same offsets): holes
 // dropped, np set to the particle count, cell order through tile_slot;
 // max_n: the most slots any tile holds (its capacity will do), which sizes
-// the shared-memory staging
+// the shared-memory staging; a timed-out wait on the staging copies sets
+// ERR_TIMEOUT in err
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
-                            const LayoutConst &L, int ntiles, int max_n, cudaStream_t st);
+                            const LayoutConst &L, int ntiles, int max_n, int *err, cudaStream_t st);
 // particles (slots that are not holes) of every tile into cnt
 cudaError_t launch_count_valid(const Particles &buf, const int *off, const int *np, int *cnt, int ntiles,
                                cudaStream_t st);

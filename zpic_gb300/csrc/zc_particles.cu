@@ -235,9 +235,13 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 // reuse (spec_sort, em2d/particles.c:942-1007); here the per-tile sort gives
 // the push lanes runs of particles in one cell.
 //
-// The tile is staged in shared memory: every thread starts asynchronous
-// copies of its particles' records (16 + 8 bytes each), so that a whole tile
-// is in flight at once; the count reads shared memory.  A tile that fits
+// The tile is staged in shared memory by bulk copies (TMA) of its records,
+// 16 + 8 bytes a particle, that one thread starts: a whole tile is in flight
+// at once, without a load instruction a particle; the count reads shared
+// memory.  Tile offsets are multiples of 32 particles, so both copies start
+// 16-byte aligned; an odd last float2 is loaded plainly.  The wait on the
+// copies is bounded: on a timeout the tile is left as it was and the error
+// word says so.  A tile that fits
 // (n <= S) is then written out in slot order: every particle notes its index
 // at its slot (a 16-bit permutation), and the threads store slot j = thread,
 // thread + NT, ... from the staged records, coalesced (the lane-run layout
@@ -250,7 +254,7 @@ __global__ void k_scatter_list(Particles list, const int *n_ptr, int n_cap, Part
 #endif
 template <int NT>
 __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Particles dst, const int *off, int *np,
-                                                             LayoutConst L, int S) {
+                                                             LayoutConst L, int S, int *err) {
   constexpr int MAXC = 1024, CPT = MAXC / NT;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   int *cursor = reinterpret_cast<int *>(sm_raw);
@@ -258,17 +262,28 @@ __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Parti
   float2 *sxy = reinterpret_cast<float2 *>(su + S);
   unsigned short *perm = reinterpret_cast<unsigned short *>(sxy + S);
   __shared__ int swarp[NT / 32];
+  __shared__ __align__(8) uint64_t bar;
   const int t = blockIdx.x;
   const int ncell = L.TX * L.TY;
   const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
   const int n = np[t];
   const int ns = min(n, S);
+  const int nb = ns & ~1;  // float2 records copied in bulk (whole 16-byte units)
   const long long b = off[t];
-  for (int k = threadIdx.x; k < ns; k += NT) {
-    cp_async16(&su[k], &src.u[b + k]);
-    cp_async8(&sxy[k], &src.xy[b + k]);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
   }
-  cp_async_commit();
+  __syncthreads();
+  if (threadIdx.x == 0 && ns > 0) {
+    mbar_expect_tx(&bar, (uint32_t)ns * 16u + (uint32_t)nb * 8u);
+    constexpr int kPiece = 4096;  // records a copy
+    for (int k = 0; k < ns; k += kPiece)
+      bulk_load(&su[k], &src.u[b + k], (uint32_t)min(kPiece, ns - k) * 16u, &bar);
+    for (int k = 0; k < nb; k += kPiece)
+      bulk_load(&sxy[k], &src.xy[b + k], (uint32_t)min(kPiece, nb - k) * 8u, &bar);
+  }
+  if (threadIdx.x == 0 && nb < ns) sxy[nb] = src.xy[b + nb];
   for (int c = threadIdx.x; c < MAXC; c += NT) cursor[c] = 0;
   auto cell_of_word = [&](float w) {  // -1 for a hole
     const unsigned u = (unsigned)__float_as_int(w);
@@ -276,7 +291,15 @@ __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Parti
     const int c = ((int)(u & 0xffffu) - cx0) + ((int)(u >> 16) - cy0) * L.TX;
     return min(max(c, 0), ncell - 1);
   };
-  cp_async_wait<0>();
+  const bool loaded = ns == 0 || mbar_wait_bounded(&bar, 0);
+  if (!loaded) {
+    // leave the tile; a second bounded wait lets the copies land first
+    if (threadIdx.x == 0) {
+      mbar_wait_bounded(&bar, 0);
+      atomicOr(err, ERR_TIMEOUT);
+    }
+    return;
+  }
   __syncthreads();
   for (int k = threadIdx.x; k < n; k += NT) {
     const int c = cell_of_word(k < ns ? su[k].w : __ldg(&src.u[b + k].w));
@@ -676,7 +699,7 @@ constexpr int kSortStageMax = 8704;
 constexpr int kSortStageBytes = (int)(sizeof(float4) + sizeof(float2) + sizeof(unsigned short));
 
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
-                            const LayoutConst &L, int ntiles, int max_n, cudaStream_t st) {
+                            const LayoutConst &L, int ntiles, int max_n, int *err, cudaStream_t st) {
   // the shared-memory opt-in, once per device
   static std::atomic<unsigned long long> opted{0};
   int dev = 0;
@@ -691,7 +714,7 @@ cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const in
   }
   const int S = std::max(1, std::min(max_n, kSortStageMax));
   const size_t smem = 1024 * sizeof(int) + (size_t)S * kSortStageBytes;
-  k_cellsort<ZC_SORT_NT><<<ntiles, ZC_SORT_NT, smem, st>>>(src, dst, off, np, L, S);
+  k_cellsort<ZC_SORT_NT><<<ntiles, ZC_SORT_NT, smem, st>>>(src, dst, off, np, L, S, err);
   return cudaGetLastError();
 }
 
