@@ -117,6 +117,7 @@ struct SpeciesState {
   int *d_spill_cnt = nullptr;  // [2]
   int spill_cap = 0;
   int max_cap = 0;             // largest tile capacity
+  int sort_stage = 0;          // particles a tile's sort stages in shared memory
   int spill_cur = 0;
   // outboxes: leavers posted by one push, pulled by the next (ob[ob_in]
   // holds the pending ones; its counts are all zero when nothing is pending)
@@ -201,6 +202,11 @@ struct zc_sim {
   int deterministic = 0;
   int fast = 0;                   // FMA build of the push kernels
   int sort_every = 8;             // steps between per-tile cell sorts
+  // batches holding this simulation: while it shares the GPU with other
+  // runs, its cell sort stages nothing in shared memory (a staged sort block
+  // takes most of a multiprocessor's shared memory from the other runs'
+  // kernels)
+  int batches = 0;
   float slack = 0.5f;
   int accumulated_err = 0;
   int queued_steps = 0;           // steps zc_step_async queued since the last wait
@@ -370,8 +376,10 @@ zc_status plan_tiles(zc_sim *s, SpeciesState &p, const std::vector<int> &cnt, Ti
   pl.cap.assign(nt, 0);
   pl.tot = 0;
   int max_cap = 0;
+  long long max_fill = 0;
   for (int t = 0; t < nt; ++t) {
     long long base = std::max<long long>(cnt[t], nominal);
+    max_fill = std::max(max_fill, base);
     long long c = (long long)std::ceil(base * (1.0 + s->slack)) + 32;
     c = (c + 31) / 32 * 32;
     if (c > (1LL << 30)) return fail(ZC_ENOMEM, "tile capacity too large");
@@ -383,6 +391,12 @@ zc_status plan_tiles(zc_sim *s, SpeciesState &p, const std::vector<int> &cnt, Ti
   if (pl.tot >= (1LL << 31)) return fail(ZC_ENOMEM, "species too large for 32-bit tile offsets");
   TRY(ensure_outbox(s, p, max_cap));
   p.max_cap = max_cap;
+  // the cell sort stages the fullest tile's particles at this layout plus a
+  // quarter (fuller tiles take their excess from global memory): staging
+  // room sized to the capacity, three times the particles with a large
+  // slack, would leave one sort block a multiprocessor where batched runs
+  // share the GPU
+  p.sort_stage = (int)std::min<long long>(max_cap, max_fill + max_fill / 4 + 64);
   pl.grow = pl.tot > p.alloc;
   if (pl.grow) {
     TRY(alloc_particles(pl.nbuf[0], pl.tot));
@@ -657,8 +671,8 @@ zc_status spec_advance_impl(zc_sim *s, int k, bool kin_later = false) {
   if (s->sort_every > 0 && p.iter % s->sort_every == 0) {
     // keep the tiles sorted by cell (the push warps then share cells)
     Phase ph(s, ZC_PHASE_SORT, 1);
-    CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles, p.max_cap, s->d_err,
-                       st));
+    CK(launch_cellsort(p.buf[p.cur], p.buf[1 - p.cur], p.d_off, p.d_np, layout(s), s->ntiles,
+                       s->batches > 0 ? 0 : p.sort_stage, s->d_err, st));
     p.cur = 1 - p.cur;
     a.pin = p.buf[p.cur];
     a.pout = p.buf[1 - p.cur];
@@ -2321,6 +2335,7 @@ struct zc_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> ev_sim;  // one per member, joins of its stream
   float last_ms = 0;
+  bool marked = false;  // the members count this batch (zc_sim::batches)
 };
 
 namespace {
@@ -2510,6 +2525,11 @@ zc_status zc_batch_create(zc_sim *const *sims, int nsims, zc_batch **out) {
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
       return bad(fail(ZC_ECUDA, "cudaEventCreate failed"));
   if ((st = form_groups(b, default_groups(nsims))) != ZC_OK) return bad(st);
+  for (zc_sim *s : b->sims) {
+    s->batches += 1;
+    invalidate_graph(s);  // recorded blocks hold the sort of a run alone
+  }
+  b->marked = true;
   *out = b;
   return ZC_OK;
 }
@@ -2532,6 +2552,11 @@ zc_status zc_batch_destroy(zc_batch *b) {
   DeviceGuard g(b->device);
   if (b->st) cudaStreamSynchronize(b->st);
   drop_groups(b);
+  if (b->marked)
+    for (zc_sim *s : b->sims) {
+      s->batches -= 1;
+      if (s->batches == 0) invalidate_graph(s);  // recorded blocks hold the batch's sort
+    }
   dfree(b->d_errp);
   dfree(b->d_errs);
   if (b->h_errs) cudaFreeHost(b->h_errs);

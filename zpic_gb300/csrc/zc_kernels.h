@@ -135,9 +135,10 @@ cudaError_t launch_fixed_to_float(const unsigned long long *src, float *dst, siz
 cudaError_t launch_float_to_fixed(const float *src, unsigned long long *dst, size_t n, cudaStream_t st);
 // counting sort of every tile by cell (src -> dst, same offsets): holes
 // dropped, np set to the particle count, cell order through tile_slot;
-// max_n: the most slots any tile holds (its capacity will do), which sizes
-// the shared-memory staging; a timed-out wait on the staging copies sets
-// ERR_TIMEOUT in err
+// max_n: the particles a tile stages in shared memory (a tile with more
+// takes the rest from global memory; 0: no staging, the sort for runs that
+// share the GPU); a timed-out wait on the staging copies sets ERR_TIMEOUT
+// in err
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
                             const LayoutConst &L, int ntiles, int max_n, int *err, cudaStream_t st);
 // particles (slots that are not holes) of every tile into cnt

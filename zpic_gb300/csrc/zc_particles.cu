@@ -354,6 +354,85 @@ __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Parti
   if (threadIdx.x == 0) np[t] = nvalid;
 }
 
+// The same sort without staging, for runs that share the GPU with others
+// (batches): every thread keeps two particles' loads in flight, the count
+// and the scatter read global memory, and a block needs 4 KB of shared
+// memory, so sort blocks sit beside the other runs' kernels.
+template <int NT>
+__global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort_direct(Particles src, Particles dst, const int *off,
+                                                                    int *np, LayoutConst L) {
+  constexpr int MAXC = 1024, ILP = 2, CPT = MAXC / NT;
+  __shared__ int cursor[MAXC];
+  __shared__ int swarp[NT / 32];
+  const int t = blockIdx.x;
+  const int ncell = L.TX * L.TY;
+  const int cx0 = (t % L.ntx) * L.TX, cy0 = (t / L.ntx) * L.TY;
+  const int n = np[t];
+  const long long b = off[t];
+  for (int c = threadIdx.x; c < MAXC; c += NT) cursor[c] = 0;
+  __syncthreads();
+  auto cell_of_word = [&](float w) {  // -1 for a hole
+    const unsigned u = (unsigned)__float_as_int(w);
+    if (u == kHole) return -1;
+    const int c = ((int)(u & 0xffffu) - cx0) + ((int)(u >> 16) - cy0) * L.TX;
+    return min(max(c, 0), ncell - 1);
+  };
+  const float hole = __int_as_float((int)kHole);
+  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * NT) {
+    float w[ILP];
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int k = k0 + q * NT;
+      w[q] = (k < n) ? __ldg(&src.u[b + k].w) : hole;
+    }
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int c = cell_of_word(w[q]);
+      if (c >= 0) atomicAdd(&cursor[c], 1);
+    }
+  }
+  __syncthreads();
+  int nvalid;
+  {
+    int v[CPT], sum = 0;
+#pragma unroll
+    for (int e = 0; e < CPT; ++e) {
+      v[e] = cursor[threadIdx.x * CPT + e];
+      sum += v[e];
+    }
+    int pre = block_exclusive_scan<NT>(sum, nvalid, swarp);
+#pragma unroll
+    for (int e = 0; e < CPT; ++e) {
+      cursor[threadIdx.x * CPT + e] = pre;
+      pre += v[e];
+    }
+  }
+  __syncthreads();
+  for (int k0 = threadIdx.x; k0 < n; k0 += ILP * NT) {
+    float4 u[ILP];
+    float2 xy[ILP];
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int k = k0 + q * NT;
+      if (k < n) {
+        u[q] = __ldg(&src.u[b + k]);
+        xy[q] = __ldg(&src.xy[b + k]);
+      } else {
+        u[q].w = hole;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < ILP; ++q) {
+      const int c = cell_of_word(u[q].w);
+      if (c < 0) continue;
+      const int slot = tile_slot(atomicAdd(&cursor[c], 1), nvalid);
+      dst.u[b + slot] = u[q];
+      dst.xy[b + slot] = xy[q];
+    }
+  }
+  if (threadIdx.x == 0) np[t] = nvalid;
+}
+
 // appends a list to the tiles in place (moving-window injection); overflow
 // goes to the spill list that the next push processes
 __global__ void k_append_list(Particles list, int n, Particles buf, TileSet T, Spill S, LayoutConst L,
@@ -700,6 +779,10 @@ constexpr int kSortStageBytes = (int)(sizeof(float4) + sizeof(float2) + sizeof(u
 
 cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const int *off, int *np,
                             const LayoutConst &L, int ntiles, int max_n, int *err, cudaStream_t st) {
+  if (max_n <= 0) {
+    k_cellsort_direct<ZC_SORT_NT><<<ntiles, ZC_SORT_NT, 0, st>>>(src, dst, off, np, L);
+    return cudaGetLastError();
+  }
   // the shared-memory opt-in, once per device
   static std::atomic<unsigned long long> opted{0};
   int dev = 0;
@@ -712,7 +795,7 @@ cudaError_t launch_cellsort(const Particles &src, const Particles &dst, const in
     if (e != cudaSuccess) return e;
     opted.fetch_or(bit);
   }
-  const int S = std::max(1, std::min(max_n, kSortStageMax));
+  const int S = std::min(max_n, kSortStageMax);
   const size_t smem = 1024 * sizeof(int) + (size_t)S * kSortStageBytes;
   k_cellsort<ZC_SORT_NT><<<ntiles, ZC_SORT_NT, smem, st>>>(src, dst, off, np, L, S, err);
   return cudaGetLastError();
