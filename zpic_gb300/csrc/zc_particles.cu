@@ -292,7 +292,8 @@ __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Parti
     return min(max(c, 0), ncell - 1);
   };
   const bool loaded = ns == 0 || mbar_wait_bounded(&bar, 0);
-  if (!loaded) {
+  // one verdict for the block (each thread's wait ran out on its own)
+  if (__syncthreads_or(!loaded)) {
     // leave the tile; a second bounded wait lets the copies land first
     if (threadIdx.x == 0) {
       mbar_wait_bounded(&bar, 0);
@@ -300,7 +301,6 @@ __global__ void __launch_bounds__(NT, 2048 / NT) k_cellsort(Particles src, Parti
     }
     return;
   }
-  __syncthreads();
   for (int k = threadIdx.x; k < n; k += NT) {
     const int c = cell_of_word(k < ns ? su[k].w : __ldg(&src.u[b + k].w));
     if (c >= 0) atomicAdd(&cursor[c], 1);
