@@ -85,3 +85,19 @@ def test_thermal_deck_matches_oracle(tmp_path, mirrors):
     assert abs(float(v["kinetic"]) - cpu.energy(0)) <= 1e-5 * abs(cpu.energy(0))
     emf = float(cpu.emf_energy().sum())
     assert abs(float(v["field"]) - emf) <= 1e-5 * abs(emf)
+
+
+def test_mirror_passes_split_over_threads(tmp_path):
+    """The drop-in's threaded compare and copy of the host mirrors (no GPU
+    call): spans around the 4 MB split between threads, flipped bytes at
+    the ends and in the middle."""
+    from zpic_gb300 import build
+
+    build.build()
+    exe = str(tmp_path / "mirror_passes")
+    subprocess.run(["gcc", "-O2", "-std=c99", "-D_DEFAULT_SOURCE", "-pthread", "-w",
+                    os.path.join(ROOT, "tests", "c_deck", "mirror_passes.c"),
+                    os.path.join(ROOT, "zpic_gb300", "csrc", "em2d", "zdf_io.c"), "-L", LIB, "-lzpic_cuda",
+                    f"-Wl,-rpath,{LIB}", "-lm", "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
